@@ -1,0 +1,267 @@
+"""Time-dependent coefficients compiled to a bytecode the device evaluates.
+
+The reference evaluates each term's coefficient ``c_k(t)`` on the host once per
+right-hand-side call (``_BaseElement.matmul_data_t``,
+qutip/core/cy/_element.pyx:166-182).  Coefficients given as strings are compiled
+by Cython at run time (qutip/core/coefficient.py:399-450) and the combinators
+``Conj``/``Sum``/``Mul``/``Constant`` live in qutip/core/cy/coefficient.pyx:688-950.
+
+Here a coefficient becomes a small stack program over complex doubles.  The
+device evaluates it at every stage time inside the kernels, so a time-dependent
+right-hand side needs no host round trip.  The host parses the expression with
+:mod:`ast` once; ``args`` are folded in as constants.
+
+Program layout (shared with ``csrc/coeff_vm.cuh``): an ``int32`` code stream
+where ``OP_CONST`` is followed by an index into the ``complex128`` constant pool.
+"""
+from __future__ import annotations
+
+import ast
+import cmath
+import math
+from typing import Mapping
+
+import numpy as np
+
+__all__ = ["Coefficient", "coefficient", "OPCODES", "MAX_STACK", "pack_programs"]
+
+OPCODES = {
+    "END": 0, "CONST": 1, "T": 2, "ADD": 3, "SUB": 4, "MUL": 5, "DIV": 6, "NEG": 7,
+    "COS": 8, "SIN": 9, "EXP": 10, "LOG": 11, "SQRT": 12, "CONJ": 13, "REAL": 14,
+    "IMAG": 15, "ABS": 16, "POW": 17, "COSH": 18, "SINH": 19, "TANH": 20, "TAN": 21,
+    "ARCTAN": 22,
+}
+MAX_STACK = 16
+_FUNCS = {"cos": "COS", "sin": "SIN", "exp": "EXP", "log": "LOG", "sqrt": "SQRT",
+          "conj": "CONJ", "conjugate": "CONJ", "real": "REAL", "imag": "IMAG",
+          "abs": "ABS", "cosh": "COSH", "sinh": "SINH", "tanh": "TANH", "tan": "TAN",
+          "arctan": "ARCTAN"}
+_NAMES = {"pi": math.pi, "e": math.e, "j": 1j}
+_BINOPS = {ast.Add: "ADD", ast.Sub: "SUB", ast.Mult: "MUL", ast.Div: "DIV", ast.Pow: "POW"}
+
+
+class Coefficient:
+    """A device-evaluable scalar function ``c(t)``.
+
+    ``code``/``consts`` are the program; ``expr`` is a human-readable form.
+    """
+
+    def __init__(self, code, consts, expr: str):
+        self.code = [int(c) for c in code]
+        self.consts = [complex(c) for c in consts]
+        self.expr = expr
+        if self.code[-1] != OPCODES["END"]:
+            self.code.append(OPCODES["END"])
+        depth = _max_depth(self.code)
+        if depth > MAX_STACK:
+            raise ValueError(f"coefficient {expr!r} needs stack depth {depth} > {MAX_STACK}")
+
+    # -- algebra (mirrors Conj/Sum/Mul coefficients) ------------------------
+    def _body(self):
+        return self.code[:-1]
+
+    def _combine(self, other: "Coefficient", op: str, sym: str) -> "Coefficient":
+        shift = len(self.consts)
+        body2 = _shift_consts(other._body(), shift)
+        return Coefficient(self._body() + body2 + [OPCODES[op]],
+                           self.consts + other.consts, f"({self.expr}){sym}({other.expr})")
+
+    def conj(self) -> "Coefficient":
+        return Coefficient(self._body() + [OPCODES["CONJ"]], self.consts, f"conj({self.expr})")
+
+    def __add__(self, other):
+        return self._combine(_as_coeff(other), "ADD", "+")
+
+    def __mul__(self, other):
+        return self._combine(_as_coeff(other), "MUL", "*")
+
+    __radd__ = __add__
+    __rmul__ = __mul__
+
+    def key(self):
+        return (tuple(self.code), tuple(self.consts))
+
+    def __call__(self, t: float) -> complex:
+        """Run the program on the host (used to check the device interpreter)."""
+        return _run(self.code, self.consts, float(t))
+
+    def __repr__(self):
+        return f"Coefficient({self.expr!r})"
+
+
+def _as_coeff(x) -> Coefficient:
+    return x if isinstance(x, Coefficient) else coefficient(x)
+
+
+def _shift_consts(code, shift):
+    out, i = [], 0
+    while i < len(code):
+        out.append(code[i])
+        if code[i] == OPCODES["CONST"]:
+            out.append(code[i + 1] + shift)
+            i += 1
+        i += 1
+    return out
+
+
+def _max_depth(code):
+    d = best = 0
+    i = 0
+    unary = {OPCODES[k] for k in ("NEG", "COS", "SIN", "EXP", "LOG", "SQRT", "CONJ", "REAL",
+                                  "IMAG", "ABS", "COSH", "SINH", "TANH", "TAN", "ARCTAN")}
+    while i < len(code):
+        op = code[i]
+        if op == OPCODES["END"]:
+            break
+        if op == OPCODES["CONST"]:
+            d += 1
+            i += 1
+        elif op == OPCODES["T"]:
+            d += 1
+        elif op in unary:
+            pass
+        else:
+            d -= 1
+        best = max(best, d)
+        i += 1
+    return best
+
+
+class _Compiler(ast.NodeVisitor):
+    def __init__(self, args: Mapping):
+        self.args = dict(args or {})
+        self.code: list[int] = []
+        self.consts: list[complex] = []
+
+    def const(self, v):
+        v = complex(v)
+        if v in self.consts:
+            idx = self.consts.index(v)
+        else:
+            idx = len(self.consts)
+            self.consts.append(v)
+        self.code += [OPCODES["CONST"], idx]
+
+    def visit_Expression(self, node):
+        self.visit(node.body)
+
+    def visit_Constant(self, node):
+        if not isinstance(node.value, (int, float, complex)) or isinstance(node.value, bool):
+            raise ValueError(f"unsupported literal {node.value!r}")
+        self.const(node.value)
+
+    def visit_Name(self, node):
+        if node.id == "t":
+            self.code.append(OPCODES["T"])
+        elif node.id in self.args:
+            v = self.args[node.id]
+            if not np.isscalar(v):
+                raise ValueError(f"argument {node.id!r} must be a scalar number")
+            self.const(v)
+        elif node.id in _NAMES:
+            self.const(_NAMES[node.id])
+        else:
+            raise ValueError(f"unknown name {node.id!r} in coefficient")
+
+    def visit_Attribute(self, node):
+        # np.pi / numpy.pi
+        if isinstance(node.value, ast.Name) and node.value.id in ("np", "numpy", "math", "cmath"):
+            if node.attr in _NAMES:
+                return self.const(_NAMES[node.attr])
+        raise ValueError(f"unsupported attribute {ast.unparse(node)!r}")
+
+    def visit_UnaryOp(self, node):
+        self.visit(node.operand)
+        if isinstance(node.op, ast.USub):
+            self.code.append(OPCODES["NEG"])
+        elif not isinstance(node.op, ast.UAdd):
+            raise ValueError("unsupported unary operator")
+
+    def visit_BinOp(self, node):
+        op = _BINOPS.get(type(node.op))
+        if op is None:
+            raise ValueError(f"unsupported operator {type(node.op).__name__}")
+        self.visit(node.left)
+        self.visit(node.right)
+        self.code.append(OPCODES[op])
+
+    def visit_Call(self, node):
+        f = node.func
+        name = f.attr if isinstance(f, ast.Attribute) else getattr(f, "id", None)
+        if name not in _FUNCS or len(node.args) != 1 or node.keywords:
+            raise ValueError(f"unsupported function call {ast.unparse(node)!r}")
+        self.visit(node.args[0])
+        self.code.append(OPCODES[_FUNCS[name]])
+
+    def generic_visit(self, node):
+        raise ValueError(f"unsupported syntax {type(node).__name__}")
+
+
+def coefficient(base, args: Mapping | None = None) -> Coefficient:
+    """Build a :class:`Coefficient` from a number, a string expression or a Coefficient.
+
+    Strings follow the reference's string-coefficient syntax
+    (qutip/core/coefficient.py:63-130): a Python expression in ``t`` and the
+    names in ``args``, using ``cos, sin, exp, log, sqrt, conj, real, imag, abs,
+    cosh, sinh, tanh, tan, arctan`` (optionally prefixed ``np.``), ``pi`` and
+    ``1j``.
+    """
+    if isinstance(base, Coefficient):
+        return base
+    if isinstance(base, (int, float, complex, np.number)):
+        return Coefficient([OPCODES["CONST"], 0, OPCODES["END"]], [complex(base)], repr(base))
+    if isinstance(base, str):
+        comp = _Compiler(args)
+        comp.visit(ast.parse(base.strip(), mode="eval"))
+        a = ", ".join(f"{k}={v!r}" for k, v in sorted((args or {}).items()))
+        return Coefficient(comp.code + [OPCODES["END"]], comp.consts, f"{base} [{a}]")
+    raise TypeError(f"cannot evaluate a coefficient of type {type(base).__name__} on the device")
+
+
+def _run(code, consts, t):
+    st: list[complex] = []
+    i = 0
+    O = OPCODES
+    un = {O["COS"]: cmath.cos, O["SIN"]: cmath.sin, O["EXP"]: cmath.exp, O["LOG"]: cmath.log,
+          O["SQRT"]: cmath.sqrt, O["CONJ"]: lambda z: z.conjugate(), O["REAL"]: lambda z: z.real,
+          O["IMAG"]: lambda z: z.imag, O["ABS"]: abs, O["COSH"]: cmath.cosh,
+          O["SINH"]: cmath.sinh, O["TANH"]: cmath.tanh, O["TAN"]: cmath.tan,
+          O["ARCTAN"]: cmath.atan, O["NEG"]: lambda z: -z}
+    while True:
+        op = code[i]
+        if op == O["END"]:
+            break
+        if op == O["CONST"]:
+            i += 1
+            st.append(consts[code[i]])
+        elif op == O["T"]:
+            st.append(complex(t))
+        elif op in un:
+            st.append(complex(un[op](st.pop())))
+        else:
+            b, a = st.pop(), st.pop()
+            st.append({O["ADD"]: a + b, O["SUB"]: a - b, O["MUL"]: a * b,
+                       O["DIV"]: a / b if b != 0 else complex("nan"),
+                       O["POW"]: a ** b}[op])
+        i += 1
+    return st[-1]
+
+
+def pack_programs(coeffs):
+    """Concatenate per-group programs for the device.
+
+    Returns ``(code int32[], starts int32[G+1], consts float64[2*K])``; a ``None``
+    coefficient becomes the constant 1.
+    """
+    code: list[int] = []
+    starts = [0]
+    consts: list[complex] = []
+    for c in coeffs:
+        c = coefficient(1.0) if c is None else c
+        code += _shift_consts(c._body(), len(consts)) + [OPCODES["END"]]
+        consts += c.consts
+        starts.append(len(code))
+    cz = np.zeros(2 * max(len(consts), 1), dtype=np.float64)
+    for i, z in enumerate(consts):
+        cz[2 * i], cz[2 * i + 1] = z.real, z.imag
+    return (np.asarray(code, dtype=np.int32), np.asarray(starts, dtype=np.int32), cz)
