@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Benchmark: time-dependent Lindblad solve of the dissipative transverse-field
+Ising chain, L = 10 spins (Hilbert dim 1024, Liouvillian dim 1,048,576,
+24.6 M stored entries in two coefficient groups), Vern7 atol 1e-8 / rtol 1e-6,
+tlist = linspace(0, 10, 101), 10 e_ops.
+
+One step = one complete solve.  ``value`` is solves/s with the operator already
+resident in HBM (the operator, 0.5 GB, is larger than L2, so no flush is
+needed); ``e2e`` repeats the solve through the host API with the operator and
+initial state copied from pinned host memory every step and the expectation
+values read back.  The reported ``roofline`` is that of the fused Vern7 stage
+kernel (matvec + stage combination), timed with CUDA events on its stream.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_SITES = 10
+T_END, N_OUT = 10.0, 101
+METRIC = "solves_per_sec"
+UNIT = "solves/s"
+WORKLOAD = f"ising_chain_L{N_SITES}_mesolve_vern7"
+CONFIG = {"workload": WORKLOAD, "n_sites": N_SITES, "hilbert_dim": 2 ** N_SITES,
+          "liouvillian_dim": 4 ** N_SITES, "tlist": f"linspace(0,{T_END:g},{N_OUT})",
+          "atol": 1e-8, "rtol": 1e-6, "e_ops": N_SITES, "h_seed": 1234,
+          "l2": "operator (0.5 GB) larger than L2; no flush"}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample", type=float, default=0.5,
+                    help="simulated time of the CPU-baseline sample (of 10.0)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-i", str(self.index), "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- dist ------
+class Dist:
+    def __init__(self, n_gpus):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        self.n_gpus = n_gpus
+
+    def init(self):
+        import torch
+        torch.cuda.set_device(self.local)
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+            self.pg = dist
+
+    def barrier(self):
+        import torch
+        torch.cuda.synchronize()
+        if self.pg:
+            self.pg.barrier()
+        torch.cuda.synchronize()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ----------------------------------------------------------- cpu baseline --
+def cpu_baseline(sample_t: float):
+    """Reference vern7 mesolve (compiled from source into oracle/_ref) on the host,
+    over the first ``sample_t`` of simulated time, scaled to solves/s."""
+    from oracle import ref_workloads as RW
+    cores = os.cpu_count() or 1
+    if RW.reference_available():
+        secs, frac = RW.reference_mesolve_sample(N_SITES, T_END, N_OUT, sample_t)
+        kind = "reference"
+        what = "QuTiP reference (oracle/_ref) mesolve vern7, CSR complex128, 1-thread SpMV"
+    else:
+        from qutip_gb300 import systems as S
+        s = S.ising_chain(N_SITES)
+        secs, frac = RW.port_mesolve_sample(s.terms, s.state0, s.e_ops, T_END, N_OUT, sample_t)
+        kind = "port"
+        what = "oracle numpy/scipy restatement of vern7 mesolve, complex128"
+    value = frac / secs
+    return {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": f"{what}; integrated t in [0,{sample_t:g}] of [0,{T_END:g}] "
+                      f"({secs:.2f} s), scaled by simulated time; BLAS threads = host cores"}
+
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return
+    steps = []
+    for i in range(args.warmup + args.steps):
+        b = cpu_baseline(args.cpu_sample)
+        if i >= args.warmup:
+            steps.append(b)
+    vals = [s["value"] for s in steps]
+    v = float(np.median(vals))
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+           "data": "synthetic (seeded h_i ~ U[0.5,1.5])", "config": CONFIG,
+           "cpu_baseline": {**steps[-1], "value": v},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# ------------------------------------------------------------------ ours ----
+def stage_bytes(op, n, stage, state_b, stage_b):
+    """Algorithmic HBM bytes of one fused Vern7 stage launch."""
+    from qutip_gb300 import vern7_tableau as T
+    b = op.nnz * (op.value_bytes() + 4) + op.n_groups * (n + 1) * 4  # operator
+    b += n * stage_b            # gathered vector x, read once
+    b += n * stage_b            # k_s written
+    b += n * state_b            # y_prev read
+    if stage == T.RK_STEP - 1:
+        used = [j for j in range(stage) if T.B[j] != 0 or T.E[j] != 0]
+        b += len(used) * n * stage_b + n * state_b  # k_j read, y_front written
+    elif stage != T.RK_EXTRA_STEP - 1:
+        row = T.A[stage + 1]
+        b += sum(n * stage_b for j in range(stage) if row[j] != 0) + n * stage_b  # k_j, ytmp
+    return b
+
+
+def measure_stage_roofline(op, sysm, precision, reps=20):
+    """Average duration and algorithmic GB/s of the fused stage kernel (events on its stream)."""
+    import torch
+    from qutip_gb300.vern7 import GpuVern7
+    ig = GpuVern7(op, precision=precision)
+    ig.set_initial_value(torch.from_numpy(sysm.state0).cuda(), 0.0)
+    ig.integrate(0.05, step=True)
+    state_b = 16 if ig.state_dt == "c128" else 8
+    stage_b = 16 if ig.stage_dt == "c128" else 8
+    total_bytes = sum(stage_bytes(op, ig.n, s, state_b, stage_b) for s in range(10))
+    st = torch.cuda.current_stream()
+    for _ in range(2):
+        ig._compute_step(ig.dt_safe)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    import ctypes as C
+    from qutip_gb300 import _lib
+    from qutip_gb300.operator import stream_ptr
+    lib = _lib.load()
+    rk = ig._rk()
+    sp_ = stream_ptr()
+    for _ in range(reps):
+        for s in range(10):
+            _lib.check(lib.qg_vern7_stage(C.byref(op.struct), C.byref(rk), s, 0.0, ig.dt_safe,
+                                          ig.atol, ig.rtol, op.lanes, sp_))
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / (reps * 10)
+    per_launch = total_bytes / 10
+    return ms, per_launch, per_launch / (ms * 1e-3) / 1e9
+
+
+def measure_spmv(op, reps=30):
+    import torch
+    x = torch.randn(op.n_cols, dtype=op.val.dtype, device="cuda")
+    y = torch.empty(op.n_rows, dtype=op.val.dtype, device="cuda")
+    op.matvec(0.3, x, y)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        op.matvec(0.3, x, y)
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    b = op.spmv_bytes()
+    return ms, b, b / (ms * 1e-3) / 1e9
+
+
+def run_ours(args, dist):
+    import torch
+    from qutip_gb300 import _lib
+    from qutip_gb300 import systems as S
+    from qutip_gb300.operator import DeviceOperator
+    from qutip_gb300.solver import ExpectOps, solve_system
+
+    dist.init()
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    sysm = S.ising_chain(N_SITES)
+    tlist = np.linspace(0.0, T_END, N_OUT)
+    op = DeviceOperator(sysm.terms, dtype="c128")
+    op.tune_lanes()
+    ex = ExpectOps(sysm.e_ops)
+
+    def solve(o=op, prec="double"):
+        return solve_system(sysm, tlist, {"precision": prec}, op=o, ex=ex)
+
+    for _ in range(args.warmup):
+        ref = solve()
+    dist.barrier()
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    n0 = _lib.LAUNCHES[0]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        res = solve()
+    e1.record()
+    dist.barrier()
+    ms = e0.elapsed_time(e1)
+    launches = (_lib.LAUNCHES[0] - n0) // max(args.steps, 1)
+    clk = clocks.stop()
+    ms_max = dist.max(ms)
+    value = args.steps * dist.world / (ms_max / 1000.0)
+
+    # end to end: operator + initial state from pinned host memory every step, expect read back
+    host = op.host_copy()
+    h2d = sum(h.numel() * h.element_size() for h in host) + sysm.state0.nbytes
+    d2h = N_OUT * 2 * (len(sysm.e_ops) + 1) * 8
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        op.upload(host)
+        solve()
+    dist.barrier()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e = args.steps * dist.world / e2e_s
+
+    # mixed-precision form: complex64 operator/stages, FP64 state and control
+    op64 = DeviceOperator(sysm.terms, dtype="c64")
+    op64.tune_lanes()
+    resm = solve(op64, "mixed")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        resm = solve(op64, "mixed")
+    torch.cuda.synchronize()
+    mixed_v = max(1, args.steps // 2) / (time.perf_counter() - t0)
+    err_m = max(float(np.max(np.abs(resm.expect[k] - res.expect[k]))) for k in range(N_SITES))
+
+    stage_ms, stage_b, stage_gbs = measure_stage_roofline(op, sysm, "double")
+    spmv_ms, spmv_b, spmv_gbs = measure_spmv(op)
+    spmv64_ms, spmv64_b, spmv64_gbs = measure_spmv(op64)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic (seeded h_i ~ U[0.5,1.5], default_rng(1234))",
+        "config": {**CONFIG, "parallelism": "replicas" if dist.world > 1 else "single",
+                   "lanes_per_row": op.lanes},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches * args.steps),
+        "roofline": {"bound": "hbm", "achieved": stage_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": stage_gbs / hbm_peak, "traffic": None,
+                     "kernel": "spmv_groups_kernel<C128,RK> (fused Vern7 stage)",
+                     "bytes_per_launch": stage_b, "ms_per_launch": stage_ms,
+                     "peak_source": f"{peak_src} hbm_gbs"},
+        "spmv": {"c128_gbs": spmv_gbs, "c128_ms": spmv_ms, "c128_bytes": spmv_b,
+                 "c64_gbs": spmv64_gbs, "c64_ms": spmv64_ms, "c64_bytes": spmv64_b,
+                 "frac_c128": spmv_gbs / hbm_peak, "frac_c64": spmv64_gbs / hbm_peak},
+        "mixed_precision": {"value": mixed_v, "unit": UNIT,
+                            "max_abs_err_vs_fp64_expect": err_m,
+                            "form": "complex64 operator+stages (FP32 accumulation), FP64 state, "
+                                    "stage combination, error control and expectations"},
+        "solver_stats": {k: res.stats[k] for k in ("steps", "rejected", "rhs")},
+        "clocks": clk,
+    }
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        try:
+            out["cpu_baseline"] = cpu_baseline(args.cpu_sample)
+        except Exception as exc:  # noqa: BLE001
+            out["cpu_baseline"] = {"value": None, "error": repr(exc)[:300]}
+    if dist.rank == 0:
+        print(json.dumps(out))
+    dist.close()
+
+
+def main():
+    args = parse()
+    dist = Dist(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, dist)
+    else:
+        run_ours(args, dist)
+
+
+if __name__ == "__main__":
+    main()

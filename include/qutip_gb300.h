@@ -1,0 +1,177 @@
+/*
+ * qutip_gb300 -- C ABI of the GB300 (sm_103a) time-evolution hot path.
+ *
+ * Every entry point takes plain device pointers, sizes and a cudaStream_t
+ * (passed as void*), returns 0 on success or a negative QG_ERR_* code, and never
+ * allocates or frees caller memory; qg_last_error() gives the message of the
+ * last failure on the calling thread.  Buffers are owned by the caller (the
+ * Python host layer keeps them in torch tensors).
+ *
+ * Each declaration names the reference function it replaces (paths relative to
+ * the QuTiP source tree).
+ */
+#ifndef QUTIP_GB300_H
+#define QUTIP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QG_OK 0
+#define QG_ERR_ARG (-1)         /* bad argument: shape, size or pointer (reference: ValueError) */
+#define QG_ERR_CUDA (-2)        /* CUDA runtime error */
+#define QG_ERR_UNSUPPORTED (-3) /* dtype / option not supported (reference: TypeError) */
+
+#define QG_MAX_GROUPS 8   /* coefficient groups (QobjEvo terms after merging) per operator */
+#define QG_MAX_EOPS 32    /* operators per expect launch */
+
+typedef enum { QG_C128 = 0, QG_C64 = 1 } qg_dtype;
+
+/* Integrator status codes, same values as Status in
+ * qutip/solver/integrator/explicit_rk.pxd:5-12. */
+typedef enum {
+  QG_AT_FRONT = 2,
+  QG_INTERPOLATED = 1,
+  QG_NORMAL = 0,
+  QG_TOO_MUCH_WORK = -1,
+  QG_DT_UNDERFLOW = -2,
+  QG_OUTSIDE_RANGE = -3,
+  QG_NOT_INITIATED = -4,
+  QG_NORM_SEARCH_FAILED = -5, /* jump-time search exhausted (qutip/solver/mcsolve.py:363-367) */
+  QG_TIMEOUT = -6             /* cancelled through the host-visible cancel flag */
+} qg_status;
+
+/* A sum of CSR matrices with time-dependent coefficients,
+ *   A(t) = sum_g c_g(t) A_g,
+ * the device form of a QobjEvo (qutip/core/cy/qobjevo.pyx:189-245) whose terms
+ * were merged per coefficient.  Group g's row r spans
+ * [row_ptr[g*(n_rows+1)+r], row_ptr[g*(n_rows+1)+r+1]) of col/val.
+ * Coefficient programs are the bytecode of qutip_gb300/coefficients.py;
+ * coef_code == NULL means every c_g = 1. */
+typedef struct qg_csr_groups {
+  int64_t n_rows;
+  int64_t n_cols;
+  int32_t n_groups;
+  int32_t dtype; /* qg_dtype of val */
+  const int32_t* row_ptr;
+  const int32_t* col;
+  const void* val;
+  const int32_t* coef_code;
+  const int32_t* coef_start; /* [n_groups+1] */
+  const double* coef_consts; /* complex constants as (re, im) pairs */
+} qg_csr_groups;
+
+/* Dia matrix in the reference's layout (qutip/core/data/dia.pxd:17-38):
+ * data[d * n_cols + col] is the entry (col - offsets[d], col). */
+typedef struct qg_dia {
+  int64_t n_rows;
+  int64_t n_cols;
+  int32_t n_diags;
+  int32_t dtype;
+  const int32_t* offsets;
+  const void* data;
+} qg_dia;
+
+/* Buffers of one explicit Runge-Kutta step.  The state (y_prev, y_front) may be
+ * complex128 while the stages (k, ytmp) are complex64: the mixed-precision form
+ * keeps the state and the error control in FP64. */
+typedef struct qg_rk_buffers {
+  int64_t n;
+  int32_t state_dtype;
+  int32_t stage_dtype;
+  const void* y_prev;    /* [n] state_dtype */
+  void* y_front;         /* [n] state_dtype */
+  void* k;               /* [16 * n] stage_dtype, k_j at k + j*n */
+  void* ytmp;            /* [2 * n] stage_dtype, stage inputs (ping-pong) */
+  double* scratch;       /* [qg_scratch_doubles()] per-block partial sums */
+  unsigned int* counter; /* one word, zero before the first launch; left zero */
+  double* result;        /* one double: WRMS error of the step */
+} qg_rk_buffers;
+
+/* A state given lazily as base + sum_j f_j k_j (an interpolated Runge-Kutta
+ * output, qutip/solver/integrator/explicit_rk.pyx:412-430); n_k = 0 means base. */
+typedef struct qg_state_view {
+  int64_t n;
+  int32_t base_dtype;
+  int32_t k_dtype;
+  const void* base;
+  const void* k; /* k_j at k + j*n */
+  int32_t n_k;
+  int32_t pad_;
+  double f[16];
+} qg_state_view;
+
+/* ---- library ---------------------------------------------------------- */
+int qg_version(void);
+const char* qg_last_error(void);
+/* Number of doubles the scratch buffer of qg_rk_buffers / reductions needs. */
+int64_t qg_scratch_doubles(void);
+/* Copy the compiled-in Vern7 tableau (host memory, no GPU needed):
+ * a[16*16], b[10], c[16], e[10], bi[16*7]; replaces
+ * qutip/solver/integrator/verner7efficient.py:10-333. */
+int qg_vern7_tableau(double* a, double* b, double* c, double* e, double* bi);
+
+/* ---- matvec ------------------------------------------------------------- */
+/* y = alpha * sum_g c_g(t) A_g x + beta * y, vectors in A->dtype, FP64
+ * accumulation for complex128 and FP32 for complex64.  lanes = threads per row
+ * (1..32, power of two).  Replaces _matmul_csr_vector
+ * (qutip/core/data/src/matmul_csr_vector.cpp:17-54, scalar form :107-149) as
+ * driven by QobjEvo.matmul_data (qutip/core/cy/qobjevo.pyx:1103-1116) and
+ * matmul_csr_dense_dense (qutip/core/data/matmul.pyx:226-272). */
+int qg_spmv_csr(const qg_csr_groups* A, double t, const void* x, void* y, double alpha_re,
+                double alpha_im, double beta_re, double beta_im, int lanes, void* stream);
+
+/* Y = alpha * A(t) X + beta * Y for n_vec column vectors stored with leading
+ * dimension ld (F order): one operator read serves all columns.  Replaces the
+ * per-column loop of matmul_csr_dense_dense (qutip/core/data/matmul.pyx:255-270)
+ * and _matmul_csr_dense_c_order (qutip/core/data/src/matmul_csr_dense.cpp:20-70). */
+int qg_spmm_csr(const qg_csr_groups* A, double t, const void* X, void* Y, int64_t n_vec,
+                int64_t ld, double alpha_re, double alpha_im, double beta_re, double beta_im,
+                void* stream);
+
+/* y = alpha * A x + beta * y for a Dia matrix.  Replaces matmul_dia_dense_dense
+ * (qutip/core/data/matmul.pyx:429-507) and _matmul_diag_vector
+ * (qutip/core/data/src/matmul_diag_vector.cpp:13-39). */
+int qg_spmv_dia(const qg_dia* A, const void* x, void* y, double alpha_re, double alpha_im,
+                double beta_re, double beta_im, void* stream);
+
+/* ---- Vern7 step ----------------------------------------------------------- */
+/* One Runge-Kutta stage fused with the next stage's combination:
+ *   k_s = A(t_prev + c_s dt) x_s,  x_0 = y_prev,  x_s = ytmp[s & 1];
+ *   s in 0..8, 10..14:  ytmp[(s+1) & 1] = y_prev + sum_{j<=s} (dt a[s+1][j]) k_j
+ *   s == 9:  y_front = y_prev + sum_j (dt b_j) k_j and
+ *            result = sqrt(mean((|sum_j dt e_j k_j| / (atol + rtol |y_front|))^2))
+ * Replaces _compute_step / _accumulate / _error / _prep_dense_out
+ * (qutip/solver/integrator/explicit_rk.pyx:358-410) with wrmn_error_dense
+ * (qutip/core/data/ode.pyx:27-52) and iadd_dense (qutip/core/data/add.pyx:203-219). */
+int qg_vern7_stage(const qg_csr_groups* A, const qg_rk_buffers* B, int stage, double t_prev,
+                   double dt, double atol, double rtol, int lanes, void* stream);
+
+/* out = base + sum_{j<n_k} f_j k_j (out in out_dtype).  Replaces _accumulate
+ * and _interpolate_step (qutip/solver/integrator/explicit_rk.pyx:412-437). */
+int qg_rk_combine(const qg_state_view* v, void* out, int out_dtype, void* stream);
+
+/* *result = sum |x_i|^2 in FP64 (deterministic two-level reduction through
+ * scratch/counter).  Replaces frobenius_dense / l2 (qutip/core/data/norm.pyx:127-135). */
+int qg_norm2(const void* x, int dtype, int64_t n, double* scratch, unsigned int* counter,
+             double* result, void* stream);
+
+/* ---- expectation values --------------------------------------------------- */
+/* For a column-stacked density matrix rho (d x d) given by a state view:
+ * out[2g], out[2g+1] = tr(op_g rho) for each group g of ops (each group is one
+ * d x d operator, coefficients ignored) and out[2G], out[2G+1] = tr(rho), FP64.
+ * Replaces _expect_csr_dense_dm (qutip/core/data/expect.pyx:146-158) and
+ * expect_super_csr_dense (:223-236) as used by Result.add for e_ops. */
+int qg_expect_dm(const qg_csr_groups* ops, int64_t d, const qg_state_view* rho, double* out,
+                 void* stream);
+
+/* out[2g..] = <psi|op_g|psi>, out[2G..] = <psi|psi>.  Replaces
+ * _expect_csr_dense_ket (qutip/core/data/expect.pyx:133-144). */
+int qg_expect_ket(const qg_csr_groups* ops, const qg_state_view* psi, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QUTIP_GB300_H */

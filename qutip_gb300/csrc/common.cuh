@@ -1,0 +1,212 @@
+// Shared device helpers: complex arithmetic on double2/float2, cache-hinted
+// loads, block reductions in FP64 and the coefficient interpreter.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "qutip_gb300.h"
+#include "vern7_tableau.cuh"  // generated from qutip_gb300/vern7_tableau.py
+
+namespace qg {
+
+// ---------------------------------------------------------------- complex --
+struct cplx {
+  double re, im;
+};
+
+__device__ __forceinline__ cplx cmake(double r, double i) { return cplx{r, i}; }
+__device__ __forceinline__ cplx cadd(cplx a, cplx b) { return cplx{a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ cplx csub(cplx a, cplx b) { return cplx{a.re - b.re, a.im - b.im}; }
+__device__ __forceinline__ cplx cmul(cplx a, cplx b) {
+  return cplx{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+__device__ __forceinline__ cplx cscale(cplx a, double s) { return cplx{a.re * s, a.im * s}; }
+__device__ __forceinline__ double cabs2(cplx a) { return a.re * a.re + a.im * a.im; }
+
+// Storage element types.  C128 = double2 (16 B), C64 = float2 (8 B).
+template <int DT>
+struct elem;
+template <>
+struct elem<QG_C128> {
+  using T = double2;
+  using R = double;  // accumulation type of the matvec
+};
+template <>
+struct elem<QG_C64> {
+  using T = float2;
+  using R = float;
+};
+
+__device__ __forceinline__ cplx to_c(double2 v) { return cplx{v.x, v.y}; }
+__device__ __forceinline__ cplx to_c(float2 v) { return cplx{(double)v.x, (double)v.y}; }
+template <typename T>
+__device__ __forceinline__ T from_c(cplx v);
+template <>
+__device__ __forceinline__ double2 from_c<double2>(cplx v) { return make_double2(v.re, v.im); }
+template <>
+__device__ __forceinline__ float2 from_c<float2>(cplx v) {
+  return make_float2((float)v.re, (float)v.im);
+}
+
+// Streaming (read-once) loads for operator values and indices: evict-first so
+// that the gathered vector keeps its L2 residency.
+__device__ __forceinline__ double2 ld_stream(const double2* p) { return __ldcs(p); }
+__device__ __forceinline__ float2 ld_stream(const float2* p) { return __ldcs(p); }
+__device__ __forceinline__ int ld_stream(const int* p) { return __ldcs(p); }
+// Gathered vector: read-only path.
+__device__ __forceinline__ double2 ld_gather(const double2* p) { return __ldg(p); }
+__device__ __forceinline__ float2 ld_gather(const float2* p) { return __ldg(p); }
+
+// ------------------------------------------------------------ reductions --
+// Sum a double over the block; result valid in thread 0.  Fixed order, so the
+// result is reproducible for a fixed launch shape.
+template <int BLOCK>
+__device__ __forceinline__ double block_sum(double v, double* smem /* [BLOCK/32] */) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) smem[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = (threadIdx.x < BLOCK / 32) ? smem[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  __syncthreads();
+  return r;
+}
+
+// ---------------------------------------------------- coefficient programs --
+// Opcodes shared with qutip_gb300/coefficients.py (OPCODES).
+enum : int {
+  OP_END = 0, OP_CONST = 1, OP_T = 2, OP_ADD = 3, OP_SUB = 4, OP_MUL = 5, OP_DIV = 6,
+  OP_NEG = 7, OP_COS = 8, OP_SIN = 9, OP_EXP = 10, OP_LOG = 11, OP_SQRT = 12, OP_CONJ = 13,
+  OP_REAL = 14, OP_IMAG = 15, OP_ABS = 16, OP_POW = 17, OP_COSH = 18, OP_SINH = 19,
+  OP_TANH = 20, OP_TAN = 21, OP_ARCTAN = 22
+};
+constexpr int COEF_STACK = 16;
+
+__device__ __forceinline__ cplx c_exp(cplx z) {
+  double e = exp(z.re);
+  if (z.im == 0.0) return cplx{e, 0.0};
+  double s, c;
+  sincos(z.im, &s, &c);
+  return cplx{e * c, e * s};
+}
+__device__ __forceinline__ cplx c_log(cplx z) {
+  return cplx{log(hypot(z.re, z.im)), atan2(z.im, z.re)};
+}
+__device__ __forceinline__ cplx c_div(cplx a, cplx b) {
+  if (b.im == 0.0) return cplx{a.re / b.re, a.im / b.re};
+  double d = b.re * b.re + b.im * b.im;
+  return cplx{(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
+}
+__device__ __forceinline__ cplx c_sqrt(cplx z) {
+  if (z.im == 0.0) {
+    if (z.re >= 0.0) return cplx{sqrt(z.re), 0.0};
+    return cplx{0.0, sqrt(-z.re)};
+  }
+  // principal branch: sqrt(z) = sqrt((|z|+x)/2) + i sign(y) sqrt((|z|-x)/2)
+  double m = hypot(z.re, z.im);
+  double r = sqrt(0.5 * (m + z.re));
+  double i = sqrt(0.5 * (m - z.re));
+  return cplx{r, copysign(i, z.im)};
+}
+__device__ __forceinline__ cplx c_cos(cplx z) {
+  if (z.im == 0.0) return cplx{cos(z.re), 0.0};
+  return cplx{cos(z.re) * cosh(z.im), -sin(z.re) * sinh(z.im)};
+}
+__device__ __forceinline__ cplx c_sin(cplx z) {
+  if (z.im == 0.0) return cplx{sin(z.re), 0.0};
+  return cplx{sin(z.re) * cosh(z.im), cos(z.re) * sinh(z.im)};
+}
+__device__ __forceinline__ cplx c_cosh(cplx z) {
+  if (z.im == 0.0) return cplx{cosh(z.re), 0.0};
+  return cplx{cosh(z.re) * cos(z.im), sinh(z.re) * sin(z.im)};
+}
+__device__ __forceinline__ cplx c_sinh(cplx z) {
+  if (z.im == 0.0) return cplx{sinh(z.re), 0.0};
+  return cplx{sinh(z.re) * cos(z.im), cosh(z.re) * sin(z.im)};
+}
+
+// Evaluate one program at time t.  Programs are validated on the host (stack
+// depth <= COEF_STACK); the interpreter additionally clamps the stack index so a
+// malformed program cannot write outside its frame.
+__device__ inline cplx eval_coef(const int* code, const double* consts, double t) {
+  cplx st[COEF_STACK];
+  int sp = 0;
+  for (int pc = 0; pc < 4096; ++pc) {
+    int op = code[pc];
+    if (op == OP_END) break;
+    if (op == OP_CONST) {
+      int k = code[++pc];
+      if (sp < COEF_STACK) st[sp++] = cplx{consts[2 * k], consts[2 * k + 1]};
+      continue;
+    }
+    if (op == OP_T) {
+      if (sp < COEF_STACK) st[sp++] = cplx{t, 0.0};
+      continue;
+    }
+    if (sp < 1) return cplx{0.0, 0.0};
+    cplx a = st[sp - 1];
+    switch (op) {
+      case OP_NEG: st[sp - 1] = cplx{-a.re, -a.im}; continue;
+      case OP_COS: st[sp - 1] = c_cos(a); continue;
+      case OP_SIN: st[sp - 1] = c_sin(a); continue;
+      case OP_EXP: st[sp - 1] = c_exp(a); continue;
+      case OP_LOG: st[sp - 1] = c_log(a); continue;
+      case OP_SQRT: st[sp - 1] = c_sqrt(a); continue;
+      case OP_CONJ: st[sp - 1] = cplx{a.re, -a.im}; continue;
+      case OP_REAL: st[sp - 1] = cplx{a.re, 0.0}; continue;
+      case OP_IMAG: st[sp - 1] = cplx{a.im, 0.0}; continue;
+      case OP_ABS: st[sp - 1] = cplx{hypot(a.re, a.im), 0.0}; continue;
+      case OP_COSH: st[sp - 1] = c_cosh(a); continue;
+      case OP_SINH: st[sp - 1] = c_sinh(a); continue;
+      case OP_TANH: st[sp - 1] = c_div(c_sinh(a), c_cosh(a)); continue;
+      case OP_TAN: st[sp - 1] = c_div(c_sin(a), c_cos(a)); continue;
+      case OP_ARCTAN:
+        if (a.im == 0.0) {
+          st[sp - 1] = cplx{atan(a.re), 0.0};
+        } else {  // atan(z) = i/2 [log(1 - iz) - log(1 + iz)]
+          cplx l1 = c_log(cplx{1.0 + a.im, -a.re});
+          cplx l2 = c_log(cplx{1.0 - a.im, a.re});
+          cplx d = csub(l1, l2);
+          st[sp - 1] = cplx{-0.5 * d.im, 0.5 * d.re};
+        }
+        continue;
+      default: break;
+    }
+    if (sp < 2) return cplx{0.0, 0.0};
+    cplx b = st[sp - 1];
+    a = st[sp - 2];
+    cplx r;
+    switch (op) {
+      case OP_ADD: r = cadd(a, b); break;
+      case OP_SUB: r = csub(a, b); break;
+      case OP_MUL: r = cmul(a, b); break;
+      case OP_DIV: r = c_div(a, b); break;
+      case OP_POW:
+        if (a.im == 0.0 && b.im == 0.0 && (a.re > 0.0 || b.re == floor(b.re))) {
+          r = cplx{pow(a.re, b.re), 0.0};
+        } else if (a.re == 0.0 && a.im == 0.0) {
+          r = cplx{0.0, 0.0};
+        } else {
+          r = c_exp(cmul(b, c_log(a)));
+        }
+        break;
+      default: return cplx{0.0, 0.0};
+    }
+    st[sp - 2] = r;
+    --sp;
+  }
+  return sp > 0 ? st[sp - 1] : cplx{0.0, 0.0};
+}
+
+// Coefficient of group g at time t; a NULL program table means all ones.
+__device__ __forceinline__ cplx group_coef(const qg_csr_groups& A, int g, double t) {
+  if (A.coef_code == nullptr) return cplx{1.0, 0.0};
+  return eval_coef(A.coef_code + A.coef_start[g], A.coef_consts, t);
+}
+
+}  // namespace qg

@@ -1,0 +1,152 @@
+"""GPU kernels through the C ABI against the CPU oracle and the reference's golden vectors."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch.device("cuda")
+
+
+def _t(a, dtype=torch.complex128):
+    return torch.from_numpy(np.ascontiguousarray(a)).to("cuda", dtype)
+
+
+@pytest.mark.parametrize("i", [0, 1, 2])
+@pytest.mark.parametrize("lanes", [2, 4, 8, 16, 32])
+def test_spmv_c128_matches_reference(dev, i, lanes):
+    from qutip_gb300.operator import DeviceOperator
+    g = golden("kernels.npz")
+    n = len(g[f"spmv{i}_x"])
+    A = sp.csr_matrix((g[f"spmv{i}_data"], g[f"spmv{i}_indices"], g[f"spmv{i}_indptr"]), shape=(n, n))
+    op = DeviceOperator([(A, None)])
+    y = _t(g[f"spmv{i}_out0"])
+    op.matvec(0.0, _t(g[f"spmv{i}_x"]), y, alpha=0.5j, beta=1.0, lanes=lanes)
+    np.testing.assert_allclose(y.cpu().numpy(), g[f"spmv{i}_res"], rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("i", [0, 1, 2])
+def test_spmv_c64_error_bound(dev, i):
+    from oracle.kernels import spmv_csr
+    from qutip_gb300.operator import DeviceOperator
+    g = golden("kernels.npz")
+    n = len(g[f"spmv{i}_x"])
+    A = sp.csr_matrix((g[f"spmv{i}_data"], g[f"spmv{i}_indices"], g[f"spmv{i}_indptr"]), shape=(n, n))
+    op = DeviceOperator([(A, None)], dtype="c64")
+    x = g[f"spmv{i}_x"]
+    y = torch.zeros(n, dtype=torch.complex64, device="cuda")
+    op.matvec(0.0, _t(x, torch.complex64), y)
+    want = spmv_csr(A.data, A.indices, A.indptr, x)
+    # FP32 accumulation: |err| <= ~nnz_row * eps32 * sum|a||x|
+    bound = 8 * np.finfo(np.float32).eps * (abs(A) @ np.abs(x)) + 1e-30
+    assert np.all(np.abs(y.cpu().numpy() - want) <= bound)
+
+
+def test_grouped_coefficients_match_scipy(dev):
+    from qutip_gb300 import systems as S
+    from qutip_gb300.operator import DeviceOperator
+    s = S.ising_chain(4)
+    op = DeviceOperator(s.terms)
+    assert op.n_groups == 2
+    rng = np.random.default_rng(3)
+    x = rng.normal(size=op.n_cols) + 1j * rng.normal(size=op.n_cols)
+    for t in (0.0, 0.37, 5.1):
+        y = torch.zeros(op.n_rows, dtype=torch.complex128, device="cuda")
+        op.matvec(t, _t(x), y)
+        want = sum((m * (1 if c is None else c(t))) @ x for m, c in s.terms)
+        np.testing.assert_allclose(y.cpu().numpy(), want, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("expr,args", [("cos(w*t)", {"w": 1.3}),
+                                       ("exp(-1j*w*t)*sqrt(t+1)", {"w": 2.0}),
+                                       ("tanh(t-2)+arctan(t)-log(t+2)", {}),
+                                       ("conj(exp(1j*t))**2/(1+t)", {})])
+def test_device_coefficient_interpreter(dev, expr, args):
+    from qutip_gb300.coefficients import coefficient
+    from qutip_gb300.operator import DeviceOperator
+    c = coefficient(expr, args)
+    op = DeviceOperator([(sp.identity(1, format="csr"), c)])
+    x = _t(np.ones(1))
+    for t in (0.0, 0.37, 3.3):
+        y = torch.zeros(1, dtype=torch.complex128, device="cuda")
+        op.matvec(t, x, y)
+        assert abs(complex(y.cpu().numpy()[0]) - c(t)) <= 1e-13 * max(1.0, abs(c(t)))
+
+
+@pytest.mark.parametrize("i", [0, 1, 2])
+def test_dia_matches_reference(dev, i):
+    from qutip_gb300.operator import DeviceDia
+    g = golden("kernels.npz")
+    n = len(g[f"spmv{i}_x"])
+    m = sp.dia_matrix((g[f"dia{i}_data"], g[f"dia{i}_offsets"]), shape=(n, n))
+    op = DeviceDia(m)
+    y = torch.zeros(n, dtype=torch.complex128, device="cuda")
+    op.matvec(_t(g[f"spmv{i}_x"]), y)
+    np.testing.assert_allclose(y.cpu().numpy(), g[f"dia{i}_res"], rtol=1e-13, atol=1e-13)
+
+
+def test_spmm_matches_columnwise(dev):
+    from qutip_gb300.operator import DeviceOperator
+    g = golden("kernels.npz")
+    n = len(g["spmv1_x"])
+    A = sp.csr_matrix((g["spmv1_data"], g["spmv1_indices"], g["spmv1_indptr"]), shape=(n, n))
+    op = DeviceOperator([(A, None)])
+    rng = np.random.default_rng(0)
+    X = rng.normal(size=(7, n)) + 1j * rng.normal(size=(7, n))
+    Y = torch.zeros((7, n), dtype=torch.complex128, device="cuda")
+    op.matmat(0.0, _t(X), Y)
+    np.testing.assert_allclose(Y.cpu().numpy(), (A @ X.T).T, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("i", [0, 1])
+def test_expect_dm_and_ket_match_reference(dev, i):
+    from qutip_gb300 import _lib
+    from qutip_gb300.solver import ExpectOps
+    g = golden("kernels.npz")
+    n = len(g[f"spmv{i}_x"])
+    A = sp.csr_matrix((g[f"spmv{i}_data"], g[f"spmv{i}_indices"], g[f"spmv{i}_indptr"]), shape=(n, n))
+    ex = ExpectOps([A, sp.identity(n)])
+    rho = _t(g[f"exp{i}_rho"])
+    out = torch.zeros(6, dtype=torch.float64, device="cuda")
+    f = (C.c_double * 16)()
+    v = _lib.StateView(n * n, 0, 0, rho.data_ptr(), rho.data_ptr(), 0, 0, f)
+    ex.expect_dm(n, v, out)
+    o = out.cpu().numpy()
+    np.testing.assert_allclose(o[0] + 1j * o[1], g[f"exp{i}_dm"], rtol=1e-12)
+    np.testing.assert_allclose(o[4] + 1j * o[5], np.trace(g[f"exp{i}_rho"].reshape(n, n, order="F")),
+                               rtol=1e-12)
+    psi = _t(g[f"spmv{i}_x"])
+    v = _lib.StateView(n, 0, 0, psi.data_ptr(), psi.data_ptr(), 0, 0, f)
+    ex.expect_ket(v, out)
+    o = out.cpu().numpy()
+    np.testing.assert_allclose(o[0] + 1j * o[1], g[f"exp{i}_ket"], rtol=1e-12)
+    np.testing.assert_allclose(o[4], np.vdot(g[f"spmv{i}_x"], g[f"spmv{i}_x"]).real, rtol=1e-12)
+
+
+def test_norm2_and_combine(dev):
+    from qutip_gb300.operator import DeviceOperator
+    from qutip_gb300.vern7 import GpuVern7
+    n = 1000
+    op = DeviceOperator([(sp.identity(n, format="csr"), None)])
+    ig = GpuVern7(op)
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    assert abs(ig._norm(_t(x)) - np.linalg.norm(x)) < 1e-12 * np.linalg.norm(x)
+    ks = rng.normal(size=(16, n)) + 1j * rng.normal(size=(16, n))
+    ig.k.copy_(_t(ks.reshape(-1)))
+    f = rng.normal(size=16)
+    f[3] = 0.0
+    out = torch.zeros(n, dtype=torch.complex128, device="cuda")
+    ig._combine(_t(x), list(f), out)
+    np.testing.assert_allclose(out.cpu().numpy(), x + f @ ks, rtol=1e-13, atol=1e-13)

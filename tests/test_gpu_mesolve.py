@@ -1,0 +1,122 @@
+"""GPU mesolve (Vern7 on the device) against the reference's own mesolve results.
+
+Tolerances: complex128 results must agree with the reference within
+atol 1e-8 / rtol 1e-6 on expectation values; the mixed (complex64 stages, FP64
+state and control) and single forms state their error against the FP64 result.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, csr_from, golden
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+ATOL, RTOL = 1e-8, 1e-6
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _close(got, want, atol=ATOL, rtol=RTOL):
+    got, want = np.asarray(got), np.asarray(want)
+    assert np.all(np.abs(got - want) <= atol + rtol * np.abs(want)), np.abs(got - want).max()
+
+
+def test_jc_mesolve_double_matches_reference():
+    from qutip_gb300 import systems as S
+    from qutip_gb300.solver import solve_system
+    g = golden("jc_mesolve.npz")
+    s = S.jaynes_cummings()
+    res = solve_system(s, g["tlist"], {"store_final_state": True})
+    for k in range(2):
+        _close(res.expect[k].real, g["expect"][k])
+    _close(res.final_state, g["final"], atol=1e-8)
+    assert res.stats["steps"] >= len(g["step_ends"])
+
+
+def test_jc_step_sequence_is_the_reference():
+    from qutip_gb300 import systems as S
+    from qutip_gb300.operator import DeviceOperator
+    from qutip_gb300.vern7 import GpuVern7
+    g = golden("jc_mesolve.npz")
+    s = S.jaynes_cummings()
+    ig = GpuVern7(DeviceOperator(s.terms))
+    ig.set_initial_value(torch.from_numpy(g["rho0"]).cuda(), 0.0)
+    ends = []
+    while ig.t_front < 20.0:
+        ig.integrate(20.0, step=True)
+        ig.check()
+        ends.append(ig.t_front)
+    assert len(ends) == len(g["step_ends"])
+    np.testing.assert_allclose(ends, g["step_ends"], rtol=1e-8)
+
+
+@pytest.mark.parametrize("L", [3, 4])
+def test_ising_td_mesolve_double_matches_reference(L):
+    from qutip_gb300 import systems as S
+    from qutip_gb300.solver import solve_system
+    g = golden(f"ising_L{L}_mesolve.npz")
+    s = S.ising_chain(L)
+    res = solve_system(s, g["tlist"], {"store_final_state": True})
+    for k in range(L):
+        _close(res.expect[k].real, g["expect"][k])
+    _close(res.final_state, g["final"])
+
+
+@pytest.mark.parametrize("prec,bound", [("mixed", 2e-6), ("single", 2e-5)])
+def test_ising_reduced_precision_error_vs_fp64(prec, bound):
+    from qutip_gb300 import systems as S
+    from qutip_gb300.solver import solve_system
+    g = golden("ising_L4_mesolve.npz")
+    s = S.ising_chain(4)
+    res = solve_system(s, g["tlist"], {"precision": prec})
+    err = max(np.abs(res.expect[k].real - g["expect"][k]).max() for k in range(4))
+    print(f"\n{prec}: max |<sz_i> - FP64 reference| = {err:.3e}")
+    assert err < bound
+
+
+def test_too_much_work_raises_like_reference():
+    from qutip_gb300 import systems as S
+    from qutip_gb300.solver import solve_system
+    from qutip_gb300.vern7 import IntegratorError
+    s = S.jaynes_cummings()
+    with pytest.raises(IntegratorError, match="Too much work"):
+        solve_system(s, np.linspace(0, 20, 3), {"nsteps": 2})
+
+
+def test_mesolve_api_with_string_coefficient():
+    from qutip_gb300 import systems as S
+    from qutip_gb300.solver import mesolve
+    from oracle.solvers import mesolve as omesolve
+    L = 3
+    s = S.ising_chain(L)
+    (h0, _), (h1, _) = s.h_terms
+    tl = np.linspace(0, 2, 11)
+    psi0 = np.zeros(2 ** L)
+    psi0[0] = 1
+    res = mesolve([h0, [h1, "cos(w*t)"]], psi0, tl, s.c_ops, s.e_ops, args={"w": 1.3})
+    want, _ = omesolve(s.terms, s.state0, tl, s.e_ops)
+    for k in range(L):
+        _close(res.expect[k], want[k])
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(GOLDEN, "ising_L10_expect.npz")),
+                    reason="full-size golden not generated")
+def test_ising_L10_full_size_matches_reference():
+    from qutip_gb300 import systems as S
+    from qutip_gb300.solver import solve_system
+    g = golden("ising_L10_expect.npz")
+    s = S.ising_chain(10)
+    res = solve_system(s, g["tlist"])
+    for k in range(10):
+        _close(res.expect[k].real, g["expect"][k])
+    resm = solve_system(s, g["tlist"], {"precision": "mixed"})
+    err = max(np.abs(resm.expect[k].real - g["expect"][k]).max() for k in range(10))
+    print(f"\nIsing L=10 mixed: max |<sz_i> - FP64 reference| = {err:.3e}")
+    assert err < 1e-5

@@ -1,0 +1,74 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports every
+declared symbol, the compiled-in tableau is the reference's, coefficients compile."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+
+from qutip_gb300 import coefficients as CF
+
+
+def _header_functions():
+    src = open(os.path.join(ROOT, "include", "qutip_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(qg_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    from qutip_gb300 import _lib
+    lib = _lib.load()
+    declared = _header_functions()
+    assert len(declared) >= 10
+    for name in declared:
+        assert hasattr(lib, name), f"{name} declared in include/qutip_gb300.h but not exported"
+    assert set(_lib.declared_symbols()) <= set(declared)
+    assert lib.qg_version() >= 1
+
+
+def test_compiled_tableau_matches_reference():
+    import ctypes as C
+    from qutip_gb300 import _lib
+    g = golden("vern7_tableau.npz")
+    a, b, c, e, bi = (np.zeros(256), np.zeros(10), np.zeros(16), np.zeros(10), np.zeros(112))
+    rc = _lib.load().qg_vern7_tableau(*(x.ctypes.data_as(C.c_void_p) for x in (a, b, c, e, bi)))
+    assert rc == 0
+    assert np.array_equal(a.reshape(16, 16), g["a"])
+    assert np.array_equal(b, g["b"]) and np.array_equal(c, g["c"]) and np.array_equal(e, g["e"])
+    assert np.array_equal(bi.reshape(16, 7), g["bi"])
+
+
+@pytest.mark.parametrize("expr,args", [
+    ("cos(w*t)", {"w": 1.3}),
+    ("exp(-1j*w*t) + 0.5*sin(t)**2", {"w": 2.0}),
+    ("sqrt(t+1)*conj(exp(1j*t))/(1+t)", {}),
+    ("np.cos(2*np.pi*f*t) - a", {"f": 0.3, "a": 0.1}),
+    ("tanh(t-2) + arctan(t) - log(t + 2) + abs(-t) + real(1j*t+3)", {}),
+])
+def test_coefficient_programs(expr, args):
+    c = CF.coefficient(expr, args)
+    ns = {"cos": np.cos, "sin": np.sin, "exp": np.exp, "sqrt": np.sqrt, "conj": np.conj,
+          "np": np, "tanh": np.tanh, "arctan": np.arctan, "log": np.log, "abs": np.abs,
+          "real": np.real, **args}
+    for t in (0.0, 0.37, 2.5, 9.9):
+        want = complex(eval(expr, ns, {"t": t}))
+        assert abs(c(t) - want) <= 1e-12 * max(1.0, abs(want))
+    assert (c.conj()(0.7)) == c(0.7).conjugate()
+    assert abs((c + 2.0)(0.7) - (c(0.7) + 2.0)) < 1e-15
+
+
+def test_coefficient_rejects_unknown_names():
+    with pytest.raises(ValueError):
+        CF.coefficient("cos(w*t)")
+    with pytest.raises(ValueError):
+        CF.coefficient("__import__('os')")
+    with pytest.raises(TypeError):
+        CF.coefficient(lambda t: t)
+
+
+def test_pack_programs_layout():
+    code, starts, consts = CF.pack_programs([None, CF.coefficient("cos(w*t)", {"w": 2.0})])
+    assert starts[0] == 0 and starts[-1] == len(code)
+    assert code[starts[1] - 1] == CF.OPCODES["END"]
+    assert consts.dtype == np.float64 and len(consts) % 2 == 0
