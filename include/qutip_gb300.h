@@ -46,18 +46,35 @@ typedef enum {
 /* A sum of CSR matrices with time-dependent coefficients,
  *   A(t) = sum_g c_g(t) A_g,
  * the device form of a QobjEvo (qutip/core/cy/qobjevo.pyx:189-245) whose terms
- * were merged per coefficient.  Group g's row r spans
- * [row_ptr[g*(n_rows+1)+r], row_ptr[g*(n_rows+1)+r+1]) of col/val.
+ * were merged per coefficient.  Two layouts of the row pointers:
+ *   QG_LAYOUT_GROUP_MAJOR: group g's row r spans
+ *       [row_ptr[g*(n_rows+1)+r], row_ptr[g*(n_rows+1)+r+1]) of col/val;
+ *   QG_LAYOUT_ROW_MAJOR: the entries of row r are stored contiguously, group by
+ *       group: group g of row r spans [row_ptr[r*G+g], row_ptr[r*G+g+1]) and
+ *       row_ptr[n_rows*G] is the number of entries.
+ * Launch shape: lanes = threads per row (power of two, 1..32).  n_tiles > 0
+ * selects the shared-memory staged kernel (ROW_MAJOR only): tile t covers rows
+ * [tile_row[t], tile_row[t+1]) holding at most tile_nnz - 8 entries and at most
+ * QG_TILE_ROWS rows; col, val and row_ptr must then be readable for 8 entries
+ * past their end (bulk copies are rounded to 16-byte units).
  * Coefficient programs are the bytecode of qutip_gb300/coefficients.py;
  * coef_code == NULL means every c_g = 1. */
+#define QG_LAYOUT_GROUP_MAJOR 0
+#define QG_LAYOUT_ROW_MAJOR 1
+#define QG_TILE_ROWS 512
 typedef struct qg_csr_groups {
   int64_t n_rows;
   int64_t n_cols;
   int32_t n_groups;
   int32_t dtype; /* qg_dtype of val */
+  int32_t layout;
+  int32_t lanes;
+  int32_t n_tiles;
+  int32_t tile_nnz; /* 2048 or 4096 */
   const int32_t* row_ptr;
   const int32_t* col;
   const void* val;
+  const int32_t* tile_row;
   const int32_t* coef_code;
   const int32_t* coef_start; /* [n_groups+1] */
   const double* coef_consts; /* complex constants as (re, im) pairs */
@@ -75,14 +92,19 @@ typedef struct qg_dia {
 } qg_dia;
 
 /* Buffers of one explicit Runge-Kutta step.  The state (y_prev, y_front) may be
- * complex128 while the stages (k, ytmp) are complex64: the mixed-precision form
- * keeps the state and the error control in FP64. */
+ * complex128 while the stages (k, ytmp) are complex64 ("mixed" form): the
+ * state update of each accepted step and the error norm stay in FP64, the stage
+ * combinations run in FP32 from y_prev_s, a complex64 copy of y_prev that stage 9
+ * refreshes (y_front_s) together with y_front.  When state and stages share a
+ * dtype, y_prev_s / y_front_s are unused (may be NULL). */
 typedef struct qg_rk_buffers {
   int64_t n;
   int32_t state_dtype;
   int32_t stage_dtype;
   const void* y_prev;    /* [n] state_dtype */
   void* y_front;         /* [n] state_dtype */
+  const void* y_prev_s;  /* [n] stage_dtype, mixed form only */
+  void* y_front_s;       /* [n] stage_dtype, mixed form only */
   void* k;               /* [16 * n] stage_dtype, k_j at k + j*n */
   void* ytmp;            /* [2 * n] stage_dtype, stage inputs (ping-pong) */
   double* scratch;       /* [qg_scratch_doubles()] per-block partial sums */
@@ -115,13 +137,12 @@ int qg_vern7_tableau(double* a, double* b, double* c, double* e, double* bi);
 
 /* ---- matvec ------------------------------------------------------------- */
 /* y = alpha * sum_g c_g(t) A_g x + beta * y, vectors in A->dtype, FP64
- * accumulation for complex128 and FP32 for complex64.  lanes = threads per row
- * (1..32, power of two).  Replaces _matmul_csr_vector
+ * accumulation for complex128 and FP32 for complex64.  Replaces _matmul_csr_vector
  * (qutip/core/data/src/matmul_csr_vector.cpp:17-54, scalar form :107-149) as
  * driven by QobjEvo.matmul_data (qutip/core/cy/qobjevo.pyx:1103-1116) and
  * matmul_csr_dense_dense (qutip/core/data/matmul.pyx:226-272). */
 int qg_spmv_csr(const qg_csr_groups* A, double t, const void* x, void* y, double alpha_re,
-                double alpha_im, double beta_re, double beta_im, int lanes, void* stream);
+                double alpha_im, double beta_re, double beta_im, void* stream);
 
 /* Y = alpha * A(t) X + beta * Y for n_vec column vectors stored with leading
  * dimension ld (F order): one operator read serves all columns.  Replaces the
@@ -139,7 +160,8 @@ int qg_spmv_dia(const qg_dia* A, const void* x, void* y, double alpha_re, double
 
 /* ---- Vern7 step ----------------------------------------------------------- */
 /* One Runge-Kutta stage fused with the next stage's combination:
- *   k_s = A(t_prev + c_s dt) x_s,  x_0 = y_prev,  x_s = ytmp[s & 1];
+ *   k_s = A(t_prev + c_s dt) x_s,  x_0 = y_prev (y_prev_s in the mixed form),
+ *   x_s = ytmp[s & 1];
  *   s in 0..8, 10..14:  ytmp[(s+1) & 1] = y_prev + sum_{j<=s} (dt a[s+1][j]) k_j
  *   s == 9:  y_front = y_prev + sum_j (dt b_j) k_j and
  *            result = sqrt(mean((|sum_j dt e_j k_j| / (atol + rtol |y_front|))^2))
@@ -147,7 +169,11 @@ int qg_spmv_dia(const qg_dia* A, const void* x, void* y, double alpha_re, double
  * (qutip/solver/integrator/explicit_rk.pyx:358-410) with wrmn_error_dense
  * (qutip/core/data/ode.pyx:27-52) and iadd_dense (qutip/core/data/add.pyx:203-219). */
 int qg_vern7_stage(const qg_csr_groups* A, const qg_rk_buffers* B, int stage, double t_prev,
-                   double dt, double atol, double rtol, int lanes, void* stream);
+                   double dt, double atol, double rtol, void* stream);
+
+/* Non-zero when a kernel of this library gave up a bounded wait on the current
+ * device (the result of that launch is invalid); reading clears the flag. */
+int qg_device_fault(void);
 
 /* out = base + sum_{j<n_k} f_j k_j (out in out_dtype).  Replaces _accumulate
  * and _interpolate_step (qutip/solver/integrator/explicit_rk.pyx:412-437). */

@@ -17,10 +17,16 @@ QG_C128, QG_C64 = 0, 1
 QG_MAX_GROUPS, QG_MAX_EOPS = 8, 32
 
 
+QG_LAYOUT_GROUP_MAJOR, QG_LAYOUT_ROW_MAJOR = 0, 1
+QG_TILE_ROWS = 512
+
+
 class CsrGroups(C.Structure):
     _fields_ = [("n_rows", C.c_int64), ("n_cols", C.c_int64), ("n_groups", C.c_int32),
-                ("dtype", C.c_int32), ("row_ptr", C.c_void_p), ("col", C.c_void_p),
-                ("val", C.c_void_p), ("coef_code", C.c_void_p), ("coef_start", C.c_void_p),
+                ("dtype", C.c_int32), ("layout", C.c_int32), ("lanes", C.c_int32),
+                ("n_tiles", C.c_int32), ("tile_nnz", C.c_int32), ("row_ptr", C.c_void_p),
+                ("col", C.c_void_p), ("val", C.c_void_p), ("tile_row", C.c_void_p),
+                ("coef_code", C.c_void_p), ("coef_start", C.c_void_p),
                 ("coef_consts", C.c_void_p)]
 
 
@@ -31,7 +37,8 @@ class Dia(C.Structure):
 
 class RkBuffers(C.Structure):
     _fields_ = [("n", C.c_int64), ("state_dtype", C.c_int32), ("stage_dtype", C.c_int32),
-                ("y_prev", C.c_void_p), ("y_front", C.c_void_p), ("k", C.c_void_p),
+                ("y_prev", C.c_void_p), ("y_front", C.c_void_p), ("y_prev_s", C.c_void_p),
+                ("y_front_s", C.c_void_p), ("k", C.c_void_p),
                 ("ytmp", C.c_void_p), ("scratch", C.c_void_p), ("counter", C.c_void_p),
                 ("result", C.c_void_p)]
 
@@ -48,15 +55,16 @@ _SIGS = {
     "qg_last_error": (C.c_char_p, []),
     "qg_scratch_doubles": (C.c_int64, []),
     "qg_vern7_tableau": (C.c_int, [C.c_void_p] * 5),
+    "qg_device_fault": (C.c_int, []),
     "qg_spmv_csr": (C.c_int, [_P(CsrGroups), C.c_double, C.c_void_p, C.c_void_p, C.c_double,
-                              C.c_double, C.c_double, C.c_double, C.c_int, C.c_void_p]),
+                              C.c_double, C.c_double, C.c_double, C.c_void_p]),
     "qg_spmm_csr": (C.c_int, [_P(CsrGroups), C.c_double, C.c_void_p, C.c_void_p, C.c_int64,
                               C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double,
                               C.c_void_p]),
     "qg_spmv_dia": (C.c_int, [_P(Dia), C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                               C.c_double, C.c_double, C.c_void_p]),
     "qg_vern7_stage": (C.c_int, [_P(CsrGroups), _P(RkBuffers), C.c_int, C.c_double, C.c_double,
-                                 C.c_double, C.c_double, C.c_int, C.c_void_p]),
+                                 C.c_double, C.c_double, C.c_void_p]),
     "qg_rk_combine": (C.c_int, [_P(StateView), C.c_void_p, C.c_int, C.c_void_p]),
     "qg_norm2": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                            C.c_void_p]),

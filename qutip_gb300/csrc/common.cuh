@@ -203,6 +203,12 @@ __device__ inline cplx eval_coef(const int* code, const double* consts, double t
   return sp > 0 ? st[sp - 1] : cplx{0.0, 0.0};
 }
 
+// Index into row_ptr of the start of (group g, row r) for either layout.
+__device__ __forceinline__ int rp_index(const qg_csr_groups& A, int g, int r) {
+  return A.layout == QG_LAYOUT_ROW_MAJOR ? r * A.n_groups + g
+                                         : g * ((int)A.n_rows + 1) + r;
+}
+
 // Coefficient of group g at time t; a NULL program table means all ones.
 __device__ __forceinline__ cplx group_coef(const qg_csr_groups& A, int g, double t) {
   if (A.coef_code == nullptr) return cplx{1.0, 0.0};

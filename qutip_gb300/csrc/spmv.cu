@@ -4,13 +4,22 @@
 //            combination, or with y_front and the WRMS error at the last stage
 //            (qg_vern7_stage).
 //
-// Row partitioning: a sub-warp of LANES threads owns one row; consecutive
-// sub-warps own consecutive rows, so operator values and column indices are
-// read fully coalesced (each lane reads one 16 B / 8 B value and one 4 B index
-// per iteration with streaming cache hints) and the partial dot products are
-// combined with warp shuffles.  The gathered vector x stays L2-resident (it is
-// at most 1/20 of the operator's bytes at the sizes this targets).  The grid is
-// a whole number of waves over the SMs and strides over row blocks.
+// Two kernels share the row computation and the epilogues:
+//   * direct: a sub-warp of LANES threads owns one row and reads values and
+//     column indices straight from HBM (coalesced within the row);
+//   * staged: persistent CTAs walk row tiles; one elected thread moves each
+//     tile's values, column indices and row pointers into shared memory with
+//     bulk async copies (cp.async.bulk, completion on an mbarrier), double
+//     buffered so the next tile streams in while the current one is reduced.
+// In both, the gathered vector x is read through the read-only path and stays
+// L2-resident, and the grid is a whole number of waves over the SMs.
+//
+// Arithmetic: GB300 runs FP64 at a small fraction of its FP32 rate, so every
+// complex64 path computes in FP32 (compute type CT = float): the row dots, the
+// coefficient products and the stage combinations, whose factors dt * a_ij are
+// formed once on the host.  FP64 remains where it carries the result: the
+// complex128 path throughout, and in the mixed form the once-per-step state
+// update y_front = y_prev + increment and the WRMS error reduction.
 #include "capi_internal.h"
 #include "common.cuh"
 
@@ -20,213 +29,548 @@ constexpr int SPMV_BLOCK = 256;
 
 enum Epi { EPI_AXPBY = 0, EPI_RK = 1 };
 
+// ------------------------------------------------------- complex of type CT --
+template <typename CT>
+struct cx {
+  CT re, im;
+};
+template <typename CT>
+__device__ __forceinline__ cx<CT> ld_cx(const double2* p) {
+  double2 v = *p;
+  return cx<CT>{(CT)v.x, (CT)v.y};
+}
+template <typename CT>
+__device__ __forceinline__ cx<CT> ld_cx(const float2* p) {
+  float2 v = *p;
+  return cx<CT>{(CT)v.x, (CT)v.y};
+}
+__device__ __forceinline__ void st_cx(double2* p, cx<double> v) { *p = make_double2(v.re, v.im); }
+__device__ __forceinline__ void st_cx(double2* p, cx<float> v) {
+  *p = make_double2((double)v.re, (double)v.im);
+}
+__device__ __forceinline__ void st_cx(float2* p, cx<float> v) { *p = make_float2(v.re, v.im); }
+__device__ __forceinline__ void st_cx(float2* p, cx<double> v) {
+  *p = make_float2((float)v.re, (float)v.im);
+}
+template <typename CT>
+__device__ __forceinline__ cx<CT> cx_mul(cx<CT> a, cx<CT> b) {
+  return cx<CT>{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename CT>
+__device__ __forceinline__ cx<CT> cx_add(cx<CT> a, cx<CT> b) {
+  return cx<CT>{a.re + b.re, a.im + b.im};
+}
+// acc += f * k for real f
+template <typename CT>
+__device__ __forceinline__ void cx_axpy(cx<CT>& acc, CT f, cx<CT> k) {
+  acc.re = fma(f, k.re, acc.re);
+  acc.im = fma(f, k.im, acc.im);
+}
+
 struct AxpbyArgs {
   void* y;
-  cplx alpha, beta;
+  double alpha_re, alpha_im, beta_re, beta_im;
 };
 
+// Host-formed stage factors: fa = dt * a[s+1][0..s] (s < 9, 10 <= s < 15) or
+// dt * b (s == 9); fe = dt * e (s == 9).  Zero factors are skipped, as the
+// reference's iadd_data skips them (explicit_rk.pyx:34-44).
 struct RkArgs {
   const void* y_prev;
   void* y_front;
+  const void* y_prev_s;
+  void* y_front_s;
   void* k;
   void* ytmp_out;
   int64_t n;
   int stage;
-  double dt, atol, rtol;
+  double atol, rtol;
   double* scratch;
   unsigned int* counter;
   double* result;
+  double fa_d[16], fe_d[16];
+  float fa_f[16], fe_f[16];
 };
 
+__device__ unsigned int g_fault = 0u;
+
+template <typename CT>
+__device__ __forceinline__ CT fa(const RkArgs& rk, int j);
+template <>
+__device__ __forceinline__ double fa<double>(const RkArgs& rk, int j) { return rk.fa_d[j]; }
+template <>
+__device__ __forceinline__ float fa<float>(const RkArgs& rk, int j) { return rk.fa_f[j]; }
+template <typename CT>
+__device__ __forceinline__ CT fe(const RkArgs& rk, int j);
+template <>
+__device__ __forceinline__ double fe<double>(const RkArgs& rk, int j) { return rk.fe_d[j]; }
+template <>
+__device__ __forceinline__ float fe<float>(const RkArgs& rk, int j) { return rk.fe_f[j]; }
+
 // Complex multiply-accumulate in the accumulation precision.
-__device__ __forceinline__ void cmac_f(float& ar, float& ai, float2 v, float2 x) {
-  ar = fmaf(v.x, x.x, ar);
-  ar = fmaf(-v.y, x.y, ar);
-  ai = fmaf(v.x, x.y, ai);
-  ai = fmaf(v.y, x.x, ai);
-}
-__device__ __forceinline__ void cmac_d(double& ar, double& ai, double2 v, double2 x) {
+__device__ __forceinline__ void cmac_any(double& ar, double& ai, double2 v, double2 x) {
   ar = fma(v.x, x.x, ar);
   ar = fma(-v.y, x.y, ar);
   ai = fma(v.x, x.y, ai);
   ai = fma(v.y, x.x, ai);
 }
-__device__ __forceinline__ void cmac_any(double& ar, double& ai, double2 v, double2 x) {
-  cmac_d(ar, ai, v, x);
-}
 __device__ __forceinline__ void cmac_any(float& ar, float& ai, float2 v, float2 x) {
-  cmac_f(ar, ai, v, x);
+  ar = fmaf(v.x, x.x, ar);
+  ar = fmaf(-v.y, x.y, ar);
+  ai = fmaf(v.x, x.y, ai);
+  ai = fmaf(v.y, x.x, ai);
 }
 
-// Row dot product of one group for the LANES lanes of a sub-warp; every lane
-// returns the full sum.
-template <typename VT, typename R, int LANES>
-__device__ __forceinline__ cplx row_dot(const int* __restrict__ col, const VT* __restrict__ val,
-                                        const VT* __restrict__ x, int s, int e, int lane) {
-  R ar = 0, ai = 0;
-  int p = s + lane;
-  // two independent loads in flight per lane
-  for (; p + LANES < e; p += 2 * LANES) {
-    VT v0 = ld_stream(val + p), v1 = ld_stream(val + p + LANES);
-    int c0 = ld_stream(col + p), c1 = ld_stream(col + p + LANES);
-    VT x0 = ld_gather(x + c0), x1 = ld_gather(x + c1);
-    cmac_any(ar, ai, v0, x0);
-    cmac_any(ar, ai, v1, x1);
-  }
-  if (p < e) {
-    VT v0 = ld_stream(val + p);
-    int c0 = ld_stream(col + p);
-    cmac_any(ar, ai, v0, ld_gather(x + c0));
-  }
+template <int LANES, typename R>
+__device__ __forceinline__ cx<R> sub_reduce(R ar, R ai) {
 #pragma unroll
   for (int o = LANES / 2; o > 0; o >>= 1) {
     ar += __shfl_xor_sync(0xffffffffu, ar, o);
     ai += __shfl_xor_sync(0xffffffffu, ai, o);
   }
-  return cplx{(double)ar, (double)ai};
+  return cx<R>{ar, ai};
 }
 
-// DT: operator / stage / gathered-vector storage type, YDT: state storage type.
+// Partial row dot product over entries [s, e) for one lane of a LANES-wide
+// sub-warp.  GLOBAL: val/col are global arrays; otherwise shared-memory
+// pointers pre-offset so that entry p is val[p].
+template <typename VT, typename R, int LANES, bool GLOBAL>
+__device__ __forceinline__ void lane_dot(const int* __restrict__ col, const VT* __restrict__ val,
+                                         const VT* __restrict__ x, int s, int e, int lane,
+                                         R& ar, R& ai) {
+  int p = s + lane;
+  for (; p + LANES < e; p += 2 * LANES) {
+    VT v0, v1;
+    int c0, c1;
+    if (GLOBAL) {
+      v0 = ld_stream(val + p);
+      v1 = ld_stream(val + p + LANES);
+      c0 = ld_stream(col + p);
+      c1 = ld_stream(col + p + LANES);
+    } else {
+      v0 = val[p];
+      v1 = val[p + LANES];
+      c0 = col[p];
+      c1 = col[p + LANES];
+    }
+    VT x0 = ld_gather(x + c0), x1 = ld_gather(x + c1);
+    cmac_any(ar, ai, v0, x0);
+    cmac_any(ar, ai, v1, x1);
+  }
+  if (p < e) {
+    VT v0 = GLOBAL ? ld_stream(val + p) : val[p];
+    int c0 = GLOBAL ? ld_stream(col + p) : col[p];
+    cmac_any(ar, ai, v0, ld_gather(x + c0));
+  }
+}
+
+// ---------------------------------------------------------------- epilogue --
+// DT: stage dtype (operator, k, ytmp); YDT: state dtype.  CT = elem<DT>::R.
+template <int DT, int YDT, int EPI>
+__device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
+                                         const AxpbyArgs& ax, const RkArgs& rk,
+                                         typename elem<DT>::R& err_acc) {
+  using ST = typename elem<DT>::T;
+  using YT = typename elem<YDT>::T;
+  using CT = typename elem<DT>::R;
+  if constexpr (EPI == EPI_AXPBY) {
+    ST* y = static_cast<ST*>(ax.y);
+    cx<CT> r = cx_mul(cx<CT>{(CT)ax.alpha_re, (CT)ax.alpha_im}, acc);
+    if (ax.beta_re != 0.0 || ax.beta_im != 0.0)
+      r = cx_add(r, cx_mul(cx<CT>{(CT)ax.beta_re, (CT)ax.beta_im}, ld_cx<CT>(y + row)));
+    st_cx(y + row, r);
+  } else {
+    const int s = rk.stage;
+    const size_t n64 = (size_t)rk.n;
+    ST* k = static_cast<ST*>(rk.k);
+    st_cx(k + (size_t)s * n64 + row, acc);
+    const cx<CT> ks = ld_cx<CT>(k + (size_t)s * n64 + row);  // the stored (rounded) k_s
+    constexpr bool MIXED = (DT != YDT);
+    if (s != RK_STEP - 1 && s != RK_EXTRA_STEP - 1) {
+      // next stage input: base + sum_{j<=s} fa_j k_j, in the reference's order
+      cx<CT> v;
+      if constexpr (MIXED)
+        v = ld_cx<CT>(static_cast<const ST*>(rk.y_prev_s) + row);
+      else
+        v = ld_cx<CT>(static_cast<const YT*>(rk.y_prev) + row);
+      for (int j = 0; j <= s; ++j) {
+        const CT f = fa<CT>(rk, j);
+        if (f != (CT)0) cx_axpy(v, f, j == s ? ks : ld_cx<CT>(k + (size_t)j * n64 + row));
+      }
+      st_cx(static_cast<ST*>(rk.ytmp_out) + row, v);
+    } else if (s == RK_STEP - 1) {
+      cx<CT> e{0, 0};
+      CT ymag;
+      if constexpr (MIXED) {
+        cx<CT> inc{0, 0};
+        for (int j = 0; j < RK_STEP; ++j) {
+          const CT fb = fa<CT>(rk, j), fq = fe<CT>(rk, j);
+          if (fb == (CT)0 && fq == (CT)0) continue;
+          const cx<CT> kj = (j == s) ? ks : ld_cx<CT>(k + (size_t)j * n64 + row);
+          if (fb != (CT)0) cx_axpy(inc, fb, kj);
+          if (fq != (CT)0) cx_axpy(e, fq, kj);
+        }
+        // FP64 state update of the step; FP32 shadow for the next stages
+        const double2 yp = static_cast<const double2*>(rk.y_prev)[row];
+        const double2 yf = make_double2(yp.x + (double)inc.re, yp.y + (double)inc.im);
+        static_cast<double2*>(rk.y_front)[row] = yf;
+        const float2 yf32 = make_float2((float)yf.x, (float)yf.y);
+        static_cast<float2*>(rk.y_front_s)[row] = yf32;
+        ymag = (CT)sqrtf(yf32.x * yf32.x + yf32.y * yf32.y);
+      } else {
+        // reference order: y_front = y_prev, then += fb_j k_j term by term
+        cx<CT> y = ld_cx<CT>(static_cast<const YT*>(rk.y_prev) + row);
+        for (int j = 0; j < RK_STEP; ++j) {
+          const CT fb = fa<CT>(rk, j), fq = fe<CT>(rk, j);
+          if (fb == (CT)0 && fq == (CT)0) continue;
+          const cx<CT> kj = (j == s) ? ks : ld_cx<CT>(k + (size_t)j * n64 + row);
+          if (fb != (CT)0) cx_axpy(y, fb, kj);
+          if (fq != (CT)0) cx_axpy(e, fq, kj);
+        }
+        st_cx(static_cast<YT*>(rk.y_front) + row, y);
+        const cx<CT> ys = ld_cx<CT>(static_cast<const YT*>(rk.y_front) + row);
+        ymag = sqrt(ys.re * ys.re + ys.im * ys.im);
+      }
+      const CT w = sqrt(e.re * e.re + e.im * e.im) / ((CT)rk.atol + (CT)rk.rtol * ymag);
+      err_acc += w * w;
+    }
+  }
+}
+
+// Deterministic grid reduction of the stage-9 error (FP64): per-block partials,
+// the last block to finish sums them in index order.
+template <int BLOCK>
+__device__ __forceinline__ void finish_error(const RkArgs& rk, double err_acc, double* red) {
+  double bs = block_sum<BLOCK>(err_acc, red);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    rk.scratch[blockIdx.x] = bs;
+    __threadfence();
+    unsigned int done = atomicAdd(rk.counter, 1u);
+    last = (done == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    double v = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += BLOCK) v += __ldcg(rk.scratch + i);
+    double tot = block_sum<BLOCK>(v, red);
+    if (threadIdx.x == 0) {
+      *rk.result = sqrt(tot / (double)rk.n);
+      *rk.counter = 0u;
+    }
+  }
+}
+
+template <typename CT>
+__device__ __forceinline__ void load_coefs(const qg_csr_groups& A, double t, cx<CT>* coef) {
+  if (threadIdx.x < A.n_groups) {
+    cplx c = group_coef(A, threadIdx.x, t);
+    coef[threadIdx.x] = cx<CT>{(CT)c.re, (CT)c.im};
+  }
+}
+
+// ------------------------------------------------------------ direct kernel --
 template <int DT, int YDT, int LANES, int EPI>
 __global__ void __launch_bounds__(SPMV_BLOCK)
-    spmv_groups_kernel(qg_csr_groups A, double t, const typename elem<DT>::T* __restrict__ x,
+    spmv_direct_kernel(qg_csr_groups A, double t, const typename elem<DT>::T* __restrict__ x,
                        AxpbyArgs ax, RkArgs rk) {
   using ST = typename elem<DT>::T;
   using R = typename elem<DT>::R;
-  using YT = typename elem<YDT>::T;
-  __shared__ cplx coef[QG_MAX_GROUPS];
+  __shared__ cx<R> coef[QG_MAX_GROUPS];
   __shared__ double red[SPMV_BLOCK / 32];
-  const int G = A.n_groups;
-  if (threadIdx.x < G) coef[threadIdx.x] = group_coef(A, threadIdx.x, t);
+  load_coefs(A, t, coef);
   __syncthreads();
 
+  const int G = A.n_groups;
   const int n = (int)A.n_rows;
   const int sub = threadIdx.x / LANES, lane = threadIdx.x % LANES;
   constexpr int RPB = SPMV_BLOCK / LANES;
   const ST* __restrict__ val = static_cast<const ST*>(A.val);
-  double err_acc = 0.0;
+  R err_acc = 0;
 
   for (int base = blockIdx.x * RPB; base < n; base += gridDim.x * RPB) {
     const int row = base + sub;
     const bool valid = row < n;
-    cplx acc{0.0, 0.0};
+    cx<R> acc{0, 0};
     for (int g = 0; g < G; ++g) {
-      const int* rp = A.row_ptr + (size_t)g * (n + 1);
       int s = 0, e = 0;
       if (valid) {
-        s = __ldg(rp + row);
-        e = __ldg(rp + row + 1);
+        const int i = rp_index(A, g, row);
+        s = __ldg(A.row_ptr + i);
+        e = __ldg(A.row_ptr + i + 1);
       }
-      cplx d = row_dot<ST, R, LANES>(A.col, val, x, s, e, lane);
-      acc = cadd(acc, cmul(coef[g], d));
+      R ar = 0, ai = 0;
+      lane_dot<ST, R, LANES, true>(A.col, val, x, s, e, lane, ar, ai);
+      acc = cx_add(acc, cx_mul(coef[g], sub_reduce<LANES>(ar, ai)));
     }
-    if (!valid || lane != 0) continue;
-
-    if constexpr (EPI == EPI_AXPBY) {
-      ST* y = static_cast<ST*>(ax.y);
-      cplx r = cmul(ax.alpha, acc);
-      if (ax.beta.re != 0.0 || ax.beta.im != 0.0) r = cadd(r, cmul(ax.beta, to_c(y[row])));
-      y[row] = from_c<ST>(r);
-    } else {
-      const int s = rk.stage;
-      const size_t n64 = (size_t)rk.n;
-      ST* k = static_cast<ST*>(rk.k);
-      const ST ks_store = from_c<ST>(acc);
-      k[(size_t)s * n64 + row] = ks_store;
-      const cplx ks = to_c(ks_store);
-      const YT* yp = static_cast<const YT*>(rk.y_prev);
-      if (s != RK_STEP - 1 && s != RK_EXTRA_STEP - 1) {
-        const int nx = s + 1;
-        cplx v = to_c(yp[row]);
-        for (int j = 0; j <= s; ++j) {
-          const double f = rk.dt * VERN7_A[nx][j];
-          if (f != 0.0) v = cadd(v, cscale(j == s ? ks : to_c(k[(size_t)j * n64 + row]), f));
-        }
-        static_cast<ST*>(rk.ytmp_out)[row] = from_c<ST>(v);
-      } else if (s == RK_STEP - 1) {
-        cplx y = to_c(yp[row]);
-        cplx e{0.0, 0.0};
-        for (int j = 0; j < RK_STEP; ++j) {
-          const cplx kj = (j == s) ? ks : to_c(k[(size_t)j * n64 + row]);
-          const double fb = rk.dt * VERN7_B[j];
-          if (fb != 0.0) y = cadd(y, cscale(kj, fb));
-          const double fe = rk.dt * VERN7_E[j];
-          if (fe != 0.0) e = cadd(e, cscale(kj, fe));
-        }
-        const YT ys = from_c<YT>(y);
-        static_cast<YT*>(rk.y_front)[row] = ys;
-        const double w = sqrt(cabs2(e)) / (rk.atol + rk.rtol * sqrt(cabs2(to_c(ys))));
-        err_acc += w * w;
-      }
-    }
+    if (valid && lane == 0) epilogue<DT, YDT, EPI>(row, acc, ax, rk, err_acc);
   }
-
   if constexpr (EPI == EPI_RK) {
-    if (rk.stage == RK_STEP - 1) {
-      // deterministic two-level reduction: per-block partials, last block sums
-      double bs = block_sum<SPMV_BLOCK>(err_acc, red);
-      __shared__ bool last;
-      if (threadIdx.x == 0) {
-        rk.scratch[blockIdx.x] = bs;
-        __threadfence();
-        unsigned int done = atomicAdd(rk.counter, 1u);
-        last = (done == gridDim.x - 1);
-      }
-      __syncthreads();
-      if (last) {
-        __threadfence();
-        double v = 0.0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += SPMV_BLOCK)
-          v += __ldcg(rk.scratch + i);
-        // per-thread strided partials summed in a fixed order
-        double tot = block_sum<SPMV_BLOCK>(v, red);
-        if (threadIdx.x == 0) {
-          *rk.result = sqrt(tot / (double)rk.n);
-          *rk.counter = 0u;
-        }
-      }
-    }
+    if (rk.stage == RK_STEP - 1) finish_error<SPMV_BLOCK>(rk, (double)err_acc, red);
   }
 }
 
-template <int DT, int YDT, int EPI>
-static int launch_lanes(int lanes, int grid, cudaStream_t st, const qg_csr_groups& A, double t,
-                        const void* x, const AxpbyArgs& ax, const RkArgs& rk) {
+// ------------------------------------------------------------ staged kernel --
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0u;
+}
+// 1-D bulk copy global -> shared; dst, src and bytes are multiples of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Bounded wait: every thread polls for at most WAIT_CYCLES SM cycles (about a
+// second); a block-wide vote decides whether the wait completed.  A wait that
+// never completes (it cannot in a correct launch) sets the device fault flag
+// instead of hanging the GPU.
+constexpr long long WAIT_CYCLES = 2000000000LL;
+__device__ __forceinline__ bool mbar_poll(uint64_t* bar, unsigned parity) {
+  const long long t0 = clock64();
+  bool ok = mbar_try_wait(bar, parity);
+  while (!ok && clock64() - t0 < WAIT_CYCLES) ok = mbar_try_wait(bar, parity);
+  return ok;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+  const bool ok = mbar_poll(bar, parity);
+  return __syncthreads_and(ok ? 1 : 0) != 0;
+}
+
+struct TileGeom {
+  int r0, r1;  // rows
+  int pa, np;  // entries: aligned start and count (multiple of 4)
+  int ra, nr;  // row-pointer words: aligned start and count (multiple of 4)
+};
+
+__device__ __forceinline__ TileGeom tile_geom(const qg_csr_groups& A, int tile) {
+  TileGeom g;
+  const int G = A.n_groups;
+  g.r0 = __ldg(A.tile_row + tile);
+  g.r1 = __ldg(A.tile_row + tile + 1);
+  const int p0 = __ldg(A.row_ptr + g.r0 * G), p1 = __ldg(A.row_ptr + g.r1 * G);
+  g.pa = p0 & ~3;
+  g.np = (p1 - g.pa + 3) & ~3;
+  g.ra = (g.r0 * G) & ~3;
+  g.nr = (g.r1 * G + 1 - g.ra + 3) & ~3;
+  return g;
+}
+
+template <int DT, int YDT, int LANES, int EPI, int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
+    spmv_staged_kernel(qg_csr_groups A, double t, const typename elem<DT>::T* __restrict__ x,
+                       AxpbyArgs ax, RkArgs rk, int rpt) {
   using ST = typename elem<DT>::T;
-#define QG_CASE(L)                                                                      \
-  case L:                                                                               \
-    spmv_groups_kernel<DT, YDT, L, EPI><<<grid, SPMV_BLOCK, 0, st>>>(A, t, (const ST*)x, ax, \
-                                                                     rk);               \
+  using R = typename elem<DT>::R;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ cx<R> coef[QG_MAX_GROUPS];
+  __shared__ double red[BLOCK / 32];
+  __shared__ __align__(8) uint64_t bar[2];
+
+  const int G = A.n_groups;
+  const int nzt = A.tile_nnz;
+  const size_t sb = (size_t)nzt * (sizeof(ST) + 4) + (size_t)rpt * 4;
+  load_coefs(A, t, coef);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  const int sub = threadIdx.x / LANES, lane = threadIdx.x % LANES;
+  constexpr int NSUB = BLOCK / LANES;
+  R err_acc = 0;
+
+  auto issue = [&](int tile, int stage) {
+    TileGeom g = tile_geom(A, tile);
+    unsigned char* base = smem + stage * sb;
+    const unsigned bv = (unsigned)(g.np * sizeof(ST)), bc = (unsigned)(g.np * 4),
+                   br = (unsigned)(g.nr * 4);
+    mbar_expect_tx(&bar[stage], bv + bc + br);
+    bulk_g2s(base, static_cast<const ST*>(A.val) + g.pa, bv, &bar[stage]);
+    bulk_g2s(base + (size_t)nzt * sizeof(ST), A.col + g.pa, bc, &bar[stage]);
+    bulk_g2s(base + (size_t)nzt * (sizeof(ST) + 4), A.row_ptr + g.ra, br, &bar[stage]);
+  };
+
+  int tile = blockIdx.x;
+  if (threadIdx.x == 0 && tile < A.n_tiles) issue(tile, 0);
+  unsigned phase[2] = {0u, 0u};
+  bool fault = false;
+  for (int it = 0; tile < A.n_tiles; ++it, tile += gridDim.x) {
+    const int stage = it & 1;
+    const int next = tile + gridDim.x;
+    if (threadIdx.x == 0 && next < A.n_tiles) {
+      // the other buffer was released by the __syncthreads ending the previous tile
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(next, stage ^ 1);
+    }
+    if (!mbar_wait_bounded(&bar[stage], phase[stage])) {
+      fault = true;
+      break;
+    }
+    phase[stage] ^= 1u;
+
+    const TileGeom g = tile_geom(A, tile);
+    unsigned char* base = smem + stage * sb;
+    const ST* sval = reinterpret_cast<const ST*>(base) - g.pa;
+    const int* scol = reinterpret_cast<const int*>(base + (size_t)nzt * sizeof(ST)) - g.pa;
+    const int* srp = reinterpret_cast<const int*>(base + (size_t)nzt * (sizeof(ST) + 4)) - g.ra;
+    const int nrows = g.r1 - g.r0;
+    for (int b = 0; b < nrows; b += NSUB) {
+      const int rr = b + sub;
+      const bool valid = rr < nrows;
+      const int row = g.r0 + rr;
+      cx<R> acc{0, 0};
+      for (int gg = 0; gg < G; ++gg) {
+        int s = 0, e = 0;
+        if (valid) {
+          s = srp[row * G + gg];
+          e = srp[row * G + gg + 1];
+        }
+        R ar = 0, ai = 0;
+        lane_dot<ST, R, LANES, false>(scol, sval, x, s, e, lane, ar, ai);
+        acc = cx_add(acc, cx_mul(coef[gg], sub_reduce<LANES>(ar, ai)));
+      }
+      if (valid && lane == 0) epilogue<DT, YDT, EPI>(row, acc, ax, rk, err_acc);
+    }
+    __syncthreads();
+  }
+  if (fault) {
+    // drain the copies this block may still have in flight, then report
+    if (threadIdx.x == 0) {
+      atomicOr(&g_fault, 1u);
+      for (int s = 0; s < 2; ++s) (void)mbar_poll(&bar[s], phase[s]);
+    }
+    __syncthreads();
+    return;
+  }
+  if constexpr (EPI == EPI_RK) {
+    if (rk.stage == RK_STEP - 1) finish_error<BLOCK>(rk, (double)err_acc, red);
+  }
+}
+
+// ------------------------------------------------------------------ launch --
+// Opt `kernel` into `smem` bytes of dynamic shared memory and return its
+// resident blocks per SM.  The caller keeps one cache per kernel instantiation.
+struct OccCache {
+  int dev = -1, occ = 0;
+  size_t smem = 0;
+};
+template <typename K>
+static int staged_occupancy(K kernel, int block, size_t smem, OccCache& c) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev == c.dev && smem == c.smem) return c.occ;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return -1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem) != cudaSuccess)
+    return -1;
+  c.dev = dev;
+  c.smem = smem;
+  c.occ = per_sm;
+  return per_sm;
+}
+
+template <int DT, int YDT, int EPI, int LANES>
+static int launch_staged(cudaStream_t st, const qg_csr_groups& A, double t, const void* x,
+                         const AxpbyArgs& ax, const RkArgs& rk) {
+  using ST = typename elem<DT>::T;
+  constexpr int BLOCK = 256;
+  const int rpt = ((QG_TILE_ROWS * A.n_groups + 8) + 3) & ~3;
+  const size_t sb = (size_t)A.tile_nnz * (sizeof(ST) + 4) + (size_t)rpt * 4;
+  const size_t smem = 2 * sb;
+  auto kern = spmv_staged_kernel<DT, YDT, LANES, EPI, BLOCK>;
+  static OccCache cache;  // one per instantiation of this function (and so of kern)
+  const int per_sm = staged_occupancy(kern, BLOCK, smem, cache);
+  if (per_sm <= 0) return set_error(QG_ERR_ARG, "staged tile does not fit in shared memory");
+  int64_t grid = (int64_t)sm_count() * per_sm;
+  if (grid > A.n_tiles) grid = A.n_tiles;
+  if (grid > qg_scratch_doubles()) grid = qg_scratch_doubles();
+  kern<<<(int)grid, BLOCK, smem, st>>>(A, t, (const ST*)x, ax, rk, rpt);
+  return check_launch("spmv_staged_kernel");
+}
+
+template <int DT, int YDT, int EPI>
+static int launch_any(cudaStream_t st, const qg_csr_groups& A, double t, const void* x,
+                      const AxpbyArgs& ax, const RkArgs& rk) {
+  using ST = typename elem<DT>::T;
+  const int lanes = A.lanes > 0 ? A.lanes : 4;
+  if (A.n_tiles > 0) {
+    switch (lanes) {
+      case 1: return launch_staged<DT, YDT, EPI, 1>(st, A, t, x, ax, rk);
+      case 2: return launch_staged<DT, YDT, EPI, 2>(st, A, t, x, ax, rk);
+      case 4: return launch_staged<DT, YDT, EPI, 4>(st, A, t, x, ax, rk);
+      case 8: return launch_staged<DT, YDT, EPI, 8>(st, A, t, x, ax, rk);
+      case 16: return launch_staged<DT, YDT, EPI, 16>(st, A, t, x, ax, rk);
+      default: return set_error(QG_ERR_ARG, "staged kernel: lanes must be 1..16");
+    }
+  }
+  const int rpb = SPMV_BLOCK / lanes;
+  int64_t blocks = (A.n_rows + rpb - 1) / rpb;
+  int64_t cap = (int64_t)sm_count() * (2048 / SPMV_BLOCK);
+  if (cap > qg_scratch_doubles()) cap = qg_scratch_doubles();
+  const int grid = (int)(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
+#define QG_CASE(L)                                                                          \
+  case L:                                                                                   \
+    spmv_direct_kernel<DT, YDT, L, EPI><<<grid, SPMV_BLOCK, 0, st>>>(A, t, (const ST*)x, ax, \
+                                                                     rk);                   \
     break;
   switch (lanes) {
+    QG_CASE(1)
     QG_CASE(2)
     QG_CASE(4)
     QG_CASE(8)
     QG_CASE(16)
     QG_CASE(32)
     default:
-      return set_error(QG_ERR_ARG, "lanes must be one of 2, 4, 8, 16, 32");
+      return set_error(QG_ERR_ARG, "lanes must be a power of two in 1..32");
   }
 #undef QG_CASE
-  return check_launch("spmv_groups_kernel");
-}
-
-static int grid_for_rows(int64_t n_rows, int lanes) {
-  const int rpb = SPMV_BLOCK / lanes;
-  int64_t blocks = (n_rows + rpb - 1) / rpb;
-  int64_t cap = (int64_t)sm_count() * 8;  // 8 resident 256-thread blocks per SM
-  if (cap > qg_scratch_doubles()) cap = qg_scratch_doubles();
-  return (int)(blocks < cap ? (blocks < 1 ? 1 : blocks) : cap);
+  return check_launch("spmv_direct_kernel");
 }
 
 static int check_groups(const qg_csr_groups* A) {
   if (!A || !A->row_ptr || !A->col || !A->val) return set_error(QG_ERR_ARG, "null operator");
   if (A->n_groups < 1 || A->n_groups > QG_MAX_GROUPS)
     return set_error(QG_ERR_ARG, "n_groups out of range");
-  if (A->n_rows < 0 || A->n_rows >= (int64_t)INT32_MAX || A->n_cols < 0)
+  if (A->n_rows < 0 || A->n_rows >= (int64_t)INT32_MAX / QG_MAX_GROUPS || A->n_cols < 0)
     return set_error(QG_ERR_ARG, "bad operator shape");
   if (A->dtype != QG_C128 && A->dtype != QG_C64)
     return set_error(QG_ERR_UNSUPPORTED, "operator dtype must be QG_C128 or QG_C64");
+  if (A->layout != QG_LAYOUT_GROUP_MAJOR && A->layout != QG_LAYOUT_ROW_MAJOR)
+    return set_error(QG_ERR_ARG, "unknown row-pointer layout");
+  if (A->n_tiles > 0) {
+    if (A->layout != QG_LAYOUT_ROW_MAJOR || !A->tile_row)
+      return set_error(QG_ERR_ARG, "tiles need the row-major layout and tile_row");
+    if (A->tile_nnz != 2048 && A->tile_nnz != 4096)
+      return set_error(QG_ERR_ARG, "tile_nnz must be 2048 or 4096");
+  }
   if (A->coef_code && (!A->coef_start || !A->coef_consts))
     return set_error(QG_ERR_ARG, "coefficient program tables incomplete");
   return QG_OK;
@@ -236,25 +580,30 @@ static int check_groups(const qg_csr_groups* A) {
 
 using namespace qg;
 
+extern "C" int qg_device_fault(void) {
+  unsigned int v = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_fault, sizeof(v)) != cudaSuccess)
+    return set_error(QG_ERR_CUDA, "cannot read the device fault flag");
+  if (v) cudaMemcpyToSymbol(g_fault, &zero, sizeof(zero));
+  return (int)v;
+}
+
 extern "C" int qg_spmv_csr(const qg_csr_groups* A, double t, const void* x, void* y,
                            double alpha_re, double alpha_im, double beta_re, double beta_im,
-                           int lanes, void* stream) {
+                           void* stream) {
   int rc = check_groups(A);
   if (rc) return rc;
   if (!x || !y) return set_error(QG_ERR_ARG, "null vector");
   if (A->n_rows == 0) return QG_OK;
-  AxpbyArgs ax{y, cplx{alpha_re, alpha_im}, cplx{beta_re, beta_im}};
+  AxpbyArgs ax{y, alpha_re, alpha_im, beta_re, beta_im};
   RkArgs rk{};
-  const int grid = grid_for_rows(A->n_rows, lanes);
   cudaStream_t st = (cudaStream_t)stream;
-  if (A->dtype == QG_C128)
-    return launch_lanes<QG_C128, QG_C128, EPI_AXPBY>(lanes, grid, st, *A, t, x, ax, rk);
-  return launch_lanes<QG_C64, QG_C64, EPI_AXPBY>(lanes, grid, st, *A, t, x, ax, rk);
+  if (A->dtype == QG_C128) return launch_any<QG_C128, QG_C128, EPI_AXPBY>(st, *A, t, x, ax, rk);
+  return launch_any<QG_C64, QG_C64, EPI_AXPBY>(st, *A, t, x, ax, rk);
 }
 
 extern "C" int qg_vern7_stage(const qg_csr_groups* A, const qg_rk_buffers* B, int stage,
-                              double t_prev, double dt, double atol, double rtol, int lanes,
-                              void* stream) {
+                              double t_prev, double dt, double atol, double rtol, void* stream) {
   int rc = check_groups(A);
   if (rc) return rc;
   if (!B || !B->y_prev || !B->y_front || !B->k || !B->ytmp)
@@ -264,29 +613,54 @@ extern "C" int qg_vern7_stage(const qg_csr_groups* A, const qg_rk_buffers* B, in
     return set_error(QG_ERR_ARG, "operator must be square with n rows");
   if (B->stage_dtype != A->dtype)
     return set_error(QG_ERR_UNSUPPORTED, "stage dtype must equal the operator dtype");
+  const bool mixed = B->state_dtype != B->stage_dtype;
+  if (mixed && (!B->y_prev_s || !B->y_front_s))
+    return set_error(QG_ERR_ARG, "mixed form needs y_prev_s and y_front_s");
   if (stage == RK_STEP - 1 && (!B->scratch || !B->counter || !B->result))
     return set_error(QG_ERR_ARG, "error reduction buffers missing");
   if (B->n == 0) return QG_OK;
   const size_t n = (size_t)B->n;
   const size_t es = B->stage_dtype == QG_C128 ? 16 : 8;
-  RkArgs rk{B->y_prev, B->y_front, B->k,
-            (char*)B->ytmp + ((stage + 1) & 1) * n * es, B->n, stage, dt, atol, rtol,
-            B->scratch, B->counter, B->result};
+  RkArgs rk{};
+  rk.y_prev = B->y_prev;
+  rk.y_front = B->y_front;
+  rk.y_prev_s = B->y_prev_s;
+  rk.y_front_s = B->y_front_s;
+  rk.k = B->k;
+  rk.ytmp_out = (char*)B->ytmp + ((stage + 1) & 1) * n * es;
+  rk.n = B->n;
+  rk.stage = stage;
+  rk.atol = atol;
+  rk.rtol = rtol;
+  rk.scratch = B->scratch;
+  rk.counter = B->counter;
+  rk.result = B->result;
+  // factors dt * tableau, formed in double and rounded once for the FP32 paths
+  for (int j = 0; j < 16; ++j) {
+    double a = 0.0, e = 0.0;
+    if (stage == RK_STEP - 1) {
+      if (j < RK_STEP) {
+        a = dt * VERN7_B_HOST[j];
+        e = dt * VERN7_E_HOST[j];
+      }
+    } else if (stage + 1 < RK_EXTRA_STEP && j <= stage) {
+      a = dt * VERN7_A_HOST[stage + 1][j];
+    }
+    rk.fa_d[j] = a;
+    rk.fe_d[j] = e;
+    rk.fa_f[j] = (float)a;
+    rk.fe_f[j] = (float)e;
+  }
   AxpbyArgs ax{};
-  const int grid = grid_for_rows(A->n_rows, lanes);
   cudaStream_t st = (cudaStream_t)stream;
   const double t = t_prev + VERN7_C_HOST[stage] * dt;
-  // Stage 0 gathers y_prev itself when state and stages share a dtype; in the
-  // mixed form it gathers ytmp[0], which the caller fills with the rounded
-  // y_prev (qg_rk_combine with n_k = 0).
-  const bool mixed = B->state_dtype != B->stage_dtype;
-  const void* x = (stage == 0 && !mixed) ? B->y_prev
-                                         : (const char*)B->ytmp + (stage & 1) * n * es;
+  const void* x = stage == 0 ? (mixed ? B->y_prev_s : B->y_prev)
+                             : (const char*)B->ytmp + (stage & 1) * n * es;
   if (B->state_dtype == QG_C128 && B->stage_dtype == QG_C128)
-    return launch_lanes<QG_C128, QG_C128, EPI_RK>(lanes, grid, st, *A, t, x, ax, rk);
+    return launch_any<QG_C128, QG_C128, EPI_RK>(st, *A, t, x, ax, rk);
   if (B->state_dtype == QG_C128 && B->stage_dtype == QG_C64)
-    return launch_lanes<QG_C64, QG_C128, EPI_RK>(lanes, grid, st, *A, t, x, ax, rk);
+    return launch_any<QG_C64, QG_C128, EPI_RK>(st, *A, t, x, ax, rk);
   if (B->state_dtype == QG_C64 && B->stage_dtype == QG_C64)
-    return launch_lanes<QG_C64, QG_C64, EPI_RK>(lanes, grid, st, *A, t, x, ax, rk);
+    return launch_any<QG_C64, QG_C64, EPI_RK>(st, *A, t, x, ax, rk);
   return set_error(QG_ERR_UNSUPPORTED, "unsupported state/stage dtype pair");
 }

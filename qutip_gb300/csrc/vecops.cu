@@ -25,13 +25,45 @@ __device__ __forceinline__ cplx view_at(const qg_state_view& v, size_t i) {
   return r;
 }
 
+// out = base + sum_j f_j k_j.  Complex128 stages: FP64, term by term in the
+// reference's order.  Complex64 stages: the increment is summed in FP32 (GB300's
+// FP64 rate is a small fraction of FP32) and added to a complex128 base in FP64.
 template <int BDT, int KDT, int ODT>
 __global__ void __launch_bounds__(VEC_BLOCK) combine_kernel(qg_state_view v, void* out) {
   using OT = typename elem<ODT>::T;
+  __shared__ float ff[16];
+  if (threadIdx.x < 16) ff[threadIdx.x] = (float)v.f[threadIdx.x];
+  __syncthreads();
   OT* o = static_cast<OT*>(out);
-  for (size_t i = (size_t)blockIdx.x * VEC_BLOCK + threadIdx.x; i < (size_t)v.n;
-       i += (size_t)gridDim.x * VEC_BLOCK)
-    o[i] = from_c<OT>(view_at<BDT, KDT>(v, i));
+  const size_t n = (size_t)v.n;
+  for (size_t i = (size_t)blockIdx.x * VEC_BLOCK + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * VEC_BLOCK) {
+    if constexpr (KDT == QG_C128) {
+      o[i] = from_c<OT>(view_at<BDT, KDT>(v, i));
+    } else {
+      const float2* k = static_cast<const float2*>(v.k);
+      float ir = 0.f, ii = 0.f;
+      if constexpr (BDT == QG_C64) {
+        const float2 b = static_cast<const float2*>(v.base)[i];
+        ir = b.x;
+        ii = b.y;
+      }
+      for (int j = 0; j < v.n_k; ++j) {
+        const float f = ff[j];
+        if (f != 0.f) {
+          const float2 kj = k[(size_t)j * n + i];
+          ir = fmaf(f, kj.x, ir);
+          ii = fmaf(f, kj.y, ii);
+        }
+      }
+      if constexpr (BDT == QG_C64) {
+        o[i] = from_c<OT>(cplx{(double)ir, (double)ii});
+      } else {
+        const double2 b = static_cast<const double2*>(v.base)[i];
+        o[i] = from_c<OT>(cplx{b.x + (double)ir, b.y + (double)ii});
+      }
+    }
+  }
 }
 
 template <int DT>
@@ -74,10 +106,10 @@ __global__ void __launch_bounds__(VEC_BLOCK)
   double ar = 0.0, ai = 0.0;
   if (g < G) {
     const int n = (int)ops.n_rows;
-    const int* rp = ops.row_ptr + (size_t)g * (n + 1);
     const OT* val = static_cast<const OT*>(ops.val);
     for (int r = threadIdx.x; r < n; r += VEC_BLOCK) {
-      const int s = rp[r], e = rp[r + 1];
+      const int i = rp_index(ops, g, r);
+      const int s = ops.row_ptr[i], e = ops.row_ptr[i + 1];
       if (s == e) continue;
       cplx acc{0.0, 0.0};
       for (int p = s; p < e; ++p) {
@@ -159,8 +191,8 @@ __global__ void __launch_bounds__(VEC_BLOCK)
 #pragma unroll
       for (int q = 0; q < MM_COLS; ++q) acc[q] = cplx{0.0, 0.0};
       for (int g = 0; g < A.n_groups; ++g) {
-        const int* rp = A.row_ptr + (size_t)g * (n + 1);
-        const int s = valid ? rp[row] : 0, e = valid ? rp[row + 1] : 0;
+        const int i = valid ? rp_index(A, g, row) : 0;
+        const int s = valid ? A.row_ptr[i] : 0, e = valid ? A.row_ptr[i + 1] : 0;
         cplx part[MM_COLS];
 #pragma unroll
         for (int q = 0; q < MM_COLS; ++q) part[q] = cplx{0.0, 0.0};

@@ -42,11 +42,64 @@ def stream_ptr() -> int:
     return torch.cuda.current_stream().cuda_stream
 
 
+def row_major_layout(mats):
+    """Interleave coefficient groups row by row.
+
+    Returns ``(row_ptr[n*G+1], col[nnz], val[nnz])`` with the entries of row r
+    stored contiguously, group 0 first: group g of row r spans
+    ``[row_ptr[r*G+g], row_ptr[r*G+g+1])``.
+    """
+    mats = [sp.csr_matrix(m, dtype=np.complex128) for m in mats]
+    for m in mats:
+        m.sort_indices()
+    n, m_cols = mats[0].shape
+    G = len(mats)
+    counts = np.stack([np.diff(m.indptr) for m in mats], axis=1).reshape(-1)
+    rp = np.zeros(n * G + 1, dtype=np.int64)
+    np.cumsum(counts, out=rp[1:])
+    nnz = int(rp[-1])
+    col = np.empty(nnz, dtype=np.int32)
+    val = np.empty(nnz, dtype=np.complex128)
+    # destination of entry q of group g, row r: rp[r*G+g] + (q - indptr_g[r])
+    for g, m in enumerate(mats):
+        rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(m.indptr))
+        dst = rp[rows * G + g] + (np.arange(m.nnz, dtype=np.int64) - m.indptr[rows])
+        col[dst] = m.indices
+        val[dst] = m.data
+    return rp, col, val
+
+
+def row_tiles(row_start, tile_nnz, max_rows):
+    """Greedy row tiles holding at most ``tile_nnz - 8`` entries and ``max_rows`` rows.
+
+    ``row_start`` is the entry offset of each row (length n+1).  Returns the
+    first row of each tile (length n_tiles+1) or ``None`` if a row is too long.
+    """
+    n = len(row_start) - 1
+    cap = tile_nnz - 8
+    if n == 0 or np.max(np.diff(row_start)) > cap:
+        return None
+    out = [0]
+    r = 0
+    while r < n:
+        r1 = int(np.searchsorted(row_start, row_start[r] + cap, side="right")) - 1
+        r1 = min(r1, r + max_rows, n)
+        out.append(r1)
+        r = r1
+    return np.asarray(out, dtype=np.int32)
+
+
 class DeviceOperator:
     """``A(t) = sum_g c_g(t) A_g`` resident on the GPU.
 
-    ``terms`` is a list of ``(scipy matrix, Coefficient | None)``.
+    ``terms`` is a list of ``(scipy matrix, Coefficient | None)``.  Entries are
+    stored row-major (all groups of a row contiguous) with 8 entries of padding
+    so that row tiles can be bulk-copied in 16-byte units; the launch shape
+    (direct sub-warp kernel or shared-memory staged tiles, threads per row) is
+    chosen by :meth:`tune`.
     """
+
+    PAD = 8
 
     def __init__(self, terms, dtype: str = "c128", device="cuda", merge: bool = True):
         if dtype not in _TORCH:
@@ -67,22 +120,26 @@ class DeviceOperator:
         self.dtype = dtype
         self.coeffs = [c for _, c in terms]
         self.device = torch.device(device)
-        rps, cols, vals = [], [], []
-        off = 0
-        for op, _ in terms:
-            m = sp.csr_matrix(op, dtype=np.complex128)
-            m.sort_indices()
-            rps.append(m.indptr.astype(np.int64) + off)
-            cols.append(m.indices.astype(np.int32))
-            vals.append(m.data)
-            off += m.nnz
-        if off >= 2**31:
+        G = len(terms)
+        mats = [op for op, _ in terms]
+        self.group_nnz = [int(sp.csr_matrix(m).nnz) for m in mats]
+        rp, col, val = row_major_layout(mats)
+        if len(col) >= 2**31 - 16 or self.n_rows * G >= 2**31 - 16:
             raise ValueError("operators beyond 2^31 stored entries need 64-bit indices")
-        self.nnz = off
-        self.group_nnz = [len(c) for c in cols]
-        self.row_ptr = torch.from_numpy(np.concatenate(rps).astype(np.int32)).to(self.device)
-        self.col = torch.from_numpy(np.concatenate(cols)).to(self.device)
-        self.val = torch.from_numpy(np.concatenate(vals)).to(self.device, _TORCH[dtype])
+        self.nnz = len(col)
+        P = self.PAD
+        self.row_ptr = torch.zeros(len(rp) + P, dtype=torch.int32, device=self.device)
+        self.row_ptr[:len(rp)] = torch.from_numpy(rp.astype(np.int32)).to(self.device)
+        self.col = torch.zeros(self.nnz + P, dtype=torch.int32, device=self.device)
+        self.col[:self.nnz] = torch.from_numpy(col).to(self.device)
+        self.val = torch.zeros(self.nnz + P, dtype=_TORCH[dtype], device=self.device)
+        self.val[:self.nnz] = torch.from_numpy(val).to(self.device, _TORCH[dtype])
+        row_start = rp[::G]
+        self._tiles = {}
+        for tn in (2048, 4096):
+            t = row_tiles(row_start, tn, _lib.QG_TILE_ROWS)
+            if t is not None:
+                self._tiles[tn] = torch.from_numpy(t).to(self.device)
         if all(c is None for c in self.coeffs):
             self.coef_code = self.coef_start = self.coef_consts = None
         else:
@@ -91,9 +148,70 @@ class DeviceOperator:
             self.coef_start = torch.from_numpy(starts).to(self.device)
             self.coef_consts = torch.from_numpy(consts).to(self.device)
         self.struct = _lib.CsrGroups(
-            self.n_rows, self.n_cols, len(terms), _QG[dtype], _ptr(self.row_ptr), _ptr(self.col),
-            _ptr(self.val), _ptr(self.coef_code), _ptr(self.coef_start), _ptr(self.coef_consts))
-        self.lanes = self.default_lanes()
+            self.n_rows, self.n_cols, G, _QG[dtype], _lib.QG_LAYOUT_ROW_MAJOR, 4, 0, 0,
+            _ptr(self.row_ptr), _ptr(self.col), _ptr(self.val), None, _ptr(self.coef_code),
+            _ptr(self.coef_start), _ptr(self.coef_consts))
+        self.set_launch(self.default_launch())
+
+    # -- launch shape ------------------------------------------------------
+    def default_launch(self):
+        """Staged tiles for short rows, a sub-warp per row otherwise (before tuning)."""
+        mean = self.nnz / max(self.n_rows, 1)
+        tn = 4096 if self.dtype == "c64" else 2048
+        if tn in self._tiles and mean <= 64:
+            return ("staged", tn, 4 if mean >= 12 else 2)
+        lanes = 2
+        while lanes < 32 and lanes * 2 <= max(mean / self.n_groups / 1.5, 2):
+            lanes *= 2
+        return ("direct", 0, lanes)
+
+    def set_launch(self, launch):
+        kind, tile_nnz, lanes = launch
+        if kind == "staged":
+            if tile_nnz not in self._tiles:
+                raise ValueError(f"no {tile_nnz}-entry tiling (a row is too long)")
+            t = self._tiles[tile_nnz]
+            self.struct.n_tiles = len(t) - 1
+            self.struct.tile_nnz = tile_nnz
+            self.struct.tile_row = t.data_ptr()
+        else:
+            self.struct.n_tiles = 0
+            self.struct.tile_nnz = 0
+            self.struct.tile_row = None
+        self.struct.lanes = lanes
+        self.launch = (kind, tile_nnz, lanes)
+
+    def launch_desc(self) -> str:
+        kind, tn, lanes = self.launch
+        return f"{kind}(lanes={lanes}" + (f", tile_nnz={tn})" if kind == "staged" else ")")
+
+    def candidates(self):
+        out = [("direct", 0, l) for l in (1, 2, 4, 8, 16, 32)]
+        for tn in sorted(self._tiles):
+            out += [("staged", tn, l) for l in (1, 2, 4, 8, 16)]
+        return out
+
+    def tune(self, reps: int = 5, candidates=None):
+        """Time the matvec for every launch shape on this device and keep the fastest."""
+        x = torch.randn(self.n_cols, dtype=_TORCH[self.dtype], device=self.device)
+        y = torch.empty(self.n_rows, dtype=_TORCH[self.dtype], device=self.device)
+        results = {}
+        for cand in candidates or self.candidates():
+            self.set_launch(cand)
+            self.matvec(0.37, x, y)
+            st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            st.record()
+            for _ in range(reps):
+                self.matvec(0.37, x, y)
+            en.record()
+            en.synchronize()
+            results[cand] = st.elapsed_time(en) / reps
+        best = min(results, key=results.get)
+        self.set_launch(best)
+        self.tune_results = results
+        return best
+
+    tune_lanes = tune
 
     def device_arrays(self):
         return [t for t in (self.row_ptr, self.col, self.val, self.coef_code, self.coef_start,
@@ -124,25 +242,16 @@ class DeviceOperator:
     def isconstant(self) -> bool:
         return all(c is None for c in self.coeffs)
 
-    def default_lanes(self) -> int:
-        """Threads per row: the power of two nearest half the largest group's mean row length."""
-        mean = max(g / max(self.n_rows, 1) for g in self.group_nnz)
-        lanes = 2
-        while lanes < 32 and lanes * 2 <= max(mean / 1.5, 2):
-            lanes *= 2
-        return lanes
-
     def value_bytes(self) -> int:
         return 16 if self.dtype == "c128" else 8
 
     def spmv_bytes(self, accumulate: bool = False) -> int:
         """Algorithmic HBM bytes of one matvec: values + indices + row pointers + x + y."""
-        sv, sx = self.value_bytes(), self.value_bytes()
-        return (self.nnz * (sv + 4) + self.n_groups * (self.n_rows + 1) * 4 + self.n_cols * sx
-                + self.n_rows * sx * (2 if accumulate else 1))
+        sv = self.value_bytes()
+        return (self.nnz * (sv + 4) + (self.n_groups * self.n_rows + 1) * 4 + self.n_cols * sv
+                + self.n_rows * sv * (2 if accumulate else 1))
 
-    def matvec(self, t: float, x: torch.Tensor, y: torch.Tensor, alpha=1.0, beta=0.0,
-               lanes: int | None = None):
+    def matvec(self, t: float, x: torch.Tensor, y: torch.Tensor, alpha=1.0, beta=0.0):
         """``y = alpha A(t) x + beta y`` on the current stream (vectors in ``self.dtype``)."""
         if x.dtype != _TORCH[self.dtype] or y.dtype != _TORCH[self.dtype]:
             raise TypeError("vector dtype must match the operator dtype")
@@ -152,7 +261,7 @@ class DeviceOperator:
             raise ValueError("vectors must be contiguous")
         a, b = complex(alpha), complex(beta)
         _lib.call("qg_spmv_csr", C.byref(self.struct), float(t), x.data_ptr(), y.data_ptr(),
-                  a.real, a.imag, b.real, b.imag, int(lanes or self.lanes), stream_ptr())
+                  a.real, a.imag, b.real, b.imag, stream_ptr())
         return y
 
     def matmat(self, t: float, X: torch.Tensor, Y: torch.Tensor, alpha=1.0, beta=0.0):
@@ -166,32 +275,12 @@ class DeviceOperator:
                   X.shape[0], X.stride(0), a.real, a.imag, b.real, b.imag, stream_ptr())
         return Y
 
-    def tune_lanes(self, candidates=(2, 4, 8, 16, 32), reps: int = 5) -> int:
-        """Time the matvec for each sub-warp width on this device and keep the fastest."""
-        x = torch.randn(self.n_cols, dtype=_TORCH[self.dtype], device=self.device)
-        y = torch.empty(self.n_rows, dtype=_TORCH[self.dtype], device=self.device)
-        best, best_t = self.lanes, float("inf")
-        for lanes in candidates:
-            self.matvec(0.37, x, y, lanes=lanes)
-            st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            st.record()
-            for _ in range(reps):
-                self.matvec(0.37, x, y, lanes=lanes)
-            en.record()
-            en.synchronize()
-            ms = st.elapsed_time(en) / reps
-            if ms < best_t:
-                best, best_t = lanes, ms
-        self.lanes = best
-        return best
-
 
 class DeviceDia:
     """A Dia matrix (qutip/core/data/dia.pxd:17-38) resident on the GPU."""
 
     def __init__(self, mat, dtype: str = "c128", device="cuda"):
-        m = sp.dia_matrix(mat)
-        m.sum_duplicates()
+        m = sp.dia_matrix(sp.csr_matrix(mat))  # duplicates summed by the CSR conversion
         self.shape = m.shape
         self.dtype = dtype
         n_cols = m.shape[1]

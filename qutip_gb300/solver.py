@@ -78,8 +78,9 @@ def _wide_groups(ops, dtype, device):
     w.col = torch.from_numpy(np.concatenate(cols)).to(device)
     w.val = torch.from_numpy(np.concatenate(vals)).to(device, tdt)
     n = ops[0].shape[0]
-    w.struct = _lib.CsrGroups(n, n, len(ops), 0 if dtype == "c128" else 1, w.row_ptr.data_ptr(),
-                              w.col.data_ptr(), w.val.data_ptr(), None, None, None)
+    w.struct = _lib.CsrGroups(n, n, len(ops), 0 if dtype == "c128" else 1,
+                              _lib.QG_LAYOUT_GROUP_MAJOR, 1, 0, 0, w.row_ptr.data_ptr(),
+                              w.col.data_ptr(), w.val.data_ptr(), None, None, None, None)
     return w
 
 

@@ -94,6 +94,13 @@ class GpuVern7:
         self.result = torch.zeros(4, dtype=torch.float64, device=dev)
         self._host = torch.zeros(4, dtype=torch.float64).pin_memory()
         self.y_prev, self.y_front = self._ya, self._yb
+        # mixed form: complex64 copies of y_prev / y_front (stage inputs), swapped with them
+        self.mixed = self.state_dt != self.stage_dt
+        if self.mixed:
+            self.y_prev_s = torch.zeros(n, dtype=kdt, device=dev)
+            self.y_front_s = torch.zeros(n, dtype=kdt, device=dev)
+        else:
+            self.y_prev_s = self.y_front_s = None
         self._set = False
         self.status = NOT_INITIATED
         self.stats = {"steps": 0, "rejected": 0, "rhs": 0}
@@ -101,10 +108,17 @@ class GpuVern7:
 
     # -- buffers ---------------------------------------------------------
     def _rk(self) -> _lib.RkBuffers:
+        ps = self.y_prev_s.data_ptr() if self.mixed else None
+        fs = self.y_front_s.data_ptr() if self.mixed else None
         return _lib.RkBuffers(self.n, qg_dtype(self.state_dt), qg_dtype(self.stage_dt),
-                              self.y_prev.data_ptr(), self.y_front.data_ptr(), self.k.data_ptr(),
-                              self.ytmp.data_ptr(), self.scratch.data_ptr(),
+                              self.y_prev.data_ptr(), self.y_front.data_ptr(), ps, fs,
+                              self.k.data_ptr(), self.ytmp.data_ptr(), self.scratch.data_ptr(),
                               self.counter.data_ptr(), self.result.data_ptr())
+
+    def _swap(self):
+        self.y_prev, self.y_front = self.y_front, self.y_prev
+        if self.mixed:
+            self.y_prev_s, self.y_front_s = self.y_front_s, self.y_prev_s
 
     def _view(self, base: torch.Tensor, factors=()) -> _lib.StateView:
         f = (C.c_double * 16)(*([float(x) for x in factors] + [0.0] * (16 - len(factors))))
@@ -146,6 +160,9 @@ class GpuVern7:
             raise ValueError(f"state of size {y0.numel()} for a generator of size {self.n}")
         self.y_prev.copy_(y0.reshape(-1).to(self.y_prev.device, self.y_prev.dtype))
         self.y_front.copy_(self.y_prev)
+        if self.mixed:
+            self._combine(self.y_prev, (), self.y_prev_s)
+            self.y_front_s.copy_(self.y_prev_s)
         self.t = self.t_prev = self.t_front = float(t)
         self.dt_int = 0.0
         self._out = ("front", None)
@@ -159,6 +176,10 @@ class GpuVern7:
             return y
         self._combine(y, (), self._ytmp(0))
         return self._ytmp(0)
+
+    def _stage_base(self) -> torch.Tensor:
+        """Base of the stage combinations: y_prev, or its complex64 copy when mixed."""
+        return self.y_prev_s if self.mixed else self.y_prev
 
     def _estimate_first_step(self, t, y0):
         # explicit_rk.pyx:232-276
@@ -212,7 +233,7 @@ class GpuVern7:
             t = self.t_front
         while self.t_front < t and self.status >= 0:
             # y_prev <- y_front: swap the buffers (the old y_prev is dead)
-            self.y_prev, self.y_front = self.y_front, self.y_prev
+            self._swap()
             self.t_prev = self.t_front
             nsteps_left -= self._step_in_err(t, nsteps_left)
             if step:
@@ -253,13 +274,11 @@ class GpuVern7:
     def _compute_step(self, dt):
         # explicit_rk.pyx:358-397: ten fused stages; the last returns the error
         rk = self._rk()
-        if self.state_dt != self.stage_dt:
-            self._combine(self.y_prev, (), self._ytmp(0))
         lib = _lib.load()
         s = stream_ptr()
         for i in range(T.RK_STEP):
             _lib.check(lib.qg_vern7_stage(C.byref(self.op.struct), C.byref(rk), i, self.t_prev, dt,
-                                          self.atol, self.rtol, self.op.lanes, s), "qg_vern7_stage")
+                                          self.atol, self.rtol, s), "qg_vern7_stage")
         self.stats["rhs"] += T.RK_STEP
         self.t_front = self.t_prev + dt
         return self._read_result()
@@ -268,13 +287,13 @@ class GpuVern7:
         # explicit_rk.pyx:399-410
         dt = self.dt_int
         rk = self._rk()
-        self._combine(self.y_prev, [dt * self.a[T.RK_STEP, j] for j in range(T.RK_STEP)],
+        self._combine(self._stage_base(), [dt * self.a[T.RK_STEP, j] for j in range(T.RK_STEP)],
                       self._ytmp(T.RK_STEP & 1))
         lib = _lib.load()
         s = stream_ptr()
         for i in range(T.RK_STEP, T.RK_EXTRA_STEP):
             _lib.check(lib.qg_vern7_stage(C.byref(self.op.struct), C.byref(rk), i, self.t_prev, dt,
-                                          self.atol, self.rtol, self.op.lanes, s), "qg_vern7_stage")
+                                          self.atol, self.rtol, s), "qg_vern7_stage")
         self.stats["rhs"] += T.RK_EXTRA_STEP - T.RK_STEP
 
     def dense_factors(self, t):

@@ -24,16 +24,42 @@ def _t(a, dtype=torch.complex128):
 
 
 @pytest.mark.parametrize("i", [0, 1, 2])
-@pytest.mark.parametrize("lanes", [2, 4, 8, 16, 32])
-def test_spmv_c128_matches_reference(dev, i, lanes):
+def test_spmv_c128_matches_reference_every_launch_shape(dev, i):
     from qutip_gb300.operator import DeviceOperator
     g = golden("kernels.npz")
     n = len(g[f"spmv{i}_x"])
     A = sp.csr_matrix((g[f"spmv{i}_data"], g[f"spmv{i}_indices"], g[f"spmv{i}_indptr"]), shape=(n, n))
     op = DeviceOperator([(A, None)])
-    y = _t(g[f"spmv{i}_out0"])
-    op.matvec(0.0, _t(g[f"spmv{i}_x"]), y, alpha=0.5j, beta=1.0, lanes=lanes)
-    np.testing.assert_allclose(y.cpu().numpy(), g[f"spmv{i}_res"], rtol=1e-13, atol=1e-13)
+    cands = op.candidates()
+    assert any(c[0] == "staged" for c in cands)
+    for cand in cands:
+        op.set_launch(cand)
+        y = _t(g[f"spmv{i}_out0"])
+        op.matvec(0.0, _t(g[f"spmv{i}_x"]), y, alpha=0.5j, beta=1.0)
+        np.testing.assert_allclose(y.cpu().numpy(), g[f"spmv{i}_res"], rtol=1e-13, atol=1e-13,
+                                   err_msg=str(cand))
+
+
+def test_staged_tiles_cover_many_tiles_and_groups(dev):
+    """A multi-tile, two-group operator: every launch shape equals the scipy result."""
+    from qutip_gb300 import systems as S
+    from qutip_gb300.operator import DeviceOperator
+    s = S.ising_chain(6)
+    rng = np.random.default_rng(5)
+    for dt, tol in (("c128", 1e-12), ("c64", 2e-5)):
+        op = DeviceOperator(s.terms, dtype=dt)
+        assert len(op._tiles[2048]) > 10
+        x = rng.normal(size=op.n_cols) + 1j * rng.normal(size=op.n_cols)
+        want = sum((m * (1 if c is None else c(0.9))) @ x for m, c in s.terms)
+        xt = _t(x, torch.complex128 if dt == "c128" else torch.complex64)
+        for cand in op.candidates():
+            op.set_launch(cand)
+            y = torch.zeros(op.n_rows, dtype=xt.dtype, device="cuda")
+            op.matvec(0.9, xt, y)
+            np.testing.assert_allclose(y.cpu().numpy(), want, rtol=tol, atol=tol * np.abs(want).max(),
+                                       err_msg=f"{dt} {cand}")
+    from qutip_gb300 import _lib
+    assert _lib.load().qg_device_fault() == 0
 
 
 @pytest.mark.parametrize("i", [0, 1, 2])
@@ -44,6 +70,7 @@ def test_spmv_c64_error_bound(dev, i):
     n = len(g[f"spmv{i}_x"])
     A = sp.csr_matrix((g[f"spmv{i}_data"], g[f"spmv{i}_indices"], g[f"spmv{i}_indptr"]), shape=(n, n))
     op = DeviceOperator([(A, None)], dtype="c64")
+    op.tune()
     x = g[f"spmv{i}_x"]
     y = torch.zeros(n, dtype=torch.complex64, device="cuda")
     op.matvec(0.0, _t(x, torch.complex64), y)
