@@ -40,7 +40,8 @@ typedef enum {
   QG_OUTSIDE_RANGE = -3,
   QG_NOT_INITIATED = -4,
   QG_NORM_SEARCH_FAILED = -5, /* jump-time search exhausted (qutip/solver/mcsolve.py:363-367) */
-  QG_TIMEOUT = -6             /* cancelled through the host-visible cancel flag */
+  QG_TIMEOUT = -6,            /* cancelled through the host-visible cancel flag */
+  QG_JUMP_OVERFLOW = -7       /* more jumps than the batch's max_jumps */
 } qg_status;
 
 /* A sum of CSR matrices with time-dependent coefficients,
@@ -57,10 +58,17 @@ typedef enum {
  * [tile_row[t], tile_row[t+1]) holding at most tile_nnz - 8 entries and at most
  * QG_TILE_ROWS rows; col, val and row_ptr must then be readable for 8 entries
  * past their end (bulk copies are rounded to 16-byte units).
+ * QG_LAYOUT_SLICED (sliced ELLPACK, 32-row slices): slice s holds rows
+ *   [32 s, 32 s + 32); row_ptr[s] is the entry offset of the slice (n_slices + 1
+ *   values, n_slices = n_tiles) and tile_row[s*G + g] the width of group g in that
+ *   slice; entry j of group g of the row at lane l sits at
+ *   row_ptr[s] + 32 * (sum_{g'<g} width_g') + 32 j + l.  Padding entries have
+ *   value 0 and a valid column.  One thread per row; lanes and tile_nnz unused.
  * Coefficient programs are the bytecode of qutip_gb300/coefficients.py;
  * coef_code == NULL means every c_g = 1. */
 #define QG_LAYOUT_GROUP_MAJOR 0
 #define QG_LAYOUT_ROW_MAJOR 1
+#define QG_LAYOUT_SLICED 2
 #define QG_TILE_ROWS 512
 typedef struct qg_csr_groups {
   int64_t n_rows;
@@ -128,6 +136,10 @@ typedef struct qg_state_view {
 /* ---- library ---------------------------------------------------------- */
 int qg_version(void);
 const char* qg_last_error(void);
+/* sizeof of the ABI structs, in this order: qg_csr_groups, qg_dia, qg_rk_buffers,
+ * qg_state_view, qg_batch_system, qg_batch_item, qg_batch (host only; lets a
+ * binding check its struct layouts).  Returns the number written. */
+int qg_abi_sizes(int64_t* out, int n);
 /* Number of doubles the scratch buffer of qg_rk_buffers / reductions needs. */
 int64_t qg_scratch_doubles(void);
 /* Copy the compiled-in Vern7 tableau (host memory, no GPU needed):
@@ -196,6 +208,92 @@ int qg_expect_dm(const qg_csr_groups* ops, int64_t d, const qg_state_view* rho, 
 /* out[2g..] = <psi|op_g|psi>, out[2G..] = <psi|psi>.  Replaces
  * _expect_csr_dense_ket (qutip/core/data/expect.pyx:133-144). */
 int qg_expect_ket(const qg_csr_groups* ops, const qg_state_view* psi, double* out, void* stream);
+
+/* ---- batched, persistent solves ----------------------------------------- */
+/* One system of a batch.  Its generator is a row-major grouped CSR in the
+ * operator pools (rows r: row_ptr[rp_off + r*G + g], absolute entry offsets);
+ * kind 0 = master equation on a column-stacked density matrix (n = d*d),
+ * kind 1 = Monte-Carlo trajectory of a ket (n = d) with the effective
+ * non-Hermitian generator and n_cops collapse operators. */
+typedef struct qg_batch_system {
+  int32_t n;         /* state length */
+  int32_t d;         /* Hilbert-space dimension */
+  int32_t n_groups;  /* generator coefficient groups */
+  int32_t n_eops;    /* e_ops (CSR d x d, group-major, one group each) */
+  int64_t rp_off;    /* generator row pointers in op_rp */
+  int64_t coef_off;  /* n_groups+1 program starts in coef_start (-1: constant generator) */
+  int64_t eop_rp_off;  /* e_op e row r: eop_rp[eop_rp_off + e*(d+1) + r] */
+  int64_t cop_rp_off;  /* collapse op c row r: cop_rp[cop_rp_off + c*(d+1) + r] */
+  int64_t tlist_off; /* n_out output times in tlist */
+  int32_t n_out;
+  int32_t kind;
+  int32_t n_cops;
+  int32_t nsteps;    /* maximum steps per output interval (reference option nsteps) */
+  double atol, rtol;
+} qg_batch_system;
+
+/* One unit of work: a system solved from an initial state, or one trajectory
+ * of an MC system with its own PCG64 stream (state and increment as 128-bit
+ * pairs, numpy's PCG64 state after seeding). */
+typedef struct qg_batch_item {
+  int32_t system;
+  int32_t pad_;
+  int64_t y0_off;   /* initial state (complex128) in y0 */
+  int64_t out_off;  /* n_out * (n_eops+1) complex128 results in out */
+  uint64_t rng_state_hi, rng_state_lo, rng_inc_hi, rng_inc_lo;
+} qg_batch_item;
+
+typedef struct qg_batch {
+  int32_t n_systems;
+  int32_t n_items;
+  int32_t dtype;     /* generator / stage dtype; the state is complex128 */
+  int32_t max_n;     /* largest state length (workspace per slot) */
+  const qg_batch_system* systems; /* device */
+  const qg_batch_item* items;     /* device; processed in this order */
+  const int32_t* op_rp;
+  const int32_t* op_col;
+  const void* op_val;
+  const int32_t* coef_code;
+  const int32_t* coef_start;
+  const double* coef_consts;
+  const int32_t* eop_rp;
+  const int32_t* eop_col;
+  const double* eop_val;  /* complex128 pairs */
+  const int32_t* cop_rp;
+  const int32_t* cop_col;
+  const double* cop_val;  /* complex128 pairs */
+  const double* tlist;
+  const double* y0;       /* complex128 pairs */
+  double* out;            /* e_op values (complex128 pairs); the last slot per output is
+                             tr(rho) (kind 0) or <psi|psi> (kind 1, after normalisation) */
+  int32_t* status;        /* [n_items * 4]: qg_status, steps, rhs calls, jumps */
+  double* jump_t;         /* [n_items * max_jumps] */
+  int32_t* jump_which;    /* [n_items * max_jumps] */
+  int32_t max_jumps;
+  int32_t n_slots;        /* CTAs; each owns one workspace slot */
+  void* work;             /* n_slots * qg_batch_slot_bytes(max_n, dtype) bytes */
+  unsigned int* queue;    /* two words, zero before the launch; left zero */
+  const volatile int32_t* cancel; /* optional host-visible flag; non-zero stops all items */
+  int32_t norm_steps;     /* MC options (qutip/solver/mcsolve.py:449-466) */
+  int32_t pad_;
+  double norm_t_tol, norm_tol, norm_min_step, mc_corr_eps;
+} qg_batch;
+
+/* Workspace bytes of one slot. */
+int64_t qg_batch_slot_bytes(int64_t max_n, int dtype);
+/* Resident CTAs (useful n_slots) on the current device for this max_n / dtype;
+ * negative QG_ERR_* on failure. */
+int qg_batch_max_slots(int64_t max_n, int dtype);
+
+/* Solve every item of the batch in one persistent launch: each CTA takes items
+ * from an atomic queue and runs the adaptive Vern7 integration of
+ * Explicit_RungeKutta (qutip/solver/integrator/explicit_rk.pyx:278-467) with
+ * its own step size, writing expectation values at the output times as
+ * Result.add does (qutip/solver/solver_base.py:138-157, qutip/core/expect.py:91).
+ * kind-1 items run MCIntegrator's jump loop (qutip/solver/mcsolve.py:286-406):
+ * norm check after each step, log-ratio bisection of the jump time on the
+ * dense output, collapse choice and PCG64 draws in the reference's order. */
+int qg_batch_vern7(const qg_batch* B, void* stream);
 
 #ifdef __cplusplus
 }

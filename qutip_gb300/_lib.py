@@ -17,7 +17,7 @@ QG_C128, QG_C64 = 0, 1
 QG_MAX_GROUPS, QG_MAX_EOPS = 8, 32
 
 
-QG_LAYOUT_GROUP_MAJOR, QG_LAYOUT_ROW_MAJOR = 0, 1
+QG_LAYOUT_GROUP_MAJOR, QG_LAYOUT_ROW_MAJOR, QG_LAYOUT_SLICED = 0, 1, 2
 QG_TILE_ROWS = 512
 
 
@@ -70,6 +70,10 @@ _SIGS = {
                            C.c_void_p]),
     "qg_expect_dm": (C.c_int, [_P(CsrGroups), C.c_int64, _P(StateView), C.c_void_p, C.c_void_p]),
     "qg_expect_ket": (C.c_int, [_P(CsrGroups), _P(StateView), C.c_void_p, C.c_void_p]),
+    "qg_abi_sizes": (C.c_int, [C.c_void_p, C.c_int]),
+    "qg_batch_slot_bytes": (C.c_int64, [C.c_int64, C.c_int]),
+    "qg_batch_max_slots": (C.c_int, [C.c_int64, C.c_int]),
+    "qg_batch_vern7": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
 
 _lib = None
@@ -78,7 +82,7 @@ _lib = None
 # benchmark can report how many of this library's kernels ran in a timed region.
 COMPUTE_ENTRY_POINTS = {
     "qg_spmv_csr", "qg_spmm_csr", "qg_spmv_dia", "qg_vern7_stage", "qg_rk_combine", "qg_norm2",
-    "qg_expect_dm", "qg_expect_ket",
+    "qg_expect_dm", "qg_expect_ket", "qg_batch_vern7",
 }
 LAUNCHES = [0]
 

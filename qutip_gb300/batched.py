@@ -1,0 +1,366 @@
+"""Batched, persistent solves: many small systems or trajectories in one launch.
+
+The reference runs one solve per call (``Solver.run``, qutip/solver/solver_base.py:159-226)
+and maps trajectories over a Python loop or a process pool
+(``MultiTrajSolver.run``, qutip/solver/multitraj.py:169-258; ``parallel_map``,
+qutip/solver/parallel.py:267-338).  Here every system's generator, e_ops and
+collapse operators are packed into shared device pools; each *item* (a
+master-equation solve, or one Monte-Carlo trajectory with its own PCG64 stream)
+is an entry of an item table, and ``qg_batch_vern7`` runs all of them in one
+persistent launch, one CTA per item at a time, each with its own adaptive step.
+
+Trajectories reuse their system's operators (one copy in HBM however many
+trajectories run).  Per-trajectory random streams are numpy's PCG64 states
+after seeding, so the device draws the same numbers as
+``numpy.random.default_rng(seed)`` (qutip/solver/multitraj.py:382-393).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+from . import _lib
+from .coefficients import pack_programs
+from .operator import row_major_layout, stream_ptr
+from .systems import OpenSystem, merge_terms
+
+__all__ = ["BatchProblem", "mesolve_batch", "mcsolve_batch", "MCResult", "pcg_state_of"]
+
+SYSTEM_DTYPE = np.dtype([("n", "<i4"), ("d", "<i4"), ("n_groups", "<i4"), ("n_eops", "<i4"),
+                         ("rp_off", "<i8"), ("coef_off", "<i8"), ("eop_rp_off", "<i8"),
+                         ("cop_rp_off", "<i8"), ("tlist_off", "<i8"), ("n_out", "<i4"),
+                         ("kind", "<i4"), ("n_cops", "<i4"), ("nsteps", "<i4"),
+                         ("atol", "<f8"), ("rtol", "<f8")], align=True)
+ITEM_DTYPE = np.dtype([("system", "<i4"), ("pad", "<i4"), ("y0_off", "<i8"), ("out_off", "<i8"),
+                       ("sh", "<u8"), ("sl", "<u8"), ("ih", "<u8"), ("il", "<u8")], align=True)
+
+
+class BatchStruct(C.Structure):
+    _fields_ = [("n_systems", C.c_int32), ("n_items", C.c_int32), ("dtype", C.c_int32),
+                ("max_n", C.c_int32), ("systems", C.c_void_p), ("items", C.c_void_p),
+                ("op_rp", C.c_void_p), ("op_col", C.c_void_p), ("op_val", C.c_void_p),
+                ("coef_code", C.c_void_p), ("coef_start", C.c_void_p),
+                ("coef_consts", C.c_void_p), ("eop_rp", C.c_void_p), ("eop_col", C.c_void_p),
+                ("eop_val", C.c_void_p), ("cop_rp", C.c_void_p), ("cop_col", C.c_void_p),
+                ("cop_val", C.c_void_p), ("tlist", C.c_void_p), ("y0", C.c_void_p),
+                ("out", C.c_void_p), ("status", C.c_void_p), ("jump_t", C.c_void_p),
+                ("jump_which", C.c_void_p), ("max_jumps", C.c_int32), ("n_slots", C.c_int32),
+                ("work", C.c_void_p), ("queue", C.c_void_p), ("cancel", C.c_void_p),
+                ("norm_steps", C.c_int32), ("pad_", C.c_int32), ("norm_t_tol", C.c_double),
+                ("norm_tol", C.c_double), ("norm_min_step", C.c_double),
+                ("mc_corr_eps", C.c_double)]
+
+
+MC_DEFAULTS = dict(norm_steps=25, norm_t_tol=1e-6, norm_tol=1e-4, norm_min_step=0.1,
+                   mc_corr_eps=1e-10)
+
+
+def pcg_state_of(seed) -> tuple[int, int]:
+    """numpy PCG64 (state, increment) of ``default_rng(seed)``."""
+    st = np.random.default_rng(seed).bit_generator.state["state"]
+    return int(st["state"]), int(st["inc"])
+
+
+def _split128(v: int):
+    return (v >> 64) & (2**64 - 1), v & (2**64 - 1)
+
+
+def _group_major(ops, d):
+    """CSR arrays of several d x d operators, one group each: rp[g*(d+1)+r]."""
+    rps, cols, vals, off = [], [], [], 0
+    for o in ops:
+        m = sp.csr_matrix(o, dtype=np.complex128)
+        m.sort_indices()
+        rps.append(m.indptr.astype(np.int64) + off)
+        cols.append(m.indices.astype(np.int32))
+        vals.append(m.data)
+        off += m.nnz
+    if not ops:
+        return np.zeros(0, np.int64), np.zeros(0, np.int32), np.zeros(0, np.complex128)
+    return np.concatenate(rps), np.concatenate(cols), np.concatenate(vals)
+
+
+@dataclass
+class MCResult:
+    times: np.ndarray
+    runs_expect: np.ndarray            # [n_eops, ntraj, n_t] (real parts for Hermitian e_ops)
+    expect: list
+    col_times: list
+    col_which: list
+    stats: dict = field(default_factory=dict)
+
+
+class BatchProblem:
+    """Host-side builder of the device pools and item table of one batched launch."""
+
+    def __init__(self, dtype: str = "c64", device="cuda"):
+        if dtype not in ("c64", "c128"):
+            raise TypeError("dtype must be 'c64' or 'c128'")
+        self.dtype = dtype
+        self.device = torch.device(device)
+        self.systems = []
+        self.items = []
+        self._op_rp, self._op_col, self._op_val = [], [], []
+        self._entries = 0
+        self._rp_len = 0
+        self._coef_code, self._coef_start, self._coef_consts = [], [], []
+        self._code_len = self._start_len = self._const_len = 0
+        self._eop_rp, self._eop_col, self._eop_val, self._eop_entries, self._eop_rp_len = [], [], [], 0, 0
+        self._cop_rp, self._cop_col, self._cop_val, self._cop_entries, self._cop_rp_len = [], [], [], 0, 0
+        self._tlist, self._tlist_len = [], 0
+        self._y0, self._y0_len = [], 0
+        self._out_len = 0
+        self.sys_info = []
+
+    def add_system(self, terms, e_ops, tlist, kind="me", c_ops=(), dim=None, atol=1e-8,
+                   rtol=1e-6, nsteps=1000) -> int:
+        """Register a generator (list of (matrix, coefficient)), its e_ops and tlist."""
+        terms = merge_terms(terms)
+        if len(terms) > _lib.QG_MAX_GROUPS:
+            raise ValueError(f"at most {_lib.QG_MAX_GROUPS} coefficient groups")
+        n = terms[0][0].shape[0]
+        d = dim if dim is not None else (int(round(np.sqrt(n))) if kind == "me" else n)
+        if kind == "me" and d * d != n:
+            raise ValueError("master-equation generators act on column-stacked d x d states")
+        mats = [m for m, _ in terms]
+        rp, col, val = row_major_layout(mats)
+        self._op_rp.append((rp + self._entries).astype(np.int64))
+        self._op_col.append(col)
+        self._op_val.append(val)
+        rp_off = self._rp_len
+        self._rp_len += len(rp)
+        self._entries += len(col)
+        coeffs = [c for _, c in terms]
+        if all(c is None for c in coeffs):
+            coef_off = -1
+        else:
+            code, starts, consts = pack_programs(coeffs)
+            # starts index the global code pool; constants are shifted inside the code
+            code = code.copy()
+            i = 0
+            while i < len(code):
+                if code[i] == 1:  # OP_CONST
+                    code[i + 1] += self._const_len // 2
+                    i += 1
+                i += 1
+            self._coef_code.append(code)
+            self._coef_start.append(starts + self._code_len)
+            self._coef_consts.append(consts)
+            coef_off = self._start_len
+            self._code_len += len(code)
+            self._start_len += len(starts)
+            self._const_len += len(consts)
+        e_rp, e_col, e_val = _group_major(e_ops, d)
+        self._eop_rp.append(e_rp + self._eop_entries)
+        self._eop_col.append(e_col)
+        self._eop_val.append(e_val)
+        eop_rp_off = self._eop_rp_len
+        self._eop_rp_len += len(e_rp)
+        self._eop_entries += len(e_col)
+        c_rp, c_col, c_val = _group_major(list(c_ops), d)
+        self._cop_rp.append(c_rp + self._cop_entries)
+        self._cop_col.append(c_col)
+        self._cop_val.append(c_val)
+        cop_rp_off = self._cop_rp_len
+        self._cop_rp_len += len(c_rp)
+        self._cop_entries += len(c_col)
+        tl = np.asarray(tlist, dtype=np.float64)
+        self._tlist.append(tl)
+        tlist_off = self._tlist_len
+        self._tlist_len += len(tl)
+        self.systems.append((n, d, len(terms), len(e_ops), rp_off, coef_off, eop_rp_off,
+                             cop_rp_off, tlist_off, len(tl), 0 if kind == "me" else 1,
+                             len(c_ops), int(nsteps), float(atol), float(rtol)))
+        self.sys_info.append(dict(n=n, d=d, kind=kind, n_eops=len(e_ops), n_out=len(tl),
+                                  nnz=len(col), tlist=tl))
+        return len(self.systems) - 1
+
+    def add_item(self, system: int, y0, seed=None) -> int:
+        info = self.sys_info[system]
+        y0 = np.asarray(y0, dtype=np.complex128).reshape(-1)
+        if y0.shape[0] != info["n"]:
+            raise ValueError(f"initial state of length {y0.shape[0]} for a system of size {info['n']}")
+        self._y0.append(y0)
+        y0_off = self._y0_len
+        self._y0_len += len(y0)
+        out_off = self._out_len
+        self._out_len += info["n_out"] * (info["n_eops"] + 1)
+        sh = sl = ih = il = 0
+        if seed is not None:
+            state, inc = seed if isinstance(seed, tuple) else pcg_state_of(seed)
+            sh, sl = _split128(state)
+            ih, il = _split128(inc)
+        self.items.append((system, 0, y0_off, out_off, sh, sl, ih, il))
+        return len(self.items) - 1
+
+    # -- device upload and launch --------------------------------------------
+    def _t(self, arrs, dtype, np_dtype, pad=8):
+        a = np.concatenate(arrs).astype(np_dtype) if arrs and sum(len(x) for x in arrs) else \
+            np.zeros(0, np_dtype)
+        a = np.concatenate([a, np.zeros(pad, np_dtype)])
+        return torch.from_numpy(a).to(self.device, dtype)
+
+    def build(self, max_jumps=0, mc_options=None, order=None, n_slots=None):
+        """Upload pools; ``order`` permutes the items (longest first balances the queue)."""
+        if not self.items:
+            raise ValueError("no items")
+        lib = _lib.load()
+        cdt = torch.complex64 if self.dtype == "c64" else torch.complex128
+        qdt = _lib.QG_C64 if self.dtype == "c64" else _lib.QG_C128
+        self.op_rp = self._t(self._op_rp, torch.int32, np.int64)
+        self.op_col = self._t(self._op_col, torch.int32, np.int32)
+        self.op_val = self._t(self._op_val, cdt, np.complex128)
+        self.coef_code = self._t(self._coef_code, torch.int32, np.int32)
+        self.coef_start = self._t(self._coef_start, torch.int32, np.int64)
+        self.coef_consts = self._t(self._coef_consts, torch.float64, np.float64)
+        self.eop_rp = self._t(self._eop_rp, torch.int32, np.int64)
+        self.eop_col = self._t(self._eop_col, torch.int32, np.int32)
+        self.eop_val = self._t(self._eop_val, torch.complex128, np.complex128)
+        self.cop_rp = self._t(self._cop_rp, torch.int32, np.int64)
+        self.cop_col = self._t(self._cop_col, torch.int32, np.int32)
+        self.cop_val = self._t(self._cop_val, torch.complex128, np.complex128)
+        self.tlist_d = self._t(self._tlist, torch.float64, np.float64)
+        self.y0_d = self._t(self._y0, torch.complex128, np.complex128)
+        sys_np = np.array(self.systems, dtype=SYSTEM_DTYPE)
+        items = list(self.items)
+        self.order = np.arange(len(items)) if order is None else np.asarray(order)
+        items = [items[i] for i in self.order]
+        item_np = np.array(items, dtype=ITEM_DTYPE)
+        self.systems_d = torch.from_numpy(sys_np.view(np.uint8).copy()).to(self.device)
+        self.items_d = torch.from_numpy(item_np.view(np.uint8).copy()).to(self.device)
+        n_items = len(items)
+        self.out = torch.zeros(max(self._out_len, 1), dtype=torch.complex128, device=self.device)
+        self.status = torch.zeros(4 * n_items, dtype=torch.int32, device=self.device)
+        self.max_jumps = int(max_jumps)
+        self.jump_t = torch.zeros(max(n_items * self.max_jumps, 1), dtype=torch.float64,
+                                  device=self.device)
+        self.jump_which = torch.zeros(max(n_items * self.max_jumps, 1), dtype=torch.int32,
+                                      device=self.device)
+        self.max_n = max(info["n"] for info in self.sys_info)
+        slots = lib.qg_batch_max_slots(self.max_n, qdt)
+        if slots < 0:
+            _lib.check(slots, "qg_batch_max_slots")
+        self.n_slots = int(min(n_items, slots if n_slots is None else n_slots))
+        slot_bytes = int(lib.qg_batch_slot_bytes(self.max_n, qdt))
+        self.work = torch.empty(self.n_slots * slot_bytes, dtype=torch.uint8, device=self.device)
+        self.queue = torch.zeros(4, dtype=torch.int32, device=self.device)
+        mc = {**MC_DEFAULTS, **(mc_options or {})}
+        p = lambda t: t.data_ptr()  # noqa: E731
+        self.struct = BatchStruct(
+            len(self.systems), n_items, qdt, self.max_n, p(self.systems_d), p(self.items_d),
+            p(self.op_rp), p(self.op_col), p(self.op_val), p(self.coef_code), p(self.coef_start),
+            p(self.coef_consts), p(self.eop_rp), p(self.eop_col), p(self.eop_val), p(self.cop_rp),
+            p(self.cop_col), p(self.cop_val), p(self.tlist_d), p(self.y0_d), p(self.out),
+            p(self.status), p(self.jump_t), p(self.jump_which), self.max_jumps, self.n_slots,
+            p(self.work), p(self.queue), None, int(mc["norm_steps"]), 0, float(mc["norm_t_tol"]),
+            float(mc["norm_tol"]), float(mc["norm_min_step"]), float(mc["mc_corr_eps"]))
+        return self
+
+    def set_cancel(self, host_flag_tensor):
+        """Point the kernel at a host-mapped int32 flag (pinned tensor); None clears it."""
+        self.struct.cancel = None if host_flag_tensor is None else host_flag_tensor.data_ptr()
+
+    def launch(self):
+        _lib.call("qg_batch_vern7", C.byref(self.struct), stream_ptr())
+
+    def results(self, normalize=True):
+        """Per item (original order): expect [n_out, n_eops], status row, jumps."""
+        out = self.out.cpu().numpy()
+        status = self.status.cpu().numpy().reshape(-1, 4)
+        jt = self.jump_t.cpu().numpy()
+        jw = self.jump_which.cpu().numpy()
+        inv = np.empty_like(self.order)
+        inv[self.order] = np.arange(len(self.order))
+        res = []
+        for i, it in enumerate(self.items):
+            k = inv[i]
+            info = self.sys_info[it[0]]
+            ne, no = info["n_eops"], info["n_out"]
+            raw = out[it[3]:it[3] + no * (ne + 1)].reshape(no, ne + 1)
+            vals = raw[:, :ne]
+            if normalize:
+                vals = vals / raw[:, ne:ne + 1]
+            st = status[k]
+            nj = int(st[3])
+            res.append(dict(expect=vals, norm=raw[:, ne], status=int(st[0]), steps=int(st[1]),
+                            rhs=int(st[2]), jumps=nj,
+                            col_times=jt[k * self.max_jumps:k * self.max_jumps + min(nj, self.max_jumps)].copy(),
+                            col_which=jw[k * self.max_jumps:k * self.max_jumps + min(nj, self.max_jumps)].copy()))
+        return res
+
+
+STATUS_TEXT = {
+    -1: "Too much work done in one call. Try to increase the nsteps parameter or increasing "
+        "the tolerance.",
+    -2: "Step size becomes too small. Try increasing tolerance.",
+    -3: "Step outside available range.",
+    -5: "Could not find the collapse time within desired tolerance. Increase accuracy of the "
+        "ODE solver or lower the tolerance with the options 'norm_steps', 'norm_tol', "
+        "'norm_t_tol'.",
+    -6: "Cancelled.",
+    -7: "More jumps than max_jumps.",
+}
+
+
+def check_status(res):
+    for r in res:
+        if r["status"] < 0:
+            if r["status"] == -5:
+                raise RuntimeError(STATUS_TEXT[-5])
+            raise RuntimeError(STATUS_TEXT.get(r["status"], f"status {r['status']}"))
+
+
+def mesolve_batch(systems, tlists, precision="mixed", atol=1e-8, rtol=1e-6, nsteps=1000):
+    """Solve many master equations in one persistent launch.
+
+    ``systems`` are :class:`~qutip_gb300.systems.OpenSystem` of kind ``"me"``;
+    ``precision`` ``"mixed"`` (complex64 generator and stages, FP64 state and
+    control) or ``"double"``.  Returns one expect array list per system.
+    """
+    dt = "c64" if precision == "mixed" else "c128"
+    bp = BatchProblem(dt)
+    tlists = tlists if isinstance(tlists, (list, tuple)) else [tlists] * len(systems)
+    for s, tl in zip(systems, tlists):
+        sid = bp.add_system(s.terms, s.e_ops, tl, "me", atol=atol, rtol=rtol, nsteps=nsteps)
+        bp.add_item(sid, s.state0)
+    cost = [bp.sys_info[it[0]]["nnz"] for it in bp.items]
+    bp.build(order=np.argsort(cost)[::-1])
+    bp.launch()
+    res = bp.results()
+    check_status(res)
+    return [[r["expect"][:, k] for k in range(r["expect"].shape[1])] for r in res], res
+
+
+def mcsolve_batch(system: OpenSystem, tlist, ntraj, seeds=None, precision="mixed", atol=1e-8,
+                  rtol=1e-6, nsteps=1000, max_jumps=512, mc_options=None) -> MCResult:
+    """All ``ntraj`` trajectories of one Monte-Carlo system in one persistent launch.
+
+    ``seeds``: an int / SeedSequence (spawned like the reference's ``_read_seed``,
+    qutip/solver/multitraj.py:354-374) or a list of per-trajectory seeds.
+    """
+    if system.kind != "mc":
+        raise ValueError("mcsolve_batch needs a system built with kind='mc'")
+    if seeds is None or not isinstance(seeds, (list, tuple)):
+        ss = seeds if isinstance(seeds, np.random.SeedSequence) else np.random.SeedSequence(seeds)
+        seeds = ss.spawn(ntraj)
+    dt = "c64" if precision == "mixed" else "c128"
+    bp = BatchProblem(dt)
+    sid = bp.add_system(system.terms, system.e_ops, tlist, "mc", c_ops=system.c_ops,
+                        atol=atol, rtol=rtol, nsteps=nsteps)
+    for i in range(ntraj):
+        bp.add_item(sid, system.state0, seed=seeds[i])
+    t0 = time.perf_counter()
+    bp.build(max_jumps=max_jumps, mc_options=mc_options)
+    bp.launch()
+    res = bp.results()
+    check_status(res)
+    runs = np.stack([r["expect"].T for r in res], axis=1)  # [n_eops, ntraj, n_t]
+    return MCResult(np.asarray(tlist), runs, [runs[k].mean(axis=0) for k in range(runs.shape[0])],
+                    [r["col_times"] for r in res], [r["col_which"] for r in res],
+                    {"run time": time.perf_counter() - t0, "steps": sum(r["steps"] for r in res),
+                     "rhs": sum(r["rhs"] for r in res)})

@@ -133,7 +133,7 @@ __device__ __forceinline__ cplx c_sinh(cplx z) {
 // Evaluate one program at time t.  Programs are validated on the host (stack
 // depth <= COEF_STACK); the interpreter additionally clamps the stack index so a
 // malformed program cannot write outside its frame.
-__device__ inline cplx eval_coef(const int* code, const double* consts, double t) {
+static __device__ __noinline__ cplx eval_coef(const int* code, const double* consts, double t) {
   cplx st[COEF_STACK];
   int sp = 0;
   for (int pc = 0; pc < 4096; ++pc) {

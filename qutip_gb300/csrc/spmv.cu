@@ -473,6 +473,64 @@ __global__ void __launch_bounds__(BLOCK)
   }
 }
 
+// ------------------------------------------------------------ sliced kernel --
+// Sliced ELLPACK: a warp owns a 32-row slice, one thread per row.  Entry j of
+// every row in the slice is adjacent in memory, so each load instruction reads
+// 32 consecutive values / column indices (256 B / 128 B), and with entries
+// ordered by (col XOR row) the gathered x entries of a warp fall in the same few
+// lines.  Four entries per thread are kept in flight.
+template <int DT, int YDT, int EPI>
+__global__ void __launch_bounds__(SPMV_BLOCK)
+    spmv_sliced_kernel(qg_csr_groups A, double t, const typename elem<DT>::T* __restrict__ x,
+                       AxpbyArgs ax, RkArgs rk) {
+  using ST = typename elem<DT>::T;
+  using R = typename elem<DT>::R;
+  __shared__ cx<R> coef[QG_MAX_GROUPS];
+  __shared__ double red[SPMV_BLOCK / 32];
+  load_coefs(A, t, coef);
+  __syncthreads();
+  const int G = A.n_groups;
+  const int n = (int)A.n_rows;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * SPMV_BLOCK + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * SPMV_BLOCK) >> 5;
+  const ST* __restrict__ val = static_cast<const ST*>(A.val);
+  const int* __restrict__ col = A.col;
+  R err_acc = 0;
+  for (int sl = warp; sl < A.n_tiles; sl += nwarps) {
+    int off = __ldg(A.row_ptr + sl) + lane;
+    const int row = sl * 32 + lane;
+    cx<R> acc{0, 0};
+    for (int g = 0; g < G; ++g) {
+      const int w = __ldg(A.tile_row + sl * G + g);
+      R ar = 0, ai = 0;
+      int j = 0;
+      for (; j + 4 <= w; j += 4) {
+        const ST v0 = ld_stream(val + off), v1 = ld_stream(val + off + 32),
+                 v2 = ld_stream(val + off + 64), v3 = ld_stream(val + off + 96);
+        const int c0 = ld_stream(col + off), c1 = ld_stream(col + off + 32),
+                  c2 = ld_stream(col + off + 64), c3 = ld_stream(col + off + 96);
+        const ST x0 = ld_gather(x + c0), x1 = ld_gather(x + c1), x2 = ld_gather(x + c2),
+                 x3 = ld_gather(x + c3);
+        cmac_any(ar, ai, v0, x0);
+        cmac_any(ar, ai, v1, x1);
+        cmac_any(ar, ai, v2, x2);
+        cmac_any(ar, ai, v3, x3);
+        off += 128;
+      }
+      for (; j < w; ++j) {
+        cmac_any(ar, ai, ld_stream(val + off), ld_gather(x + ld_stream(col + off)));
+        off += 32;
+      }
+      acc = cx_add(acc, cx_mul(coef[g], cx<R>{ar, ai}));
+    }
+    if (row < n) epilogue<DT, YDT, EPI>(row, acc, ax, rk, err_acc);
+  }
+  if constexpr (EPI == EPI_RK) {
+    if (rk.stage == RK_STEP - 1) finish_error<SPMV_BLOCK>(rk, (double)err_acc, red);
+  }
+}
+
 // ------------------------------------------------------------------ launch --
 // Opt `kernel` into `smem` bytes of dynamic shared memory and return its
 // resident blocks per SM.  The caller keeps one cache per kernel instantiation.
@@ -521,6 +579,15 @@ static int launch_any(cudaStream_t st, const qg_csr_groups& A, double t, const v
                       const AxpbyArgs& ax, const RkArgs& rk) {
   using ST = typename elem<DT>::T;
   const int lanes = A.lanes > 0 ? A.lanes : 4;
+  if (A.layout == QG_LAYOUT_SLICED) {
+    int64_t warps_needed = A.n_tiles;
+    int64_t blocks = (warps_needed * 32 + SPMV_BLOCK - 1) / SPMV_BLOCK;
+    int64_t cap = (int64_t)sm_count() * (2048 / SPMV_BLOCK);
+    if (cap > qg_scratch_doubles()) cap = qg_scratch_doubles();
+    const int grid = (int)(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
+    spmv_sliced_kernel<DT, YDT, EPI><<<grid, SPMV_BLOCK, 0, st>>>(A, t, (const ST*)x, ax, rk);
+    return check_launch("spmv_sliced_kernel");
+  }
   if (A.n_tiles > 0) {
     switch (lanes) {
       case 1: return launch_staged<DT, YDT, EPI, 1>(st, A, t, x, ax, rk);
@@ -563,9 +630,13 @@ static int check_groups(const qg_csr_groups* A) {
     return set_error(QG_ERR_ARG, "bad operator shape");
   if (A->dtype != QG_C128 && A->dtype != QG_C64)
     return set_error(QG_ERR_UNSUPPORTED, "operator dtype must be QG_C128 or QG_C64");
-  if (A->layout != QG_LAYOUT_GROUP_MAJOR && A->layout != QG_LAYOUT_ROW_MAJOR)
+  if (A->layout != QG_LAYOUT_GROUP_MAJOR && A->layout != QG_LAYOUT_ROW_MAJOR &&
+      A->layout != QG_LAYOUT_SLICED)
     return set_error(QG_ERR_ARG, "unknown row-pointer layout");
-  if (A->n_tiles > 0) {
+  if (A->layout == QG_LAYOUT_SLICED) {
+    if (!A->tile_row || A->n_tiles != (A->n_rows + 31) / 32)
+      return set_error(QG_ERR_ARG, "sliced layout needs n_tiles = ceil(n_rows/32) and widths");
+  } else if (A->n_tiles > 0) {
     if (A->layout != QG_LAYOUT_ROW_MAJOR || !A->tile_row)
       return set_error(QG_ERR_ARG, "tiles need the row-major layout and tile_row");
     if (A->tile_nnz != 2048 && A->tile_nnz != 4096)

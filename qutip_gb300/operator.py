@@ -69,6 +69,45 @@ def row_major_layout(mats):
     return rp, col, val
 
 
+def sliced_layout(mats, n_cols):
+    """Sliced ELLPACK (32-row slices) of coefficient groups.
+
+    Entries of each row and group are ordered by ``col XOR row``; in Kronecker-
+    structured Liouvillians entry j of every row then flips the same index bits,
+    so a warp's gathers land in the same few cache lines.  Returns
+    ``(slice_ptr[S+1], widths[S*G], col, val, padded_entries)``.
+    """
+    mats = [sp.csr_matrix(m, dtype=np.complex128) for m in mats]
+    n = mats[0].shape[0]
+    G = len(mats)
+    S = (n + 31) // 32
+    counts = np.zeros((S * 32, G), dtype=np.int64)
+    for g, m in enumerate(mats):
+        counts[:n, g] = np.diff(m.indptr)
+    widths = counts.reshape(S, 32, G).max(axis=1)                 # [S, G]
+    slice_size = 32 * widths.sum(axis=1)
+    slice_ptr = np.zeros(S + 1, dtype=np.int64)
+    np.cumsum(slice_size, out=slice_ptr[1:])
+    total = int(slice_ptr[-1])
+    # padding: value 0, column = the row's own index (clipped) so gathers stay coalesced
+    pos_slice = np.repeat(np.arange(S, dtype=np.int64), slice_size)
+    lane = (np.arange(total, dtype=np.int64) - slice_ptr[pos_slice]) % 32
+    col = np.minimum(pos_slice * 32 + lane, n_cols - 1).astype(np.int32)
+    val = np.zeros(total, dtype=np.complex128)
+    gprefix = np.concatenate([np.zeros((S, 1), np.int64), np.cumsum(widths, axis=1)[:, :-1]], 1)
+    for g, m in enumerate(mats):
+        rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(m.indptr))
+        key = m.indices.astype(np.int64) ^ rows
+        order = np.lexsort((key, rows))
+        ci, dv = m.indices[order], m.data[order]
+        q = np.arange(m.nnz, dtype=np.int64) - m.indptr[rows]
+        sl = rows // 32
+        dst = slice_ptr[sl] + 32 * (gprefix[sl, g] + q) + rows % 32
+        col[dst] = ci
+        val[dst] = dv
+    return slice_ptr, widths.reshape(-1).astype(np.int32), col, val, total
+
+
 def row_tiles(row_start, tile_nnz, max_rows):
     """Greedy row tiles holding at most ``tile_nnz - 8`` entries and ``max_rows`` rows.
 
@@ -101,7 +140,8 @@ class DeviceOperator:
 
     PAD = 8
 
-    def __init__(self, terms, dtype: str = "c128", device="cuda", merge: bool = True):
+    def __init__(self, terms, dtype: str = "c128", device="cuda", merge: bool = True,
+                 fmt: str = "auto"):
         if dtype not in _TORCH:
             raise TypeError(f"unsupported dtype {dtype!r}")
         terms = merge_terms(terms) if merge else [(sp.csr_matrix(o), c) for o, c in terms]
@@ -121,25 +161,38 @@ class DeviceOperator:
         self.coeffs = [c for _, c in terms]
         self.device = torch.device(device)
         G = len(terms)
-        mats = [op for op, _ in terms]
-        self.group_nnz = [int(sp.csr_matrix(m).nnz) for m in mats]
-        rp, col, val = row_major_layout(mats)
-        if len(col) >= 2**31 - 16 or self.n_rows * G >= 2**31 - 16:
-            raise ValueError("operators beyond 2^31 stored entries need 64-bit indices")
-        self.nnz = len(col)
+        mats = [sp.csr_matrix(op) for op, _ in terms]
+        self.group_nnz = [int(m.nnz) for m in mats]
+        self.nnz = sum(self.group_nnz)
+        if fmt == "auto":
+            fmt = self._choose_format(mats)
+        if fmt not in ("csr", "sliced"):
+            raise ValueError("fmt must be 'auto', 'csr' or 'sliced'")
+        self.fmt = fmt
         P = self.PAD
+        self._tiles = {}
+        if fmt == "sliced":
+            rp, widths, col, val, total = sliced_layout(mats, self.n_cols)
+            self.stored = total
+            self.slice_width = torch.from_numpy(widths).to(self.device)
+        else:
+            rp, col, val = row_major_layout(mats)
+            self.stored = len(col)
+            self.slice_width = None
+        if self.stored >= 2**31 - 16 or self.n_rows * G >= 2**31 - 16:
+            raise ValueError("operators beyond 2^31 stored entries need 64-bit indices")
         self.row_ptr = torch.zeros(len(rp) + P, dtype=torch.int32, device=self.device)
         self.row_ptr[:len(rp)] = torch.from_numpy(rp.astype(np.int32)).to(self.device)
-        self.col = torch.zeros(self.nnz + P, dtype=torch.int32, device=self.device)
-        self.col[:self.nnz] = torch.from_numpy(col).to(self.device)
-        self.val = torch.zeros(self.nnz + P, dtype=_TORCH[dtype], device=self.device)
-        self.val[:self.nnz] = torch.from_numpy(val).to(self.device, _TORCH[dtype])
-        row_start = rp[::G]
-        self._tiles = {}
-        for tn in (2048, 4096):
-            t = row_tiles(row_start, tn, _lib.QG_TILE_ROWS)
-            if t is not None:
-                self._tiles[tn] = torch.from_numpy(t).to(self.device)
+        self.col = torch.zeros(self.stored + P, dtype=torch.int32, device=self.device)
+        self.col[:self.stored] = torch.from_numpy(col).to(self.device)
+        self.val = torch.zeros(self.stored + P, dtype=_TORCH[dtype], device=self.device)
+        self.val[:self.stored] = torch.from_numpy(val).to(self.device, _TORCH[dtype])
+        if fmt == "csr":
+            row_start = rp[::G]
+            for tn in (2048, 4096):
+                t = row_tiles(row_start, tn, _lib.QG_TILE_ROWS)
+                if t is not None:
+                    self._tiles[tn] = torch.from_numpy(t).to(self.device)
         if all(c is None for c in self.coeffs):
             self.coef_code = self.coef_start = self.coef_consts = None
         else:
@@ -147,15 +200,31 @@ class DeviceOperator:
             self.coef_code = torch.from_numpy(code).to(self.device)
             self.coef_start = torch.from_numpy(starts).to(self.device)
             self.coef_consts = torch.from_numpy(consts).to(self.device)
+        layout = _lib.QG_LAYOUT_SLICED if fmt == "sliced" else _lib.QG_LAYOUT_ROW_MAJOR
         self.struct = _lib.CsrGroups(
-            self.n_rows, self.n_cols, G, _QG[dtype], _lib.QG_LAYOUT_ROW_MAJOR, 4, 0, 0,
+            self.n_rows, self.n_cols, G, _QG[dtype], layout, 4, 0, 0,
             _ptr(self.row_ptr), _ptr(self.col), _ptr(self.val), None, _ptr(self.coef_code),
             _ptr(self.coef_start), _ptr(self.coef_consts))
         self.set_launch(self.default_launch())
 
+    def _choose_format(self, mats) -> str:
+        """Sliced ELLPACK when its padding costs at most 15 % more entries, else CSR."""
+        n = self.n_rows
+        if n < 1024:
+            return "csr"
+        S = (n + 31) // 32
+        padded = 0
+        for m in mats:
+            c = np.zeros(S * 32, dtype=np.int64)
+            c[:n] = np.diff(m.indptr)
+            padded += 32 * int(c.reshape(S, 32).max(axis=1).sum())
+        return "sliced" if padded <= 1.15 * max(self.nnz, 1) else "csr"
+
     # -- launch shape ------------------------------------------------------
     def default_launch(self):
         """Staged tiles for short rows, a sub-warp per row otherwise (before tuning)."""
+        if self.fmt == "sliced":
+            return ("sliced", 0, 1)
         mean = self.nnz / max(self.n_rows, 1)
         tn = 4096 if self.dtype == "c64" else 2048
         if tn in self._tiles and mean <= 64:
@@ -167,7 +236,13 @@ class DeviceOperator:
 
     def set_launch(self, launch):
         kind, tile_nnz, lanes = launch
-        if kind == "staged":
+        if (kind == "sliced") != (self.fmt == "sliced"):
+            raise ValueError(f"launch {kind!r} does not match the {self.fmt!r} storage")
+        if kind == "sliced":
+            self.struct.n_tiles = (self.n_rows + 31) // 32
+            self.struct.tile_nnz = 0
+            self.struct.tile_row = self.slice_width.data_ptr()
+        elif kind == "staged":
             if tile_nnz not in self._tiles:
                 raise ValueError(f"no {tile_nnz}-entry tiling (a row is too long)")
             t = self._tiles[tile_nnz]
@@ -183,9 +258,13 @@ class DeviceOperator:
 
     def launch_desc(self) -> str:
         kind, tn, lanes = self.launch
+        if kind == "sliced":
+            return f"sliced(32-row slices, {self.stored / max(self.nnz, 1):.3f}x stored/nnz)"
         return f"{kind}(lanes={lanes}" + (f", tile_nnz={tn})" if kind == "staged" else ")")
 
     def candidates(self):
+        if self.fmt == "sliced":
+            return [("sliced", 0, 1)]
         out = [("direct", 0, l) for l in (1, 2, 4, 8, 16, 32)]
         for tn in sorted(self._tiles):
             out += [("staged", tn, l) for l in (1, 2, 4, 8, 16)]
@@ -214,8 +293,8 @@ class DeviceOperator:
     tune_lanes = tune
 
     def device_arrays(self):
-        return [t for t in (self.row_ptr, self.col, self.val, self.coef_code, self.coef_start,
-                            self.coef_consts) if t is not None]
+        return [t for t in (self.row_ptr, self.col, self.val, self.slice_width, self.coef_code,
+                            self.coef_start, self.coef_consts) if t is not None]
 
     def host_copy(self, pinned: bool = True):
         """Host copies of the device arrays (pinned), for end-to-end transfer timing."""
@@ -270,6 +349,8 @@ class DeviceOperator:
             raise TypeError("vector dtype must match the operator dtype")
         if X.dim() != 2 or X.shape[1] != self.n_cols or Y.shape != (X.shape[0], self.n_rows):
             raise ValueError("incompatible shapes")
+        if self.fmt != "csr":
+            raise TypeError("multi-vector products need the CSR storage (fmt='csr')")
         a, b = complex(alpha), complex(beta)
         _lib.call("qg_spmm_csr", C.byref(self.struct), float(t), X.data_ptr(), Y.data_ptr(),
                   X.shape[0], X.stride(0), a.real, a.imag, b.real, b.imag, stream_ptr())

@@ -36,3 +36,18 @@ def pcg_state(row):
                              "state": {"state": (row[0] << 64) | row[1], "inc": (row[2] << 64) | row[3]},
                              "has_uint32": 0, "uinteger": 0}
     return g
+
+
+def jump_records_match(got_t, got_w, g, tr):
+    """Same jump count and channels, each time inside the reference's own bisection
+    window (recorded per jump in the golden fixture)."""
+    o0, o1 = int(g["col_off"][tr]), int(g["col_off"][tr + 1])
+    want_t, want_w, win = g["col_times"][o0:o1], g["col_which"][o0:o1], g["col_window"][o0:o1]
+    if len(got_t) != len(want_t) or [int(w) for w in got_w] != [int(w) for w in want_w]:
+        return False
+    return bool(np.all(np.abs(np.asarray(got_t) - want_t) <= win))
+
+
+def jump_times_close(got_t, g, tr, tol=1e-6):
+    o0, o1 = int(g["col_off"][tr]), int(g["col_off"][tr + 1])
+    return len(got_t) == o1 - o0 and np.allclose(got_t, g["col_times"][o0:o1], rtol=tol, atol=tol)

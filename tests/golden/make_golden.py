@@ -173,7 +173,35 @@ def _bh_qobjs(cutoff, J=1.0, U=0.5, F=0.3, kappa=0.1):
     return H, c_ops, psi0, n
 
 
+def _hook_collapse_windows():
+    """Record, per recorded jump, the time window the reference's own bisection
+    tolerance allows: |norm^2(t) - target| < norm_tol * target around the jump,
+    with the slope of norm^2 taken from the initial bracket of the search
+    (qutip/solver/mcsolve.py:321-369)."""
+    import importlib
+    M = importlib.import_module("qutip.solver.mcsolve")
+    windows = []
+    find0, do0 = M.MCIntegrator._find_collapse_time, M.MCIntegrator._do_collapse
+
+    def find(self, norm_old, norm, t_prev, t_final):
+        slope = abs(norm_old - norm) / max(t_final - t_prev, 1e-300)
+        self._gold_window = (2 * self.options["norm_tol"] * self.target_norm / max(slope, 1e-300)
+                             + 2 * self.options["norm_t_tol"])
+        return find0(self, norm_old, norm, t_prev, t_final)
+
+    def do(self, t, state):
+        n0 = len(self.collapses)
+        do0(self, t, state)
+        if len(self.collapses) > n0:
+            windows.append(self._gold_window)
+
+    M.MCIntegrator._find_collapse_time = find
+    M.MCIntegrator._do_collapse = do
+    return windows, (M, find0, do0)
+
+
 def _mc_fixture(fname, H, c_ops, psi0, e_ops, tlist, ntraj, seed):
+    windows, undo = _hook_collapse_windows()
     ss = np.random.SeedSequence(seed)
     seeds = ss.spawn(ntraj)
     states = []
@@ -186,6 +214,8 @@ def _mc_fixture(fname, H, c_ops, psi0, e_ops, tlist, ntraj, seed):
                         options={"method": "vern7", "keep_runs_results": True,
                                  "progress_bar": False, "map": "serial"})
     wall = time.time() - t0
+    M, find0, do0 = undo
+    M.MCIntegrator._find_collapse_time, M.MCIntegrator._do_collapse = find0, do0
     col_t, col_w, col_off = [], [], [0]
     for tr in range(ntraj):
         col_t += list(res.col_times[tr])
@@ -195,7 +225,8 @@ def _mc_fixture(fname, H, c_ops, psi0, e_ops, tlist, ntraj, seed):
     Hd = _data.to(_data.CSR, H.data).as_scipy().tocsr()
     out = dict(tlist=tlist, seed=seed, ntraj=ntraj, pcg_state=np.array(states, dtype=np.uint64),
                col_times=np.array(col_t), col_which=np.array(col_w, dtype=np.int32),
-               col_off=np.array(col_off, dtype=np.int32), runs_expect=runs,
+               col_off=np.array(col_off, dtype=np.int32), col_window=np.array(windows),
+               runs_expect=runs,
                avg_expect=np.array([np.asarray(e) for e in res.expect]), wall=wall,
                psi0=psi0.full().ravel(), **_csr_arrays("H", Hd))
     for i, c in enumerate(c_ops):
@@ -210,6 +241,9 @@ def mc_fixtures():
     _mc_fixture("bh_mcsolve.npz", H, c_ops, psi0, n, np.linspace(0, 50, 501), 24, 20261203)
     H, c_ops, psi0, e_ops = _jc_qobjs(5, 2 * np.pi, 2 * np.pi, 2 * np.pi * 0.08, 0.3, 0.2)
     _mc_fixture("jc_mcsolve.npz", H, c_ops, psi0, e_ops, np.linspace(0, 20, 101), 32, 4242)
+    # a strongly driven, strongly damped trimer: several jumps per trajectory
+    H, c_ops, psi0, n = _bh_qobjs(4, F=1.0, kappa=0.5)
+    _mc_fixture("bh_jumpy_mcsolve.npz", H, c_ops, psi0, n, np.linspace(0, 10, 101), 32, 777)
 
 
 def pcg64():

@@ -1,0 +1,105 @@
+"""Batched persistent solves (one launch, many systems / trajectories) against the
+reference's golden results and against the single-system GPU path."""
+import numpy as np
+import pytest
+
+from conftest import csr_from, golden, jump_records_match, jump_times_close, pcg_state
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _close(got, want, atol=1e-8, rtol=1e-6):
+    got, want = np.asarray(got), np.asarray(want)
+    assert np.all(np.abs(got - want) <= atol + rtol * np.abs(want)), np.abs(got - want).max()
+
+
+@pytest.mark.parametrize("precision,atol", [("double", 1e-8), ("mixed", 2e-6)])
+def test_batched_jc_config1_matches_reference(precision, atol):
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import mesolve_batch
+    g = golden("jc_mesolve.npz")
+    s = S.jaynes_cummings()
+    ex, res = mesolve_batch([s, s, s], g["tlist"], precision=precision)
+    for e in ex:
+        for k in range(2):
+            _close(e[k].real, g["expect"][k], atol=atol)
+    assert res[0]["steps"] >= len(g["step_ends"])
+
+
+def test_mixed_sizes_alone_equals_in_the_mix():
+    """Each system of a mixed-size batch gives the result it gives when solved alone."""
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import mesolve_batch
+    tl = np.linspace(0, 4, 21)
+    systems = [S.jaynes_cummings(n_cav=n, g=2 * np.pi * (0.02 + 0.01 * n), kappa=0.01 * n,
+                                 gamma=0.02) for n in (3, 7, 12, 5)] + [S.ising_chain(3),
+                                                                      S.ising_chain(4)]
+    for prec in ("double", "mixed"):
+        mix, _ = mesolve_batch(systems, tl, precision=prec)
+        for i, s in enumerate(systems):
+            alone, _ = mesolve_batch([s], tl, precision=prec)
+            for k in range(len(s.e_ops)):
+                np.testing.assert_array_equal(mix[i][k], alone[0][k])
+
+
+def test_batched_ising_td_matches_reference():
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import mesolve_batch
+    g = golden("ising_L4_mesolve.npz")
+    ex, _ = mesolve_batch([S.ising_chain(4)], g["tlist"], precision="double")
+    for k in range(4):
+        _close(ex[0][k].real, g["expect"][k])
+
+
+def _mc_golden(name, build, precision):
+    from qutip_gb300.batched import mcsolve_batch
+    g = golden(name)
+    s = build()
+    ntraj = int(g["ntraj"])
+    seeds = []
+    for tr in range(ntraj):
+        row = [int(v) for v in g["pcg_state"][tr]]
+        seeds.append(((row[0] << 64) | row[1], (row[2] << 64) | row[3]))
+    r = mcsolve_batch(s, g["tlist"], ntraj, seeds=seeds, precision=precision)
+    same = sum(jump_records_match(r.col_times[tr], r.col_which[tr], g, tr) for tr in range(ntraj))
+    for tr in range(ntraj):
+        if jump_times_close(r.col_times[tr], g, tr):
+            _close(r.runs_expect[:, tr, :].real, g["runs_expect"][:, tr, :], atol=1e-5, rtol=1e-5)
+    return g, r, same, ntraj
+
+
+MC_CASES = {
+    "bh_mcsolve.npz": lambda S: S.bose_hubbard_trimer(8),
+    "bh_jumpy_mcsolve.npz": lambda S: S.bose_hubbard_trimer(4, F=1.0, kappa=0.5, kind="mc"),
+    "jc_mcsolve.npz": lambda S: S.jaynes_cummings(5, g=2 * np.pi * 0.08, kappa=0.3, gamma=0.2,
+                                                  kind="mc"),
+}
+
+
+@pytest.mark.parametrize("name", sorted(MC_CASES))
+def test_mc_jump_records_identical_double(name):
+    """complex128: every trajectory has the reference's jump count and channels, each
+    jump time inside the reference's own bisection window."""
+    from qutip_gb300 import systems as S
+    g, r, same, ntraj = _mc_golden(name, lambda: MC_CASES[name](S), "double")
+    assert same == ntraj
+
+
+@pytest.mark.parametrize("name", sorted(MC_CASES))
+def test_mc_mixed_precision_jump_records(name):
+    """complex64 stages: jump records match for the vast majority of trajectories;
+    the averaged expectations agree within statistical error."""
+    from qutip_gb300 import systems as S
+    g, r, same, ntraj = _mc_golden(name, lambda: MC_CASES[name](S), "mixed")
+    print(f"\n{name} mixed: {same}/{ntraj} identical jump records")
+    assert same >= int(0.75 * ntraj)
+    sem = g["runs_expect"].std(axis=1) / np.sqrt(ntraj)
+    diff = np.abs(r.runs_expect.real.mean(axis=1) - g["runs_expect"].mean(axis=1))
+    assert np.all(diff <= 5 * sem + 1e-3)

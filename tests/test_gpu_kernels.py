@@ -47,7 +47,7 @@ def test_staged_tiles_cover_many_tiles_and_groups(dev):
     s = S.ising_chain(6)
     rng = np.random.default_rng(5)
     for dt, tol in (("c128", 1e-12), ("c64", 2e-5)):
-        op = DeviceOperator(s.terms, dtype=dt)
+        op = DeviceOperator(s.terms, dtype=dt, fmt="csr")
         assert len(op._tiles[2048]) > 10
         x = rng.normal(size=op.n_cols) + 1j * rng.normal(size=op.n_cols)
         want = sum((m * (1 if c is None else c(0.9))) @ x for m, c in s.terms)
@@ -78,6 +78,35 @@ def test_spmv_c64_error_bound(dev, i):
     # FP32 accumulation: |err| <= ~nnz_row * eps32 * sum|a||x|
     bound = 8 * np.finfo(np.float32).eps * (abs(A) @ np.abs(x)) + 1e-30
     assert np.all(np.abs(y.cpu().numpy() - want) <= bound)
+
+
+@pytest.mark.parametrize("L", [5, 7])
+def test_sliced_layout_matches_scipy(dev, L):
+    """Sliced ELLPACK storage (32-row slices, XOR-ordered rows) for both dtypes and
+    both epilogues: AXPBY against scipy, and a Vern7 step against the CSR storage."""
+    from qutip_gb300 import systems as S
+    from qutip_gb300.operator import DeviceOperator
+    from qutip_gb300.vern7 import GpuVern7
+    s = S.ising_chain(L)
+    rng = np.random.default_rng(L)
+    x = rng.normal(size=4 ** L) + 1j * rng.normal(size=4 ** L)
+    want = sum((m * (1 if c is None else c(1.7))) @ x for m, c in s.terms)
+    for dt, tol in (("c128", 1e-12), ("c64", 2e-5)):
+        op = DeviceOperator(s.terms, dtype=dt, fmt="sliced")
+        assert op.launch[0] == "sliced" and op.stored >= op.nnz
+        xt = _t(x, torch.complex128 if dt == "c128" else torch.complex64)
+        y = _t(np.ones(op.n_rows), xt.dtype)
+        op.matvec(1.7, xt, y, alpha=2.0, beta=-1.0)
+        np.testing.assert_allclose(y.cpu().numpy(), 2 * want - 1, rtol=tol,
+                                   atol=tol * np.abs(want).max())
+    outs = []
+    for fmt in ("sliced", "csr"):
+        op = DeviceOperator(s.terms, dtype="c128", fmt=fmt)
+        ig = GpuVern7(op)
+        ig.set_initial_value(torch.from_numpy(s.state0).cuda(), 0.0)
+        ig.integrate(0.7)
+        outs.append(ig.get_state().cpu().numpy())
+    np.testing.assert_allclose(outs[0], outs[1], rtol=1e-12, atol=1e-14)
 
 
 def test_grouped_coefficients_match_scipy(dev):
