@@ -295,6 +295,27 @@ int qg_batch_max_slots(int64_t max_n, int dtype);
  * dense output, collapse choice and PCG64 draws in the reference's order. */
 int qg_batch_vern7(const qg_batch* B, void* stream);
 
+/* Size of the static workspace of qg_batch_vern7_noalloc (16 MiB per GPU). */
+#define QG_NOALLOC_WORK_BYTES (16u << 20)
+
+/* qg_batch_vern7 without any allocation -- no counterpart in the reference.
+ * For callers that cannot allocate device memory: a host framework that hands
+ * this library only pointers from its own memory pool and forbids allocations
+ * outside it, or a latency-critical service loop that must not take the
+ * synchronisation of cudaMalloc/cudaFree.  The caller still passes every input
+ * and output of qg_batch (pools, out, status, jump buffers); B->work, B->queue
+ * and B->n_slots are ignored.  The workspace is a 16 MiB static device array
+ * (QG_NOALLOC_WORK_BYTES) that every GPU using the library holds until the
+ * process exits; batches whose single slot (qg_batch_slot_bytes(max_n, dtype))
+ * does not fit are rejected with QG_ERR_ARG, and the number of concurrent items
+ * is what fits.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current), so make that first call
+ * before any stream capture.  All calls share the array and its queue words:
+ * calls that overlap on the GPU (different streams, or different host threads)
+ * race and corrupt each other; serialise them.  No cudaMalloc, cudaFree or
+ * allocating library routine is called. */
+int qg_batch_vern7_noalloc(const qg_batch* B, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

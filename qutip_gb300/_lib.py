@@ -74,6 +74,7 @@ _SIGS = {
     "qg_batch_slot_bytes": (C.c_int64, [C.c_int64, C.c_int]),
     "qg_batch_max_slots": (C.c_int, [C.c_int64, C.c_int]),
     "qg_batch_vern7": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "qg_batch_vern7_noalloc": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
 
 _lib = None
@@ -82,7 +83,7 @@ _lib = None
 # benchmark can report how many of this library's kernels ran in a timed region.
 COMPUTE_ENTRY_POINTS = {
     "qg_spmv_csr", "qg_spmm_csr", "qg_spmv_dia", "qg_vern7_stage", "qg_rk_combine", "qg_norm2",
-    "qg_expect_dm", "qg_expect_ket", "qg_batch_vern7",
+    "qg_expect_dm", "qg_expect_ket", "qg_batch_vern7", "qg_batch_vern7_noalloc",
 }
 LAUNCHES = [0]
 

@@ -16,6 +16,8 @@
 // shared memory, so all threads follow one control path.  Every loop is bounded:
 // steps per output (nsteps), bisection tries (norm_steps), jumps (max_jumps), a
 // host-visible cancel flag checked at each output time.
+#include <mutex>
+
 #include "capi_internal.h"
 #include "common.cuh"
 
@@ -802,6 +804,78 @@ __global__ void __launch_bounds__(BB) batch_vern7_kernel(qg_batch B) {
 }
 
 }  // namespace qg
+
+// ------------------------------------------------- allocation-free variant --
+// Workspace and queue words of qg_batch_vern7_noalloc.  Loading the library
+// reserves these on every GPU it is used on, until the process exits.
+namespace qg {
+constexpr size_t NOALLOC_WORK_BYTES = (size_t)QG_NOALLOC_WORK_BYTES;
+static __device__ __align__(256) unsigned char g_noalloc_work[NOALLOC_WORK_BYTES];
+static __device__ __align__(256) unsigned int g_noalloc_queue[4];
+
+// Device addresses of the arrays above, looked up once per device with that
+// device current (the host-side names are stand-ins, not device addresses).
+struct NoallocAddr {
+  void* work = nullptr;
+  unsigned int* queue = nullptr;
+};
+static NoallocAddr g_noalloc_addr[64];
+static std::mutex g_noalloc_mu;
+
+static int noalloc_setup(int dev, NoallocAddr& out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  NoallocAddr& a = g_noalloc_addr[dev];
+  if (!a.work) {
+    void* w = nullptr;
+    void* q = nullptr;
+    if (cudaGetSymbolAddress(&w, g_noalloc_work) != cudaSuccess || !w)
+      return set_error(QG_ERR_CUDA, "cudaGetSymbolAddress failed for the static workspace");
+    if (cudaGetSymbolAddress(&q, g_noalloc_queue) != cudaSuccess || !q)
+      return set_error(QG_ERR_CUDA, "cudaGetSymbolAddress failed for the static queue words");
+    a.work = w;
+    a.queue = static_cast<unsigned int*>(q);
+  }
+  out = a;
+  return QG_OK;
+}
+}  // namespace qg
+
+extern "C" int qg_batch_vern7_noalloc(const qg_batch* B, void* stream) {
+  if (!B || !B->systems || !B->items || !B->op_rp || !B->op_col || !B->op_val || !B->tlist ||
+      !B->y0 || !B->out || !B->status)
+    return set_error(QG_ERR_ARG, "null batch pointer");
+  if (B->dtype != QG_C128 && B->dtype != QG_C64)
+    return set_error(QG_ERR_UNSUPPORTED, "batch dtype must be QG_C128 or QG_C64");
+  if (B->n_items < 0 || B->max_n <= 0) return set_error(QG_ERR_ARG, "bad batch sizes");
+  if (B->max_jumps > 0 && (!B->jump_t || !B->jump_which))
+    return set_error(QG_ERR_ARG, "jump record buffers missing");
+  const int64_t slot = slot_layout(B->max_n, B->dtype).total;
+  if (slot > (int64_t)NOALLOC_WORK_BYTES)
+    return set_error(QG_ERR_ARG,
+                     "max_n too large: one workspace slot exceeds the static workspace "
+                     "(QG_NOALLOC_WORK_BYTES); use qg_batch_vern7 with caller-owned memory");
+  if (B->n_items == 0) return QG_OK;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return set_error(QG_ERR_CUDA, "no current CUDA device");
+  NoallocAddr a;
+  int rc = noalloc_setup(dev, a);
+  if (rc) return rc;
+  int occ = qg_batch_max_slots(B->max_n, B->dtype);
+  if (occ <= 0) return occ < 0 ? occ : set_error(QG_ERR_CUDA, "no resident CTA");
+  int64_t slots = (int64_t)NOALLOC_WORK_BYTES / slot;
+  if (slots > occ) slots = occ;
+  if (slots > B->n_items) slots = B->n_items;
+  qg_batch b = *B;
+  b.work = a.work;
+  b.queue = a.queue;
+  b.n_slots = (int32_t)slots;
+  cudaStream_t st = (cudaStream_t)stream;
+  // the queue words must start at zero (a previous launch leaves them zero; clear anyway)
+  if (cudaMemsetAsync(a.queue, 0, 4 * sizeof(unsigned int), st) != cudaSuccess)
+    return set_error(QG_ERR_CUDA, "clearing the static queue words failed");
+  return qg_batch_vern7(&b, stream);
+}
 
 extern "C" int64_t qg_batch_slot_bytes(int64_t max_n, int dtype) {
   return slot_layout(max_n, dtype).total;

@@ -13,7 +13,7 @@ from qutip_gb300 import coefficients as CF
 
 def _header_functions():
     src = open(os.path.join(ROOT, "include", "qutip_gb300.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(qg_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^(?:int|int64_t|const char\s*\*)\s*(qg_\w+)\s*\(", src, re.M)))
 
 
 def test_library_exports_every_declared_symbol():
