@@ -4,12 +4,17 @@ Ising chain, L = 10 spins (Hilbert dim 1024, Liouvillian dim 1,048,576,
 24.6 M stored entries in two coefficient groups), Vern7 atol 1e-8 / rtol 1e-6,
 tlist = linspace(0, 10, 101), 10 e_ops.
 
-One step = one complete solve.  ``value`` is solves/s with the operator already
-resident in HBM (the operator, 0.5 GB, is larger than L2, so no flush is
-needed); ``e2e`` repeats the solve through the host API with the operator and
+One step = one complete solve in the mixed form (complex64 generator and stages
+with FP32 accumulation; FP64 state, step control and expectation values), whose
+error against the complex128 solve is reported with it.  ``value`` is solves/s
+with the operator already resident in HBM (0.3 GB, larger than L2, so no flush
+is needed); ``e2e`` repeats the solve through the host API with the operator and
 initial state copied from pinned host memory every step and the expectation
-values read back.  The reported ``roofline`` is that of the fused Vern7 stage
-kernel (matvec + stage combination), timed with CUDA events on its stream.
+values read back.  ``roofline`` is that of the fused Vern7 stage kernel (sliced
+ELLPACK matvec + stage combination), timed with CUDA events on its stream.
+Also reported: the complex128 form, the served mixed-size Jaynes-Cummings stream
+(continuous batching vs the plain complex128 per-request drop-in) and the
+batched 4096-trajectory Bose-Hubbard mcsolve.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -37,7 +42,12 @@ WORKLOAD = f"ising_chain_L{N_SITES}_mesolve_vern7"
 CONFIG = {"workload": WORKLOAD, "n_sites": N_SITES, "hilbert_dim": 2 ** N_SITES,
           "liouvillian_dim": 4 ** N_SITES, "tlist": f"linspace(0,{T_END:g},{N_OUT})",
           "atol": 1e-8, "rtol": 1e-6, "e_ops": N_SITES, "h_seed": 1234,
-          "l2": "operator (0.5 GB) larger than L2; no flush"}
+          "l2": "operator (0.3 GB complex64) larger than L2; no flush"}
+
+
+def log(msg):
+    """Progress to stderr (the JSON result line goes to stdout)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
 
 
 def parse():
@@ -46,9 +56,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample", type=float, default=0.5,
+    ap.add_argument("--cpu-sample", type=float, default=0.3,
                     help="simulated time of the CPU-baseline sample (of 10.0)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="headline workload only")
+    ap.add_argument("--served-jobs", type=int, default=1000)
+    ap.add_argument("--served-ntraj", type=int, default=100)
+    ap.add_argument("--served-plain-sample", type=int, default=60)
+    ap.add_argument("--mc-ntraj", type=int, default=4096)
     ap.add_argument("--profile", default=None, choices=["stage"],
                     help="run a small profiling case only (Ising L=9: 262144 rows, 0.12 GB "
                          "operator): tuned matvecs then Vern7 steps; prints nothing to parse")
@@ -186,44 +201,43 @@ def run_reference(args, dist):
 
 
 # ------------------------------------------------------------------ ours ----
-def stage_bytes(op, n, stage, state_b, stage_b):
-    """Algorithmic HBM bytes of one fused Vern7 stage launch."""
+def stage_bytes(op, n, stage, mixed):
+    """Algorithmic HBM bytes of one fused Vern7 stage launch (see DESIGN section 4)."""
     from qutip_gb300 import vern7_tableau as T
-    b = op.nnz * (op.value_bytes() + 4) + op.n_groups * (n + 1) * 4  # operator
-    b += n * stage_b            # gathered vector x, read once
-    b += n * stage_b            # k_s written
-    b += n * state_b            # y_prev read
+    sk = op.value_bytes()                       # stage dtype (k, ytmp, x)
+    base = 8 if mixed else 16                   # y_prev_s (mixed) or y_prev
+    b = op.nnz * (sk + 4) + (op.n_groups * n + 1) * 4  # operator entries + row structure
+    b += n * sk                                 # gathered x, read once
+    b += n * sk                                 # k_s written
     if stage == T.RK_STEP - 1:
         used = [j for j in range(stage) if T.B[j] != 0 or T.E[j] != 0]
-        b += len(used) * n * stage_b + n * state_b  # k_j read, y_front written
+        b += len(used) * n * sk + 16 * n + 16 * n + (8 * n if mixed else 0)  # k_j, y_prev, y_front(+s)
     elif stage != T.RK_EXTRA_STEP - 1:
         row = T.A[stage + 1]
-        b += sum(n * stage_b for j in range(stage) if row[j] != 0) + n * stage_b  # k_j, ytmp
+        b += sum(n * sk for j in range(stage) if row[j] != 0) + n * base + n * sk  # k_j, base, next x
     return b
 
 
 def measure_stage_roofline(op, sysm, precision, reps=20):
     """Average duration and algorithmic GB/s of the fused stage kernel (events on its stream)."""
+    import ctypes as C
     import torch
+    from qutip_gb300 import _lib
+    from qutip_gb300.operator import stream_ptr
     from qutip_gb300.vern7 import GpuVern7
     ig = GpuVern7(op, precision=precision)
     ig.set_initial_value(torch.from_numpy(sysm.state0).cuda(), 0.0)
     ig.integrate(0.05, step=True)
-    state_b = 16 if ig.state_dt == "c128" else 8
-    stage_b = 16 if ig.stage_dt == "c128" else 8
-    total_bytes = sum(stage_bytes(op, ig.n, s, state_b, stage_b) for s in range(10))
+    total_bytes = sum(stage_bytes(op, ig.n, s, ig.mixed) for s in range(10))
     st = torch.cuda.current_stream()
     for _ in range(2):
         ig._compute_step(ig.dt_safe)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(st)
-    import ctypes as C
-    from qutip_gb300 import _lib
-    from qutip_gb300.operator import stream_ptr
     lib = _lib.load()
     rk = ig._rk()
     sp_ = stream_ptr()
+    torch.cuda.synchronize()
+    e0.record(st)
     for _ in range(reps):
         for s in range(10):
             _lib.check(lib.qg_vern7_stage(C.byref(op.struct), C.byref(rk), s, 0.0, ig.dt_safe,
@@ -252,6 +266,91 @@ def measure_spmv(op, reps=30):
     return ms, b, b / (ms * 1e-3) / 1e9
 
 
+def run_served(args):
+    """Served mixed-size Jaynes-Cummings stream: continuous batching (complex64 stages,
+    FP64 state) vs the plain complex128 per-request drop-in."""
+    import torch
+    from qutip_gb300.serving import (Server, build_job, fifo_latencies, jc_request_stream,
+                                     percentiles, solve_plain)
+    n = args.served_jobs
+    specs = jc_request_stream(n, rate=1.0, ntraj=args.served_ntraj, seed=2026)
+    jobs = [build_job(sp) for sp in specs]
+    log(f"served: {n} jobs built")
+    warm = [build_job(sp) for sp in specs[:8]]
+    Server("mixed").serve(warm, realtime=False)
+    # throughput: every job available at t = 0
+    srv = Server("mixed", launch_timeout=60.0)
+    _, wall = srv.serve(jobs, realtime=False)
+    thr = n / wall
+    log(f"served: throughput {thr:.1f} solves/s")
+    # latency at a Poisson rate of half the measured throughput
+    rate = 0.5 * thr
+    specs_r = jc_request_stream(n, rate=rate, ntraj=args.served_ntraj, seed=2026)
+    jobs_r = [build_job(sp) for sp in specs_r]
+    srv_r = Server("mixed", launch_timeout=60.0)
+    _, wall_r = srv_r.serve(jobs_r, realtime=True)
+    lat = percentiles([j.latency for j in jobs_r])
+    log(f"served: latency {lat}")
+    # plain complex128 per-request drop-in: measured service times on a sample
+    k = min(args.served_plain_sample, n)
+    service = []
+    for j in jobs[:k]:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        solve_plain(j, "double")
+        torch.cuda.synchronize()
+        service.append(time.perf_counter() - t0)
+    plain_thr = 1.0 / float(np.mean(service))
+    svc = [service[i % k] for i in range(n)]
+    plain_lat = percentiles(fifo_latencies([sp.arrival for sp in specs_r], svc))
+    # error of the served mixed form vs the plain complex128 solve on the sample's mesolve jobs
+    err = 0.0
+    for j in jobs[:k]:
+        if j.spec.kind == "me":
+            ref = solve_plain(j, "double")
+            err = max(err, max(float(np.max(np.abs(np.real(a) - np.real(b))))
+                               for a, b in zip(j.result, ref)))
+    n_me = sum(sp.kind == "me" for sp in specs)
+    return {
+        "workload": f"{n} Jaynes-Cummings jobs, N~U{{5..60}}, {n_me} mesolve / {n - n_me} mcsolve "
+                    f"(ntraj={args.served_ntraj}), tlist linspace(0,20,101), seed 2026",
+        "served_mixed": {"solves_per_sec": thr, "wall_s": wall, "launches": srv.stats["launches"],
+                         "latency_at_rate": {**lat, "rate_per_s": rate, "wall_s": wall_r,
+                                             "max_concurrent_launches": srv_r.stats["max_concurrent"]}},
+        "plain_c128": {"solves_per_sec": plain_thr, "service_sample_jobs": k,
+                       "latency_at_rate": {**plain_lat, "rate_per_s": rate,
+                                           "method": "measured service times, FIFO queue on the "
+                                                     "same arrivals"}},
+        "speedup_solves_per_sec": thr / plain_thr,
+        "speedup_p99": plain_lat["p99_ms"] / lat["p99_ms"],
+        "max_abs_err_vs_c128_expect": err,
+    }
+
+
+def run_mc_batch(args):
+    """Batched mcsolve of the dissipative Bose-Hubbard trimer, 4096 trajectories."""
+    import torch
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import mcsolve_batch
+    s = S.bose_hubbard_trimer(8)
+    tl = np.linspace(0.0, 50.0, 501)
+    mcsolve_batch(s, tl, 64, seeds=1, precision="mixed")
+    out = {}
+    for prec in ("mixed", "double"):
+        log(f"mc batch {prec}")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = mcsolve_batch(s, tl, args.mc_ntraj, seeds=20261203, precision=prec)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[prec] = {"trajectories_per_sec": args.mc_ntraj / dt, "wall_s": dt,
+                     "jumps": int(sum(len(c) for c in r.col_times)),
+                     "n_mean": [float(x.real.mean()) for x in r.expect]}
+    out["workload"] = (f"Bose-Hubbard trimer cutoff 8 (dim 512), {args.mc_ntraj} trajectories, "
+                       "tlist linspace(0,50,501), one persistent launch")
+    return out
+
+
 def run_ours(args, dist):
     import torch
     from qutip_gb300 import _lib
@@ -267,17 +366,23 @@ def run_ours(args, dist):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
 
+    log("building the Ising L=10 Liouvillian")
     sysm = S.ising_chain(N_SITES)
     tlist = np.linspace(0.0, T_END, N_OUT)
+    op64 = DeviceOperator(sysm.terms, dtype="c64")
+    op64.tune()
     op = DeviceOperator(sysm.terms, dtype="c128")
     op.tune()
     ex = ExpectOps(sysm.e_ops)
 
-    def solve(o=op, prec="double"):
+    def solve(o=op64, prec="mixed"):
         return solve_system(sysm, tlist, {"precision": prec}, op=o, ex=ex)
 
+    log("FP64 reference solve")
+    ref = solve(op, "double")  # FP64 result the mixed form is checked against
+    log("warm-up")
     for _ in range(args.warmup):
-        ref = solve()
+        solve()
     dist.barrier()
     clocks = ClockSampler(dist.local)
     clocks.start()
@@ -289,66 +394,74 @@ def run_ours(args, dist):
     e1.record()
     dist.barrier()
     ms = e0.elapsed_time(e1)
-    launches = (_lib.LAUNCHES[0] - n0) // max(args.steps, 1)
+    launches = _lib.LAUNCHES[0] - n0
     clk = clocks.stop()
     ms_max = dist.max(ms)
     value = args.steps * dist.world / (ms_max / 1000.0)
+    err_m = max(float(np.max(np.abs(res.expect[k] - ref.expect[k]))) for k in range(N_SITES))
 
+    log(f"headline {value:.3f} solves/s; end-to-end")
     # end to end: operator + initial state from pinned host memory every step, expect read back
-    host = op.host_copy()
+    host = op64.host_copy()
     h2d = sum(h.numel() * h.element_size() for h in host) + sysm.state0.nbytes
     d2h = N_OUT * 2 * (len(sysm.e_ops) + 1) * 8
     dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        op.upload(host)
+        op64.upload(host)
         solve()
     dist.barrier()
-    e2e_s = dist.max(time.perf_counter() - t0)
-    e2e = args.steps * dist.world / e2e_s
+    e2e = args.steps * dist.world / dist.max(time.perf_counter() - t0)
 
-    # mixed-precision form: complex64 operator/stages, FP64 state and control
-    op64 = DeviceOperator(sysm.terms, dtype="c64")
-    op64.tune()
-    resm = solve(op64, "mixed")
+    # complex128 form (the plain drop-in precision)
+    nd = max(1, args.steps // 2)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(max(1, args.steps // 2)):
-        resm = solve(op64, "mixed")
+    for _ in range(nd):
+        solve(op, "double")
     torch.cuda.synchronize()
-    mixed_v = max(1, args.steps // 2) / (time.perf_counter() - t0)
-    err_m = max(float(np.max(np.abs(resm.expect[k] - res.expect[k]))) for k in range(N_SITES))
+    double_v = nd / (time.perf_counter() - t0)
 
-    stage_ms, stage_b, stage_gbs = measure_stage_roofline(op, sysm, "double")
+    log("roofline measurements")
+    stage_ms, stage_b, stage_gbs = measure_stage_roofline(op64, sysm, "mixed")
+    stage128_ms, stage128_b, stage128_gbs = measure_stage_roofline(op, sysm, "double")
     spmv_ms, spmv_b, spmv_gbs = measure_spmv(op)
     spmv64_ms, spmv64_b, spmv64_gbs = measure_spmv(op64)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 stages / f64 state (mixed)",
+        "accuracy": {"max_abs_err_vs_fp64_expect": err_m, "bound": 1e-6,
+                     "fp64_reference": "the same solve in complex128 on the GPU, which matches "
+                                       "the reference QuTiP within atol 1e-8 / rtol 1e-6"},
         "data": "synthetic (seeded h_i ~ U[0.5,1.5], default_rng(1234))",
         "config": {**CONFIG, "parallelism": "replicas" if dist.world > 1 else "single",
-                   "spmv_launch": op.launch_desc()},
+                   "spmv_launch": op64.launch_desc()},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": int(launches * args.steps),
+        "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": stage_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": stage_gbs / hbm_peak, "traffic": None,
-                     "kernel": "spmv_groups_kernel<C128,RK> (fused Vern7 stage)",
+                     "kernel": "spmv_sliced_kernel<C64,C128,RK> (fused Vern7 stage, mixed)",
                      "bytes_per_launch": stage_b, "ms_per_launch": stage_ms,
-                     "peak_source": f"{peak_src} hbm_gbs"},
-        "spmv": {"c128_gbs": spmv_gbs, "c128_ms": spmv_ms, "c128_bytes": spmv_b,
-                 "c64_gbs": spmv64_gbs, "c64_ms": spmv64_ms, "c64_bytes": spmv64_b,
-                 "frac_c128": spmv_gbs / hbm_peak, "frac_c64": spmv64_gbs / hbm_peak},
-        "mixed_precision": {"value": mixed_v, "unit": UNIT,
-                            "max_abs_err_vs_fp64_expect": err_m,
-                            "form": "complex64 operator+stages (FP32 accumulation), FP64 state, "
-                                    "stage combination, error control and expectations"},
+                     "peak_source": f"{peak_src} hbm_gbs (of measured)"},
+        "double_precision": {"value": double_v, "unit": UNIT,
+                             "stage_kernel_gbs": stage128_gbs, "stage_kernel_ms": stage128_ms,
+                             "bound": "FP64 throughput (about 4 DFMA per stored entry)"},
+        "spmv": {"c64_gbs": spmv64_gbs, "c64_ms": spmv64_ms, "c64_bytes": spmv64_b,
+                 "frac_c64": spmv64_gbs / hbm_peak, "c128_gbs": spmv_gbs, "c128_ms": spmv_ms,
+                 "c128_bytes": spmv_b, "frac_c128": spmv_gbs / hbm_peak},
         "solver_stats": {k: res.stats[k] for k in ("steps", "rejected", "rhs")},
         "clocks": clk,
     }
+    if dist.rank == 0 and not args.quick:
+        log("served stream")
+        out["served"] = run_served(args)
+        log("batched mcsolve")
+        out["mc_batched"] = run_mc_batch(args)
     if dist.rank == 0 and not args.no_cpu_baseline:
+        log("CPU baseline")
         try:
             out["cpu_baseline"] = cpu_baseline(args.cpu_sample)
         except Exception as exc:  # noqa: BLE001

@@ -274,6 +274,8 @@ typedef struct qg_batch {
   void* work;             /* n_slots * qg_batch_slot_bytes(max_n, dtype) bytes */
   unsigned int* queue;    /* two words, zero before the launch; left zero */
   const volatile int32_t* cancel; /* optional host-visible flag; non-zero stops all items */
+  int64_t* progress;      /* optional [n_slots]: (item << 32) | output index of each slot */
+  double* debug;          /* optional [n_slots * 64]: last trajectory-loop states per slot */
   int32_t norm_steps;     /* MC options (qutip/solver/mcsolve.py:449-466) */
   int32_t pad_;
   double norm_t_tol, norm_tol, norm_min_step, mc_corr_eps;

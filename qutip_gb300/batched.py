@@ -51,6 +51,7 @@ class BatchStruct(C.Structure):
                 ("out", C.c_void_p), ("status", C.c_void_p), ("jump_t", C.c_void_p),
                 ("jump_which", C.c_void_p), ("max_jumps", C.c_int32), ("n_slots", C.c_int32),
                 ("work", C.c_void_p), ("queue", C.c_void_p), ("cancel", C.c_void_p),
+                ("progress", C.c_void_p), ("debug", C.c_void_p),
                 ("norm_steps", C.c_int32), ("pad_", C.c_int32), ("norm_t_tol", C.c_double),
                 ("norm_tol", C.c_double), ("norm_min_step", C.c_double),
                 ("mc_corr_eps", C.c_double)]
@@ -257,7 +258,8 @@ class BatchProblem:
             p(self.coef_consts), p(self.eop_rp), p(self.eop_col), p(self.eop_val), p(self.cop_rp),
             p(self.cop_col), p(self.cop_val), p(self.tlist_d), p(self.y0_d), p(self.out),
             p(self.status), p(self.jump_t), p(self.jump_which), self.max_jumps, self.n_slots,
-            p(self.work), p(self.queue), None, int(mc["norm_steps"]), 0, float(mc["norm_t_tol"]),
+            p(self.work), p(self.queue), None, None, None, int(mc["norm_steps"]), 0,
+            float(mc["norm_t_tol"]),
             float(mc["norm_tol"]), float(mc["norm_min_step"]), float(mc["mc_corr_eps"]))
         return self
 

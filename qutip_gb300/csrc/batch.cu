@@ -1,6 +1,7 @@
 // Batched, persistent adaptive Vern7: many independent small solves in one
-// launch.  Each CTA owns a workspace slot and takes items (a system solved from
-// an initial state, or one Monte-Carlo trajectory) from an atomic queue; every
+// launch.  Each group of threads (a warp for states up to WARP_MAX_N entries, a
+// CTA above that) owns a workspace slot and takes items -- a system solved from
+// an initial state, or one Monte-Carlo trajectory -- from an atomic queue; every
 // item runs the reference's integrator control flow with its own step size:
 //   Explicit_RungeKutta.set_initial_value / _estimate_first_step / integrate /
 //   _step_in_err / _compute_step / _prep_dense_out / _interpolate_step /
@@ -9,13 +10,20 @@
 // _do_collapse (qutip/solver/mcsolve.py:245-406) with numpy's PCG64 draws in the
 // reference's order.
 //
-// Inside a CTA: one thread per state row for the generator matvec, whose
-// epilogue forms the next stage input (fused as in the single-system kernel);
-// FP64 block reductions for the error norm, state norms and expectation values;
-// thread 0 runs the scalar step control in FP64 and publishes every decision in
-// shared memory, so all threads follow one control path.  Every loop is bounded:
-// steps per output (nsteps), bisection tries (norm_steps), jumps (max_jumps), a
-// host-visible cancel flag checked at each output time.
+// Replicated control: every thread of a group keeps its own copy of the scalar
+// integrator state (times, step sizes, status, dense-output factors, the PCG64
+// stream) and takes every decision itself from group reductions that return the
+// same bits to every thread (warp XOR butterflies are order-symmetric; the CTA
+// reduction sums the per-warp results in one fixed order).  No thread publishes
+// control state to the others, so all threads of a group follow one path by
+// construction.  Vector data live in the slot's global workspace, ordered by
+// group syncs.  The row-parallel work (matvec + fused stage combination, norms,
+// expectation values) is spread over the group's threads.
+//
+// Every loop is bounded: steps per output interval (nsteps), iterations of the
+// trajectory loop, bisection tries (norm_steps), jumps (max_jumps); an optional
+// host-visible cancel flag is polled at each output time and inside long
+// trajectory intervals.
 #include <mutex>
 
 #include "capi_internal.h"
@@ -45,6 +53,21 @@ __device__ inline double pcg_random(Pcg& r) {
   return (double)(pcg_next(r) >> 11) * (1.0 / 9007199254740992.0);
 }
 
+// Host-visible flag read with system-scope acquire semantics.
+__device__ __forceinline__ int read_flag(const volatile int32_t* p) {
+  int v;
+  asm volatile("ld.acquire.sys.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Largest state handled by one warp per item; larger states use one CTA per item.
+constexpr int WARP_MAX_N = 2048;
+constexpr int WARP_BLOCK = 128;   // 4 warps (4 items) per CTA in warp mode
+constexpr int CTA_BLOCK = 256;    // threads per item in CTA mode
+// Iterations of the trajectory loop within one output interval (each advances
+// time by one accepted step) before the item stops with QG_TOO_MUCH_WORK.
+constexpr int MC_MAX_ITER = 1 << 22;
+
 // ------------------------------------------------------------ workspace -----
 __host__ __device__ inline int64_t align256(int64_t b) { return (b + 255) & ~(int64_t)255; }
 
@@ -63,21 +86,56 @@ __host__ __device__ inline SlotLayout slot_layout(int64_t n, int dt) {
   return L;
 }
 
-// ------------------------------------------------------------- control ------
-struct Ctl {
-  double t, t_prev, t_front, dt_safe, dt_int, err, red;
-  double fa[16], fe[16];   // stage factors (FP64); float copies below
-  float faf[16], fef[16];
-  double bf[16];           // dense-output factors of the current output
-  int status, cur, interp_ready, out_front, nsteps_done, rhs, steps_total;
-  int flag;                // generic decision broadcast
+// ----------------------------------------------------------------- groups ----
+struct WarpGroup {
+  static constexpr int SIZE = 32;
+  int rank;
+  __device__ __forceinline__ void sync() const { __syncwarp(); }
+  __device__ __forceinline__ double sum(double v) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+  }
+  __device__ __forceinline__ int bcast(int v) const { return __shfl_sync(0xffffffffu, v, 0); }
 };
 
-template <int DT, int BB>
+template <int BB>
+struct CtaGroup {
+  static constexpr int SIZE = BB;
+  int rank;
+  double* red;  // shared [BB/32]
+  int* ibuf;    // shared [1]
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+  __device__ __forceinline__ double sum(double v) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();  // earlier readers of red are done
+    if ((rank & 31) == 0) red[rank >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+#pragma unroll
+    for (int i = 0; i < BB / 32; ++i) t += red[i];
+    return t;
+  }
+  __device__ __forceinline__ int bcast(int v) const {
+    __syncthreads();
+    if (rank == 0) *ibuf = v;
+    __syncthreads();
+    return *ibuf;
+  }
+};
+
+// ---------------------------------------------------------------- context ----
+// Per-thread replicated control state of the item being integrated.
+struct Ctl {
+  double t, t_prev, t_front, dt_safe, dt_int;
+  double bf[16];  // dense-output factors (dt-scaled) of the current output
+  int status, cur, interp_ready, out_front, steps, rhs;
+};
+
+template <int DT>
 struct Ctx {
   using ST = typename elem<DT>::T;
-  using CT = typename elem<DT>::R;
-  static constexpr bool MIXED = (DT == QG_C64);
   const qg_batch* B;
   const qg_batch_system* S;
   int n, d, G;
@@ -86,34 +144,36 @@ struct Ctx {
   ST* k;
   ST* ytmp;
   double2* ctmp[2];
-  Ctl* c;
-  double* red;           // [BB/32]
-  double2* coef;         // [QG_MAX_GROUPS] FP64 coefficient values (stage time)
   const ST* opval;
+  double2 coef[QG_MAX_GROUPS];  // coefficients at the current stage time
 };
 
-template <int BB>
-__device__ __forceinline__ double bsum(double v, double* red) {
-  return block_sum<BB>(v, red);  // result valid in thread 0
+template <typename T>
+__device__ __forceinline__ void st2(T* p, double re, double im);
+template <>
+__device__ __forceinline__ void st2<double2>(double2* p, double re, double im) {
+  *p = make_double2(re, im);
+}
+template <>
+__device__ __forceinline__ void st2<float2>(float2* p, double re, double im) {
+  *p = make_float2((float)re, (float)im);
 }
 
-// coefficients of the system's groups at time t -> shared memory
-template <int DT, int BB>
-__device__ void load_coef(Ctx<DT, BB>& X, double t) {
-  if (threadIdx.x < X.G) {
+template <int DT>
+__device__ __forceinline__ void load_coef(Ctx<DT>& X, double t) {
+  for (int g = 0; g < X.G; ++g) {
     cplx c{1.0, 0.0};
     if (X.S->coef_off >= 0) {
-      const int st = __ldg(X.B->coef_start + X.S->coef_off + threadIdx.x);
+      const int st = __ldg(X.B->coef_start + X.S->coef_off + g);
       c = eval_coef(X.B->coef_code + st, X.B->coef_consts, t);
     }
-    X.coef[threadIdx.x] = make_double2(c.re, c.im);
+    X.coef[g] = make_double2(c.re, c.im);
   }
-  __syncthreads();
 }
 
-// row r of A(t) x (coefficients already loaded), in the compute type CT
-template <int DT, int BB, typename XT>
-__device__ __forceinline__ void row_matvec(const Ctx<DT, BB>& X, int r, const XT* x,
+// row r of A(t) x in the compute type
+template <int DT, typename XT>
+__device__ __forceinline__ void row_matvec(const Ctx<DT>& X, int r, const XT* x,
                                            typename elem<DT>::R& ar, typename elem<DT>::R& ai) {
   using CT = typename elem<DT>::R;
   ar = 0;
@@ -136,73 +196,45 @@ __device__ __forceinline__ void row_matvec(const Ctx<DT, BB>& X, int r, const XT
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void st2(T* p, double re, double im);
-template <>
-__device__ __forceinline__ void st2<double2>(double2* p, double re, double im) {
-  *p = make_double2(re, im);
-}
-template <>
-__device__ __forceinline__ void st2<float2>(float2* p, double re, double im) {
-  *p = make_float2((float)re, (float)im);
-}
-
-// k_j = A(t) x for an arbitrary stage-dtype input (first-step estimate)
-template <int DT, int BB>
-__device__ void matvec_to_k(Ctx<DT, BB>& X, double t, const typename elem<DT>::T* x, int j) {
+// k_j = A(t) x for a stage-dtype input (first-step estimate)
+template <int DT, class GT>
+__device__ void matvec_to_k(const GT& g, Ctx<DT>& X, Ctl& c, double t,
+                            const typename elem<DT>::T* x, int j) {
   using CT = typename elem<DT>::R;
   load_coef(X, t);
-  for (int r = threadIdx.x; r < X.n; r += BB) {
+  for (int r = g.rank; r < X.n; r += GT::SIZE) {
     CT ar, ai;
     row_matvec(X, r, x, ar, ai);
     st2(X.k + (int64_t)j * X.n + r, (double)ar, (double)ai);
   }
-  __syncthreads();
+  c.rhs += 1;
+  g.sync();
 }
 
-// stage factors -> shared memory (thread 0)
-template <int DT, int BB>
-__device__ void set_factors(Ctx<DT, BB>& X, int stage, double dt) {
-  if (threadIdx.x < 16) {
-    const int j = threadIdx.x;
+// One fused stage: k_s = A(t_prev + c_s dt) x_s and the next stage input, or at
+// s == 9 y_front and the WRMS error (returned).
+template <int DT, class GT>
+__device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, double dt) {
+  using ST = typename elem<DT>::T;
+  using CT = typename elem<DT>::R;
+  constexpr bool MIXED = (DT == QG_C64);
+  CT fa[16], fe[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
     double a = 0.0, e = 0.0;
-    if (stage == RK_STEP - 1) {
+    if (s == RK_STEP - 1) {
       if (j < RK_STEP) {
         a = dt * VERN7_B[j];
         e = dt * VERN7_E[j];
       }
-    } else if (stage + 1 < RK_EXTRA_STEP && j <= stage) {
-      a = dt * VERN7_A[stage + 1][j];
+    } else if (s + 1 < RK_EXTRA_STEP && j <= s) {
+      a = dt * VERN7_A[s + 1][j];
     }
-    X.c->fa[j] = a;
-    X.c->fe[j] = e;
-    X.c->faf[j] = (float)a;
-    X.c->fef[j] = (float)e;
+    fa[j] = (CT)a;
+    fe[j] = (CT)e;
   }
-  __syncthreads();
-}
-
-template <int DT, int BB>
-__device__ __forceinline__ typename elem<DT>::R factor_a(const Ctx<DT, BB>& X, int j) {
-  if constexpr (DT == QG_C64) return X.c->faf[j];
-  else return X.c->fa[j];
-}
-template <int DT, int BB>
-__device__ __forceinline__ typename elem<DT>::R factor_e(const Ctx<DT, BB>& X, int j) {
-  if constexpr (DT == QG_C64) return X.c->fef[j];
-  else return X.c->fe[j];
-}
-
-// One fused stage: k_s = A(t_prev + c_s dt) x_s and the next stage input, or at
-// s == 9 y_front and the WRMS error (-> X.c->err).
-template <int DT, int BB>
-__device__ __noinline__ void stage(Ctx<DT, BB>& X, int s, double dt) {
-  using ST = typename elem<DT>::T;
-  using CT = typename elem<DT>::R;
-  constexpr bool MIXED = Ctx<DT, BB>::MIXED;
-  const int cur = X.c->cur;
-  set_factors(X, s, dt);
-  load_coef(X, X.c->t_prev + VERN7_C[s] * dt);
+  load_coef(X, c.t_prev + VERN7_C[s] * dt);
+  const int cur = c.cur;
   const ST* x;
   if (s == 0) {
     if constexpr (MIXED) x = X.ys[cur];
@@ -213,7 +245,7 @@ __device__ __noinline__ void stage(Ctx<DT, BB>& X, int s, double dt) {
   ST* out = X.ytmp + (int64_t)((s + 1) & 1) * X.n;
   const int64_t n = X.n;
   double err_acc = 0.0;
-  for (int r = threadIdx.x; r < X.n; r += BB) {
+  for (int r = g.rank; r < X.n; r += GT::SIZE) {
     CT ar, ai;
     row_matvec(X, r, x, ar, ai);
     st2(X.k + s * n + r, (double)ar, (double)ai);
@@ -228,7 +260,7 @@ __device__ __noinline__ void stage(Ctx<DT, BB>& X, int s, double dt) {
         vi = (CT)X.y[cur][r].y;
       }
       for (int j = 0; j <= s; ++j) {
-        const CT f = factor_a(X, j);
+        const CT f = fa[j];
         if (f != (CT)0) {
           const ST kj = (j == s) ? ks : X.k[j * n + r];
           vr = fma(f, (CT)kj.x, vr);
@@ -241,7 +273,7 @@ __device__ __noinline__ void stage(Ctx<DT, BB>& X, int s, double dt) {
       double yr, yi;
       if constexpr (MIXED) {
         for (int j = 0; j < RK_STEP; ++j) {
-          const CT fb = factor_a(X, j), fq = factor_e(X, j);
+          const CT fb = fa[j], fq = fe[j];
           if (fb == (CT)0 && fq == (CT)0) continue;
           const ST kj = (j == s) ? ks : X.k[j * n + r];
           ir = fma(fb, (CT)kj.x, ir);
@@ -256,7 +288,7 @@ __device__ __noinline__ void stage(Ctx<DT, BB>& X, int s, double dt) {
         yr = X.y[cur][r].x;
         yi = X.y[cur][r].y;
         for (int j = 0; j < RK_STEP; ++j) {
-          const double fb = X.c->fa[j], fq = X.c->fe[j];
+          const double fb = (double)fa[j], fq = (double)fe[j];
           if (fb == 0.0 && fq == 0.0) continue;
           const ST kj = (j == s) ? ks : X.k[j * n + r];
           if (fb != 0.0) {
@@ -275,21 +307,20 @@ __device__ __noinline__ void stage(Ctx<DT, BB>& X, int s, double dt) {
       err_acc += w * w;
     }
   }
-  if (s == RK_STEP - 1) {
-    const double tot = bsum<BB>(err_acc, X.red);
-    if (threadIdx.x == 0) X.c->err = sqrt(tot / (double)X.n);
-  }
-  if (threadIdx.x == 0) X.c->rhs += 1;
-  __syncthreads();
+  c.rhs += 1;
+  double err = 0.0;
+  if (s == RK_STEP - 1) err = sqrt(g.sum(err_acc) / (double)X.n);
+  g.sync();
+  return err;
 }
 
-// out (complex128 or stage dtype) = base + sum_{j<nk} f_j k_j, with f in X.c->bf
-template <int DT, int BB, typename OT, typename BT>
-__device__ void combine(Ctx<DT, BB>& X, OT* out, const BT* base, int nk) {
-  for (int r = threadIdx.x; r < X.n; r += BB) {
+// out = base + sum_{j<nk} c.bf[j] k_j
+template <int DT, class GT, typename OT, typename BT>
+__device__ void combine(const GT& g, Ctx<DT>& X, const Ctl& c, OT* out, const BT* base, int nk) {
+  for (int r = g.rank; r < X.n; r += GT::SIZE) {
     double vr = (double)base[r].x, vi = (double)base[r].y;
     for (int j = 0; j < nk; ++j) {
-      const double f = X.c->bf[j];
+      const double f = c.bf[j];
       if (f != 0.0) {
         vr = fma(f, (double)X.k[(int64_t)j * X.n + r].x, vr);
         vi = fma(f, (double)X.k[(int64_t)j * X.n + r].y, vi);
@@ -297,17 +328,16 @@ __device__ void combine(Ctx<DT, BB>& X, OT* out, const BT* base, int nk) {
     }
     st2(out + r, vr, vi);
   }
-  __syncthreads();
+  g.sync();
 }
 
 // entry i of the current state: y_front, or y_prev + sum_j bf_j k_j
-template <int DT, int BB>
-__device__ __forceinline__ double2 state_at(const Ctx<DT, BB>& X, int i) {
-  const int cur = X.c->cur;
-  if (X.c->out_front) return X.y[cur ^ 1][i];
-  double vr = X.y[cur][i].x, vi = X.y[cur][i].y;
+template <int DT>
+__device__ __forceinline__ double2 state_at(const Ctx<DT>& X, const Ctl& c, int i) {
+  if (c.out_front) return X.y[c.cur ^ 1][i];
+  double vr = X.y[c.cur][i].x, vi = X.y[c.cur][i].y;
   for (int j = 0; j < RK_EXTRA_STEP; ++j) {
-    const double f = X.c->bf[j];
+    const double f = c.bf[j];
     if (f != 0.0) {
       vr = fma(f, (double)X.k[(int64_t)j * X.n + i].x, vr);
       vi = fma(f, (double)X.k[(int64_t)j * X.n + i].y, vi);
@@ -316,49 +346,32 @@ __device__ __forceinline__ double2 state_at(const Ctx<DT, BB>& X, int i) {
   return make_double2(vr, vi);
 }
 
-template <int DT, int BB>
-__device__ double state_norm2(Ctx<DT, BB>& X) {
+template <int DT, class GT>
+__device__ double state_norm2(const GT& g, const Ctx<DT>& X, const Ctl& c) {
   double acc = 0.0;
-  for (int r = threadIdx.x; r < X.n; r += BB) {
-    const double2 v = state_at(X, r);
+  for (int r = g.rank; r < X.n; r += GT::SIZE) {
+    const double2 v = state_at(X, c, r);
     acc += v.x * v.x + v.y * v.y;
   }
-  const double tot = bsum<BB>(acc, X.red);
-  if (threadIdx.x == 0) X.c->red = tot;
-  __syncthreads();
-  return X.c->red;
+  return g.sum(acc);
 }
 
-template <int BB>
-__device__ double vec_norm2(const double2* v, int n, double* red, Ctl* c) {
+template <class GT, typename T>
+__device__ double vec_norm2(const GT& g, const T* v, int n) {
   double acc = 0.0;
-  for (int r = threadIdx.x; r < n; r += BB) acc += v[r].x * v[r].x + v[r].y * v[r].y;
-  const double tot = bsum<BB>(acc, red);
-  if (threadIdx.x == 0) c->red = tot;
-  __syncthreads();
-  return c->red;
-}
-
-// ||x||^2 of a stage-dtype vector
-template <int DT, int BB>
-__device__ double stage_norm2(Ctx<DT, BB>& X, const typename elem<DT>::T* v) {
-  double acc = 0.0;
-  for (int r = threadIdx.x; r < X.n; r += BB)
+  for (int r = g.rank; r < n; r += GT::SIZE)
     acc += (double)v[r].x * (double)v[r].x + (double)v[r].y * (double)v[r].y;
-  const double tot = bsum<BB>(acc, X.red);
-  if (threadIdx.x == 0) X.c->red = tot;
-  __syncthreads();
-  return X.c->red;
+  return g.sum(acc);
 }
 
 // ------------------------------------------------------ integrator (RK) ------
-// set_initial_value: state from src (complex128), first-step estimate
-template <int DT, int BB>
-__device__ __noinline__ void set_initial(Ctx<DT, BB>& X, const double2* src, double t) {
+// set_initial_value (explicit_rk.pyx:204-230) with _estimate_first_step (:232-276)
+template <int DT, class GT>
+__device__ __noinline__ void set_initial(const GT& g, Ctx<DT>& X, Ctl& c, const double2* src, double t) {
   using ST = typename elem<DT>::T;
-  constexpr bool MIXED = Ctx<DT, BB>::MIXED;
-  const int cur = X.c->cur;
-  for (int r = threadIdx.x; r < X.n; r += BB) {
+  constexpr bool MIXED = (DT == QG_C64);
+  const int cur = c.cur;
+  for (int r = g.rank; r < X.n; r += GT::SIZE) {
     const double2 v = src[r];
     X.y[cur][r] = v;
     X.y[cur ^ 1][r] = v;
@@ -367,24 +380,21 @@ __device__ __noinline__ void set_initial(Ctx<DT, BB>& X, const double2* src, dou
       X.ys[cur ^ 1][r] = make_float2((float)v.x, (float)v.y);
     }
   }
-  if (threadIdx.x == 0) {
-    X.c->t = X.c->t_prev = X.c->t_front = t;
-    X.c->dt_int = 0.0;
-    X.c->interp_ready = 0;
-    X.c->out_front = 1;
-    X.c->status = QG_NORMAL;
-  }
-  __syncthreads();
-  // _estimate_first_step (explicit_rk.pyx:232-276)
+  g.sync();
+  c.t = c.t_prev = c.t_front = t;
+  c.dt_int = 0.0;
+  c.interp_ready = 0;
+  c.out_front = 1;
+  c.status = QG_NORMAL;
   const double atol = X.S->atol, rtol = X.S->rtol;
-  double norm = sqrt(vec_norm2<BB>(X.y[cur], X.n, X.red, X.c));
+  double norm = sqrt(vec_norm2(g, X.y[cur], X.n));
   const double tol = atol + norm * rtol;
   const ST* x0;
   if constexpr (MIXED) x0 = X.ys[cur];
   else x0 = reinterpret_cast<const ST*>(X.y[cur]);
-  matvec_to_k(X, t, x0, 0);
+  matvec_to_k(g, X, c, t, x0, 0);
   if (norm <= atol) norm = 1.0;
-  double tmp = sqrt(stage_norm2(X, X.k));
+  double tmp = sqrt(vec_norm2(g, X.k, X.n));
   double fact = 1.0;
   for (int i = 1; i <= RK_ORDER; ++i) fact *= i;
   double dt1;
@@ -393,165 +403,137 @@ __device__ __noinline__ void set_initial(Ctx<DT, BB>& X, const double2* src, dou
   else
     dt1 = pow(tol * fact, 1.0 / (RK_ORDER + 1)) * norm * 0.5;
   const double t1 = t + dt1 / 100;
-  if (threadIdx.x == 0) {
-    for (int j = 0; j < 16; ++j) X.c->bf[j] = 0.0;
-    X.c->bf[0] = dt1 / 100;
-  }
-  __syncthreads();
+  for (int j = 0; j < 16; ++j) c.bf[j] = 0.0;
+  c.bf[0] = dt1 / 100;
   ST* yt = X.ytmp + X.n;
-  combine(X, yt, x0, 1);
-  matvec_to_k(X, t1, yt, 1);
-  tmp = sqrt(stage_norm2(X, X.k + X.n));
+  combine(g, X, c, yt, x0, 1);
+  matvec_to_k(g, X, c, t1, yt, 1);
+  tmp = sqrt(vec_norm2(g, X.k + X.n, X.n));
   double dt2;
   if (tmp >= atol * 1e-6)
     dt2 = pow(tol * fact * pow(norm, (double)RK_ORDER), 1.0 / (RK_ORDER + 1)) / tmp;
   else
     dt2 = dt1;
-  double dt = fmin(dt1, dt2);
-  dt = fmax(1e-15, dt);  // min_step defaults to 1e-15 (explicit_rk.pyx:133)
-  if (threadIdx.x == 0) {
-    X.c->dt_safe = dt;
-    X.c->rhs += 2;
-  }
-  __syncthreads();
+  c.dt_safe = fmax(1e-15, fmin(dt1, dt2));  // min_step defaults to 1e-15 (explicit_rk.pyx:133)
 }
 
-template <int DT, int BB>
-__device__ __noinline__ void prep_dense_out(Ctx<DT, BB>& X) {
+// _prep_dense_out (explicit_rk.pyx:399-410)
+template <int DT, class GT>
+__device__ __noinline__ void prep_dense_out(const GT& g, Ctx<DT>& X, Ctl& c) {
   using ST = typename elem<DT>::T;
-  const double dt = X.c->dt_int;
-  const int cur = X.c->cur;
-  if (threadIdx.x < 16) X.c->bf[threadIdx.x] = threadIdx.x < RK_STEP ? dt * VERN7_A[RK_STEP][threadIdx.x] : 0.0;
-  __syncthreads();
+  const double dt = c.dt_int;
+  for (int j = 0; j < 16; ++j) c.bf[j] = j < RK_STEP ? dt * VERN7_A[RK_STEP][j] : 0.0;
   const ST* base;
-  if constexpr (Ctx<DT, BB>::MIXED) base = X.ys[cur];
-  else base = reinterpret_cast<const ST*>(X.y[cur]);
-  combine(X, X.ytmp + (int64_t)(RK_STEP & 1) * X.n, base, RK_STEP);
-  for (int s = RK_STEP; s < RK_EXTRA_STEP; ++s) stage(X, s, dt);
-  if (threadIdx.x == 0) X.c->interp_ready = 1;
-  __syncthreads();
+  if constexpr (DT == QG_C64) base = X.ys[c.cur];
+  else base = reinterpret_cast<const ST*>(X.y[c.cur]);
+  combine(g, X, c, X.ytmp + (int64_t)(RK_STEP & 1) * X.n, base, RK_STEP);
+  for (int s = RK_STEP; s < RK_EXTRA_STEP; ++s) stage(g, X, c, s, dt);
+  c.interp_ready = 1;
 }
 
 // dense-output factors at t (Horner in tau, explicit_rk.pyx:412-430)
-template <int DT, int BB>
-__device__ void set_interp(Ctx<DT, BB>& X, double t) {
-  if (threadIdx.x < RK_EXTRA_STEP) {
-    const int i = threadIdx.x;
-    const double tau = (t - X.c->t_prev) / X.c->dt_int;
+__device__ __forceinline__ void set_interp(Ctl& c, double t) {
+  const double tau = (t - c.t_prev) / c.dt_int;
+  for (int i = 0; i < RK_EXTRA_STEP; ++i) {
     double acc = 0.0;
     for (int j = DENSE_ORDER - 1; j >= 0; --j) {
       acc += VERN7_BI[i][j];
       acc *= tau;
     }
-    X.c->bf[i] = X.c->dt_int * acc;
+    c.bf[i] = c.dt_int * acc;
   }
-  if (threadIdx.x == 0) {
-    X.c->out_front = 0;
-    X.c->t = t;
-  }
-  __syncthreads();
+  c.out_front = 0;
+  c.t = t;
 }
 
-// _step_in_err (explicit_rk.pyx:333-356) with interpolate=True time steps
-template <int DT, int BB>
-__device__ void step_in_err(Ctx<DT, BB>& X, int& nsteps_left) {
+// _step_in_err (explicit_rk.pyx:333-356) with interpolate=True time steps;
+// returns the number of trial steps
+template <int DT, class GT>
+__device__ int step_in_err(const GT& g, Ctx<DT>& X, Ctl& c, int nsteps_left) {
   int nsteps = 0;
   while (true) {
-    const double dt = X.c->dt_safe;
-    for (int s = 0; s < RK_STEP; ++s) stage(X, s, dt);
-    if (threadIdx.x == 0) {
-      Ctl* c = X.c;
-      c->t_front = c->t_prev + dt;
-      const double err = c->err;
-      c->dt_int = dt;
-      double factor;
-      if (err == 0.0) factor = 10.0;
-      else factor = fmax(0.2, fmin(10.0, 0.9 * pow(err, -1.0 / (RK_ORDER + 1))));
-      c->dt_safe = fmax(1e-15, dt * factor);
-      c->nsteps_done += 1;
-      c->steps_total += 1;
-      c->flag = 0;  // 0: retry, 1: accepted, 2: failed
-      if (dt == 1e-15 && err > 1.0) {
-        c->status = QG_DT_UNDERFLOW;
-        c->flag = 2;
-      } else if (++nsteps > nsteps_left) {
-        c->status = QG_TOO_MUCH_WORK;
-        c->flag = 2;
-      } else if (err < 1.0) {
-        c->flag = 1;
-      }
-      c->interp_ready = 0;
+    const double dt = c.dt_safe;
+    double err = 0.0;
+    for (int s = 0; s < RK_STEP; ++s) {
+      const double e = stage(g, X, c, s, dt);
+      if (s == RK_STEP - 1) err = e;
     }
-    __syncthreads();
-    if (X.c->flag != 0) break;
+    c.t_front = c.t_prev + dt;
+    c.dt_int = dt;
+    double factor;
+    if (err == 0.0) factor = 10.0;
+    else factor = fmax(0.2, fmin(10.0, 0.9 * pow(err, -1.0 / (RK_ORDER + 1))));
+    c.dt_safe = fmax(1e-15, dt * factor);
+    c.interp_ready = 0;
+    c.steps += 1;
+    ++nsteps;
+    if (dt == 1e-15 && err > 1.0) {
+      c.status = QG_DT_UNDERFLOW;
+      break;
+    }
+    if (nsteps > nsteps_left) {
+      c.status = QG_TOO_MUCH_WORK;
+      break;
+    }
+    if (err < 1.0) break;
   }
-  // the same count on every thread, read after the loop's final barrier
-  nsteps_left -= X.c->nsteps_done;  // caller resets nsteps_done per integrate call
+  return nsteps;
 }
 
-// integrate (explicit_rk.pyx:278-331); on return the state at X.c->t is
-// y_front (out_front) or the dense output with factors bf.
-template <int DT, int BB>
-__device__ void integrate(Ctx<DT, BB>& X, double t, bool step) {
-  if (t == X.c->t) return;
-  if (t < X.c->t_prev) {
-    if (threadIdx.x == 0) X.c->status = QG_OUTSIDE_RANGE;
-    __syncthreads();
+// integrate (explicit_rk.pyx:278-331); afterwards the state at c.t is y_front
+// (out_front) or the dense output with factors bf.
+template <int DT, class GT>
+__device__ void integrate(const GT& g, Ctx<DT>& X, Ctl& c, double t, bool step) {
+  if (t == c.t) return;
+  if (t < c.t_prev) {
+    c.status = QG_OUTSIDE_RANGE;
     return;
   }
-  if (t < X.c->t_front) {
-    if (!X.c->interp_ready) prep_dense_out(X);
-    set_interp(X, t);
+  if (t < c.t_front) {
+    if (!c.interp_ready) prep_dense_out(g, X, c);
+    set_interp(c, t);
     return;
   }
-  if (threadIdx.x == 0) X.c->status = QG_NORMAL;
-  __syncthreads();
-  if (step && X.c->t < X.c->t_front && t > X.c->t_front) t = X.c->t_front;
+  c.status = QG_NORMAL;
+  if (step && c.t < c.t_front && t > c.t_front) t = c.t_front;
   int nsteps_left = X.S->nsteps;
-  while (X.c->t_front < t && X.c->status >= 0) {
-    if (threadIdx.x == 0) {
-      X.c->cur ^= 1;  // y_prev <- y_front (buffer swap)
-      X.c->t_prev = X.c->t_front;
-      X.c->nsteps_done = 0;
-    }
-    __syncthreads();
-    step_in_err(X, nsteps_left);
+  while (c.t_front < t && c.status >= 0) {
+    c.cur ^= 1;  // y_prev <- y_front (buffer swap)
+    c.t_prev = c.t_front;
+    nsteps_left -= step_in_err(g, X, c, nsteps_left);
     if (step) break;
   }
-  if (X.c->status < 0) return;
-  if (X.c->t_front > t) {
-    prep_dense_out(X);
-    set_interp(X, t);
+  if (c.status < 0) return;
+  if (c.t_front > t) {
+    prep_dense_out(g, X, c);
+    set_interp(c, t);
   } else {
-    if (threadIdx.x == 0) {
-      X.c->out_front = 1;
-      X.c->t = X.c->t_front;
-    }
-    __syncthreads();
+    c.out_front = 1;
+    c.t = c.t_front;
   }
 }
 
 // ------------------------------------------------------------- outputs ------
-// expectation values of the current state into out[o] (raw; host normalises)
-template <int DT, int BB>
-__device__ __noinline__ void record(Ctx<DT, BB>& X, double2* out, bool ket) {
+// expectation values of the current state into out[0..ne] (raw; host normalises)
+template <int DT, class GT>
+__device__ __noinline__ void record(const GT& g, const Ctx<DT>& X, const Ctl& c, double2* out, bool ket) {
   const int ne = X.S->n_eops;
   const int d = X.d;
   for (int e = 0; e < ne; ++e) {
     const int* rp = X.B->eop_rp + X.S->eop_rp_off + (int64_t)e * (d + 1);
     double ar = 0.0, ai = 0.0;
-    for (int r = threadIdx.x; r < d; r += BB) {
+    for (int r = g.rank; r < d; r += GT::SIZE) {
       const int s = __ldg(rp + r), en = __ldg(rp + r + 1);
       double sr = 0.0, si = 0.0;
       for (int p = s; p < en; ++p) {
-        const int c = __ldg(X.B->eop_col + p);
+        const int col = __ldg(X.B->eop_col + p);
         const double vr = __ldg(X.B->eop_val + 2 * p), vi = __ldg(X.B->eop_val + 2 * p + 1);
-        const double2 z = state_at(X, ket ? c : c + r * d);
+        const double2 z = state_at(X, c, ket ? col : col + r * d);
         sr += vr * z.x - vi * z.y;
         si += vr * z.y + vi * z.x;
       }
       if (ket) {
-        const double2 pr = state_at(X, r);
+        const double2 pr = state_at(X, c, r);
         const double tr = pr.x * sr + pr.y * si, ti = pr.x * si - pr.y * sr;
         sr = tr;
         si = ti;
@@ -559,78 +541,223 @@ __device__ __noinline__ void record(Ctx<DT, BB>& X, double2* out, bool ket) {
       ar += sr;
       ai += si;
     }
-    const double tr_ = bsum<BB>(ar, X.red);
-    const double ti_ = bsum<BB>(ai, X.red);
-    if (threadIdx.x == 0) out[e] = make_double2(tr_, ti_);
+    const double tr_ = g.sum(ar);
+    const double ti_ = g.sum(ai);
+    if (g.rank == 0) out[e] = make_double2(tr_, ti_);
   }
   double ar = 0.0, ai = 0.0;
   if (ket) {
-    for (int r = threadIdx.x; r < X.n; r += BB) {
-      const double2 z = state_at(X, r);
+    for (int r = g.rank; r < X.n; r += GT::SIZE) {
+      const double2 z = state_at(X, c, r);
       ar += z.x * z.x + z.y * z.y;
     }
   } else {
-    for (int r = threadIdx.x; r < d; r += BB) {
-      const double2 z = state_at(X, r + r * d);
+    for (int r = g.rank; r < d; r += GT::SIZE) {
+      const double2 z = state_at(X, c, r + r * d);
       ar += z.x;
       ai += z.y;
     }
   }
-  const double tr_ = bsum<BB>(ar, X.red);
-  const double ti_ = bsum<BB>(ai, X.red);
-  if (threadIdx.x == 0) out[ne] = make_double2(tr_, ti_);
-  __syncthreads();
+  const double tr_ = g.sum(ar);
+  const double ti_ = g.sum(ai);
+  if (g.rank == 0) out[ne] = make_double2(tr_, ti_);
 }
 
-// ------------------------------------------------------------------ MC -------
 // ||c_i psi||^2 for psi in ctmp[0]; optionally store c_i psi in ctmp[1]
-template <int DT, int BB>
-__device__ double cop_apply(Ctx<DT, BB>& X, int i, bool store) {
+template <int DT, class GT>
+__device__ double cop_apply(const GT& g, Ctx<DT>& X, int i, bool store) {
   const int d = X.d;
   const int* rp = X.B->cop_rp + X.S->cop_rp_off + (int64_t)i * (d + 1);
   double acc = 0.0;
-  for (int r = threadIdx.x; r < d; r += BB) {
+  for (int r = g.rank; r < d; r += GT::SIZE) {
     const int s = __ldg(rp + r), e = __ldg(rp + r + 1);
     double sr = 0.0, si = 0.0;
     for (int p = s; p < e; ++p) {
-      const int c = __ldg(X.B->cop_col + p);
+      const int col = __ldg(X.B->cop_col + p);
       const double vr = __ldg(X.B->cop_val + 2 * p), vi = __ldg(X.B->cop_val + 2 * p + 1);
-      const double2 z = X.ctmp[0][c];
+      const double2 z = X.ctmp[0][col];
       sr += vr * z.x - vi * z.y;
       si += vr * z.y + vi * z.x;
     }
     if (store) X.ctmp[1][r] = make_double2(sr, si);
     acc += sr * sr + si * si;
   }
-  const double tot = bsum<BB>(acc, X.red);
-  if (threadIdx.x == 0) X.c->red = tot;
-  __syncthreads();
-  return X.c->red;
+  const double tot = g.sum(acc);
+  g.sync();
+  return tot;
 }
 
-}  // namespace qg
+// ------------------------------------------------------------------ item -----
+template <int DT, class GT>
+__device__ void run_item(const GT& g, const qg_batch& B, Ctx<DT>& X, int item) {
+  const qg_batch_item I = B.items[item];
+  const qg_batch_system* S = B.systems + I.system;
+  X.S = S;
+  X.n = S->n;
+  X.d = S->d;
+  X.G = S->n_groups;
+  const bool ket = S->kind == 1;
+  double2* out = reinterpret_cast<double2*>(B.out + 2 * I.out_off);
+  const double* tl = B.tlist + S->tlist_off;
+  const int ne1 = S->n_eops + 1;
+  Ctl c;
+  c.cur = 0;
+  c.rhs = 0;
+  c.steps = 0;
+  Pcg rng{I.rng_state_hi, I.rng_state_lo, I.rng_inc_hi, I.rng_inc_lo};
+  double target = ket ? pcg_random(rng) : 0.0;  // MCIntegrator.set_state draws first
+  int njumps = 0;
+  set_initial(g, X, c, reinterpret_cast<const double2*>(B.y0) + I.y0_off, tl[0]);
+  record(g, X, c, out, ket);
+  for (int o = 1; o < S->n_out && c.status >= 0; ++o) {
+    const double t = tl[o];
+    if (B.progress && g.rank == 0)
+      B.progress[(int64_t)blockIdx.x * (blockDim.x / GT::SIZE) + threadIdx.x / GT::SIZE] =
+          ((int64_t)item << 32) | (int64_t)(unsigned)o;
+    if (B.cancel) {
+      const int f = g.bcast(g.rank == 0 ? read_flag(B.cancel) : 0);
+      if (f) {
+        c.status = QG_TIMEOUT;
+        break;
+      }
+    }
+    if (!ket) {
+      integrate(g, X, c, t, false);
+    } else {
+      // MCIntegrator.integrate (mcsolve.py:286-302)
+      double t_old = c.t;
+      double norm_old = state_norm2(g, X, c);
+      int iters = 0;
+      while (t_old < t && c.status >= 0) {
+        if (++iters > MC_MAX_ITER) {
+          c.status = QG_TOO_MUCH_WORK;
+          break;
+        }
+        if (B.cancel && (iters & 63) == 0) {
+          const int f = g.bcast(g.rank == 0 ? read_flag(B.cancel) : 0);
+          if (f) {
+            c.status = QG_TIMEOUT;
+            break;
+          }
+        }
+        if (B.debug && g.rank == 0) {  // ring of the last 8 loop states per slot
+          const int64_t slot =
+              (int64_t)blockIdx.x * (blockDim.x / GT::SIZE) + threadIdx.x / GT::SIZE;
+          double* dbg = B.debug + slot * 64 + (iters & 7) * 8;
+          dbg[0] = (double)item;
+          dbg[1] = (double)o;
+          dbg[2] = c.t;
+          dbg[3] = c.t_prev;
+          dbg[4] = c.t_front;
+          dbg[5] = c.dt_safe;
+          dbg[6] = (double)iters;
+          dbg[7] = target;
+        }
+        integrate(g, X, c, t, true);
+        if (c.status < 0) break;
+        const double t_step = c.t;
+        const double nrm = state_norm2(g, X, c);
+        if (nrm > target) {
+          t_old = t_step;
+          norm_old = nrm;
+          continue;
+        }
+        // _find_collapse_time (mcsolve.py:321-369)
+        double tp = t_old, tf = t_step, no = norm_old, nn = nrm, t_guess = tf;
+        int tries = 0;
+        while (tries < B.norm_steps) {
+          ++tries;
+          if ((tf - tp) < B.norm_t_tol) {
+            t_guess = tf;
+            break;
+          }
+          const double dtb = tf - tp;
+          double ratio = log(no / target) / log(no / nn);
+          if (ratio < B.norm_min_step) ratio = B.norm_min_step;
+          if (ratio > 1.0 - B.norm_min_step) ratio = 1.0 - B.norm_min_step;
+          t_guess = tp + dtb * ratio;
+          if ((t_guess - tp) < B.norm_t_tol) t_guess = tp + B.norm_t_tol;
+          integrate(g, X, c, t_guess, true);
+          if (c.status < 0) break;
+          const double n2 = state_norm2(g, X, c);
+          if (fabs(target - n2) < B.norm_tol * target) break;
+          if (n2 < target) {
+            tf = t_guess;
+            nn = n2;
+          } else {
+            tp = t_guess;
+            no = n2;
+          }
+        }
+        if (c.status < 0) break;
+        if (tries >= B.norm_steps) {
+          c.status = QG_NORM_SEARCH_FAILED;
+          break;
+        }
+        // _do_collapse (mcsolve.py:371-406): psi = state at t_guess
+        for (int r = g.rank; r < X.n; r += GT::SIZE) X.ctmp[0][r] = state_at(X, c, r);
+        g.sync();
+        int which = 0;
+        const int nc = S->n_cops;
+        if (nc > 1) {
+          double probs[16];
+          double sum = 0.0;
+          const int m = nc < 16 ? nc : 16;
+          for (int i = 0; i < m; ++i) {
+            probs[i] = cop_apply(g, X, i, false);
+            sum += probs[i];
+          }
+          double tgt = sum * pcg_random(rng) - probs[0];
+          while (tgt > 0 && which < m - 1) {
+            ++which;
+            tgt -= probs[which];
+          }
+        }
+        const double new_norm = sqrt(cop_apply(g, X, which, true));
+        if (new_norm < B.mc_corr_eps) {
+          // the jump is numerical noise: renormalise the state, keep the target
+          const double pn = sqrt(vec_norm2(g, X.ctmp[0], X.n));
+          for (int r = g.rank; r < X.n; r += GT::SIZE)
+            X.ctmp[1][r] = make_double2(X.ctmp[0][r].x / pn, X.ctmp[0][r].y / pn);
+        } else {
+          for (int r = g.rank; r < X.n; r += GT::SIZE)
+            X.ctmp[1][r] = make_double2(X.ctmp[1][r].x / new_norm, X.ctmp[1][r].y / new_norm);
+          if (njumps >= B.max_jumps) {
+            c.status = QG_JUMP_OVERFLOW;
+            break;
+          }
+          if (g.rank == 0) {
+            B.jump_t[(int64_t)item * B.max_jumps + njumps] = t_guess;
+            B.jump_which[(int64_t)item * B.max_jumps + njumps] = which;
+          }
+          ++njumps;
+          target = pcg_random(rng);
+        }
+        g.sync();
+        set_initial(g, X, c, X.ctmp[1], t_guess);
+        t_old = c.t;
+        norm_old = 1.0;
+      }
+    }
+    if (c.status < 0) break;
+    record(g, X, c, out + (int64_t)o * ne1, ket);
+  }
+  if (g.rank == 0) {
+    int32_t* st = B.status + 4 * (int64_t)item;
+    st[0] = c.status < 0 ? c.status : 0;
+    st[1] = c.steps;
+    st[2] = c.rhs;
+    st[3] = njumps;
+  }
+  g.sync();
+}
 
-using namespace qg;
-
-namespace qg {
-
-template <int DT, int BB>
-__global__ void __launch_bounds__(BB) batch_vern7_kernel(qg_batch B) {
+template <int DT>
+__device__ __forceinline__ void bind_slot(Ctx<DT>& X, const qg_batch& B, int64_t slot_index) {
   using ST = typename elem<DT>::T;
-  __shared__ Ctl ctl;
-  __shared__ double red[BB / 32];
-  __shared__ double2 coef[QG_MAX_GROUPS];
-  __shared__ int item_s;
-  __shared__ Pcg rng;
-  __shared__ double target;
-
   const SlotLayout L = slot_layout(B.max_n, DT);
-  char* slot = static_cast<char*>(B.work) + (int64_t)blockIdx.x * L.total;
-  Ctx<DT, BB> X;
+  char* slot = static_cast<char*>(B.work) + slot_index * L.total;
   X.B = &B;
-  X.c = &ctl;
-  X.red = red;
-  X.coef = coef;
   X.opval = static_cast<const ST*>(B.op_val);
   X.y[0] = reinterpret_cast<double2*>(slot + L.y);
   X.y[1] = X.y[0] + B.max_n;
@@ -640,170 +767,66 @@ __global__ void __launch_bounds__(BB) batch_vern7_kernel(qg_batch B) {
   X.ytmp = reinterpret_cast<ST*>(slot + L.ytmp);
   X.ctmp[0] = reinterpret_cast<double2*>(slot + L.ctmp);
   X.ctmp[1] = X.ctmp[0] + B.max_n;
+}
 
-  while (true) {
-    if (threadIdx.x == 0) {
-      int it = (int)atomicAdd(B.queue, 1u);
-      if (B.cancel && *B.cancel) it = B.n_items;  // stop taking work
-      item_s = it;
-    }
-    __syncthreads();
-    const int item = item_s;
-    if (item >= B.n_items) break;
-    const qg_batch_item I = B.items[item];
-    const qg_batch_system* S = B.systems + I.system;
-    X.S = S;
-    X.n = S->n;
-    X.d = S->d;
-    X.G = S->n_groups;
-    const bool ket = S->kind == 1;
-    double2* out = reinterpret_cast<double2*>(B.out + 2 * I.out_off);
-    const double* tl = B.tlist + S->tlist_off;
-    const int ne1 = S->n_eops + 1;
-    int njumps = 0;
-    if (threadIdx.x == 0) {
-      ctl.cur = 0;
-      ctl.rhs = 0;
-      ctl.nsteps_done = 0;
-      ctl.steps_total = 0;
-      rng = Pcg{I.rng_state_hi, I.rng_state_lo, I.rng_inc_hi, I.rng_inc_lo};
-      target = ket ? pcg_random(rng) : 0.0;  // MCIntegrator.set_state draws first
-    }
-    __syncthreads();
-    set_initial(X, reinterpret_cast<const double2*>(B.y0) + I.y0_off, tl[0]);
-    record(X, out, ket);
-    for (int o = 1; o < S->n_out && ctl.status >= 0; ++o) {
-      const double t = tl[o];
-      if (B.cancel) {  // host-visible cancel flag, read once per output by thread 0
-        if (threadIdx.x == 0 && *B.cancel) ctl.status = QG_TIMEOUT;
-        __syncthreads();
-        if (ctl.status < 0) break;
-      }
-      if (!ket) {
-        integrate(X, t, false);
-      } else {
-        // MCIntegrator.integrate (mcsolve.py:286-302)
-        double t_old = ctl.t;
-        double norm_old = state_norm2(X);
-        while (t_old < t && ctl.status >= 0) {
-          integrate(X, t, true);
-          if (ctl.status < 0) break;
-          const double t_step = ctl.t;
-          const double nrm = state_norm2(X);
-          if (nrm <= target) {
-            // _find_collapse_time (mcsolve.py:321-369)
-            double tp = t_old, tf = t_step, no = norm_old, nn = nrm, t_guess = tf;
-            int tries = 0;
-            while (tries < B.norm_steps) {
-              ++tries;
-              if ((tf - tp) < B.norm_t_tol) {
-                t_guess = tf;
-                break;
-              }
-              const double dtb = tf - tp;
-              double ratio = log(no / target) / log(no / nn);
-              if (ratio < B.norm_min_step) ratio = B.norm_min_step;
-              if (ratio > 1.0 - B.norm_min_step) ratio = 1.0 - B.norm_min_step;
-              t_guess = tp + dtb * ratio;
-              if ((t_guess - tp) < B.norm_t_tol) t_guess = tp + B.norm_t_tol;
-              integrate(X, t_guess, true);
-              if (ctl.status < 0) break;
-              const double n2 = state_norm2(X);
-              if (fabs(target - n2) < B.norm_tol * target) break;
-              if (n2 < target) {
-                tf = t_guess;
-                nn = n2;
-              } else {
-                tp = t_guess;
-                no = n2;
-              }
-            }
-            if (ctl.status < 0) break;
-            if (tries >= B.norm_steps) {
-              if (threadIdx.x == 0) ctl.status = QG_NORM_SEARCH_FAILED;
-              __syncthreads();
-              break;
-            }
-            // _do_collapse (mcsolve.py:371-406): psi = state at t_guess
-            for (int r = threadIdx.x; r < X.n; r += BB) X.ctmp[0][r] = state_at(X, r);
-            __syncthreads();
-            int which = 0;
-            if (S->n_cops > 1) {
-              double probs[16];
-              double sum = 0.0;
-              const int nc = S->n_cops < 16 ? S->n_cops : 16;
-              for (int i = 0; i < nc; ++i) {
-                probs[i] = cop_apply(X, i, false);
-                sum += probs[i];
-              }
-              if (threadIdx.x == 0) {
-                double tgt = sum * pcg_random(rng) - probs[0];
-                int w = 0;
-                while (tgt > 0 && w < nc - 1) {
-                  ++w;
-                  tgt -= probs[w];
-                }
-                ctl.flag = w;
-              }
-              __syncthreads();
-              which = ctl.flag;
-            }
-            const double new_n2 = cop_apply(X, which, true);
-            const double new_norm = sqrt(new_n2);
-            const double2* src;
-            if (new_norm < B.mc_corr_eps) {
-              const double pn = sqrt(vec_norm2<BB>(X.ctmp[0], X.n, X.red, X.c));
-              for (int r = threadIdx.x; r < X.n; r += BB)
-                X.ctmp[1][r] = make_double2(X.ctmp[0][r].x / pn, X.ctmp[0][r].y / pn);
-            } else {
-              for (int r = threadIdx.x; r < X.n; r += BB)
-                X.ctmp[1][r] = make_double2(X.ctmp[1][r].x / new_norm, X.ctmp[1][r].y / new_norm);
-              if (threadIdx.x == 0) {
-                if (njumps < B.max_jumps) {
-                  B.jump_t[(int64_t)item * B.max_jumps + njumps] = t_guess;
-                  B.jump_which[(int64_t)item * B.max_jumps + njumps] = which;
-                } else {
-                  ctl.status = QG_JUMP_OVERFLOW;
-                }
-                target = pcg_random(rng);
-              }
-              ++njumps;
-            }
-            __syncthreads();
-            src = X.ctmp[1];
-            set_initial(X, src, t_guess);
-            if (ctl.status < 0) break;
-            t_old = ctl.t;
-            norm_old = 1.0;
-          } else {
-            t_old = t_step;
-            norm_old = nrm;
-          }
-        }
-      }
-      if (ctl.status < 0) break;
-      record(X, out + (int64_t)o * ne1, ket);
-    }
-    if (threadIdx.x == 0) {
-      int32_t* st = B.status + 4 * (int64_t)item;
-      st[0] = ctl.status < 0 ? ctl.status : 0;
-      st[1] = ctl.steps_total;
-      st[2] = ctl.rhs;
-      st[3] = njumps;
-    }
-    __syncthreads();
-  }
-  // the last CTA to finish resets the queue words for the next launch
-  if (threadIdx.x == 0) {
-    __threadfence();
-    if (atomicAdd(B.queue + 1, 1u) == gridDim.x - 1) {
-      B.queue[0] = 0u;
-      B.queue[1] = 0u;
-    }
+// the group that finishes last resets the queue words for the next launch
+__device__ __forceinline__ void finish_queue(const qg_batch& B, unsigned int n_groups) {
+  __threadfence();
+  if (atomicAdd(B.queue + 1, 1u) == n_groups - 1) {
+    B.queue[0] = 0u;
+    B.queue[1] = 0u;
   }
 }
 
+// One warp per item; slot = global warp index (n_slots warps own slots).
+template <int DT>
+__global__ void __launch_bounds__(WARP_BLOCK) batch_warp_kernel(qg_batch B) {
+  WarpGroup g{(int)(threadIdx.x & 31)};
+  const int64_t slot = (int64_t)blockIdx.x * (WARP_BLOCK / 32) + (threadIdx.x >> 5);
+  const unsigned int n_groups = gridDim.x * (WARP_BLOCK / 32);
+  if (slot < B.n_slots) {
+    Ctx<DT> X;
+    bind_slot(X, B, slot);
+    while (true) {
+      int it = 0;
+      if (g.rank == 0) {
+        it = (int)atomicAdd(B.queue, 1u);
+        if (B.cancel && read_flag(B.cancel)) it = B.n_items;  // stop taking work
+      }
+      it = g.bcast(it);
+      if (it >= B.n_items) break;
+      run_item(g, B, X, it);
+    }
+  }
+  if (g.rank == 0) finish_queue(B, n_groups);
+}
+
+// One CTA per item; slot = block index.
+template <int DT>
+__global__ void __launch_bounds__(CTA_BLOCK) batch_cta_kernel(qg_batch B) {
+  __shared__ double red[CTA_BLOCK / 32];
+  __shared__ int ibuf;
+  CtaGroup<CTA_BLOCK> g{(int)threadIdx.x, red, &ibuf};
+  Ctx<DT> X;
+  bind_slot(X, B, blockIdx.x);
+  while (true) {
+    int it = 0;
+    if (g.rank == 0) {
+      it = (int)atomicAdd(B.queue, 1u);
+      if (B.cancel && read_flag(B.cancel)) it = B.n_items;
+    }
+    it = g.bcast(it);
+    if (it >= B.n_items) break;
+    run_item(g, B, X, it);
+  }
+  if (g.rank == 0) finish_queue(B, gridDim.x);
+}
+
+static bool warp_mode(int64_t max_n) { return max_n <= WARP_MAX_N; }
+
 }  // namespace qg
+
+using namespace qg;
 
 // ------------------------------------------------- allocation-free variant --
 // Workspace and queue words of qg_batch_vern7_noalloc.  Loading the library
@@ -884,18 +907,20 @@ extern "C" int64_t qg_batch_slot_bytes(int64_t max_n, int dtype) {
 extern "C" int qg_batch_max_slots(int64_t max_n, int dtype) {
   int per_sm = 0;
   cudaError_t e;
+  const bool warp = warp_mode(max_n);
   if (dtype == QG_C64)
-    e = max_n <= 128 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                           &per_sm, batch_vern7_kernel<QG_C64, 128>, 128, 0)
-                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                           &per_sm, batch_vern7_kernel<QG_C64, 256>, 256, 0);
+    e = warp ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_warp_kernel<QG_C64>,
+                                                             WARP_BLOCK, 0)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_cta_kernel<QG_C64>,
+                                                             CTA_BLOCK, 0);
   else
-    e = max_n <= 128 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                           &per_sm, batch_vern7_kernel<QG_C128, 128>, 128, 0)
-                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                           &per_sm, batch_vern7_kernel<QG_C128, 256>, 256, 0);
+    e = warp ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_warp_kernel<QG_C128>,
+                                                             WARP_BLOCK, 0)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_cta_kernel<QG_C128>,
+                                                             CTA_BLOCK, 0);
   if (e != cudaSuccess || per_sm <= 0) return set_error(QG_ERR_CUDA, "occupancy query failed");
-  return sm_count() * per_sm;
+  // slots are warps in warp mode, CTAs otherwise
+  return sm_count() * per_sm * (warp ? WARP_BLOCK / 32 : 1);
 }
 
 extern "C" int qg_batch_vern7(const qg_batch* B, void* stream) {
@@ -910,13 +935,14 @@ extern "C" int qg_batch_vern7(const qg_batch* B, void* stream) {
     return set_error(QG_ERR_ARG, "jump record buffers missing");
   if (B->n_items == 0) return QG_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  const int bb = B->max_n <= 128 ? 128 : 256;
-  if (B->dtype == QG_C64) {
-    if (bb == 128) batch_vern7_kernel<QG_C64, 128><<<B->n_slots, 128, 0, st>>>(*B);
-    else batch_vern7_kernel<QG_C64, 256><<<B->n_slots, 256, 0, st>>>(*B);
-  } else {
-    if (bb == 128) batch_vern7_kernel<QG_C128, 128><<<B->n_slots, 128, 0, st>>>(*B);
-    else batch_vern7_kernel<QG_C128, 256><<<B->n_slots, 256, 0, st>>>(*B);
+  if (warp_mode(B->max_n)) {
+    const int per = WARP_BLOCK / 32;
+    const int grid = (B->n_slots + per - 1) / per;
+    if (B->dtype == QG_C64) batch_warp_kernel<QG_C64><<<grid, WARP_BLOCK, 0, st>>>(*B);
+    else batch_warp_kernel<QG_C128><<<grid, WARP_BLOCK, 0, st>>>(*B);
+    return check_launch("batch_warp_kernel");
   }
-  return check_launch("batch_vern7_kernel");
+  if (B->dtype == QG_C64) batch_cta_kernel<QG_C64><<<B->n_slots, CTA_BLOCK, 0, st>>>(*B);
+  else batch_cta_kernel<QG_C128><<<B->n_slots, CTA_BLOCK, 0, st>>>(*B);
+  return check_launch("batch_cta_kernel");
 }

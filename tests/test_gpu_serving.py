@@ -1,0 +1,51 @@
+"""Continuous-batching server: every job's result in the served mix is the result the
+same job gets alone, and the mixed-precision results stay within the stated error of
+the plain complex128 per-request solve."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _jobs(n=40, rate=400.0):
+    from qutip_gb300.serving import build_job, jc_request_stream
+    specs = jc_request_stream(n, rate=rate, ntraj=6, seed=5, n_min=3, n_max=12)
+    tl = np.linspace(0, 5, 26)
+    return [build_job(s, tl) for s in specs]
+
+
+def test_served_results_equal_alone_results():
+    from qutip_gb300.serving import Server, percentiles
+    jobs = _jobs()
+    srv = Server("mixed", n_streams=3, max_jobs_per_launch=7)
+    jobs, wall = srv.serve(jobs, realtime=True)
+    assert srv.stats["launches"] >= 3 and srv.stats["max_concurrent"] >= 1
+    assert all(j.done is not None for j in jobs)
+    p = percentiles([j.latency for j in jobs])
+    assert p["p99_ms"] >= p["p50_ms"] > 0
+    alone_srv = Server("mixed", n_streams=1, max_jobs_per_launch=1)
+    for j in jobs[:12]:
+        ref = _jobs()[j.spec.id]
+        alone_srv.serve([ref], realtime=False)
+        for a, b in zip(j.result, ref.result):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_served_mixed_precision_error_vs_plain_double():
+    from qutip_gb300.serving import Server, solve_plain
+    jobs = [j for j in _jobs() if j.spec.kind == "me"][:8]
+    Server("mixed").serve(jobs, realtime=False)
+    worst = 0.0
+    for j in jobs:
+        plain = solve_plain(j, "double")
+        for a, b in zip(j.result, plain):
+            worst = max(worst, float(np.max(np.abs(np.real(a) - np.real(b)))))
+    print(f"\nserved mixed vs plain complex128: max |<e_op>| difference {worst:.2e}")
+    assert worst < 1e-5
