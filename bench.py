@@ -65,8 +65,9 @@ def parse():
     ap.add_argument("--served-plain-sample", type=int, default=60)
     ap.add_argument("--mc-ntraj", type=int, default=4096)
     ap.add_argument("--profile", default=None, choices=["stage"],
-                    help="run a small profiling case only (Ising L=9: 262144 rows, 0.12 GB "
-                         "operator): tuned matvecs then Vern7 steps; prints nothing to parse")
+                    help="run the ncu profiling case only (fused stage kernel, untuned); "
+                         "prints nothing to parse")
+    ap.add_argument("--profile-sites", type=int, default=10)
     return ap.parse_args()
 
 
@@ -202,7 +203,9 @@ def run_reference(args, dist):
 
 # ------------------------------------------------------------------ ours ----
 def stage_bytes(op, n, stage, mixed):
-    """Algorithmic HBM bytes of one fused Vern7 stage launch."""
+    """Algorithmic HBM bytes of one fused Vern7 stage launch: operator entries and row
+    structure, the gathered input read once, k_s written, and the vectors the stage
+    combination reads and writes (earlier k_j, the base state, the next stage input)."""
     from qutip_gb300 import vern7_tableau as T
     sk = op.value_bytes()                       # stage dtype (k, ytmp, x)
     base = 8 if mixed else 16                   # y_prev_s (mixed) or y_prev
@@ -216,6 +219,21 @@ def stage_bytes(op, n, stage, mixed):
         row = T.A[stage + 1]
         b += sum(n * sk for j in range(stage) if row[j] != 0) + n * base + n * sk  # k_j, base, next x
     return b
+
+
+TRAFFIC_PROFILE = "profiles/spmv_sliced_ising_L10_stage.md"
+
+
+def profiled_traffic():
+    """DRAM bytes per fused stage launch from the committed ncu summary, or None."""
+    try:
+        with open(os.path.join(ROOT, TRAFFIC_PROFILE)) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
 
 
 def measure_stage_roofline(op, sysm, precision, reps=20):
@@ -442,7 +460,10 @@ def run_ours(args, dist):
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": stage_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": stage_gbs / hbm_peak, "traffic": None,
+                     "frac": stage_gbs / hbm_peak, "traffic": profiled_traffic(),
+                     "traffic_source": f"{TRAFFIC_PROFILE} (ncu dram__bytes_read.sum + "
+                                       "dram__bytes_write.sum, mean over the 10 stage launches "
+                                       "of a step, same operator)",
                      "kernel": "spmv_sliced_kernel<C64,C128,RK> (fused Vern7 stage, mixed)",
                      "bytes_per_launch": stage_b, "ms_per_launch": stage_ms,
                      "peak_source": f"{peak_src} hbm_gbs (of measured)"},
@@ -472,22 +493,23 @@ def run_ours(args, dist):
 
 
 def run_profile_case(args):
-    """Small case for ncu captures: the operator still exceeds L2 (0.12 GB)."""
+    """Case for ncu captures: the headline fused stage kernel on the Ising chain with
+    ``--profile-sites`` spins (default 10: 1,048,576 rows, 0.32 GB complex64 operator,
+    larger than L2; about 1.5 GB on the device).  First-step estimate (2 matvecs),
+    then two Vern7 steps of 10 fused stage launches each, without autotuning."""
     import torch
     from qutip_gb300 import systems as S
     from qutip_gb300.operator import DeviceOperator
     from qutip_gb300.vern7 import GpuVern7
     torch.cuda.set_device(0)
-    s = S.ising_chain(9)
-    for dt, prec in (("c128", "double"), ("c64", "mixed")):
-        op = DeviceOperator(s.terms, dtype=dt)
-        op.tune()
-        ig = GpuVern7(op, precision=prec)
-        ig.set_initial_value(torch.from_numpy(s.state0).cuda(), 0.0)
-        for _ in range(3):
-            ig.integrate(ig.t_front + 0.05, step=True)
-        torch.cuda.synchronize()
-        print(f"{dt}: launch {op.launch_desc()}")
+    s = S.ising_chain(args.profile_sites)
+    op = DeviceOperator(s.terms, dtype="c64")
+    ig = GpuVern7(op, precision="mixed")
+    ig.set_initial_value(torch.from_numpy(s.state0).cuda(), 0.0)
+    for _ in range(2):
+        ig.integrate(ig.t_front + 0.05, step=True)
+    torch.cuda.synchronize()
+    print(f"c64 mixed: launch {op.launch_desc()}, {op.spmv_bytes() / 1e9:.3f} GB per matvec")
 
 
 def main():

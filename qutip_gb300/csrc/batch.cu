@@ -211,14 +211,36 @@ __device__ void matvec_to_k(const GT& g, Ctx<DT>& X, Ctl& c, double t,
   g.sync();
 }
 
+// Float-float accumulation for the mixed form: hi + lo += (fh + fl) * k with the
+// product error from one FMA (TwoProduct) and the addition error from Knuth's
+// TwoSum (Ogita, Rump & Oishi, "Accurate sum and dot product", SIAM J. Sci.
+// Comput. 26 (2005)).  The _rn intrinsics keep the compiler from contracting
+// the product into the sum.  Vern7's stage weights are large and of both signs,
+// so a plain FP32 sum of f_j k_j loses several bits of the stage input; this
+// keeps it to the final rounding to FP32.
+__device__ __forceinline__ void ff_acc(float& hi, float& lo, float fh, float fl, float k) {
+  const float p = __fmul_rn(fh, k);
+  float pe = fmaf(fh, k, -p);
+  pe = fmaf(fl, k, pe);
+  const float sum = __fadd_rn(hi, p);
+  const float bp = __fsub_rn(sum, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bp)), __fsub_rn(p, bp));
+  hi = sum;
+  lo = __fadd_rn(lo, __fadd_rn(e, pe));
+}
+
 // One fused stage: k_s = A(t_prev + c_s dt) x_s and the next stage input, or at
-// s == 9 y_front and the WRMS error (returned).
+// s == 9 y_front and the WRMS error (returned).  In the mixed form the stage
+// input x_{s+1} = y_prev + sum_j dt a_{s+1,j} k_j is accumulated in float-float
+// from the complex128 y_prev and rounded once to complex64; the step increment
+// is accumulated the same way and added to y_prev in FP64.
 template <int DT, class GT>
 __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, double dt) {
   using ST = typename elem<DT>::T;
   using CT = typename elem<DT>::R;
   constexpr bool MIXED = (DT == QG_C64);
   CT fa[16], fe[16];
+  float fl[16];  // low parts of the factors (mixed form)
 #pragma unroll
   for (int j = 0; j < 16; ++j) {
     double a = 0.0, e = 0.0;
@@ -232,6 +254,7 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
     }
     fa[j] = (CT)a;
     fe[j] = (CT)e;
+    fl[j] = (float)(a - (double)fa[j]);
   }
   load_coef(X, c.t_prev + VERN7_C[s] * dt);
   const int cur = c.cur;
@@ -251,38 +274,45 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
     st2(X.k + s * n + r, (double)ar, (double)ai);
     const ST ks = X.k[s * n + r];
     if (s != RK_STEP - 1 && s != RK_EXTRA_STEP - 1) {
-      CT vr, vi;
       if constexpr (MIXED) {
-        vr = X.ys[cur][r].x;
-        vi = X.ys[cur][r].y;
-      } else {
-        vr = (CT)X.y[cur][r].x;
-        vi = (CT)X.y[cur][r].y;
-      }
-      for (int j = 0; j <= s; ++j) {
-        const CT f = fa[j];
-        if (f != (CT)0) {
-          const ST kj = (j == s) ? ks : X.k[j * n + r];
-          vr = fma(f, (CT)kj.x, vr);
-          vi = fma(f, (CT)kj.y, vi);
+        float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;
+        for (int j = 0; j <= s; ++j) {
+          if (fa[j] != 0.f || fl[j] != 0.f) {
+            const ST kj = (j == s) ? ks : X.k[j * n + r];
+            ff_acc(hr, lr, fa[j], fl[j], kj.x);
+            ff_acc(hi, li, fa[j], fl[j], kj.y);
+          }
         }
+        const double2 yv = X.y[cur][r];
+        st2(out + r, yv.x + ((double)hr + (double)lr), yv.y + ((double)hi + (double)li));
+      } else {
+        CT vr = X.y[cur][r].x, vi = X.y[cur][r].y;
+        for (int j = 0; j <= s; ++j) {
+          const CT f = fa[j];
+          if (f != (CT)0) {
+            const ST kj = (j == s) ? ks : X.k[j * n + r];
+            vr = fma(f, (CT)kj.x, vr);
+            vi = fma(f, (CT)kj.y, vi);
+          }
+        }
+        st2(out + r, (double)vr, (double)vi);
       }
-      st2(out + r, (double)vr, (double)vi);
     } else if (s == RK_STEP - 1) {
-      CT ir = 0, ii = 0, er = 0, ei = 0;
+      CT er = 0, ei = 0;
       double yr, yi;
       if constexpr (MIXED) {
+        float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;
         for (int j = 0; j < RK_STEP; ++j) {
           const CT fb = fa[j], fq = fe[j];
-          if (fb == (CT)0 && fq == (CT)0) continue;
+          if (fb == (CT)0 && fl[j] == 0.f && fq == (CT)0) continue;
           const ST kj = (j == s) ? ks : X.k[j * n + r];
-          ir = fma(fb, (CT)kj.x, ir);
-          ii = fma(fb, (CT)kj.y, ii);
+          ff_acc(hr, lr, fb, fl[j], kj.x);
+          ff_acc(hi, li, fb, fl[j], kj.y);
           er = fma(fq, (CT)kj.x, er);
           ei = fma(fq, (CT)kj.y, ei);
         }
-        yr = X.y[cur][r].x + (double)ir;
-        yi = X.y[cur][r].y + (double)ii;
+        yr = X.y[cur][r].x + ((double)hr + (double)lr);
+        yi = X.y[cur][r].y + ((double)hi + (double)li);
         X.ys[cur ^ 1][r] = make_float2((float)yr, (float)yi);
       } else {
         yr = X.y[cur][r].x;
@@ -420,13 +450,10 @@ __device__ __noinline__ void set_initial(const GT& g, Ctx<DT>& X, Ctl& c, const 
 // _prep_dense_out (explicit_rk.pyx:399-410)
 template <int DT, class GT>
 __device__ __noinline__ void prep_dense_out(const GT& g, Ctx<DT>& X, Ctl& c) {
-  using ST = typename elem<DT>::T;
   const double dt = c.dt_int;
   for (int j = 0; j < 16; ++j) c.bf[j] = j < RK_STEP ? dt * VERN7_A[RK_STEP][j] : 0.0;
-  const ST* base;
-  if constexpr (DT == QG_C64) base = X.ys[c.cur];
-  else base = reinterpret_cast<const ST*>(X.y[c.cur]);
-  combine(g, X, c, X.ytmp + (int64_t)(RK_STEP & 1) * X.n, base, RK_STEP);
+  // FP64 combination from the complex128 y_prev, rounded once to the stage type
+  combine(g, X, c, X.ytmp + (int64_t)(RK_STEP & 1) * X.n, X.y[c.cur], RK_STEP);
   for (int s = RK_STEP; s < RK_EXTRA_STEP; ++s) stage(g, X, c, s, dt);
   c.interp_ready = 1;
 }

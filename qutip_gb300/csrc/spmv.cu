@@ -26,6 +26,8 @@
 namespace qg {
 
 constexpr int SPMV_BLOCK = 256;
+// Resident blocks per SM the sliced kernel is compiled for (40 registers).
+constexpr int SLICED_MIN_BLOCKS = 6;
 
 enum Epi { EPI_AXPBY = 0, EPI_RK = 1 };
 
@@ -480,7 +482,7 @@ __global__ void __launch_bounds__(BLOCK)
 // ordered by (col XOR row) the gathered x entries of a warp fall in the same few
 // lines.  Four entries per thread are kept in flight.
 template <int DT, int YDT, int EPI>
-__global__ void __launch_bounds__(SPMV_BLOCK)
+__global__ void __launch_bounds__(SPMV_BLOCK, SLICED_MIN_BLOCKS)
     spmv_sliced_kernel(qg_csr_groups A, double t, const typename elem<DT>::T* __restrict__ x,
                        AxpbyArgs ax, RkArgs rk) {
   using ST = typename elem<DT>::T;
@@ -580,12 +582,17 @@ static int launch_any(cudaStream_t st, const qg_csr_groups& A, double t, const v
   using ST = typename elem<DT>::T;
   const int lanes = A.lanes > 0 ? A.lanes : 4;
   if (A.layout == QG_LAYOUT_SLICED) {
+    // one wave: every block resident at once, warps striding over the slices
+    auto kern = spmv_sliced_kernel<DT, YDT, EPI>;
+    static OccCache cache;  // one per instantiation
+    const int per_sm = staged_occupancy(kern, SPMV_BLOCK, 0, cache);
+    if (per_sm <= 0) return set_error(QG_ERR_CUDA, "occupancy query failed");
     int64_t warps_needed = A.n_tiles;
     int64_t blocks = (warps_needed * 32 + SPMV_BLOCK - 1) / SPMV_BLOCK;
-    int64_t cap = (int64_t)sm_count() * (2048 / SPMV_BLOCK);
+    int64_t cap = (int64_t)sm_count() * per_sm;
     if (cap > qg_scratch_doubles()) cap = qg_scratch_doubles();
     const int grid = (int)(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
-    spmv_sliced_kernel<DT, YDT, EPI><<<grid, SPMV_BLOCK, 0, st>>>(A, t, (const ST*)x, ax, rk);
+    kern<<<grid, SPMV_BLOCK, 0, st>>>(A, t, (const ST*)x, ax, rk);
     return check_launch("spmv_sliced_kernel");
   }
   if (A.n_tiles > 0) {
