@@ -1,0 +1,686 @@
+"""QuTiP plugin: the GB300 path behind QuTiP's own extension points.
+
+Importing this module (QuTiP must be importable) registers:
+
+* :class:`GpuDense`, a ``qutip.core.data.Data`` type whose matrix lives in device
+  memory (complex128, column-major, so a column-stacked density matrix and its
+  square form share one buffer).  Conversions to and from ``Dense`` and the
+  alias ``"gpu"`` go through ``qutip.data.to.add_conversions`` /
+  ``register_aliases`` (qutip/core/data/convert.pyx:208-331).
+* Data-layer specialisations for ``GpuDense`` operands
+  (qutip/core/data/dispatch.pyx:291-294 fixes their signatures): ``matmul``
+  with a CSR or GpuDense left operand runs the library's SpMV
+  (``qg_spmv_csr`` / ``qg_spmm_csr``; the reference's
+  ``matmul_csr_dense_dense``, qutip/core/data/matmul.pyx:226-272);
+  ``expect`` / ``expect_super`` with a CSR operator run ``qg_expect_dm`` /
+  ``qg_expect_ket`` (``expect_csr_dense`` and friends,
+  qutip/core/data/expect.pyx:133-236); ``zeros``, ``add``, ``iadd``, ``sub``,
+  ``mul``, ``imul``, ``neg``, ``trace``, ``trace_oper_ket``, ``norm.l2``,
+  ``norm.frobenius``, ``column_stack``, ``column_unstack``, ``inner``,
+  ``wrmn_error``, ``adjoint``, ``conj`` and ``transpose`` stay on the device
+  (torch element-wise kernels; they are not on the integration hot path).
+* :class:`IntegratorGpuVern7` as ``method="gpu_vern7"`` on ``MESolver``,
+  ``SESolver`` and ``MCSolver`` (``Solver.add_integrator``,
+  qutip/solver/solver_base.py:475-492).  It takes the solver
+  (``rhs_format = "solver"``), turns its ``QobjEvo`` right-hand side into one
+  device operator with device-evaluated coefficients, and integrates with the
+  fused Vern7 stage kernels; its options are the reference Vern7's
+  (qutip/solver/integrator/qutip_integrator.py:51-59) plus ``precision``
+  (``"double"`` or ``"mixed"``).
+* ``map="gpu"`` for ``MCSolver`` (``qutip.solver.parallel._maps``,
+  qutip/solver/parallel.py:541-559): all trajectories of a ``run`` go to one
+  persistent ``qg_batch_vern7`` launch, and each comes back to
+  ``MultiTrajResult.add`` as a trajectory result with its expectation values
+  and collapse record.
+
+Nothing here computes on the host: a coefficient the device cannot evaluate, a
+time-dependent collapse operator in a batched run, or a missing CUDA library is
+an error, not a fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from collections import OrderedDict
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+import qutip
+from qutip.core import data as _data
+from qutip.core.cy import coefficient as _cyc
+from qutip.core.data import CSR, Dense, Data
+from qutip.core.data import ode as _ode
+from qutip.solver.integrator import Integrator, IntegratorException
+from qutip.solver.mcsolve import MCSolver
+from qutip.solver.mesolve import MESolver
+from qutip.solver.sesolve import SESolver
+from qutip.solver import parallel as _parallel
+
+from . import _lib
+from .coefficients import Coefficient, coefficient
+from .operator import DeviceOperator, stream_ptr
+from .vern7 import GpuVern7, IntegratorError
+
+__all__ = ["GpuDense", "IntegratorGpuVern7", "device_coefficient", "qobjevo_terms",
+           "gpu_map", "register"]
+
+_CDT = torch.complex128
+
+
+def _device():
+    if not torch.cuda.is_available():
+        raise RuntimeError("GpuDense needs a CUDA device")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+# ------------------------------------------------------------------ data type --
+class GpuDense(Data):
+    """Dense complex128 matrix in device memory, column-major.
+
+    ``buf`` is a flat torch CUDA tensor of length ``rows * cols`` holding the
+    columns one after the other (the F order of ``qutip.core.data.Dense``).
+    """
+
+    def __init__(self, data, shape=None, copy=True):
+        if isinstance(data, GpuDense):
+            buf = data.buf.clone() if copy else data.buf
+            shape = data.shape if shape is None else shape
+        elif isinstance(data, torch.Tensor):
+            t = data
+            if t.dim() == 2:
+                shape = tuple(t.shape) if shape is None else shape
+                buf = t.transpose(0, 1).reshape(-1)
+            else:
+                if shape is None:
+                    shape = (t.numel(), 1)
+                buf = t.reshape(-1)
+            buf = buf.to(_device(), _CDT)
+            if copy and buf.data_ptr() == t.data_ptr():
+                buf = buf.clone()
+        else:
+            arr = np.asarray(data, dtype=np.complex128)
+            if arr.ndim == 1:
+                arr = arr[:, None]
+            if arr.ndim != 2:
+                raise ValueError("GpuDense needs a 1-D or 2-D array")
+            shape = arr.shape if shape is None else shape
+            buf = torch.from_numpy(np.ascontiguousarray(arr.T).reshape(-1)).to(_device())
+        shape = (int(shape[0]), int(shape[1]))
+        if buf.numel() != shape[0] * shape[1]:
+            raise ValueError(f"buffer of {buf.numel()} entries for shape {shape}")
+        super().__init__(shape)
+        self.buf = buf
+
+    @classmethod
+    def sparcity(cls):
+        return "dense"
+
+    # torch (rows, cols) view of the column-major buffer
+    def matrix(self) -> torch.Tensor:
+        return self.buf.view(self.shape[1], self.shape[0]).transpose(0, 1)
+
+    def to_array(self):
+        return self.buf.cpu().numpy().reshape(self.shape[1], self.shape[0]).T
+
+    def trace(self):
+        m, n = self.shape
+        if m != n:
+            raise ValueError("trace needs a square matrix")
+        return complex(self.buf[::m + 1].sum().item())
+
+    def copy(self):
+        return GpuDense(self.buf.clone(), shape=self.shape, copy=False)
+
+    def conj(self):
+        return GpuDense(torch.conj(self.buf).resolve_conj(), shape=self.shape, copy=False)
+
+    def transpose(self):
+        return GpuDense(self.matrix().transpose(0, 1), copy=False)
+
+    def adjoint(self):
+        return GpuDense(torch.conj(self.matrix().transpose(0, 1)).resolve_conj(), copy=False)
+
+    def __repr__(self):
+        return f"GpuDense(shape={self.shape}, device={self.buf.device})"
+
+
+def _wrap(buf: torch.Tensor, shape) -> GpuDense:
+    return GpuDense(buf, shape=shape, copy=False)
+
+
+def _dense_to_gpu(matrix):
+    return GpuDense(matrix.to_array())
+
+
+def _gpu_to_dense(matrix):
+    return Dense(matrix.to_array(), copy=False)
+
+
+# ------------------------------------------------------------ device operator --
+class _OpCache:
+    """Device copies of host operators, keyed by object identity (the object is kept
+    alive by the cache, so an id is never reused while its entry exists)."""
+
+    def __init__(self, size=64):
+        self.size = size
+        self._d = OrderedDict()
+
+    def get(self, obj, build):
+        key = id(obj)
+        hit = self._d.get(key)
+        if hit is not None and hit[0] is obj:
+            self._d.move_to_end(key)
+            return hit[1]
+        val = build(obj)
+        self._d[key] = (obj, val)
+        if len(self._d) > self.size:
+            self._d.popitem(last=False)
+        return val
+
+
+_OPS = _OpCache()
+_EOPS = _OpCache()
+_SUPER_EOPS = _OpCache()
+
+
+def _scipy(matrix) -> sp.csr_matrix:
+    if isinstance(matrix, CSR):
+        return matrix.as_scipy()
+    return sp.csr_matrix(matrix.to_array())
+
+
+def _device_op(matrix) -> DeviceOperator:
+    return _OPS.get(matrix, lambda m: DeviceOperator([(_scipy(m), None)], dtype="c128",
+                                                     device=_device(), fmt="csr"))
+
+
+def matmul_csr_gpu(left, right, scale=1, out=None):
+    if left.shape[1] != right.shape[0]:
+        raise ValueError(f"incompatible matrix shapes {left.shape} and {right.shape}")
+    op = _device_op(left)
+    rows, cols = left.shape[0], right.shape[1]
+    if out is None:
+        y = torch.empty(rows * cols, dtype=_CDT, device=right.buf.device)
+        beta = 0.0
+    else:
+        y, beta = out.buf, 1.0
+    if cols == 1:
+        op.matvec(0.0, right.buf, y, alpha=scale, beta=beta)
+    else:
+        op.matmat(0.0, right.buf.view(cols, right.shape[0]), y.view(cols, rows),
+                  alpha=scale, beta=beta)
+    return out if out is not None else _wrap(y, (rows, cols))
+
+
+def matmul_gpu(left, right, scale=1, out=None):
+    if left.shape[1] != right.shape[0]:
+        raise ValueError(f"incompatible matrix shapes {left.shape} and {right.shape}")
+    prod = (left.matrix() @ right.matrix()) * complex(scale)
+    if out is not None:
+        out.buf += prod.transpose(0, 1).reshape(-1)
+        return out
+    return GpuDense(prod, copy=False)
+
+
+def zeros_gpu(rows, cols):
+    return _wrap(torch.zeros(int(rows) * int(cols), dtype=_CDT, device=_device()), (rows, cols))
+
+
+def _same_shape(a, b):
+    if a.shape != b.shape:
+        raise ValueError(f"incompatible matrix shapes {a.shape} and {b.shape}")
+
+
+def add_gpu(left, right, scale=1):
+    _same_shape(left, right)
+    return _wrap(left.buf + complex(scale) * right.buf, left.shape)
+
+
+def iadd_gpu(left, right, scale=1):
+    _same_shape(left, right)
+    left.buf.add_(right.buf, alpha=complex(scale))
+    return left
+
+
+def sub_gpu(left, right):
+    _same_shape(left, right)
+    return _wrap(left.buf - right.buf, left.shape)
+
+
+def mul_gpu(matrix, value):
+    return _wrap(matrix.buf * complex(value), matrix.shape)
+
+
+def imul_gpu(matrix, value):
+    matrix.buf.mul_(complex(value))
+    return matrix
+
+
+def neg_gpu(matrix):
+    return _wrap(-matrix.buf, matrix.shape)
+
+
+def trace_gpu(matrix):
+    return matrix.trace()
+
+
+def trace_oper_ket_gpu(matrix):
+    n = matrix.shape[0]
+    d = int(math.isqrt(n))
+    if d * d != n or matrix.shape[1] != 1:
+        raise ValueError("trace_oper_ket needs a column-stacked square operator")
+    return complex(matrix.buf[::d + 1].sum().item())
+
+
+def l2_gpu(matrix):
+    if matrix.shape[0] != 1 and matrix.shape[1] != 1:
+        raise ValueError("L2 norm is only defined on vectors")
+    return float(torch.linalg.vector_norm(matrix.buf).item())
+
+
+def frobenius_gpu(matrix):
+    return float(torch.linalg.vector_norm(matrix.buf).item())
+
+
+def column_stack_gpu(matrix):
+    return _wrap(matrix.buf, (matrix.shape[0] * matrix.shape[1], 1))
+
+
+def column_unstack_gpu(matrix, rows):
+    rows = int(rows)
+    if matrix.shape[1] != 1 or rows <= 0 or matrix.shape[0] % rows:
+        raise ValueError(f"cannot unstack a {matrix.shape} vector into {rows} rows")
+    return _wrap(matrix.buf, (rows, matrix.shape[0] // rows))
+
+
+def inner_gpu(left, right, scalar_is_ket=False):
+    if left.shape[0] == 1:      # bra
+        return complex(torch.dot(left.buf, right.buf).item())
+    return complex(torch.vdot(left.buf, right.buf).item())
+
+
+def wrmn_error_gpu(diff, state, atol, rtol):
+    w = torch.abs(diff.buf) / (atol + rtol * torch.abs(state.buf))
+    return float(torch.sqrt(torch.mean(w * w)).item())
+
+
+def adjoint_gpu(matrix):
+    return matrix.adjoint()
+
+
+def conj_gpu(matrix):
+    return matrix.conj()
+
+
+def transpose_gpu(matrix):
+    return matrix.transpose()
+
+
+class _ExpectOp:
+    """One operator as a single-group device operator for qg_expect_*."""
+
+    def __init__(self, m: sp.csr_matrix):
+        m = sp.csr_matrix(m, dtype=np.complex128)
+        m.sort_indices()
+        dev = _device()
+        self.n = m.shape[0]
+        self.row_ptr = torch.from_numpy(m.indptr.astype(np.int32)).to(dev)
+        self.col = torch.from_numpy(m.indices.astype(np.int32)).to(dev)
+        self.val = torch.from_numpy(m.data).to(dev)
+        self.struct = _lib.CsrGroups(self.n, m.shape[1], 1, _lib.QG_C128,
+                                     _lib.QG_LAYOUT_GROUP_MAJOR, 1, 0, 0,
+                                     self.row_ptr.data_ptr(), self.col.data_ptr(),
+                                     self.val.data_ptr(), None, None, None, None)
+        self.out = torch.zeros(4, dtype=torch.float64, device=dev)
+
+
+def _view(buf: torch.Tensor) -> _lib.StateView:
+    return _lib.StateView(buf.numel(), _lib.QG_C128, _lib.QG_C128, buf.data_ptr(), None, 0, 0,
+                          (C.c_double * 16)())
+
+
+def expect_csr_gpu(op, state):
+    """``<psi|op|psi>`` for a ket, ``tr(op rho)`` for a square state."""
+    e = _EOPS.get(op, lambda o: _ExpectOp(_scipy(o)))
+    if state.shape[1] == 1:
+        if op.shape[1] != state.shape[0]:
+            raise ValueError(f"incompatible shapes {op.shape} and {state.shape}")
+        _lib.call("qg_expect_ket", C.byref(e.struct), C.byref(_view(state.buf)),
+                  e.out.data_ptr(), stream_ptr())
+    else:
+        d = state.shape[0]
+        if state.shape != (d, d) or op.shape != (d, d):
+            raise ValueError(f"incompatible shapes {op.shape} and {state.shape}")
+        _lib.call("qg_expect_dm", C.byref(e.struct), d, C.byref(_view(state.buf)),
+                  e.out.data_ptr(), stream_ptr())
+    v = e.out.cpu()
+    return complex(float(v[0]), float(v[1]))
+
+
+def expect_super_csr_gpu(op, state):
+    """``tr(unvec(op @ vec(rho)))``: the rows of ``op`` on the diagonal of rho,
+    summed (expect_super_csr_dense, qutip/core/data/expect.pyx:223-236)."""
+    n = state.shape[0]
+    d = int(math.isqrt(n))
+    if d * d != n or state.shape[1] != 1 or op.shape[1] != n:
+        raise ValueError(f"incompatible shapes {op.shape} and {state.shape}")
+
+    def build(o):
+        rows = _scipy(o)[np.arange(d) * (d + 1)]
+        return _ExpectOp(sp.csr_matrix(np.ones((1, d))) @ rows)   # 1 x n summed row
+    e = _SUPER_EOPS.get(op, build)
+    y = torch.zeros(1, dtype=_CDT, device=state.buf.device)
+    # one-row operator times the state: a matvec with n_rows = 1
+    _lib.call("qg_spmv_csr", C.byref(e.struct), 0.0, state.buf.data_ptr(), y.data_ptr(),
+              1.0, 0.0, 0.0, 0.0, stream_ptr())
+    return complex(y.item())
+
+
+# ---------------------------------------------------------- coefficients ------
+def _cy_state(c):
+    r = c.__reduce_ex__(2)
+    if len(r) > 2 and r[2] is not None:
+        return r[2]
+    args = r[1]
+    if len(args) > 2 and isinstance(args[2], tuple):
+        return args[2]
+    return ()
+
+
+def _members(c):
+    return [x for x in _cy_state(c) if isinstance(x, _cyc.Coefficient)]
+
+
+def _decode(c) -> Coefficient:
+    if isinstance(c, _cyc.ConstantCoefficient):
+        return coefficient(complex(c(0.0)))
+    if isinstance(c, _cyc.ConjCoefficient):
+        (b,) = _members(c)
+        return _decode(b).conj()
+    if isinstance(c, _cyc.NormCoefficient):
+        (b,) = _members(c)
+        db = _decode(b)
+        return db.conj() * db
+    if isinstance(c, _cyc.SumCoefficient):
+        a, b = _members(c)
+        return _decode(a) + _decode(b)
+    if isinstance(c, _cyc.MulCoefficient):
+        a, b = _members(c)
+        return _decode(a) * _decode(b)
+    if isinstance(c, _cyc.StrFunctionCoefficient):
+        base, args = c.__reduce__()[1]
+        return coefficient(base, args)
+    if type(c).__name__ == "StrCoefficient":
+        # Cython-compiled string coefficient (qutip/core/coefficient.py:529-560):
+        # its state holds the argument values, the source string, then the names.
+        st = list(_cy_state(c))
+        k = next(i for i, x in enumerate(st) if isinstance(x, str))
+        names = [x for x in st[k + 1:] if isinstance(x, str)]
+        values = [x for x in st[:k] if isinstance(x, (int, float, complex))]
+        return coefficient(st[k], dict(zip(names, values[:len(names)])))
+    raise TypeError(f"a {type(c).__name__} cannot be evaluated on the device")
+
+
+_CHECK_TIMES = (0.0, 0.3183, 1.7321, 4.4721, 11.0)
+
+
+def device_coefficient(c) -> Coefficient:
+    """The device program of a QuTiP coefficient, checked against the coefficient
+    itself at a few times; raises ``TypeError`` when it cannot be built."""
+    try:
+        prog = _decode(c)
+    except (TypeError, ValueError, StopIteration) as exc:
+        raise TypeError(f"coefficient {c!r} cannot be evaluated on the device: {exc}") from None
+    for t in _CHECK_TIMES:
+        want, got = complex(c(t)), complex(prog(t))
+        if not (np.isclose(got, want, rtol=1e-12, atol=1e-12)
+                or (np.isnan(got) and np.isnan(want))):
+            raise TypeError(f"coefficient {c!r} cannot be evaluated on the device "
+                            f"(device program gives {got} at t={t}, the coefficient {want})")
+    return prog
+
+
+def qobjevo_terms(evo):
+    """``(scipy CSR, device Coefficient | None)`` terms of a QobjEvo or Qobj."""
+    if isinstance(evo, qutip.Qobj):
+        return [(_scipy(evo.data), None)]
+    out = []
+    for el in evo.to_list():
+        if isinstance(el, qutip.Qobj):
+            out.append((_scipy(el.data), None))
+        elif isinstance(el, (list, tuple)) and len(el) == 2 and isinstance(el[0], qutip.Qobj):
+            c = el[1]
+            if not isinstance(c, _cyc.Coefficient):
+                c = qutip.coefficient(c)
+            out.append((_scipy(el[0].data), device_coefficient(c)))
+        else:
+            raise TypeError("QobjEvo element of this kind cannot be evaluated on the device")
+    return out
+
+
+# ---------------------------------------------------------------- integrator --
+def _as_gpu(state) -> GpuDense:
+    if isinstance(state, GpuDense):
+        return state
+    return GpuDense(state.to_array())
+
+
+class IntegratorGpuVern7(Integrator):
+    """Verner 7(6) with dense output on the GPU: the reference's ``vern7`` control
+    flow (qutip/solver/integrator/explicit_rk.pyx:204-467) on fused device stages.
+
+    Usable with ``method="gpu_vern7"``; ``precision="mixed"`` keeps the operator and
+    stage vectors in complex64 (FP32 accumulation) and the state, step control,
+    stage combinations and norms in FP64.
+    """
+    integrator_options = {
+        "atol": 1e-8,
+        "rtol": 1e-6,
+        "nsteps": 1000,
+        "first_step": 0,
+        "max_step": 0,
+        "min_step": 0,
+        "interpolate": True,
+        "precision": "double",
+    }
+    rhs_format = "solver"
+    support_time_dependant = True
+    supports_blackbox = False
+    method = "gpu_vern7"
+
+    def __init__(self, system, options):
+        self.system = system
+        self._is_set = False
+        self._back = (np.inf, None)
+        self._options = self.integrator_options.copy()
+        self.options = options
+        self._prepare()
+
+    def _rhs(self):
+        rhs = self.system.rhs
+        return rhs if isinstance(rhs, (qutip.QobjEvo, qutip.Qobj)) else rhs()
+
+    def _prepare(self):
+        prec = self._options["precision"]
+        if prec not in ("double", "mixed"):
+            raise ValueError("precision must be 'double' or 'mixed'")
+        dt = "c128" if prec == "double" else "c64"
+        self._op = DeviceOperator(qobjevo_terms(self._rhs()), dtype=dt, device=_device())
+        self._ode = GpuVern7(self._op, atol=self._options["atol"], rtol=self._options["rtol"],
+                             nsteps=self._options["nsteps"],
+                             first_step=self._options["first_step"],
+                             min_step=self._options["min_step"],
+                             max_step=self._options["max_step"],
+                             interpolate=self._options["interpolate"], precision=prec)
+        self._shape = (self._op.n_rows, 1)
+        self.name = f"{self.method} ({prec})"
+
+    def set_state(self, t, state0):
+        self._ode.set_initial_value(_as_gpu(state0).buf, t)
+        self._shape = state0.shape
+        self._is_set = True
+
+    def get_state(self, copy=True):
+        y = self._ode.get_state()
+        return self._ode.t, GpuDense(y.clone() if copy else y, shape=self._shape, copy=False)
+
+    def _check(self):
+        try:
+            self._ode.check()
+        except IntegratorError as exc:
+            raise IntegratorException(str(exc)) from None
+
+    def integrate(self, t, copy=True):
+        self._ode.integrate(t, step=False)
+        self._check()
+        return self.get_state(copy)
+
+    def mcstep(self, t, copy=True):
+        self._ode.integrate(t, step=True)
+        self._check()
+        return self.get_state(copy)
+
+    def reset(self, hard=False):
+        if self._is_set:
+            state = self.get_state()
+        if hard:
+            self._prepare()
+        if self._is_set:
+            self.set_state(*state)
+
+    @property
+    def options(self):
+        """atol, rtol, nsteps, first_step, max_step, min_step, interpolate: as the
+        reference ``vern7``; precision: ``"double"`` or ``"mixed"``."""
+        return self._options
+
+    @options.setter
+    def options(self, new_options):
+        Integrator.options.fset(self, new_options)
+
+
+# ------------------------------------------------------------- trajectories ---
+def _constant_matrix(op, what):
+    if isinstance(op, qutip.QobjEvo):
+        if not op.isconstant:
+            raise TypeError(f"time-dependent {what} are not supported by map='gpu'")
+        op = op(0)
+    if not isinstance(op, qutip.Qobj):
+        raise TypeError(f"{what} must be Qobj (map='gpu' records expectation values on the "
+                        "device)")
+    return _scipy(op.data)
+
+
+def gpu_map(task, values, task_args=None, task_kwargs=None, reduce_func=None, map_kw=None,
+            progress_bar=None, progress_bar_kwargs={}):
+    """``map="gpu"``: run every trajectory of an ``MCSolver.run`` in one persistent
+    launch and hand each to ``reduce_func`` as the reference's trajectory result."""
+    from .batched import BatchProblem, MC_DEFAULTS
+    solver = getattr(task, "__self__", None)
+    if not isinstance(solver, MCSolver) or getattr(task, "__name__", "") != "_run_one_traj":
+        raise TypeError("map='gpu' runs MCSolver trajectories only")
+    if task_kwargs:
+        raise TypeError("map='gpu' does not support improved sampling or mixed initial states")
+    state0, tlist, e_ops = task_args
+    opts = solver.options
+    if opts.get("bitgenerator") not in (None, "PCG64"):
+        raise TypeError("map='gpu' draws from PCG64 streams (the default bit generator)")
+    if opts.get("store_states") or opts.get("store_final_state"):
+        raise TypeError("map='gpu' records expectation values only; pass e_ops and leave "
+                        "store_states / store_final_state off")
+    if isinstance(e_ops, dict):
+        e_list = list(e_ops.values())
+    elif e_ops is None:
+        e_list = []
+    elif isinstance(e_ops, (list, tuple)):
+        e_list = list(e_ops)
+    else:
+        e_list = [e_ops]
+    if not e_list:
+        raise TypeError("map='gpu' needs e_ops")
+    e_mats = [_constant_matrix(e, "e_ops") for e in e_list]
+    c_mats = [_constant_matrix(c, "collapse operators") for c in solver._c_ops]
+    terms = qobjevo_terms(solver.rhs())
+    iopts = {**IntegratorGpuVern7.integrator_options,
+             **{k: opts[k] for k in IntegratorGpuVern7.integrator_options if k in opts}}
+    prec = iopts["precision"]
+    psi0 = np.asarray(_as_gpu(state0).to_array()).reshape(-1)
+    bp = BatchProblem("c128" if prec == "double" else "c64")
+    sid = bp.add_system(terms, e_mats, np.asarray(tlist, dtype=np.float64), "mc",
+                        c_ops=c_mats, atol=iopts["atol"], rtol=iopts["rtol"],
+                        nsteps=iopts["nsteps"])
+    seeds = list(values)
+    for s in seeds:
+        bp.add_item(sid, psi0, seed=s)
+    mc = {k: opts[k] for k in MC_DEFAULTS if k in opts}
+    bp.build(max_jumps=int((map_kw or {}).get("max_jumps", 4096)), mc_options=mc)
+    bp.launch()
+    res = bp.results()
+    for r in res:
+        if r["status"] == -5:
+            raise RuntimeError("Could not find the collapse time within desired tolerance. "
+                               "Increase accuracy of the ODE solver or lower the tolerance "
+                               "with the options 'norm_steps', 'norm_tol', 'norm_t_tol'.")
+        if r["status"] < 0:
+            raise IntegratorException(f"trajectory failed with status {r['status']}")
+    for seed, r in zip(seeds, res):
+        traj = solver._trajectory_resultclass(e_ops, opts)
+        traj.times = [float(t) for t in tlist]
+        for k, key in enumerate(traj.e_data):
+            traj.e_data[key] = list(r["expect"][:, k])
+        traj.collapse = [(float(t), int(w)) for t, w in zip(r["col_times"], r["col_which"])]
+        if reduce_func is not None:
+            left = reduce_func((seed, traj, 1.0))
+            if left is not None and left <= 0:
+                break
+    return None
+
+
+# ---------------------------------------------------------------- register ----
+_REGISTERED = False
+
+
+def register():
+    """Register the data type, specialisations, integrator and map (idempotent)."""
+    global _REGISTERED
+    if _REGISTERED:
+        return
+    _lib.load()
+    _data.to.add_conversions([
+        (GpuDense, Dense, _dense_to_gpu, 1),
+        (Dense, GpuDense, _gpu_to_dense, 1),
+    ])
+    _data.to.register_aliases(["gpu", "GpuDense", "gpudense"], GpuDense)
+    _data.zeros.add_specialisations([(GpuDense, zeros_gpu)])
+    _data.matmul.add_specialisations([
+        (CSR, GpuDense, GpuDense, matmul_csr_gpu),
+        (GpuDense, GpuDense, GpuDense, matmul_gpu),
+    ])
+    _data.add.add_specialisations([(GpuDense, GpuDense, GpuDense, add_gpu)])
+    _data.iadd.add_specialisations([(GpuDense, GpuDense, GpuDense, iadd_gpu)])
+    _data.sub.add_specialisations([(GpuDense, GpuDense, GpuDense, sub_gpu)])
+    _data.mul.add_specialisations([(GpuDense, GpuDense, mul_gpu)])
+    _data.imul.add_specialisations([(GpuDense, GpuDense, imul_gpu)])
+    _data.neg.add_specialisations([(GpuDense, GpuDense, neg_gpu)])
+    _data.expect.add_specialisations([(CSR, GpuDense, expect_csr_gpu)])
+    _data.expect_super.add_specialisations([(CSR, GpuDense, expect_super_csr_gpu)])
+    _data.trace.add_specialisations([(GpuDense, trace_gpu)])
+    _data.trace_oper_ket.add_specialisations([(GpuDense, trace_oper_ket_gpu)])
+    _data.norm.l2.add_specialisations([(GpuDense, l2_gpu)])
+    _data.norm.frobenius.add_specialisations([(GpuDense, frobenius_gpu)])
+    _data.column_stack.add_specialisations([(GpuDense, GpuDense, column_stack_gpu)])
+    _data.column_unstack.add_specialisations([(GpuDense, GpuDense, column_unstack_gpu)])
+    _data.inner.add_specialisations([(GpuDense, GpuDense, inner_gpu)])
+    _ode.wrmn_error.add_specialisations([(GpuDense, GpuDense, wrmn_error_gpu)])
+    _data.adjoint.add_specialisations([(GpuDense, GpuDense, adjoint_gpu)])
+    _data.conj.add_specialisations([(GpuDense, GpuDense, conj_gpu)])
+    _data.transpose.add_specialisations([(GpuDense, GpuDense, transpose_gpu)])
+    for solver in (MESolver, SESolver, MCSolver):
+        solver.add_integrator(IntegratorGpuVern7, "gpu_vern7")
+    _parallel._maps["gpu"] = gpu_map
+    _REGISTERED = True
+
+
+register()

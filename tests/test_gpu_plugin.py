@@ -1,0 +1,168 @@
+"""The QuTiP plugin on the GPU, against the reference QuTiP itself (oracle/_ref) on
+the same inputs: ``mesolve`` / ``sesolve`` / ``mcsolve`` with ``method="gpu_vern7"``
+unchanged from the user's side, ``map="gpu"`` batched trajectories, and the
+GpuDense data-layer operations.
+
+complex128 tolerance: atol 1e-8 / rtol 1e-6 on expectation values and states (the
+reference's own solver tolerances).  Jump records: same count and channels, times
+inside the reference's bisection window (2 norm_tol target / slope + 2 norm_t_tol,
+bounded here by a fixed 1e-3 for these systems)."""
+import numpy as np
+import pytest
+
+from oracle.ref_workloads import reference_available
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def qt():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    if not reference_available():
+        pytest.skip("reference QuTiP not built (oracle/build_ref.py)")
+    from oracle.ref_workloads import import_reference
+    return import_reference()
+
+
+@pytest.fixture(scope="module")
+def plugin(qt):
+    from qutip_gb300 import qutip_plugin
+    return qutip_plugin
+
+
+def _jc(qt, N=10):
+    a = qt.tensor(qt.destroy(N), qt.qeye(2))
+    sm = qt.tensor(qt.qeye(N), qt.sigmam())
+    sz = qt.tensor(qt.qeye(N), qt.sigmaz())
+    w = 2 * np.pi
+    g = 2 * np.pi * 0.05
+    H = w * a.dag() * a + w * sz / 2 + g * (a * sm.dag() + a.dag() * sm)
+    c_ops = [np.sqrt(0.005) * a, np.sqrt(0.05) * sm]
+    psi0 = qt.tensor(qt.basis(N, 0), qt.basis(2, 0))
+    return H, c_ops, psi0, [a.dag() * a, sz]
+
+
+def _ising(qt, L=4, omega=1.3, seed=1234):
+    h = np.random.default_rng(seed).uniform(0.5, 1.5, L)
+    op = lambda o, i: qt.tensor(*[o if k == i else qt.qeye(2) for k in range(L)])  # noqa: E731
+    H0 = sum(-1.0 * op(qt.sigmaz(), i) * op(qt.sigmaz(), i + 1) for i in range(L - 1))
+    H1 = sum(-h[i] * op(qt.sigmax(), i) for i in range(L))
+    H = qt.QobjEvo([H0, [H1, "cos(w*t)"]], args={"w": omega})
+    c_ops = [np.sqrt(0.05) * op(qt.sigmam(), i) for i in range(L)] + \
+            [np.sqrt(0.02) * op(qt.sigmaz(), i) for i in range(L)]
+    psi0 = qt.tensor(*[qt.basis(2, 0)] * L)
+    return H, c_ops, psi0, [op(qt.sigmaz(), i) for i in range(L)]
+
+
+def _assert_expect(got, want):
+    for g, w in zip(got, want):
+        np.testing.assert_allclose(np.asarray(g), np.asarray(w), rtol=1e-6, atol=1e-8)
+
+
+def test_mesolve_jaynes_cummings_drop_in(qt, plugin):
+    H, c_ops, psi0, e_ops = _jc(qt)
+    rho0 = qt.ket2dm(psi0)
+    tl = np.linspace(0, 20, 201)
+    ref = qt.mesolve(H, rho0, tl, c_ops, e_ops=e_ops, options={"method": "vern7"})
+    got = qt.mesolve(H, rho0, tl, c_ops, e_ops=e_ops,
+                     options={"method": "gpu_vern7", "store_final_state": True})
+    _assert_expect(got.expect, ref.expect)
+    fs = got.final_state
+    assert isinstance(fs.data, plugin.GpuDense)
+    ref_fs = qt.mesolve(H, rho0, tl, c_ops, options={"method": "vern7",
+                                                      "store_final_state": True}).final_state
+    np.testing.assert_allclose(fs.full(), ref_fs.full(), rtol=1e-6, atol=1e-8)
+
+
+def test_mesolve_time_dependent_ising(qt, plugin):
+    H, c_ops, psi0, e_ops = _ising(qt, L=4)
+    rho0 = qt.ket2dm(psi0)
+    tl = np.linspace(0, 10, 101)
+    ref = qt.mesolve(H, rho0, tl, c_ops, e_ops=e_ops, options={"method": "vern7"})
+    got = qt.mesolve(H, rho0, tl, c_ops, e_ops=e_ops, options={"method": "gpu_vern7"})
+    _assert_expect(got.expect, ref.expect)
+
+
+def test_mesolve_mixed_precision_error_stated(qt, plugin):
+    H, c_ops, psi0, e_ops = _ising(qt, L=4)
+    rho0 = qt.ket2dm(psi0)
+    tl = np.linspace(0, 10, 101)
+    ref = qt.mesolve(H, rho0, tl, c_ops, e_ops=e_ops, options={"method": "vern7"})
+    got = qt.mesolve(H, rho0, tl, c_ops, e_ops=e_ops,
+                     options={"method": "gpu_vern7", "precision": "mixed"})
+    err = max(float(np.max(np.abs(np.asarray(g) - np.asarray(w))))
+              for g, w in zip(got.expect, ref.expect))
+    print(f"\nmixed form vs reference complex128: max |<e_op>| difference {err:.2e}")
+    assert err < 1e-6
+
+
+def test_sesolve_drop_in(qt, plugin):
+    H, _, psi0, e_ops = _ising(qt, L=5)
+    tl = np.linspace(0, 5, 51)
+    ref = qt.sesolve(H, psi0, tl, e_ops=e_ops, options={"method": "vern7"})
+    got = qt.sesolve(H, psi0, tl, e_ops=e_ops, options={"method": "gpu_vern7"})
+    _assert_expect(got.expect, ref.expect)
+
+
+def _records(res):
+    return [(np.array([t for t, _ in c]), [w for _, w in c]) for c in res.collapse]
+
+
+def _same_jumps(got, want, tol=1e-3):
+    assert len(got) == len(want)
+    for (gt, gw), (wt, ww) in zip(got, want):
+        assert gw == ww
+        assert np.all(np.abs(gt - wt) <= tol)
+
+
+def test_mcsolve_per_trajectory_integrator(qt, plugin):
+    H, c_ops, psi0, e_ops = _jc(qt, N=6)
+    tl = np.linspace(0, 20, 101)
+    opts = {"method": "vern7", "map": "serial", "keep_runs_results": True}
+    ref = qt.mcsolve(H, psi0, tl, c_ops, e_ops=e_ops, ntraj=4, seeds=11, options=opts)
+    got = qt.mcsolve(H, psi0, tl, c_ops, e_ops=e_ops, ntraj=4, seeds=11,
+                     options={**opts, "method": "gpu_vern7"})
+    _same_jumps(_records(got), _records(ref))
+    _assert_expect(got.expect, ref.expect)
+
+
+def test_mcsolve_gpu_map_batched(qt, plugin):
+    H, c_ops, psi0, e_ops = _jc(qt, N=6)
+    tl = np.linspace(0, 20, 101)
+    opts = {"method": "vern7", "map": "serial", "keep_runs_results": True}
+    ref = qt.mcsolve(H, psi0, tl, c_ops, e_ops=e_ops, ntraj=32, seeds=5, options=opts)
+    got = qt.mcsolve(H, psi0, tl, c_ops, e_ops=e_ops, ntraj=32, seeds=5,
+                     options={**opts, "method": "gpu_vern7", "map": "gpu"})
+    _same_jumps(_records(got), _records(ref))
+    for g, w in zip(got.expect, ref.expect):
+        np.testing.assert_allclose(np.asarray(g), np.asarray(w), atol=2e-6)
+
+
+def test_gpudense_data_layer(qt, plugin):
+    from qutip.core import data as D
+    rng = np.random.default_rng(7)
+    d = 12
+    m = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    op = qt.rand_herm(d, density=0.3, seed=3).data
+    g = plugin.GpuDense(m)
+    np.testing.assert_allclose(g.to_array(), m)
+    np.testing.assert_allclose(D.to(D.Dense, g).to_array(), m)
+    vec = D.column_stack(g)
+    assert vec.shape == (d * d, 1)
+    np.testing.assert_allclose(vec.to_array()[:, 0], m.ravel(order="F"))
+    back = D.column_unstack(vec, d)
+    np.testing.assert_allclose(back.to_array(), m)
+    np.testing.assert_allclose(D.matmul(op, g).to_array(), op.to_array() @ m, atol=1e-12)
+    np.testing.assert_allclose(D.expect(op, g), np.trace(op.to_array() @ m), rtol=1e-12)
+    ket = plugin.GpuDense(m[:, :1])
+    want = np.vdot(m[:, 0], op.to_array() @ m[:, 0])
+    np.testing.assert_allclose(D.expect(op, ket), want, rtol=1e-12)
+    np.testing.assert_allclose(D.trace(g), np.trace(m), rtol=1e-13)
+    np.testing.assert_allclose(D.norm.l2(ket), np.linalg.norm(m[:, 0]), rtol=1e-13)
+    np.testing.assert_allclose(D.add(g, g, 0.5j).to_array(), m + 0.5j * m)
+    np.testing.assert_allclose(D.mul(g, 2 - 1j).to_array(), (2 - 1j) * m)
+    np.testing.assert_allclose(g.adjoint().to_array(), m.conj().T)
+    np.testing.assert_allclose(g.transpose().to_array(), m.T)
+    assert isinstance(D.zeros["gpu"](3, 4), plugin.GpuDense)
