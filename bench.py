@@ -125,33 +125,50 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- dist ------
 class Dist:
-    def __init__(self, n_gpus):
+    """Replicas over ranks: one process per GPU (NCCL), or CPU processes (gloo) for
+    host-side tests.  Each rank solves its own copy of the workload; ranks only
+    meet at barriers and in the max of the per-rank times."""
+
+    def __init__(self, n_gpus, backend=None):
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.rank = int(os.environ.get("RANK", "0"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
         self.pg = None
         self.n_gpus = n_gpus
+        self.backend = backend
+
+    def _cuda(self):
+        import torch
+        return self.backend != "gloo" and torch.cuda.is_available()
 
     def init(self):
         import torch
-        torch.cuda.set_device(self.local)
+        if self.backend is None:
+            self.backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if self._cuda():
+            torch.cuda.set_device(self.local)
         if self.world > 1:
             import torch.distributed as dist
-            dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+            if self.backend == "nccl":
+                dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+            else:
+                dist.init_process_group("gloo")
             self.pg = dist
 
     def barrier(self):
         import torch
-        torch.cuda.synchronize()
+        if self._cuda():
+            torch.cuda.synchronize()
         if self.pg:
             self.pg.barrier()
-        torch.cuda.synchronize()
+        if self._cuda():
+            torch.cuda.synchronize()
 
     def max(self, x: float) -> float:
         if not self.pg:
             return x
         import torch
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        t = torch.tensor([x], dtype=torch.float64, device="cuda" if self._cuda() else "cpu")
         self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
         return float(t.item())
 
