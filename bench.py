@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--served-ntraj", type=int, default=100)
     ap.add_argument("--served-plain-sample", type=int, default=60)
     ap.add_argument("--mc-ntraj", type=int, default=4096)
-    ap.add_argument("--profile", default=None, choices=["stage"],
+    ap.add_argument("--profile", default=None, choices=["stage", "batch"],
                     help="run the ncu profiling case only (fused stage kernel, untuned); "
                          "prints nothing to parse")
     ap.add_argument("--profile-sites", type=int, default=10)
@@ -363,26 +363,59 @@ def run_served(args):
 
 
 def run_mc_batch(args):
-    """Batched mcsolve of the dissipative Bose-Hubbard trimer, 4096 trajectories."""
+    """Batched mcsolve of the dissipative Bose-Hubbard trimer, 4096 trajectories: the
+    launch shape picked by the autotuner, the launch captured in a CUDA graph and
+    replayed with fresh seeds each timed step."""
     import torch
     from qutip_gb300 import systems as S
-    from qutip_gb300.batched import mcsolve_batch
+    from qutip_gb300.batched import BatchProblem, check_status, tune_batch
+    from qutip_gb300 import _lib
     s = S.bose_hubbard_trimer(8)
     tl = np.linspace(0.0, 50.0, 501)
-    mcsolve_batch(s, tl, 64, seeds=1, precision="mixed")
+    n = args.mc_ntraj
+
+    def make(ntraj, dt, tlist, seeds):
+        bp = BatchProblem(dt)
+        sid = bp.add_system(s.terms, s.e_ops, tlist, "mc", c_ops=s.c_ops)
+        for sd in seeds[:ntraj]:
+            bp.add_item(sid, s.state0, seed=sd)
+        return bp
+
     out = {}
-    for prec in ("mixed", "double"):
-        log(f"mc batch {prec}")
+    lib = _lib.load()
+    for prec, dt in (("mixed", "c64"), ("double", "c128")):
+        log(f"mc batch {prec}: tuning")
+        tune_seeds = np.random.SeedSequence(7).spawn(2432)
+        best = tune_batch(lambda k: make(k, dt, tl[:51], tune_seeds), sample_items=2432, reps=1)
+        qdt = _lib.QG_C64 if dt == "c64" else _lib.QG_C128
+        full = lib.qg_batch_group_slots(512, qdt, {"warp": 1, "cta": 2}[best["group"]])
+        seeds0 = np.random.SeedSequence(20261203).spawn(n)
+        bp = make(n, dt, tl, seeds0)
+        bp.build(max_jumps=512, group=best["group"], n_slots=max(1, int(full * best["slot_fraction"])))
+        bp.capture()
+        bp.replay()                      # warm-up replay
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r = mcsolve_batch(s, tl, args.mc_ntraj, seeds=20261203, precision=prec)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        out[prec] = {"trajectories_per_sec": args.mc_ntraj / dt, "wall_s": dt,
-                     "jumps": int(sum(len(c) for c in r.col_times)),
-                     "n_mean": [float(x.real.mean()) for x in r.expect]}
-    out["workload"] = (f"Bose-Hubbard trimer cutoff 8 (dim 512), {args.mc_ntraj} trajectories, "
-                       "tlist linspace(0,50,501), one persistent launch")
+        times = []
+        for step in range(2):
+            seeds = np.random.SeedSequence(20261204 + step).spawn(n)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            bp.replay(seeds=seeds)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        res = bp.results()
+        check_status(res)
+        runs = np.stack([r["expect"].T for r in res], axis=1)
+        dt_s = float(np.median(times))
+        out[prec] = {"trajectories_per_sec": n / dt_s, "wall_s": dt_s,
+                     "jumps": int(sum(r["jumps"] for r in res)),
+                     "n_mean_final": [float(runs[k, :, -1].real.mean()) for k in range(runs.shape[0])],
+                     "launch": {"group": best["group"], "slot_fraction": best["slot_fraction"],
+                                "n_slots": int(bp.n_slots), "tuned_ms": best["timings"]
+                                and {f"{g}@{f}": round(ms, 2) for (g, f), ms in best["timings"].items()},
+                                "graph": "captured once, replayed with new seeds (in-place item table)"}}
+    out["workload"] = (f"Bose-Hubbard trimer cutoff 8 (dim 512), {n} trajectories, "
+                       "tlist linspace(0,50,501), one persistent launch per step")
     return out
 
 
@@ -529,10 +562,26 @@ def run_profile_case(args):
     print(f"c64 mixed: launch {op.launch_desc()}, {op.spmv_bytes() / 1e9:.3f} GB per matvec")
 
 
+def run_profile_batch(args):
+    """ncu case for the batched trajectory kernel: 256 Bose-Hubbard trajectories,
+    t in [0, 5] (51 outputs), mixed form, default launch shape."""
+    import torch
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import mcsolve_batch
+    torch.cuda.set_device(0)
+    s = S.bose_hubbard_trimer(8)
+    r = mcsolve_batch(s, np.linspace(0.0, 5.0, 51), 256, seeds=5, precision="mixed")
+    torch.cuda.synchronize()
+    print(f"batch: {len(r.col_times)} trajectories, {sum(len(c) for c in r.col_times)} jumps")
+
+
 def main():
     args = parse()
-    if args.profile:
+    if args.profile == "stage":
         run_profile_case(args)
+        return
+    if args.profile == "batch":
+        run_profile_batch(args)
         return
     dist = Dist(args.gpus)
     if args.impl == "reference":

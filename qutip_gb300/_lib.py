@@ -19,6 +19,7 @@ QG_MAX_GROUPS, QG_MAX_EOPS = 8, 32
 
 QG_LAYOUT_GROUP_MAJOR, QG_LAYOUT_ROW_MAJOR, QG_LAYOUT_SLICED = 0, 1, 2
 QG_TILE_ROWS = 512
+QG_GROUP_AUTO, QG_GROUP_WARP, QG_GROUP_CTA = 0, 1, 2
 
 
 class CsrGroups(C.Structure):
@@ -73,6 +74,7 @@ _SIGS = {
     "qg_abi_sizes": (C.c_int, [C.c_void_p, C.c_int]),
     "qg_batch_slot_bytes": (C.c_int64, [C.c_int64, C.c_int]),
     "qg_batch_max_slots": (C.c_int, [C.c_int64, C.c_int]),
+    "qg_batch_group_slots": (C.c_int, [C.c_int64, C.c_int, C.c_int]),
     "qg_batch_vern7": (C.c_int, [C.c_void_p, C.c_void_p]),
     "qg_batch_vern7_noalloc": (C.c_int, [C.c_void_p, C.c_void_p]),
 }

@@ -7,7 +7,11 @@ qutip/solver/parallel.py:267-338).  Here every system's generator, e_ops and
 collapse operators are packed into shared device pools; each *item* (a
 master-equation solve, or one Monte-Carlo trajectory with its own PCG64 stream)
 is an entry of an item table, and ``qg_batch_vern7`` runs all of them in one
-persistent launch, one CTA per item at a time, each with its own adaptive step.
+persistent launch, one warp (small states) or one CTA (large states) per item at
+a time, each with its own adaptive step.  :meth:`BatchProblem.capture` records
+the launch in a CUDA graph that :meth:`BatchProblem.replay` re-runs with new
+seeds written in place; :func:`tune_batch` picks the group shape and slot count
+by timing them on a sample of the items.
 
 Trajectories reuse their system's operators (one copy in HBM however many
 trajectories run).  Per-trajectory random streams are numpy's PCG64 states
@@ -52,7 +56,7 @@ class BatchStruct(C.Structure):
                 ("jump_which", C.c_void_p), ("max_jumps", C.c_int32), ("n_slots", C.c_int32),
                 ("work", C.c_void_p), ("queue", C.c_void_p), ("cancel", C.c_void_p),
                 ("progress", C.c_void_p), ("debug", C.c_void_p),
-                ("norm_steps", C.c_int32), ("pad_", C.c_int32), ("norm_t_tol", C.c_double),
+                ("norm_steps", C.c_int32), ("group", C.c_int32), ("norm_t_tol", C.c_double),
                 ("norm_tol", C.c_double), ("norm_min_step", C.c_double),
                 ("mc_corr_eps", C.c_double)]
 
@@ -206,8 +210,11 @@ class BatchProblem:
         a = np.concatenate([a, np.zeros(pad, np_dtype)])
         return torch.from_numpy(a).to(self.device, dtype)
 
-    def build(self, max_jumps=0, mc_options=None, order=None, n_slots=None):
-        """Upload pools; ``order`` permutes the items (longest first balances the queue)."""
+    def build(self, max_jumps=0, mc_options=None, order=None, n_slots=None, group="auto"):
+        """Upload pools; ``order`` permutes the items (longest first balances the queue).
+
+        ``group`` is ``"auto"``, ``"warp"`` or ``"cta"`` (threads per item);
+        ``n_slots`` caps the resident groups (default: all that fit)."""
         if not self.items:
             raise ValueError("no items")
         lib = _lib.load()
@@ -243,9 +250,12 @@ class BatchProblem:
         self.jump_which = torch.zeros(max(n_items * self.max_jumps, 1), dtype=torch.int32,
                                       device=self.device)
         self.max_n = max(info["n"] for info in self.sys_info)
-        slots = lib.qg_batch_max_slots(self.max_n, qdt)
+        if group not in GROUPS:
+            raise ValueError(f"group must be one of {sorted(GROUPS)}")
+        self.group = group
+        slots = lib.qg_batch_group_slots(self.max_n, qdt, GROUPS[group])
         if slots < 0:
-            _lib.check(slots, "qg_batch_max_slots")
+            _lib.check(slots, "qg_batch_group_slots")
         self.n_slots = int(min(n_items, slots if n_slots is None else n_slots))
         slot_bytes = int(lib.qg_batch_slot_bytes(self.max_n, qdt))
         self.work = torch.empty(self.n_slots * slot_bytes, dtype=torch.uint8, device=self.device)
@@ -258,7 +268,7 @@ class BatchProblem:
             p(self.coef_consts), p(self.eop_rp), p(self.eop_col), p(self.eop_val), p(self.cop_rp),
             p(self.cop_col), p(self.cop_val), p(self.tlist_d), p(self.y0_d), p(self.out),
             p(self.status), p(self.jump_t), p(self.jump_which), self.max_jumps, self.n_slots,
-            p(self.work), p(self.queue), None, None, None, int(mc["norm_steps"]), 0,
+            p(self.work), p(self.queue), None, None, None, int(mc["norm_steps"]), GROUPS[group],
             float(mc["norm_t_tol"]),
             float(mc["norm_tol"]), float(mc["norm_min_step"]), float(mc["mc_corr_eps"]))
         return self
@@ -269,6 +279,43 @@ class BatchProblem:
 
     def launch(self):
         _lib.call("qg_batch_vern7", C.byref(self.struct), stream_ptr())
+
+    # -- CUDA graph --------------------------------------------------------
+    def capture(self):
+        """Record one launch in a CUDA graph (on a side stream, as torch requires).
+
+        The graph keeps this problem's device pointers; :meth:`replay` re-runs it
+        after writing new per-item seeds into the item table in place."""
+        self._items_np = np.array([self.items[i] for i in self.order], dtype=ITEM_DTYPE)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.launch()
+        torch.cuda.synchronize()
+        return self.graph
+
+    def replay(self, seeds=None):
+        """Re-run the captured launch; ``seeds`` (one per item, in item order) gives
+        every trajectory a new PCG64 stream (SeedSequence / int / (state, inc))."""
+        if getattr(self, "graph", None) is None:
+            raise RuntimeError("capture() first")
+        if seeds is not None:
+            seeds = list(seeds)
+            if len(seeds) != len(self.items):
+                raise ValueError("one seed per item")
+            inv = np.empty_like(self.order)
+            inv[self.order] = np.arange(len(self.order))
+            for i, sd in enumerate(seeds):
+                state, inc = sd if isinstance(sd, tuple) else pcg_state_of(sd)
+                row = inv[i]
+                self._items_np[row]["sh"], self._items_np[row]["sl"] = _split128(state)
+                self._items_np[row]["ih"], self._items_np[row]["il"] = _split128(inc)
+                it = list(self.items[i])
+                it[4:8] = [*_split128(state), *_split128(inc)]
+                self.items[i] = tuple(it)
+            host = torch.from_numpy(self._items_np.view(np.uint8).copy())
+            self.items_d.copy_(host, non_blocking=False)
+        self.graph.replay()
 
     def results(self, normalize=True):
         """Per item (original order): expect [n_out, n_eops], status row, jumps."""
@@ -294,6 +341,59 @@ class BatchProblem:
                             col_times=jt[k * self.max_jumps:k * self.max_jumps + min(nj, self.max_jumps)].copy(),
                             col_which=jw[k * self.max_jumps:k * self.max_jumps + min(nj, self.max_jumps)].copy()))
         return res
+
+
+GROUPS = {"auto": _lib.QG_GROUP_AUTO, "warp": _lib.QG_GROUP_WARP, "cta": _lib.QG_GROUP_CTA}
+
+_TUNED: dict = {}
+
+
+def tune_batch(make_problem, sample_items=256, candidates=None, reps=2):
+    """Pick the group shape and slot count of a batch by timing them.
+
+    ``make_problem(n_items)`` returns an unbuilt :class:`BatchProblem` with the
+    first ``n_items`` items of the real batch.  Each candidate ``(group,
+    slot_fraction)`` is built and launched ``reps`` times on that sample (events
+    on the current stream); the fastest is returned and cached by (dtype, max_n
+    bucket, kind).  Candidates default to warp and CTA groups at full, 3/4 and
+    1/2 of the resident slots.
+    """
+    probe = make_problem(sample_items)
+    kind = probe.sys_info[0]["kind"] if probe.sys_info else 0
+    max_n = max(info["n"] for info in probe.sys_info)
+    key = (probe.dtype, int(np.ceil(np.log2(max(max_n, 2)))), kind)
+    if key in _TUNED:
+        return _TUNED[key]
+    candidates = candidates or [(g, f) for g in ("warp", "cta") for f in (1.0, 0.75, 0.5)]
+    lib = _lib.load()
+    qdt = _lib.QG_C64 if probe.dtype == "c64" else _lib.QG_C128
+    best = None
+    timings = {}
+    for group, frac in candidates:
+        full = lib.qg_batch_group_slots(max_n, qdt, GROUPS[group])
+        if full <= 0:
+            continue
+        n_slots = max(1, int(full * frac))
+        bp = make_problem(sample_items)
+        bp.build(max_jumps=probe_max_jumps(bp), n_slots=n_slots, group=group)
+        bp.launch()  # warm-up
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        for _ in range(reps):
+            bp.launch()
+        end.record()
+        end.synchronize()
+        ms = start.elapsed_time(end) / reps
+        timings[(group, frac)] = ms
+        if best is None or ms < best[2]:
+            best = (group, frac, ms)
+    _TUNED[key] = {"group": best[0], "slot_fraction": best[1], "ms": best[2],
+                   "timings": timings, "sample_items": sample_items}
+    return _TUNED[key]
+
+
+def probe_max_jumps(bp):
+    return 4096 if any(info["kind"] == 1 for info in bp.sys_info) else 0
 
 
 STATUS_TEXT = {
@@ -339,11 +439,13 @@ def mesolve_batch(systems, tlists, precision="mixed", atol=1e-8, rtol=1e-6, nste
 
 
 def mcsolve_batch(system: OpenSystem, tlist, ntraj, seeds=None, precision="mixed", atol=1e-8,
-                  rtol=1e-6, nsteps=1000, max_jumps=512, mc_options=None) -> MCResult:
+                  rtol=1e-6, nsteps=1000, max_jumps=512, mc_options=None, group="auto",
+                  n_slots=None) -> MCResult:
     """All ``ntraj`` trajectories of one Monte-Carlo system in one persistent launch.
 
     ``seeds``: an int / SeedSequence (spawned like the reference's ``_read_seed``,
     qutip/solver/multitraj.py:354-374) or a list of per-trajectory seeds.
+    ``group`` / ``n_slots``: launch shape (see :meth:`BatchProblem.build`).
     """
     if system.kind != "mc":
         raise ValueError("mcsolve_batch needs a system built with kind='mc'")
@@ -357,7 +459,7 @@ def mcsolve_batch(system: OpenSystem, tlist, ntraj, seeds=None, precision="mixed
     for i in range(ntraj):
         bp.add_item(sid, system.state0, seed=seeds[i])
     t0 = time.perf_counter()
-    bp.build(max_jumps=max_jumps, mc_options=mc_options)
+    bp.build(max_jumps=max_jumps, mc_options=mc_options, group=group, n_slots=n_slots)
     bp.launch()
     res = bp.results()
     check_status(res)

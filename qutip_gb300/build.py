@@ -42,6 +42,13 @@ def generate_tableau() -> Path:
     h = lambda x: float(x).hex()  # noqa: E731
     arr1 = lambda v: "{" + ", ".join(h(x) for x in v) + "}"  # noqa: E731
     arr2 = lambda m: "{" + ", ".join(arr1(r) for r in m) + "}"  # noqa: E731
+    # float pairs hi + lo with hi = fl32(x), lo = fl32(x - hi) (about 48 significant bits)
+    import numpy as np
+    f32 = lambda x: float(np.float32(x))  # noqa: E731
+    hi = lambda v: [f32(x) for x in v]  # noqa: E731
+    lo = lambda v: [f32(x - f32(x)) for x in v]  # noqa: E731
+    fa1 = lambda v: "{" + ", ".join(float(x).hex() + "f" if x else "0.0f" for x in v) + "}"  # noqa: E731
+    fa2 = lambda m: "{" + ", ".join(fa1(r) for r in m) + "}"  # noqa: E731
     src = f"""// Generated from qutip_gb300/vern7_tableau.py by qutip_gb300/build.py.  Do not edit.
 #pragma once
 namespace qg {{
@@ -54,6 +61,11 @@ static __constant__ double VERN7_B[10] = {arr1(T.B)};
 static __constant__ double VERN7_C[16] = {arr1(T.C)};
 static __constant__ double VERN7_E[10] = {arr1(T.E)};
 static __constant__ double VERN7_BI[16][7] = {arr2(T.BI)};
+static __constant__ float VERN7_AH[16][16] = {fa2([hi(r) for r in a])};
+static __constant__ float VERN7_AL[16][16] = {fa2([lo(r) for r in a])};
+static __constant__ float VERN7_BH[10] = {fa1(hi(T.B))};
+static __constant__ float VERN7_BL[10] = {fa1(lo(T.B))};
+static __constant__ float VERN7_EF[10] = {fa1(hi(T.E))};
 static const double VERN7_A_HOST[16][16] = {arr2(a)};
 static const double VERN7_B_HOST[10] = {arr1(T.B)};
 static const double VERN7_C_HOST[16] = {arr1(T.C)};

@@ -72,14 +72,15 @@ constexpr int MC_MAX_ITER = 1 << 22;
 __host__ __device__ inline int64_t align256(int64_t b) { return (b + 255) & ~(int64_t)255; }
 
 struct SlotLayout {
-  int64_t y, ys, k, ytmp, ctmp, total;
+  int64_t y, ys, yl, k, ytmp, ctmp, total;
 };
 __host__ __device__ inline SlotLayout slot_layout(int64_t n, int dt) {
   const int64_t es = dt == QG_C128 ? 16 : 8;
   SlotLayout L;
   L.y = 0;                                  // 2 state buffers (complex128)
-  L.ys = L.y + align256(2 * n * 16);        // 2 stage-dtype shadows (mixed form)
-  L.k = L.ys + align256(2 * n * es);        // 16 stage derivatives
+  L.ys = L.y + align256(2 * n * 16);        // 2 stage-dtype shadows (mixed form: hi parts)
+  L.yl = L.ys + align256(2 * n * es);       // 2 low parts (mixed form only)
+  L.k = L.yl + align256(dt == QG_C64 ? 2 * n * 8 : 0);  // 16 stage derivatives
   L.ytmp = L.k + align256(16 * n * es);     // 2 stage inputs
   L.ctmp = L.ytmp + align256(2 * n * es);   // 2 complex128 temporaries (MC)
   L.total = L.ctmp + align256(2 * n * 16);
@@ -130,6 +131,7 @@ struct CtaGroup {
 struct Ctl {
   double t, t_prev, t_front, dt_safe, dt_int;
   double bf[16];  // dense-output factors (dt-scaled) of the current output
+  float bfh[16], bfl[16];  // the same as float pairs hi + lo (mixed form)
   int status, cur, interp_ready, out_front, steps, rhs;
 };
 
@@ -141,11 +143,13 @@ struct Ctx {
   int n, d, G;
   double2* y[2];
   ST* ys[2];
+  ST* yl[2];  // mixed form: y = ys + yl to about 48 bits, the stage-input base
   ST* k;
   ST* ytmp;
   double2* ctmp[2];
   const ST* opval;
   double2 coef[QG_MAX_GROUPS];  // coefficients at the current stage time
+  float2 coef_f[QG_MAX_GROUPS];  // the same in FP32 (mixed form)
 };
 
 template <typename T>
@@ -168,6 +172,7 @@ __device__ __forceinline__ void load_coef(Ctx<DT>& X, double t) {
       c = eval_coef(X.B->coef_code + st, X.B->coef_consts, t);
     }
     X.coef[g] = make_double2(c.re, c.im);
+    X.coef_f[g] = make_float2((float)c.re, (float)c.im);
   }
 }
 
@@ -190,7 +195,14 @@ __device__ __forceinline__ void row_matvec(const Ctx<DT>& X, int r, const XT* x,
       gi = fma((CT)v.x, (CT)xv.y, gi);
       gi = fma((CT)v.y, (CT)xv.x, gi);
     }
-    const CT cr = (CT)X.coef[g].x, ci = (CT)X.coef[g].y;
+    CT cr, ci;
+    if constexpr (DT == QG_C64) {
+      cr = X.coef_f[g].x;
+      ci = X.coef_f[g].y;
+    } else {
+      cr = X.coef[g].x;
+      ci = X.coef[g].y;
+    }
     ar += cr * gr - ci * gi;
     ai += cr * gi + ci * gr;
   }
@@ -229,6 +241,31 @@ __device__ __forceinline__ void ff_acc(float& hi, float& lo, float fh, float fl,
   lo = __fadd_rn(lo, __fadd_rn(e, pe));
 }
 
+// dt * a as a float pair from dt = dh + dl and a = ah + al (tableau hi/lo):
+// hi = fl(dh ah), lo = the product's rounding error plus the cross terms.
+__device__ __forceinline__ void ff_factor(float dh, float dl, float ah, float al, float& fh,
+                                          float& fl) {
+  fh = __fmul_rn(dh, ah);
+  float e = fmaf(dh, ah, -fh);
+  e = fmaf(dh, al, e);
+  fl = fmaf(dl, ah, e);
+}
+
+// fl32(bh + bl + ih + il): TwoSum of the high parts, the low parts added to its
+// error, one final rounding.
+__device__ __forceinline__ float ff_round4(float bh, float bl, float ih, float il) {
+  const float sum = __fadd_rn(bh, ih);
+  const float bp = __fsub_rn(sum, bh);
+  float e = __fadd_rn(__fsub_rn(bh, __fsub_rn(sum, bp)), __fsub_rn(ih, bp));
+  e = __fadd_rn(e, __fadd_rn(bl, il));
+  return __fadd_rn(sum, e);
+}
+
+__device__ __forceinline__ void split_f(double v, float& h, float& l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
 // One fused stage: k_s = A(t_prev + c_s dt) x_s and the next stage input, or at
 // s == 9 y_front and the WRMS error (returned).  In the mixed form the stage
 // input x_{s+1} = y_prev + sum_j dt a_{s+1,j} k_j is accumulated in float-float
@@ -239,22 +276,48 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
   using ST = typename elem<DT>::T;
   using CT = typename elem<DT>::R;
   constexpr bool MIXED = (DT == QG_C64);
+  const bool last = (s == RK_STEP - 1);
+  const bool forms_input = !last && s != RK_EXTRA_STEP - 1;
+  const int nk = last ? RK_STEP : s + 1;  // k_j that enter the combination
+  // factors: FP64 for the double form; float pairs from the hi/lo tableau for the
+  // mixed form (no FP64 work per stage)
   CT fa[16], fe[16];
-  float fl[16];  // low parts of the factors (mixed form)
+  float fl[16];
+  if constexpr (MIXED) {
+    float dh, dl;
+    split_f(dt, dh, dl);
 #pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    double a = 0.0, e = 0.0;
-    if (s == RK_STEP - 1) {
-      if (j < RK_STEP) {
-        a = dt * VERN7_B[j];
-        e = dt * VERN7_E[j];
+    for (int j = 0; j < 16; ++j) {
+      float ah = 0.f, al = 0.f, e = 0.f;
+      if (j < nk) {
+        if (last) {
+          ah = VERN7_BH[j];
+          al = VERN7_BL[j];
+          e = VERN7_EF[j];
+        } else if (forms_input) {
+          ah = VERN7_AH[s + 1][j];
+          al = VERN7_AL[s + 1][j];
+        }
       }
-    } else if (s + 1 < RK_EXTRA_STEP && j <= s) {
-      a = dt * VERN7_A[s + 1][j];
+      ff_factor(dh, dl, ah, al, fa[j], fl[j]);
+      fe[j] = dh * e;
     }
-    fa[j] = (CT)a;
-    fe[j] = (CT)e;
-    fl[j] = (float)(a - (double)fa[j]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      double a = 0.0, e = 0.0;
+      if (j < nk) {
+        if (last) {
+          a = dt * VERN7_B[j];
+          e = dt * VERN7_E[j];
+        } else if (forms_input) {
+          a = dt * VERN7_A[s + 1][j];
+        }
+      }
+      fa[j] = (CT)a;
+      fe[j] = (CT)e;
+      fl[j] = 0.f;
+    }
   }
   load_coef(X, c.t_prev + VERN7_C[s] * dt);
   const int cur = c.cur;
@@ -268,12 +331,14 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
   ST* out = X.ytmp + (int64_t)((s + 1) & 1) * X.n;
   const int64_t n = X.n;
   double err_acc = 0.0;
+  float err_accf = 0.f;
+  const float atol_f = (float)X.S->atol, rtol_f = (float)X.S->rtol;
   for (int r = g.rank; r < X.n; r += GT::SIZE) {
     CT ar, ai;
     row_matvec(X, r, x, ar, ai);
     st2(X.k + s * n + r, (double)ar, (double)ai);
     const ST ks = X.k[s * n + r];
-    if (s != RK_STEP - 1 && s != RK_EXTRA_STEP - 1) {
+    if (forms_input) {
       if constexpr (MIXED) {
         float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;
         for (int j = 0; j <= s; ++j) {
@@ -283,8 +348,8 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
             ff_acc(hi, li, fa[j], fl[j], kj.y);
           }
         }
-        const double2 yv = X.y[cur][r];
-        st2(out + r, yv.x + ((double)hr + (double)lr), yv.y + ((double)hi + (double)li));
+        const float2 bh = X.ys[cur][r], bl = X.yl[cur][r];
+        out[r] = make_float2(ff_round4(bh.x, bl.x, hr, lr), ff_round4(bh.y, bl.y, hi, li));
       } else {
         CT vr = X.y[cur][r].x, vi = X.y[cur][r].y;
         for (int j = 0; j <= s; ++j) {
@@ -297,26 +362,32 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
         }
         st2(out + r, (double)vr, (double)vi);
       }
-    } else if (s == RK_STEP - 1) {
-      CT er = 0, ei = 0;
-      double yr, yi;
+    } else if (last) {
       if constexpr (MIXED) {
-        float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;
+        float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f, er = 0.f, ei = 0.f;
         for (int j = 0; j < RK_STEP; ++j) {
-          const CT fb = fa[j], fq = fe[j];
-          if (fb == (CT)0 && fl[j] == 0.f && fq == (CT)0) continue;
+          if (fa[j] == 0.f && fl[j] == 0.f && fe[j] == 0.f) continue;
           const ST kj = (j == s) ? ks : X.k[j * n + r];
-          ff_acc(hr, lr, fb, fl[j], kj.x);
-          ff_acc(hi, li, fb, fl[j], kj.y);
-          er = fma(fq, (CT)kj.x, er);
-          ei = fma(fq, (CT)kj.y, ei);
+          ff_acc(hr, lr, fa[j], fl[j], kj.x);
+          ff_acc(hi, li, fa[j], fl[j], kj.y);
+          er = fmaf(fe[j], kj.x, er);
+          ei = fmaf(fe[j], kj.y, ei);
         }
-        yr = X.y[cur][r].x + ((double)hr + (double)lr);
-        yi = X.y[cur][r].y + ((double)hi + (double)li);
-        X.ys[cur ^ 1][r] = make_float2((float)yr, (float)yi);
+        // the once-per-step FP64 state update, then its float-pair shadow
+        const double yr = X.y[cur][r].x + ((double)hr + (double)lr);
+        const double yi = X.y[cur][r].y + ((double)hi + (double)li);
+        X.y[cur ^ 1][r] = make_double2(yr, yi);
+        float shr, slr, shi, sli;
+        split_f(yr, shr, slr);
+        split_f(yi, shi, sli);
+        X.ys[cur ^ 1][r] = make_float2(shr, shi);
+        X.yl[cur ^ 1][r] = make_float2(slr, sli);
+        // WRMS error terms in FP32 (the sum over rows is FP64)
+        const float w = sqrtf(er * er + ei * ei) / (atol_f + rtol_f * sqrtf(shr * shr + shi * shi));
+        err_accf = fmaf(w, w, err_accf);
       } else {
-        yr = X.y[cur][r].x;
-        yi = X.y[cur][r].y;
+        CT er = 0, ei = 0;
+        double yr = X.y[cur][r].x, yi = X.y[cur][r].y;
         for (int j = 0; j < RK_STEP; ++j) {
           const double fb = (double)fa[j], fq = (double)fe[j];
           if (fb == 0.0 && fq == 0.0) continue;
@@ -330,18 +401,49 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
             ei = fma((CT)fq, (CT)kj.y, ei);
           }
         }
+        X.y[cur ^ 1][r] = make_double2(yr, yi);
+        const double w = sqrt((double)er * er + (double)ei * ei) /
+                         (X.S->atol + X.S->rtol * sqrt(yr * yr + yi * yi));
+        err_acc += w * w;
       }
-      X.y[cur ^ 1][r] = make_double2(yr, yi);
-      const double w = sqrt((double)er * er + (double)ei * ei) /
-                       (X.S->atol + X.S->rtol * sqrt(yr * yr + yi * yi));
-      err_acc += w * w;
     }
   }
   c.rhs += 1;
   double err = 0.0;
-  if (s == RK_STEP - 1) err = sqrt(g.sum(err_acc) / (double)X.n);
+  if (last) err = sqrt(g.sum(MIXED ? (double)err_accf : err_acc) / (double)X.n);
   g.sync();
   return err;
+}
+
+// Mixed form: out = fl32(y_prev + sum_{j<nk} dt a_{row,j} k_j) in float pairs from
+// the (ys, yl) base -- the stage input of the first dense-output stage.
+template <int DT, class GT>
+__device__ void form_input_mixed(const GT& g, Ctx<DT>& X, const Ctl& c, typename elem<DT>::T* out,
+                                 int row, int nk, double dt) {
+  using ST = typename elem<DT>::T;
+  float fa[16], fl[16];
+  float dh, dl;
+  split_f(dt, dh, dl);
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const float ah = j < nk ? VERN7_AH[row][j] : 0.f, al = j < nk ? VERN7_AL[row][j] : 0.f;
+    ff_factor(dh, dl, ah, al, fa[j], fl[j]);
+  }
+  const int cur = c.cur;
+  const int64_t n = X.n;
+  for (int r = g.rank; r < X.n; r += GT::SIZE) {
+    float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;
+    for (int j = 0; j < nk; ++j) {
+      if (fa[j] != 0.f || fl[j] != 0.f) {
+        const ST kj = X.k[j * n + r];
+        ff_acc(hr, lr, fa[j], fl[j], kj.x);
+        ff_acc(hi, li, fa[j], fl[j], kj.y);
+      }
+    }
+    const float2 bh = X.ys[cur][r], bl = X.yl[cur][r];
+    out[r] = make_float2(ff_round4(bh.x, bl.x, hr, lr), ff_round4(bh.y, bl.y, hi, li));
+  }
+  g.sync();
 }
 
 // out = base + sum_{j<nk} c.bf[j] k_j
@@ -361,19 +463,33 @@ __device__ void combine(const GT& g, Ctx<DT>& X, const Ctl& c, OT* out, const BT
   g.sync();
 }
 
-// entry i of the current state: y_front, or y_prev + sum_j bf_j k_j
+// entry i of the current state: y_front, or y_prev + sum_j bf_j k_j (the mixed
+// form sums the increment in float pairs and adds it to y_prev in FP64)
 template <int DT>
 __device__ __forceinline__ double2 state_at(const Ctx<DT>& X, const Ctl& c, int i) {
   if (c.out_front) return X.y[c.cur ^ 1][i];
-  double vr = X.y[c.cur][i].x, vi = X.y[c.cur][i].y;
-  for (int j = 0; j < RK_EXTRA_STEP; ++j) {
-    const double f = c.bf[j];
-    if (f != 0.0) {
-      vr = fma(f, (double)X.k[(int64_t)j * X.n + i].x, vr);
-      vi = fma(f, (double)X.k[(int64_t)j * X.n + i].y, vi);
+  if constexpr (DT == QG_C64) {
+    float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;
+    for (int j = 0; j < RK_EXTRA_STEP; ++j) {
+      if (c.bfh[j] != 0.f || c.bfl[j] != 0.f) {
+        const float2 kj = X.k[(int64_t)j * X.n + i];
+        ff_acc(hr, lr, c.bfh[j], c.bfl[j], kj.x);
+        ff_acc(hi, li, c.bfh[j], c.bfl[j], kj.y);
+      }
     }
+    return make_double2(X.y[c.cur][i].x + ((double)hr + (double)lr),
+                        X.y[c.cur][i].y + ((double)hi + (double)li));
+  } else {
+    double vr = X.y[c.cur][i].x, vi = X.y[c.cur][i].y;
+    for (int j = 0; j < RK_EXTRA_STEP; ++j) {
+      const double f = c.bf[j];
+      if (f != 0.0) {
+        vr = fma(f, (double)X.k[(int64_t)j * X.n + i].x, vr);
+        vi = fma(f, (double)X.k[(int64_t)j * X.n + i].y, vi);
+      }
+    }
+    return make_double2(vr, vi);
   }
-  return make_double2(vr, vi);
 }
 
 template <int DT, class GT>
@@ -406,8 +522,11 @@ __device__ __noinline__ void set_initial(const GT& g, Ctx<DT>& X, Ctl& c, const 
     X.y[cur][r] = v;
     X.y[cur ^ 1][r] = v;
     if constexpr (MIXED) {
-      X.ys[cur][r] = make_float2((float)v.x, (float)v.y);
-      X.ys[cur ^ 1][r] = make_float2((float)v.x, (float)v.y);
+      float hr, lr, hi, li;
+      split_f(v.x, hr, lr);
+      split_f(v.y, hi, li);
+      X.ys[cur][r] = X.ys[cur ^ 1][r] = make_float2(hr, hi);
+      X.yl[cur][r] = X.yl[cur ^ 1][r] = make_float2(lr, li);
     }
   }
   g.sync();
@@ -450,10 +569,15 @@ __device__ __noinline__ void set_initial(const GT& g, Ctx<DT>& X, Ctl& c, const 
 // _prep_dense_out (explicit_rk.pyx:399-410)
 template <int DT, class GT>
 __device__ __noinline__ void prep_dense_out(const GT& g, Ctx<DT>& X, Ctl& c) {
+  using ST = typename elem<DT>::T;
   const double dt = c.dt_int;
-  for (int j = 0; j < 16; ++j) c.bf[j] = j < RK_STEP ? dt * VERN7_A[RK_STEP][j] : 0.0;
-  // FP64 combination from the complex128 y_prev, rounded once to the stage type
-  combine(g, X, c, X.ytmp + (int64_t)(RK_STEP & 1) * X.n, X.y[c.cur], RK_STEP);
+  ST* x10 = X.ytmp + (int64_t)(RK_STEP & 1) * X.n;
+  if constexpr (DT == QG_C64) {
+    form_input_mixed(g, X, c, x10, RK_STEP, RK_STEP, dt);
+  } else {
+    for (int j = 0; j < 16; ++j) c.bf[j] = j < RK_STEP ? dt * VERN7_A[RK_STEP][j] : 0.0;
+    combine(g, X, c, x10, X.y[c.cur], RK_STEP);
+  }
   for (int s = RK_STEP; s < RK_EXTRA_STEP; ++s) stage(g, X, c, s, dt);
   c.interp_ready = 1;
 }
@@ -468,6 +592,7 @@ __device__ __forceinline__ void set_interp(Ctl& c, double t) {
       acc *= tau;
     }
     c.bf[i] = c.dt_int * acc;
+    split_f(c.bf[i], c.bfh[i], c.bfl[i]);
   }
   c.out_front = 0;
   c.t = t;
@@ -790,6 +915,8 @@ __device__ __forceinline__ void bind_slot(Ctx<DT>& X, const qg_batch& B, int64_t
   X.y[1] = X.y[0] + B.max_n;
   X.ys[0] = reinterpret_cast<ST*>(slot + L.ys);
   X.ys[1] = X.ys[0] + B.max_n;
+  X.yl[0] = reinterpret_cast<ST*>(slot + L.yl);
+  X.yl[1] = X.yl[0] + B.max_n;
   X.k = reinterpret_cast<ST*>(slot + L.k);
   X.ytmp = reinterpret_cast<ST*>(slot + L.ytmp);
   X.ctmp[0] = reinterpret_cast<double2*>(slot + L.ctmp);
@@ -849,7 +976,9 @@ __global__ void __launch_bounds__(CTA_BLOCK) batch_cta_kernel(qg_batch B) {
   if (g.rank == 0) finish_queue(B, gridDim.x);
 }
 
-static bool warp_mode(int64_t max_n) { return max_n <= WARP_MAX_N; }
+static bool warp_mode(int64_t max_n, int group) {
+  return group == QG_GROUP_WARP || (group == QG_GROUP_AUTO && max_n <= WARP_MAX_N);
+}
 
 }  // namespace qg
 
@@ -911,7 +1040,7 @@ extern "C" int qg_batch_vern7_noalloc(const qg_batch* B, void* stream) {
   NoallocAddr a;
   int rc = noalloc_setup(dev, a);
   if (rc) return rc;
-  int occ = qg_batch_max_slots(B->max_n, B->dtype);
+  int occ = qg_batch_group_slots(B->max_n, B->dtype, B->group);
   if (occ <= 0) return occ < 0 ? occ : set_error(QG_ERR_CUDA, "no resident CTA");
   int64_t slots = (int64_t)NOALLOC_WORK_BYTES / slot;
   if (slots > occ) slots = occ;
@@ -931,10 +1060,12 @@ extern "C" int64_t qg_batch_slot_bytes(int64_t max_n, int dtype) {
   return slot_layout(max_n, dtype).total;
 }
 
-extern "C" int qg_batch_max_slots(int64_t max_n, int dtype) {
+extern "C" int qg_batch_group_slots(int64_t max_n, int dtype, int group) {
+  if (group != QG_GROUP_AUTO && group != QG_GROUP_WARP && group != QG_GROUP_CTA)
+    return set_error(QG_ERR_ARG, "group must be QG_GROUP_AUTO, QG_GROUP_WARP or QG_GROUP_CTA");
   int per_sm = 0;
   cudaError_t e;
-  const bool warp = warp_mode(max_n);
+  const bool warp = warp_mode(max_n, group);
   if (dtype == QG_C64)
     e = warp ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_warp_kernel<QG_C64>,
                                                              WARP_BLOCK, 0)
@@ -950,6 +1081,10 @@ extern "C" int qg_batch_max_slots(int64_t max_n, int dtype) {
   return sm_count() * per_sm * (warp ? WARP_BLOCK / 32 : 1);
 }
 
+extern "C" int qg_batch_max_slots(int64_t max_n, int dtype) {
+  return qg_batch_group_slots(max_n, dtype, QG_GROUP_AUTO);
+}
+
 extern "C" int qg_batch_vern7(const qg_batch* B, void* stream) {
   if (!B || !B->systems || !B->items || !B->op_rp || !B->op_col || !B->op_val || !B->tlist ||
       !B->y0 || !B->out || !B->status || !B->work || !B->queue)
@@ -960,9 +1095,11 @@ extern "C" int qg_batch_vern7(const qg_batch* B, void* stream) {
     return set_error(QG_ERR_ARG, "bad batch sizes");
   if (B->max_jumps > 0 && (!B->jump_t || !B->jump_which))
     return set_error(QG_ERR_ARG, "jump record buffers missing");
+  if (B->group != QG_GROUP_AUTO && B->group != QG_GROUP_WARP && B->group != QG_GROUP_CTA)
+    return set_error(QG_ERR_ARG, "group must be QG_GROUP_AUTO, QG_GROUP_WARP or QG_GROUP_CTA");
   if (B->n_items == 0) return QG_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  if (warp_mode(B->max_n)) {
+  if (warp_mode(B->max_n, B->group)) {
     const int per = WARP_BLOCK / 32;
     const int grid = (B->n_slots + per - 1) / per;
     if (B->dtype == QG_C64) batch_warp_kernel<QG_C64><<<grid, WARP_BLOCK, 0, st>>>(*B);

@@ -58,7 +58,7 @@ def test_batched_ising_td_matches_reference():
         _close(ex[0][k].real, g["expect"][k])
 
 
-def _mc_golden(name, build, precision):
+def _mc_golden(name, build, precision, group="auto"):
     from qutip_gb300.batched import mcsolve_batch
     g = golden(name)
     s = build()
@@ -67,7 +67,7 @@ def _mc_golden(name, build, precision):
     for tr in range(ntraj):
         row = [int(v) for v in g["pcg_state"][tr]]
         seeds.append(((row[0] << 64) | row[1], (row[2] << 64) | row[3]))
-    r = mcsolve_batch(s, g["tlist"], ntraj, seeds=seeds, precision=precision)
+    r = mcsolve_batch(s, g["tlist"], ntraj, seeds=seeds, precision=precision, group=group)
     same = sum(jump_records_match(r.col_times[tr], r.col_which[tr], g, tr) for tr in range(ntraj))
     for tr in range(ntraj):
         if jump_times_close(r.col_times[tr], g, tr):
@@ -103,3 +103,58 @@ def test_mc_mixed_precision_jump_records(name):
     sem = g["runs_expect"].std(axis=1) / np.sqrt(ntraj)
     diff = np.abs(r.runs_expect.real.mean(axis=1) - g["runs_expect"].mean(axis=1))
     assert np.all(diff <= 5 * sem + 1e-3)
+
+
+@pytest.mark.parametrize("name", sorted(MC_CASES))
+def test_mc_cta_groups_match_reference(name):
+    """The same trajectories with one 256-thread CTA per item instead of a warp."""
+    from qutip_gb300 import systems as S
+    g, r, same, ntraj = _mc_golden(name, lambda: MC_CASES[name](S), "double", group="cta")
+    assert same == ntraj
+
+
+def _jc_problem(n_items, seeds, dtype="c64"):
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import BatchProblem
+    s = S.jaynes_cummings(6, g=2 * np.pi * 0.08, kappa=0.3, gamma=0.2, kind="mc")
+    bp = BatchProblem(dtype)
+    sid = bp.add_system(s.terms, s.e_ops, np.linspace(0, 10, 51), "mc", c_ops=s.c_ops)
+    for sd in seeds[:n_items]:
+        bp.add_item(sid, s.state0, seed=sd)
+    return bp
+
+
+def test_graph_replay_matches_plain_launches():
+    """A captured launch replayed with new seeds gives what a fresh launch with those
+    seeds gives, bit for bit."""
+    seeds_a = np.random.SeedSequence(1).spawn(96)
+    seeds_b = np.random.SeedSequence(2).spawn(96)
+    plain_a = _jc_problem(96, seeds_a)
+    plain_a.build(max_jumps=64)
+    plain_a.launch()
+    ra = plain_a.results()
+    plain_b = _jc_problem(96, seeds_b)
+    plain_b.build(max_jumps=64)
+    plain_b.launch()
+    rb = plain_b.results()
+    bp = _jc_problem(96, seeds_a)
+    bp.build(max_jumps=64)
+    bp.capture()
+    bp.replay()
+    torch.cuda.synchronize()
+    for x, y in zip(bp.results(), ra):
+        np.testing.assert_array_equal(x["expect"], y["expect"])
+        np.testing.assert_array_equal(x["col_times"], y["col_times"])
+    bp.replay(seeds=seeds_b)
+    torch.cuda.synchronize()
+    for x, y in zip(bp.results(), rb):
+        np.testing.assert_array_equal(x["expect"], y["expect"])
+        np.testing.assert_array_equal(x["col_which"], y["col_which"])
+
+
+def test_tune_batch_picks_a_valid_shape():
+    from qutip_gb300.batched import tune_batch
+    seeds = np.random.SeedSequence(3).spawn(64)
+    best = tune_batch(lambda n: _jc_problem(n, seeds), sample_items=64, reps=1)
+    assert best["group"] in ("warp", "cta") and 0 < best["slot_fraction"] <= 1
+    assert best["ms"] > 0 and len(best["timings"]) >= 2
