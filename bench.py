@@ -60,10 +60,12 @@ def parse():
                     help="simulated time of the CPU-baseline sample (of 10.0)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline workload only")
-    ap.add_argument("--served-jobs", type=int, default=1000)
+    ap.add_argument("--served-jobs", type=int, default=10000)
     ap.add_argument("--served-ntraj", type=int, default=100)
     ap.add_argument("--served-plain-sample", type=int, default=60)
     ap.add_argument("--mc-ntraj", type=int, default=4096)
+    ap.add_argument("--large-sites", type=int, default=12,
+                    help="Ising chain length of the large mixed-precision section (0: skip)")
     ap.add_argument("--profile", default=None, choices=["stage", "batch"],
                     help="run the ncu profiling case only (fused stage kernel, untuned); "
                          "prints nothing to parse")
@@ -307,10 +309,17 @@ def run_served(args):
     import torch
     from qutip_gb300.serving import (Server, build_job, fifo_latencies, jc_request_stream,
                                      percentiles, solve_plain)
+    import dataclasses
+    from qutip_gb300.serving import Job
     n = args.served_jobs
     specs = jc_request_stream(n, rate=1.0, ntraj=args.served_ntraj, seed=2026)
     jobs = [build_job(sp) for sp in specs]
     log(f"served: {n} jobs built")
+
+    def rearrive(js, new_specs):
+        # same requests (the stream's parameters do not depend on the rate), new arrivals
+        return [Job(dataclasses.replace(j.spec, arrival=sp.arrival), j.system, j.tlist,
+                    j.state_len) for j, sp in zip(js, new_specs)]
     warm = [build_job(sp) for sp in specs[:8]]
     Server("mixed").serve(warm, realtime=False)
     # throughput: every job available at t = 0
@@ -321,7 +330,8 @@ def run_served(args):
     # latency at a Poisson rate of half the measured throughput
     rate = 0.5 * thr
     specs_r = jc_request_stream(n, rate=rate, ntraj=args.served_ntraj, seed=2026)
-    jobs_r = [build_job(sp) for sp in specs_r]
+    assert all(a.n_cav == b.n_cav and a.seed == b.seed for a, b in zip(specs, specs_r))
+    jobs_r = rearrive(jobs, specs_r)
     srv_r = Server("mixed", launch_timeout=60.0)
     _, wall_r = srv_r.serve(jobs_r, realtime=True)
     lat = percentiles([j.latency for j in jobs_r])
@@ -416,6 +426,83 @@ def run_mc_batch(args):
                                 "graph": "captured once, replayed with new seeds (in-place item table)"}}
     out["workload"] = (f"Bose-Hubbard trimer cutoff 8 (dim 512), {n} trajectories, "
                        "tlist linspace(0,50,501), one persistent launch per step")
+    if not args.no_cpu_baseline:
+        log("mc batch: reference CPU mcsolve sample")
+        try:
+            p = subprocess.run([sys.executable, "-m", "oracle.ref_workloads", "mcsolve"],
+                               cwd=ROOT, capture_output=True, text=True, timeout=600)
+            ref = json.loads(p.stdout.strip().splitlines()[-1])
+            out["cpu_baseline"] = {**ref, "kind": "reference",
+                                   "sample": "QuTiP reference (oracle/_ref) mcsolve vern7, same "
+                                             "system and tlist; map='serial' on 1 core and "
+                                             "map='parallel' on every host core, fresh process"}
+        except Exception as exc:  # noqa: BLE001
+            out["cpu_baseline"] = {"value": None, "error": repr(exc)[:300]}
+    return out
+
+
+def hbm_peak_gbs():
+    """Measured copy bandwidth of the GB300s (driver-written), else the fallback."""
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peaks = json.load(open(pk)) if os.path.exists(pk) else {}
+    if "hbm_gbs" in peaks:
+        return float(peaks["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_large(args):
+    """Large mixed-precision mesolve: the Ising chain at L = 12 (Liouvillian
+    16,777,216 rows), tlist linspace(0,5,51).  The operator is assembled on the device
+    (the host holds only the 4096 x 4096 operators); the complex64 solve is timed,
+    its error against the complex128 solve of the same operator on the GPU is stated,
+    and the complex64 matvec and fused-stage bandwidths are reported against HBM."""
+    import torch
+    from qutip_gb300 import systems as S
+    from qutip_gb300.operator import DeviceOperator
+    from qutip_gb300.solver import ExpectOps, solve_system
+    from qutip_gb300.superop import liouvillian_groups
+    L = args.large_sites
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s = S.ising_chain(L, build_terms=False)
+    groups = liouvillian_groups(s.h_terms, s.c_ops)
+    op128 = DeviceOperator.from_device_groups(groups, "c128")
+    del groups
+    torch.cuda.empty_cache()
+    op64 = op128.astype("c64")
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    log(f"large: L={L} operator assembled on the device in {build_s:.1f} s, "
+        f"{op64.nnz} entries ({op64.launch_desc()})")
+    ex = ExpectOps(s.e_ops)
+    tl = np.linspace(0.0, 5.0, 51)
+    r128 = solve_system(s, tl, {"precision": "double"}, op=op128, ex=ex)
+    solve_system(s, tl, {"precision": "mixed"}, op=op64, ex=ex)   # warm-up
+    times = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        r64 = solve_system(s, tl, {"precision": "mixed"}, op=op64, ex=ex)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t1)
+    err = max(float(np.max(np.abs(np.real(a) - np.real(b)))) for a, b in zip(r64.expect, r128.expect))
+    spmv_ms, spmv_b, spmv_gbs = measure_spmv(op64, reps=10)
+    stage_ms, stage_b, stage_gbs = measure_stage_roofline(op64, s, "mixed", reps=3)
+    peak, _ = hbm_peak_gbs()
+    out = {"workload": f"ising_chain_L{L}_mesolve_vern7 mixed, tlist linspace(0,5,51)",
+           "liouvillian_rows": op64.n_rows, "entries": int(op64.nnz),
+           "device_assembly_s": build_s, "solves_per_sec": 1.0 / float(np.median(times)),
+           "s_per_solve": float(np.median(times)), "rhs_calls": int(r64.stats.get("rhs", 0)),
+           "max_abs_err_vs_fp64_gpu": err,
+           "spmv_c64": {"gbs": spmv_gbs, "ms": spmv_ms, "bytes": int(spmv_b), "frac": spmv_gbs / peak},
+           "stage_c64": {"gbs": stage_gbs, "ms": stage_ms, "bytes": int(stage_b),
+                         "frac": stage_gbs / peak},
+           "cpu_baseline": None,
+           "cpu_baseline_note": "not run at this size: the reference's host Liouvillian "
+                                "construction alone takes minutes (the CPU baseline of the "
+                                "headline line is at L = 10)"}
+    del op64, op128
+    torch.cuda.empty_cache()
     return out
 
 
@@ -427,12 +514,7 @@ def run_ours(args, dist):
     from qutip_gb300.solver import ExpectOps, solve_system
 
     dist.init()
-    peaks = {}
-    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(pk):
-        peaks = json.load(open(pk))
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    hbm_peak, peak_src = hbm_peak_gbs()
 
     log("building the Ising L=10 Liouvillian")
     sysm = S.ising_chain(N_SITES)
@@ -516,7 +598,7 @@ def run_ours(args, dist):
                                        "of a step, same operator)",
                      "kernel": "spmv_sliced_kernel<C64,C128,RK> (fused Vern7 stage, mixed)",
                      "bytes_per_launch": stage_b, "ms_per_launch": stage_ms,
-                     "peak_source": f"{peak_src} hbm_gbs (of measured)"},
+                     "peak_source": f"{peak_src} hbm_gbs (of {peak_src})"},
         "double_precision": {"value": double_v, "unit": UNIT,
                              "stage_kernel_gbs": stage128_gbs, "stage_kernel_ms": stage128_ms,
                              "bound": "FP64 throughput (about 4 DFMA per stored entry)"},
@@ -531,6 +613,9 @@ def run_ours(args, dist):
         out["served"] = run_served(args)
         log("batched mcsolve")
         out["mc_batched"] = run_mc_batch(args)
+        if args.large_sites:
+            log(f"large: Ising L={args.large_sites}")
+            out["large"] = run_large(args)
     if dist.rank == 0 and not args.no_cpu_baseline:
         log("CPU baseline")
         try:

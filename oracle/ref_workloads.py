@@ -80,3 +80,48 @@ def port_mesolve_sample(terms, state0, e_ops, t_end, n_out, t_sample):
     t0 = time.perf_counter()
     mesolve(terms, state0, tl, e_ops)
     return time.perf_counter() - t0, (tl[-1] - tl[0]) / (t_end - full[0])
+
+
+def bh_trimer_qobjs(cutoff=8, J=1.0, U=0.5, F=0.3, kappa=0.1):
+    """The Bose-Hubbard trimer (ring) with the reference's own constructors."""
+    qutip = import_reference()
+    a = [qutip.tensor(*[qutip.destroy(cutoff) if k == i else qutip.qeye(cutoff)
+                        for k in range(3)]) for i in range(3)]
+    n = [x.dag() * x for x in a]
+    H = sum(-J * (a[i].dag() * a[j] + a[j].dag() * a[i]) for i, j in ((0, 1), (1, 2), (2, 0)))
+    H = H + sum(U / 2 * n[i] * (n[i] - 1) for i in range(3)) + F * (a[0] + a[0].dag())
+    c_ops = [np.sqrt(kappa) * x for x in a]
+    psi0 = qutip.tensor(*[qutip.basis(cutoff, 0)] * 3)
+    return H, c_ops, psi0, n
+
+
+def reference_mcsolve_sample(ntraj_serial=16, ntraj_parallel=64, t_end=50.0, n_out=501):
+    """Time the reference's vern7 ``mcsolve`` of the Bose-Hubbard trimer: ``map="serial"``
+    on one core and ``map="parallel"`` on every host core.  Run it in a fresh process
+    (``python -m oracle.ref_workloads mcsolve``): the parallel map forks workers.
+    Returns trajectories per second for each and the core count."""
+    import os
+    qutip = import_reference()
+    H, c_ops, psi0, e_ops = bh_trimer_qobjs()
+    tl = np.linspace(0.0, t_end, n_out)
+    base = {"method": "vern7", "atol": 1e-8, "rtol": 1e-6, "progress_bar": False}
+    qutip.mcsolve(H, psi0, tl[:3], c_ops, e_ops=e_ops, ntraj=2, seeds=1,
+                  options={**base, "map": "serial"})
+    t0 = time.perf_counter()
+    qutip.mcsolve(H, psi0, tl, c_ops, e_ops=e_ops, ntraj=ntraj_serial, seeds=2,
+                  options={**base, "map": "serial"})
+    serial = ntraj_serial / (time.perf_counter() - t0)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    qutip.mcsolve(H, psi0, tl, c_ops, e_ops=e_ops, ntraj=ntraj_parallel, seeds=3,
+                  options={**base, "map": "parallel", "num_cpus": cores})
+    parallel = ntraj_parallel / (time.perf_counter() - t0)
+    return {"serial_traj_per_sec": serial, "serial_sample": ntraj_serial,
+            "parallel_traj_per_sec": parallel, "parallel_sample": ntraj_parallel,
+            "cores": cores}
+
+
+if __name__ == "__main__":
+    import json
+    if sys.argv[1:2] == ["mcsolve"]:
+        print(json.dumps(reference_mcsolve_sample()))

@@ -193,6 +193,63 @@ class DeviceOperator:
                 t = row_tiles(row_start, tn, _lib.QG_TILE_ROWS)
                 if t is not None:
                     self._tiles[tn] = torch.from_numpy(t).to(self.device)
+        self._finish(G)
+
+    @classmethod
+    def from_device_groups(cls, groups, dtype: str = "c64"):
+        """Sliced-ELLPACK operator from device CSR groups
+        ``[(indptr, indices, data, Coefficient | None), ...]`` (for example from
+        :func:`qutip_gb300.superop.liouvillian_groups`), laid out on the device."""
+        from .superop import device_sliced_layout
+        if dtype not in _TORCH:
+            raise TypeError(f"unsupported dtype {dtype!r}")
+        if not groups or len(groups) > _lib.QG_MAX_GROUPS:
+            raise ValueError(f"1..{_lib.QG_MAX_GROUPS} coefficient groups are supported")
+        self = cls.__new__(cls)
+        indptr0 = groups[0][0]
+        n = indptr0.numel() - 1
+        self.shape = (n, n)
+        self.n_rows = self.n_cols = n
+        self.dtype = dtype
+        self.coeffs = [c for _, _, _, c in groups]
+        for c in self.coeffs:
+            if c is not None and not isinstance(c, Coefficient):
+                raise TypeError("coefficients must be qutip_gb300.coefficients.Coefficient")
+        self.device = indptr0.device
+        self.group_nnz = [int(ix.numel()) for _, ix, _, _ in groups]
+        self.nnz = sum(self.group_nnz)
+        self.fmt = "sliced"
+        self._tiles = {}
+        P = self.PAD
+        rp, widths, col, val, total = device_sliced_layout(groups, n)
+        if total >= 2**31 - 16 or n * len(groups) >= 2**31 - 16:
+            raise ValueError("operators beyond 2^31 stored entries need 64-bit indices")
+        self.stored = total
+        self.slice_width = widths
+        self.row_ptr = torch.zeros(rp.numel() + P, dtype=torch.int32, device=self.device)
+        self.row_ptr[:rp.numel()] = rp.to(torch.int32)
+        self.col = torch.zeros(total + P, dtype=torch.int32, device=self.device)
+        self.col[:total] = col
+        del col
+        self.val = torch.zeros(total + P, dtype=_TORCH[dtype], device=self.device)
+        self.val[:total] = val.to(_TORCH[dtype])
+        del val
+        self._finish(len(groups))
+        return self
+
+    def astype(self, dtype: str):
+        """The same operator and layout with values in ``dtype`` (device copy)."""
+        other = self.__class__.__new__(self.__class__)
+        other.__dict__.update(self.__dict__)
+        other.dtype = dtype
+        other.val = self.val.to(_TORCH[dtype])
+        other._finish(self.n_groups)
+        other.set_launch(self.launch)
+        return other
+
+    def _finish(self, G):
+        fmt = self.fmt
+        dtype = self.dtype
         if all(c is None for c in self.coeffs):
             self.coef_code = self.coef_start = self.coef_consts = None
         else:

@@ -1,0 +1,169 @@
+"""Liouvillians assembled in device memory from Hilbert-space operators.
+
+The reference forms superoperators on the host with sparse Kronecker products:
+``spre`` / ``spost`` / ``sprepost`` (qutip/core/superoperator.py:357-440) and
+``lindblad_dissipator`` / ``liouvillian`` (:36-200), in the column-stacking
+convention ``vec(A rho B) = (B^T (x) A) vec(rho)``.  At the L = 12 Ising chain
+(16,777,216 rows, about 4.8e8 entries) that takes minutes and tens of GB of host
+memory.
+
+Here every term ``c * (B^T (x) A)`` is expanded as the outer product of its two
+factors' COO entries on the device. Duplicate positions within a coefficient
+group are summed after one device sort of the ``row * N + col`` keys, and exact
+zeros are dropped (as scipy's sparse sum does). The result goes straight into
+the sliced-ELLPACK layout of
+:class:`~qutip_gb300.operator.DeviceOperator` (:func:`device_sliced_layout`, the
+device twin of :func:`~qutip_gb300.operator.sliced_layout`).  The host only holds
+the ``d x d`` Hilbert-space operators.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+__all__ = ["kron_coo", "coalesce", "liouvillian_groups", "device_sliced_layout"]
+
+
+def _coo(m, device):
+    m = sp.coo_matrix(m)
+    return (torch.from_numpy(m.row.astype(np.int64)).to(device),
+            torch.from_numpy(m.col.astype(np.int64)).to(device),
+            torch.from_numpy(m.data.astype(np.complex128)).to(device))
+
+
+def kron_coo(a, b, scale=1.0, device="cuda"):
+    """COO entries of ``scale * (a (x) b)`` (a, b: square scipy matrices)."""
+    ra, ca, va = _coo(a, device)
+    rb, cb, vb = _coo(b, device)
+    nb = b.shape[0]
+    rows = (ra[:, None] * nb + rb[None, :]).reshape(-1)
+    cols = (ca[:, None] * nb + cb[None, :]).reshape(-1)
+    vals = (va[:, None] * vb[None, :]).reshape(-1) * complex(scale)
+    return rows, cols, vals
+
+
+def coalesce(terms, n, device="cuda"):
+    """Sum of Kronecker terms ``[(a, b, scale), ...]`` as CSR: keys ``row * n + col``
+    are written term by term into one buffer (no per-term index arrays are kept),
+    sorted once, duplicates summed, exact zeros dropped.
+
+    Returns ``(indptr int64[n+1], indices int64[nnz], data complex128[nnz])`` with
+    rows ascending and columns ascending within each row."""
+    sizes = [sp.csr_matrix(a).nnz * sp.csr_matrix(b).nnz for a, b, _ in terms]
+    total = sum(sizes)
+    keys = torch.empty(total, dtype=torch.int64, device=device)
+    vals = torch.empty(total, dtype=torch.complex128, device=device)
+    off = 0
+    for (a, b, scale), size in zip(terms, sizes):
+        r, c, v = kron_coo(a, b, scale, device)
+        keys[off:off + size] = r * n + c
+        vals[off:off + size] = v
+        off += size
+        del r, c, v
+    keys, order = torch.sort(keys)
+    vals = vals[order]
+    del order
+    uniq, inv = torch.unique_consecutive(keys, return_inverse=True)
+    del keys
+    summed = torch.zeros(uniq.numel(), dtype=vals.dtype, device=device)
+    summed.index_add_(0, inv, vals)
+    del inv, vals
+    keep = summed != 0
+    uniq, summed = uniq[keep], summed[keep]
+    rows = torch.div(uniq, n, rounding_mode="floor")
+    cols = uniq - rows * n
+    del uniq
+    counts = torch.bincount(rows, minlength=n)
+    indptr = torch.zeros(n + 1, dtype=torch.int64, device=device)
+    torch.cumsum(counts, 0, out=indptr[1:])
+    return indptr, cols, summed
+
+
+def liouvillian_groups(h_terms, c_ops=(), device="cuda"):
+    """Coefficient groups of the Lindblad generator, assembled on the device.
+
+    ``h_terms``: list of ``(H_k, Coefficient | None)`` (d x d scipy);
+    ``c_ops``: constant collapse operators.  Group order follows the first
+    appearance of each coefficient, the constant group first if present, which
+    matches :func:`qutip_gb300.systems.merge_terms` of the host construction.
+
+    Returns ``[(indptr, indices, data, coefficient), ...]`` (device CSR).
+    """
+    d = (h_terms[0][0] if h_terms else c_ops[0]).shape[0]
+    n = d * d
+    eye = sp.identity(d, dtype=np.complex128, format="csr")
+    groups: dict = {}
+    order = []
+
+    def add(key, coeff, term):
+        if key not in groups:
+            groups[key] = (coeff, [])
+            order.append(key)
+        groups[key][1].append(term)
+
+    for h, coeff in h_terms:
+        key = None if coeff is None else coeff.key()
+        h = sp.csr_matrix(h, dtype=np.complex128)
+        add(key, coeff, (eye, h, -1j))          # -i spre(H)
+        add(key, coeff, (h.T.tocsr(), eye, 1j))  # +i spost(H)
+    for c in c_ops:
+        c = sp.csr_matrix(c, dtype=np.complex128)
+        cdc = (c.conj().T @ c).tocsr()
+        add(None, None, (c.conj(), c, 1.0))      # sprepost(c, c^dag)
+        add(None, None, (eye, cdc, -0.5))        # -1/2 spre(c^dag c)
+        add(None, None, (cdc.T.tocsr(), eye, -0.5))  # -1/2 spost(c^dag c)
+    if None in groups:                           # constant group first
+        order.remove(None)
+        order.insert(0, None)
+    out = []
+    for key in order:
+        coeff, terms = groups[key]
+        indptr, indices, data = coalesce(terms, n, device)
+        out.append((indptr, indices, data, coeff))
+    return out
+
+
+def device_sliced_layout(groups, n_cols):
+    """Sliced ELLPACK of device CSR groups: the layout of
+    :func:`qutip_gb300.operator.sliced_layout` computed with device sorts and
+    scatters.  Returns ``(slice_ptr, widths, col int32, val complex128, total)``."""
+    indptr0 = groups[0][0]
+    device = indptr0.device
+    n = indptr0.numel() - 1
+    G = len(groups)
+    S = (n + 31) // 32
+    counts = torch.zeros((S * 32, G), dtype=torch.int64, device=device)
+    for g, (indptr, _, _, _) in enumerate(groups):
+        counts[:n, g] = indptr[1:] - indptr[:-1]
+    widths = counts.view(S, 32, G).amax(dim=1)                   # [S, G]
+    slice_size = 32 * widths.sum(dim=1)
+    slice_ptr = torch.zeros(S + 1, dtype=torch.int64, device=device)
+    torch.cumsum(slice_size, 0, out=slice_ptr[1:])
+    total = int(slice_ptr[-1].item())
+    pos_slice = torch.repeat_interleave(torch.arange(S, device=device), slice_size)
+    lane = (torch.arange(total, device=device) - slice_ptr[pos_slice]) % 32
+    col = torch.clamp(pos_slice * 32 + lane, max=n_cols - 1).to(torch.int32)
+    del pos_slice, lane
+    val = torch.zeros(total, dtype=torch.complex128, device=device)
+    gprefix = torch.zeros((S, G), dtype=torch.int64, device=device)
+    if G > 1:
+        gprefix[:, 1:] = torch.cumsum(widths, dim=1)[:, :-1]
+    for g, (indptr, indices, data, _) in enumerate(groups):
+        nnz = indices.numel()
+        cnt = indptr[1:] - indptr[:-1]
+        rows = torch.repeat_interleave(torch.arange(n, device=device), cnt)
+        # order each row's entries by (col XOR row): rows stay grouped, key < 2^31
+        key = (rows << 32) | (indices ^ rows)
+        key, perm = torch.sort(key)
+        del key
+        ci, dv = indices[perm], data[perm]
+        del perm
+        q = torch.arange(nnz, device=device) - indptr[rows]
+        sl = torch.div(rows, 32, rounding_mode="floor")
+        dst = slice_ptr[sl] + 32 * (gprefix[sl, g] + q) + rows % 32
+        del q, sl
+        col[dst] = ci.to(torch.int32)
+        val[dst] = dv
+        del dst, ci, dv, rows
+    return slice_ptr, widths.reshape(-1).to(torch.int32), col, val, total

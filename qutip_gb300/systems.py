@@ -195,13 +195,15 @@ def jaynes_cummings(n_cav=10, wc=2 * np.pi, wa=2 * np.pi, g=2 * np.pi * 0.05,
 
 
 def ising_chain(n_sites=10, J=1.0, h=None, omega=1.3, gamma_minus=0.05, gamma_z=0.02,
-                seed=1234, kind="me") -> OpenSystem:
+                seed=1234, kind="me", build_terms=True) -> OpenSystem:
     """Dissipative transverse-field Ising chain with an oscillating field.
 
     ``H(t) = -J sum_i sz_i sz_{i+1} - sum_i h_i cos(omega t) sx_i`` (open chain),
     ``h_i ~ U[0.5, 1.5]`` from ``numpy.random.default_rng(seed)``; collapse
     operators ``sqrt(gamma_minus) s-_i`` and ``sqrt(gamma_z) sz_i`` on every
-    site; initial state all spins up; e_ops ``sz_i``.
+    site; initial state all spins up; e_ops ``sz_i``.  With ``build_terms=False``
+    the Liouvillian is left to :func:`qutip_gb300.superop.liouvillian_groups`
+    (device assembly) and ``terms`` is ``None``.
     """
     if h is None:
         h = np.random.default_rng(seed).uniform(0.5, 1.5, n_sites)
@@ -227,8 +229,8 @@ def ising_chain(n_sites=10, J=1.0, h=None, omega=1.3, gamma_minus=0.05, gamma_z=
         rho0 = np.zeros(dim * dim, dtype=np.complex128)
         i0 = int(np.flatnonzero(psi0)[0])
         rho0[i0 + dim * i0] = 1.0
-        return OpenSystem("ising_chain", "me", dim, _me_terms(h_terms, c_ops), rho0, sz, c_ops,
-                          h_terms, meta)
+        terms = _me_terms(h_terms, c_ops) if build_terms else None
+        return OpenSystem("ising_chain", "me", dim, terms, rho0, sz, c_ops, h_terms, meta)
     return OpenSystem("ising_chain", "mc", dim, _mc_terms(h_terms, c_ops), psi0, sz, c_ops,
                       h_terms, meta)
 
