@@ -70,6 +70,8 @@ def parse():
                     help="run the ncu profiling case only (fused stage kernel, untuned); "
                          "prints nothing to parse")
     ap.add_argument("--profile-sites", type=int, default=10)
+    ap.add_argument("--profile-ntraj", type=int, default=256)
+    ap.add_argument("--profile-tend", type=float, default=5.0)
     return ap.parse_args()
 
 
@@ -348,6 +350,16 @@ def run_served(args):
     plain_thr = 1.0 / float(np.mean(service))
     svc = [service[i % k] for i in range(n)]
     plain_lat = percentiles(fifo_latencies([sp.arrival for sp in specs_r], svc))
+    # a load the plain arm sustains: half its throughput, the first 400 requests
+    low_rate = 0.5 * (1.0 / float(np.mean(service)))
+    m = min(400, n)
+    specs_l = jc_request_stream(n, rate=low_rate, ntraj=args.served_ntraj, seed=2026)[:m]
+    jobs_l = rearrive(jobs[:m], specs_l)
+    Server("mixed", launch_timeout=60.0).serve(jobs_l, realtime=True)
+    lat_low = percentiles([j.latency for j in jobs_l])
+    plain_low = percentiles(fifo_latencies([sp.arrival for sp in specs_l],
+                                           [service[i % k] for i in range(m)]))
+    log(f"served: at {low_rate:.1f} req/s served {lat_low}, plain {plain_low}")
     # error of the served mixed form vs the plain complex128 solve on the sample's mesolve jobs
     err = 0.0
     for j in jobs[:k]:
@@ -368,6 +380,9 @@ def run_served(args):
                                                      "same arrivals"}},
         "speedup_solves_per_sec": thr / plain_thr,
         "speedup_p99": plain_lat["p99_ms"] / lat["p99_ms"],
+        "at_plain_sustainable_rate": {"rate_per_s": low_rate, "requests": m,
+                                      "served_mixed": lat_low, "plain_c128": plain_low,
+                                      "speedup_p99": plain_low["p99_ms"] / lat_low["p99_ms"]},
         "max_abs_err_vs_c128_expect": err,
     }
 
@@ -648,14 +663,17 @@ def run_profile_case(args):
 
 
 def run_profile_batch(args):
-    """ncu case for the batched trajectory kernel: 256 Bose-Hubbard trajectories,
-    t in [0, 5] (51 outputs), mixed form, default launch shape."""
+    """ncu case for the batched trajectory kernel: ``--profile-ntraj`` Bose-Hubbard
+    trajectories (default 256) over t in [0, ``--profile-tend``] (default 5, 10
+    outputs per unit time), mixed form, default launch shape."""
     import torch
     from qutip_gb300 import systems as S
     from qutip_gb300.batched import mcsolve_batch
     torch.cuda.set_device(0)
     s = S.bose_hubbard_trimer(8)
-    r = mcsolve_batch(s, np.linspace(0.0, 5.0, 51), 256, seeds=5, precision="mixed")
+    te = args.profile_tend
+    r = mcsolve_batch(s, np.linspace(0.0, te, int(round(10 * te)) + 1), args.profile_ntraj,
+                      seeds=5, precision="mixed")
     torch.cuda.synchronize()
     print(f"batch: {len(r.col_times)} trajectories, {sum(len(c) for c in r.col_times)} jumps")
 

@@ -666,11 +666,18 @@ __device__ void integrate(const GT& g, Ctx<DT>& X, Ctl& c, double t, bool step) 
 }
 
 // ------------------------------------------------------------- outputs ------
-// expectation values of the current state into out[0..ne] (raw; host normalises)
+// expectation values of the current state into out[0..ne] (raw; host normalises).
+// A ket is interpolated once into ctmp[0] and every e_op reads it there; a density
+// matrix is read entry by entry (the e_ops touch a small part of it).
 template <int DT, class GT>
 __device__ __noinline__ void record(const GT& g, const Ctx<DT>& X, const Ctl& c, double2* out, bool ket) {
   const int ne = X.S->n_eops;
   const int d = X.d;
+  const double2* psi = X.ctmp[0];
+  if (ket) {
+    for (int r = g.rank; r < X.n; r += GT::SIZE) X.ctmp[0][r] = state_at(X, c, r);
+    g.sync();
+  }
   for (int e = 0; e < ne; ++e) {
     const int* rp = X.B->eop_rp + X.S->eop_rp_off + (int64_t)e * (d + 1);
     double ar = 0.0, ai = 0.0;
@@ -680,12 +687,12 @@ __device__ __noinline__ void record(const GT& g, const Ctx<DT>& X, const Ctl& c,
       for (int p = s; p < en; ++p) {
         const int col = __ldg(X.B->eop_col + p);
         const double vr = __ldg(X.B->eop_val + 2 * p), vi = __ldg(X.B->eop_val + 2 * p + 1);
-        const double2 z = state_at(X, c, ket ? col : col + r * d);
+        const double2 z = ket ? psi[col] : state_at(X, c, col + r * d);
         sr += vr * z.x - vi * z.y;
         si += vr * z.y + vi * z.x;
       }
       if (ket) {
-        const double2 pr = state_at(X, c, r);
+        const double2 pr = psi[r];
         const double tr = pr.x * sr + pr.y * si, ti = pr.x * si - pr.y * sr;
         sr = tr;
         si = ti;
@@ -700,7 +707,7 @@ __device__ __noinline__ void record(const GT& g, const Ctx<DT>& X, const Ctl& c,
   double ar = 0.0, ai = 0.0;
   if (ket) {
     for (int r = g.rank; r < X.n; r += GT::SIZE) {
-      const double2 z = state_at(X, c, r);
+      const double2 z = psi[r];
       ar += z.x * z.x + z.y * z.y;
     }
   } else {
@@ -713,6 +720,7 @@ __device__ __noinline__ void record(const GT& g, const Ctx<DT>& X, const Ctl& c,
   const double tr_ = g.sum(ar);
   const double ti_ = g.sum(ai);
   if (g.rank == 0) out[ne] = make_double2(tr_, ti_);
+  g.sync();
 }
 
 // ||c_i psi||^2 for psi in ctmp[0]; optionally store c_i psi in ctmp[1]

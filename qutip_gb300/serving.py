@@ -124,7 +124,11 @@ class Server:
     """Continuous batching over a fixed number of CUDA streams and an HBM budget."""
 
     def __init__(self, precision="mixed", n_streams=4, hbm_budget=8 << 30, max_items=8192,
-                 max_jobs_per_launch=512, max_jumps=256, launch_timeout=120.0):
+                 max_jobs_per_launch=512, max_jumps=256, launch_timeout=120.0, group="load"):
+        """``group``: ``"load"`` gives each item a CTA in launches of at most two items
+        per SM and packs fuller launches one item per warp; ``"auto"``, ``"warp"`` or
+        ``"cta"`` fix the shape for every launch (results then do not depend on how
+        requests were grouped into launches)."""
         self.precision = precision
         self.dtype = "c64" if precision == "mixed" else "c128"
         self.qdt = _lib.QG_C64 if self.dtype == "c64" else _lib.QG_C128
@@ -134,6 +138,12 @@ class Server:
         self.max_jobs = int(max_jobs_per_launch)
         self.max_jumps = int(max_jumps)
         self.launch_timeout = float(launch_timeout)
+        if group not in ("load", "auto", "warp", "cta"):
+            raise ValueError("group must be 'load', 'auto', 'warp' or 'cta'")
+        self.group = group
+        # items per launch up to which each item gets a CTA: two per SM
+        self.cta_items = 2 * torch.cuda.get_device_properties(0).multi_processor_count \
+            if torch.cuda.is_available() else 0
         self.stats = {"launches": 0, "items": 0, "max_inflight_bytes": 0, "max_concurrent": 0,
                       "max_launch_s": 0.0}
 
@@ -150,10 +160,15 @@ class Server:
                     bp.add_item(sid, s.state0, seed=sd)
         # host-visible cancel flag (pinned, mapped): the kernel polls it at every output time
         cancel = torch.zeros(1, dtype=torch.int32).pin_memory()
+        # group shape by load: a launch with few items gives each one a CTA (more
+        # threads per item, lower latency); a full launch packs items one per warp
+        group = self.group
+        if group == "load":
+            group = "cta" if len(bp.items) <= self.cta_items else "auto"
         with torch.cuda.stream(stream):
             cost = [bp.sys_info[it[0]]["nnz"] for it in bp.items]
             bp.build(max_jumps=self.max_jumps if any(j.spec.kind == "mc" for j in jobs) else 0,
-                     order=np.argsort(cost, kind="stable")[::-1])
+                     order=np.argsort(cost, kind="stable")[::-1], group=group)
             bp.set_cancel(cancel)
             bp.cancel_flag = cancel
             bp.launch()
@@ -264,6 +279,8 @@ def solve_plain(job: Job, precision="double"):
         r = solve_system(job.system, job.tlist, {"precision": precision})
         return r.expect
     seeds = np.random.SeedSequence(job.spec.seed).spawn(job.spec.ntraj)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
     r = mcsolve_batch(job.system, job.tlist, job.spec.ntraj, seeds=seeds,
-                      precision="double" if precision == "double" else "mixed")
+                      precision="double" if precision == "double" else "mixed",
+                      group="cta" if job.spec.ntraj <= 2 * sms else "auto")
     return r.expect

@@ -24,13 +24,13 @@ def _jobs(n=40, rate=400.0):
 def test_served_results_equal_alone_results():
     from qutip_gb300.serving import Server, percentiles
     jobs = _jobs()
-    srv = Server("mixed", n_streams=3, max_jobs_per_launch=7)
+    srv = Server("mixed", n_streams=3, max_jobs_per_launch=7, group="auto")
     jobs, wall = srv.serve(jobs, realtime=True)
     assert srv.stats["launches"] >= 3 and srv.stats["max_concurrent"] >= 1
     assert all(j.done is not None for j in jobs)
     p = percentiles([j.latency for j in jobs])
     assert p["p99_ms"] >= p["p50_ms"] > 0
-    alone_srv = Server("mixed", n_streams=1, max_jobs_per_launch=1)
+    alone_srv = Server("mixed", n_streams=1, max_jobs_per_launch=1, group="auto")
     for j in jobs[:12]:
         ref = _jobs()[j.spec.id]
         alone_srv.serve([ref], realtime=False)
@@ -50,3 +50,16 @@ def test_served_mixed_precision_error_vs_plain_double():
     print(f"\nserved mixed vs plain complex128: max |<e_op>| difference {worst:.2e}")
     # the mixed form's stated bound: 1e-6 on expectation values of magnitude <= 1
     assert worst < 1e-6
+
+
+def test_load_policy_results_match_fixed_shape():
+    """With the load-dependent group shape, master-equation results equal those of a
+    fixed shape to rounding (only the order of the FP64 reductions differs)."""
+    from qutip_gb300.serving import Server
+    jobs_a = [j for j in _jobs() if j.spec.kind == "me"][:10]
+    jobs_b = [j for j in _jobs() if j.spec.kind == "me"][:10]
+    Server("mixed", group="load").serve(jobs_a, realtime=False)
+    Server("mixed", group="auto", max_jobs_per_launch=512).serve(jobs_b, realtime=False)
+    for a, b in zip(jobs_a, jobs_b):
+        for x, y in zip(a.result, b.result):
+            np.testing.assert_allclose(x, y, rtol=1e-9, atol=1e-12)
