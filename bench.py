@@ -60,6 +60,8 @@ def parse():
                     help="simulated time of the CPU-baseline sample (of 10.0)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline workload only")
+    ap.add_argument("--sections", default="served,mc,large",
+                    help="extra sections after the headline (comma list of served, mc, large)")
     ap.add_argument("--served-jobs", type=int, default=10000)
     ap.add_argument("--served-ntraj", type=int, default=100)
     ap.add_argument("--served-plain-sample", type=int, default=60)
@@ -360,6 +362,10 @@ def run_served(args):
     plain_low = percentiles(fifo_latencies([sp.arrival for sp in specs_l],
                                            [service[i % k] for i in range(m)]))
     log(f"served: at {low_rate:.1f} req/s served {lat_low}, plain {plain_low}")
+    slow = sorted(jobs_l, key=lambda j: -(j.latency or 0))[:6]
+    log("served: slowest at that rate: " + "; ".join(
+        f"{j.spec.kind} N={j.spec.n_cav} {1e3 * j.latency:.0f} ms launch={j.extra.get('launch')}"
+        for j in slow))
     # error of the served mixed form vs the plain complex128 solve on the sample's mesolve jobs
     err = 0.0
     for j in jobs[:k]:
@@ -413,7 +419,7 @@ def run_mc_batch(args):
         tune_seeds = np.random.SeedSequence(7).spawn(2432)
         best = tune_batch(lambda k: make(k, dt, tl[:51], tune_seeds), sample_items=2432, reps=1)
         qdt = _lib.QG_C64 if dt == "c64" else _lib.QG_C128
-        full = lib.qg_batch_group_slots(512, qdt, {"warp": 1, "cta": 2}[best["group"]])
+        full = lib.qg_batch_group_slots(512, qdt, {"warp": 1, "cta": 2, "cluster": 3}[best["group"]])
         seeds0 = np.random.SeedSequence(20261203).spawn(n)
         bp = make(n, dt, tl, seeds0)
         bp.build(max_jumps=512, group=best["group"], n_slots=max(1, int(full * best["slot_fraction"])))
@@ -623,14 +629,16 @@ def run_ours(args, dist):
         "solver_stats": {k: res.stats[k] for k in ("steps", "rejected", "rhs")},
         "clocks": clk,
     }
-    if dist.rank == 0 and not args.quick:
+    sections = set() if args.quick else set(args.sections.split(","))
+    if dist.rank == 0 and "served" in sections:
         log("served stream")
         out["served"] = run_served(args)
+    if dist.rank == 0 and "mc" in sections:
         log("batched mcsolve")
         out["mc_batched"] = run_mc_batch(args)
-        if args.large_sites:
-            log(f"large: Ising L={args.large_sites}")
-            out["large"] = run_large(args)
+    if dist.rank == 0 and "large" in sections and args.large_sites:
+        log(f"large: Ising L={args.large_sites}")
+        out["large"] = run_large(args)
     if dist.rank == 0 and not args.no_cpu_baseline:
         log("CPU baseline")
         try:

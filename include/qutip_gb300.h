@@ -277,23 +277,26 @@ typedef struct qg_batch {
   int64_t* progress;      /* optional [n_slots]: (item << 32) | output index of each slot */
   double* debug;          /* optional [n_slots * 64]: last trajectory-loop states per slot */
   int32_t norm_steps;     /* MC options (qutip/solver/mcsolve.py:449-466) */
-  int32_t group;          /* QG_GROUP_AUTO / QG_GROUP_WARP / QG_GROUP_CTA: threads per item */
+  int32_t group;          /* QG_GROUP_*: threads per item */
   double norm_t_tol, norm_tol, norm_min_step, mc_corr_eps;
 } qg_batch;
 
-/* Threads per item of the batched solver: one warp, one 256-thread CTA, or the
- * default (a warp when max_n <= 2048, else a CTA). */
+/* Threads per item of the batched solver: one warp, one 256-thread CTA, a
+ * cluster of 8 such CTAs (on 8 SMs, reductions through distributed shared
+ * memory), or the default (a warp when max_n <= 2048, else a CTA). */
 #define QG_GROUP_AUTO 0
 #define QG_GROUP_WARP 1
 #define QG_GROUP_CTA 2
+#define QG_GROUP_CLUSTER 3
 
 /* Workspace bytes of one slot. */
 int64_t qg_batch_slot_bytes(int64_t max_n, int dtype);
 /* Resident CTAs (useful n_slots) on the current device for this max_n / dtype;
  * negative QG_ERR_* on failure. */
 int qg_batch_max_slots(int64_t max_n, int dtype);
-/* Resident groups (warps for QG_GROUP_WARP, CTAs for QG_GROUP_CTA, either for
- * QG_GROUP_AUTO) on the current device: the useful n_slots for that group shape. */
+/* Resident groups (warps for QG_GROUP_WARP, CTAs for QG_GROUP_CTA, clusters for
+ * QG_GROUP_CLUSTER, warps or CTAs for QG_GROUP_AUTO) on the current device: the
+ * useful n_slots for that group shape. */
 int qg_batch_group_slots(int64_t max_n, int dtype, int group);
 
 /* Solve every item of the batch in one persistent launch: each CTA takes items

@@ -213,7 +213,8 @@ class BatchProblem:
     def build(self, max_jumps=0, mc_options=None, order=None, n_slots=None, group="auto"):
         """Upload pools; ``order`` permutes the items (longest first balances the queue).
 
-        ``group`` is ``"auto"``, ``"warp"`` or ``"cta"`` (threads per item);
+        ``group`` is ``"auto"``, ``"warp"``, ``"cta"`` or ``"cluster"`` (threads per
+        item: 32, 256, or 8 x 256 on a thread-block cluster);
         ``n_slots`` caps the resident groups (default: all that fit)."""
         if not self.items:
             raise ValueError("no items")
@@ -343,7 +344,8 @@ class BatchProblem:
         return res
 
 
-GROUPS = {"auto": _lib.QG_GROUP_AUTO, "warp": _lib.QG_GROUP_WARP, "cta": _lib.QG_GROUP_CTA}
+GROUPS = {"auto": _lib.QG_GROUP_AUTO, "warp": _lib.QG_GROUP_WARP, "cta": _lib.QG_GROUP_CTA,
+          "cluster": _lib.QG_GROUP_CLUSTER}
 
 _TUNED: dict = {}
 
@@ -356,7 +358,7 @@ def tune_batch(make_problem, sample_items=256, candidates=None, reps=2):
     slot_fraction)`` is built and launched ``reps`` times on that sample (events
     on the current stream); the fastest is returned and cached by (dtype, max_n
     bucket, kind).  Candidates default to warp and CTA groups at full, 3/4 and
-    1/2 of the resident slots.
+    1/2 of the resident slots, and 8-CTA clusters at all resident slots.
     """
     probe = make_problem(sample_items)
     kind = probe.sys_info[0]["kind"] if probe.sys_info else 0
@@ -364,7 +366,8 @@ def tune_batch(make_problem, sample_items=256, candidates=None, reps=2):
     key = (probe.dtype, int(np.ceil(np.log2(max(max_n, 2)))), kind)
     if key in _TUNED:
         return _TUNED[key]
-    candidates = candidates or [(g, f) for g in ("warp", "cta") for f in (1.0, 0.75, 0.5)]
+    candidates = candidates or ([(g, f) for g in ("warp", "cta") for f in (1.0, 0.75, 0.5)]
+                                + [("cluster", 1.0)])
     lib = _lib.load()
     qdt = _lib.QG_C64 if probe.dtype == "c64" else _lib.QG_C128
     best = None

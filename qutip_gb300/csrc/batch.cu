@@ -24,6 +24,7 @@
 // trajectory loop, bisection tries (norm_steps), jumps (max_jumps); an optional
 // host-visible cancel flag is polled at each output time and inside long
 // trajectory intervals.
+#include <cooperative_groups.h>
 #include <mutex>
 
 #include "capi_internal.h"
@@ -63,7 +64,8 @@ __device__ __forceinline__ int read_flag(const volatile int32_t* p) {
 // Largest state handled by one warp per item; larger states use one CTA per item.
 constexpr int WARP_MAX_N = 2048;
 constexpr int WARP_BLOCK = 128;   // 4 warps (4 items) per CTA in warp mode
-constexpr int CTA_BLOCK = 256;    // threads per item in CTA mode
+constexpr int CTA_BLOCK = 256;    // threads per item in CTA mode (per CTA in cluster mode)
+constexpr int CLUSTER_CTAS = 8;   // CTAs per item in cluster mode (portable cluster size)
 // Iterations of the trajectory loop within one output interval (each advances
 // time by one accepted step) before the item stops with QG_TOO_MUCH_WORK.
 constexpr int MC_MAX_ITER = 1 << 22;
@@ -88,9 +90,12 @@ __host__ __device__ inline SlotLayout slot_layout(int64_t n, int dt) {
 }
 
 // ----------------------------------------------------------------- groups ----
+namespace cgrp = cooperative_groups;
+
 struct WarpGroup {
   static constexpr int SIZE = 32;
   int rank;
+  int64_t slot;
   __device__ __forceinline__ void sync() const { __syncwarp(); }
   __device__ __forceinline__ double sum(double v) const {
 #pragma unroll
@@ -104,6 +109,7 @@ template <int BB>
 struct CtaGroup {
   static constexpr int SIZE = BB;
   int rank;
+  int64_t slot;
   double* red;  // shared [BB/32]
   int* ibuf;    // shared [1]
   __device__ __forceinline__ void sync() const { __syncthreads(); }
@@ -123,6 +129,45 @@ struct CtaGroup {
     if (rank == 0) *ibuf = v;
     __syncthreads();
     return *ibuf;
+  }
+};
+
+// A thread-block cluster of CS CTAs works on one item.  Reductions: each CTA's warp
+// partials go to its own shared memory; after a cluster barrier (release/acquire at
+// cluster scope, which also orders the slot's global-memory vectors) every thread
+// reads all CS x BB/32 partials through distributed shared memory in one fixed
+// order, so every thread of the cluster gets the same bits.
+template <int BB, int CS>
+struct ClusterGroup {
+  static constexpr int SIZE = BB * CS;
+  int rank;
+  int64_t slot;
+  double* red;  // shared [BB/32] of this CTA
+  int* ibuf;    // shared [1] of this CTA
+  __device__ __forceinline__ void sync() const { cgrp::this_cluster().sync(); }
+  __device__ __forceinline__ double sum(double v) const {
+    cgrp::cluster_group cl = cgrp::this_cluster();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    cl.sync();  // earlier readers of every CTA's red are done
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    cl.sync();
+    double t = 0.0;
+    for (int c = 0; c < CS; ++c) {
+      const double* rr = cl.map_shared_rank(red, c);
+#pragma unroll
+      for (int i = 0; i < BB / 32; ++i) t += rr[i];
+    }
+    return t;
+  }
+  __device__ __forceinline__ int bcast(int v) const {
+    cgrp::cluster_group cl = cgrp::this_cluster();
+    cl.sync();
+    if (rank == 0) *ibuf = v;
+    cl.sync();
+    const int r = *cl.map_shared_rank(ibuf, 0);
+    cl.sync();  // CTA 0's ibuf is read before anyone moves on
+    return r;
   }
 };
 
@@ -772,7 +817,7 @@ __device__ void run_item(const GT& g, const qg_batch& B, Ctx<DT>& X, int item) {
   for (int o = 1; o < S->n_out && c.status >= 0; ++o) {
     const double t = tl[o];
     if (B.progress && g.rank == 0)
-      B.progress[(int64_t)blockIdx.x * (blockDim.x / GT::SIZE) + threadIdx.x / GT::SIZE] =
+      B.progress[g.slot] =
           ((int64_t)item << 32) | (int64_t)(unsigned)o;
     if (B.cancel) {
       const int f = g.bcast(g.rank == 0 ? read_flag(B.cancel) : 0);
@@ -801,9 +846,7 @@ __device__ void run_item(const GT& g, const qg_batch& B, Ctx<DT>& X, int item) {
           }
         }
         if (B.debug && g.rank == 0) {  // ring of the last 8 loop states per slot
-          const int64_t slot =
-              (int64_t)blockIdx.x * (blockDim.x / GT::SIZE) + threadIdx.x / GT::SIZE;
-          double* dbg = B.debug + slot * 64 + (iters & 7) * 8;
+          double* dbg = B.debug + g.slot * 64 + (iters & 7) * 8;
           dbg[0] = (double)item;
           dbg[1] = (double)o;
           dbg[2] = c.t;
@@ -943,8 +986,8 @@ __device__ __forceinline__ void finish_queue(const qg_batch& B, unsigned int n_g
 // One warp per item; slot = global warp index (n_slots warps own slots).
 template <int DT>
 __global__ void __launch_bounds__(WARP_BLOCK) batch_warp_kernel(qg_batch B) {
-  WarpGroup g{(int)(threadIdx.x & 31)};
   const int64_t slot = (int64_t)blockIdx.x * (WARP_BLOCK / 32) + (threadIdx.x >> 5);
+  WarpGroup g{(int)(threadIdx.x & 31), slot};
   const unsigned int n_groups = gridDim.x * (WARP_BLOCK / 32);
   if (slot < B.n_slots) {
     Ctx<DT> X;
@@ -968,7 +1011,7 @@ template <int DT>
 __global__ void __launch_bounds__(CTA_BLOCK) batch_cta_kernel(qg_batch B) {
   __shared__ double red[CTA_BLOCK / 32];
   __shared__ int ibuf;
-  CtaGroup<CTA_BLOCK> g{(int)threadIdx.x, red, &ibuf};
+  CtaGroup<CTA_BLOCK> g{(int)threadIdx.x, (int64_t)blockIdx.x, red, &ibuf};
   Ctx<DT> X;
   bind_slot(X, B, blockIdx.x);
   while (true) {
@@ -984,8 +1027,53 @@ __global__ void __launch_bounds__(CTA_BLOCK) batch_cta_kernel(qg_batch B) {
   if (g.rank == 0) finish_queue(B, gridDim.x);
 }
 
+// One cluster of CLUSTER_CTAS CTAs per item; slot = cluster index.
+template <int DT>
+__global__ void __launch_bounds__(CTA_BLOCK) batch_cluster_kernel(qg_batch B) {
+  __shared__ double red[CTA_BLOCK / 32];
+  __shared__ int ibuf;
+  cgrp::cluster_group cl = cgrp::this_cluster();
+  const int crank = (int)cl.block_rank();
+  const int64_t slot = blockIdx.x / CLUSTER_CTAS;
+  ClusterGroup<CTA_BLOCK, CLUSTER_CTAS> g{crank * CTA_BLOCK + (int)threadIdx.x, slot, red, &ibuf};
+  Ctx<DT> X;
+  bind_slot(X, B, slot);
+  while (true) {
+    int it = 0;
+    if (g.rank == 0) {
+      it = (int)atomicAdd(B.queue, 1u);
+      if (B.cancel && read_flag(B.cancel)) it = B.n_items;
+    }
+    it = g.bcast(it);
+    if (it >= B.n_items) break;
+    run_item(g, B, X, it);
+  }
+  if (g.rank == 0) finish_queue(B, gridDim.x / CLUSTER_CTAS);
+  g.sync();  // no CTA leaves while another may still read its shared memory
+}
+
 static bool warp_mode(int64_t max_n, int group) {
   return group == QG_GROUP_WARP || (group == QG_GROUP_AUTO && max_n <= WARP_MAX_N);
+}
+
+static bool valid_group(int group) {
+  return group == QG_GROUP_AUTO || group == QG_GROUP_WARP || group == QG_GROUP_CTA ||
+         group == QG_GROUP_CLUSTER;
+}
+
+static cudaLaunchConfig_t cluster_config(int n_clusters, cudaStream_t st, cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)n_clusters * CLUSTER_CTAS, 1, 1);
+  cfg.blockDim = dim3(CTA_BLOCK, 1, 1);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CLUSTER_CTAS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
 }
 
 }  // namespace qg
@@ -1069,10 +1157,22 @@ extern "C" int64_t qg_batch_slot_bytes(int64_t max_n, int dtype) {
 }
 
 extern "C" int qg_batch_group_slots(int64_t max_n, int dtype, int group) {
-  if (group != QG_GROUP_AUTO && group != QG_GROUP_WARP && group != QG_GROUP_CTA)
-    return set_error(QG_ERR_ARG, "group must be QG_GROUP_AUTO, QG_GROUP_WARP or QG_GROUP_CTA");
+  if (!valid_group(group))
+    return set_error(QG_ERR_ARG,
+                     "group must be QG_GROUP_AUTO, QG_GROUP_WARP, QG_GROUP_CTA or QG_GROUP_CLUSTER");
   int per_sm = 0;
   cudaError_t e;
+  if (group == QG_GROUP_CLUSTER) {
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = cluster_config(1, nullptr, attr);
+    int clusters = 0;
+    e = dtype == QG_C64
+            ? cudaOccupancyMaxActiveClusters(&clusters, batch_cluster_kernel<QG_C64>, &cfg)
+            : cudaOccupancyMaxActiveClusters(&clusters, batch_cluster_kernel<QG_C128>, &cfg);
+    if (e != cudaSuccess || clusters <= 0)
+      return set_error(QG_ERR_CUDA, "cluster occupancy query failed");
+    return clusters;
+  }
   const bool warp = warp_mode(max_n, group);
   if (dtype == QG_C64)
     e = warp ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_warp_kernel<QG_C64>,
@@ -1103,10 +1203,20 @@ extern "C" int qg_batch_vern7(const qg_batch* B, void* stream) {
     return set_error(QG_ERR_ARG, "bad batch sizes");
   if (B->max_jumps > 0 && (!B->jump_t || !B->jump_which))
     return set_error(QG_ERR_ARG, "jump record buffers missing");
-  if (B->group != QG_GROUP_AUTO && B->group != QG_GROUP_WARP && B->group != QG_GROUP_CTA)
-    return set_error(QG_ERR_ARG, "group must be QG_GROUP_AUTO, QG_GROUP_WARP or QG_GROUP_CTA");
+  if (!valid_group(B->group))
+    return set_error(QG_ERR_ARG,
+                     "group must be QG_GROUP_AUTO, QG_GROUP_WARP, QG_GROUP_CTA or QG_GROUP_CLUSTER");
   if (B->n_items == 0) return QG_OK;
   cudaStream_t st = (cudaStream_t)stream;
+  if (B->group == QG_GROUP_CLUSTER) {
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = cluster_config(B->n_slots, st, attr);
+    const cudaError_t e = B->dtype == QG_C64
+                              ? cudaLaunchKernelEx(&cfg, batch_cluster_kernel<QG_C64>, *B)
+                              : cudaLaunchKernelEx(&cfg, batch_cluster_kernel<QG_C128>, *B);
+    if (e != cudaSuccess) return set_error(QG_ERR_CUDA, "cluster launch failed");
+    return check_launch("batch_cluster_kernel");
+  }
   if (warp_mode(B->max_n, B->group)) {
     const int per = WARP_BLOCK / 32;
     const int grid = (B->n_slots + per - 1) / per;

@@ -125,10 +125,11 @@ class Server:
 
     def __init__(self, precision="mixed", n_streams=4, hbm_budget=8 << 30, max_items=8192,
                  max_jobs_per_launch=512, max_jumps=256, launch_timeout=120.0, group="load"):
-        """``group``: ``"load"`` gives each item a CTA in launches of at most two items
-        per SM and packs fuller launches one item per warp; ``"auto"``, ``"warp"`` or
-        ``"cta"`` fix the shape for every launch (results then do not depend on how
-        requests were grouped into launches)."""
+        """``group``: ``"load"`` gives each item of a launch with few large items a
+        thread-block cluster (8 SMs), each item of a launch of at most two items per SM
+        a CTA, and packs fuller launches one item per warp; ``"auto"``, ``"warp"``,
+        ``"cta"`` or ``"cluster"`` fix the shape for every launch (results then do not
+        depend on how requests were grouped into launches)."""
         self.precision = precision
         self.dtype = "c64" if precision == "mixed" else "c128"
         self.qdt = _lib.QG_C64 if self.dtype == "c64" else _lib.QG_C128
@@ -138,14 +139,22 @@ class Server:
         self.max_jobs = int(max_jobs_per_launch)
         self.max_jumps = int(max_jumps)
         self.launch_timeout = float(launch_timeout)
-        if group not in ("load", "auto", "warp", "cta"):
-            raise ValueError("group must be 'load', 'auto', 'warp' or 'cta'")
+        if group not in ("load", "auto", "warp", "cta", "cluster"):
+            raise ValueError("group must be 'load', 'auto', 'warp', 'cta' or 'cluster'")
         self.group = group
+        self._cluster_cache = {}
         # items per launch up to which each item gets a CTA: two per SM
         self.cta_items = 2 * torch.cuda.get_device_properties(0).multi_processor_count \
             if torch.cuda.is_available() else 0
         self.stats = {"launches": 0, "items": 0, "max_inflight_bytes": 0, "max_concurrent": 0,
                       "max_launch_s": 0.0}
+
+    def _cluster_slots(self, max_n):
+        if max_n not in self._cluster_cache:
+            lib = _lib.load()
+            self._cluster_cache[max_n] = int(lib.qg_batch_group_slots(max_n, self.qdt,
+                                                                      _lib.QG_GROUP_CLUSTER))
+        return self._cluster_cache[max_n]
 
     def _launch(self, jobs, stream):
         bp = BatchProblem(self.dtype)
@@ -164,7 +173,14 @@ class Server:
         # threads per item, lower latency); a full launch packs items one per warp
         group = self.group
         if group == "load":
-            group = "cta" if len(bp.items) <= self.cta_items else "auto"
+            n_items = len(bp.items)
+            max_n = max(j.state_len for j in jobs)
+            if max_n >= 1600 and n_items <= self._cluster_slots(max_n):
+                group = "cluster"     # few large items: 8 SMs each
+            elif n_items <= self.cta_items:
+                group = "cta"
+            else:
+                group = "auto"
         with torch.cuda.stream(stream):
             cost = [bp.sys_info[it[0]]["nnz"] for it in bp.items]
             bp.build(max_jumps=self.max_jumps if any(j.spec.kind == "mc" for j in jobs) else 0,
@@ -176,6 +192,8 @@ class Server:
             ev.record(stream)
         self.stats["launches"] += 1
         self.stats["items"] += len(bp.items)
+        for j in jobs:
+            j.extra["launch"] = (group, len(bp.items), len(jobs))
         return bp, ev
 
     @staticmethod

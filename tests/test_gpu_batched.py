@@ -105,12 +105,32 @@ def test_mc_mixed_precision_jump_records(name):
     assert np.all(diff <= 5 * sem + 1e-3)
 
 
+@pytest.mark.parametrize("group", ["cta", "cluster"])
 @pytest.mark.parametrize("name", sorted(MC_CASES))
-def test_mc_cta_groups_match_reference(name):
-    """The same trajectories with one 256-thread CTA per item instead of a warp."""
+def test_mc_other_groups_match_reference(name, group):
+    """The same trajectories with one 256-thread CTA, or one 8-CTA thread-block
+    cluster, per item instead of a warp."""
     from qutip_gb300 import systems as S
-    g, r, same, ntraj = _mc_golden(name, lambda: MC_CASES[name](S), "double", group="cta")
+    g, r, same, ntraj = _mc_golden(name, lambda: MC_CASES[name](S), "double", group=group)
     assert same == ntraj
+
+
+@pytest.mark.parametrize("group", ["cta", "cluster"])
+def test_batched_me_groups_match_reference(group):
+    """Master equations (Jaynes-Cummings N=10, Ising L=4) with CTA and cluster groups."""
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import BatchProblem, check_status
+    g = golden("ising_L4_mesolve.npz")
+    s = S.ising_chain(4)
+    bp = BatchProblem("c128")
+    sid = bp.add_system(s.terms, s.e_ops, g["tlist"], "me")
+    bp.add_item(sid, s.state0)
+    bp.build(group=group)
+    bp.launch()
+    res = bp.results()
+    check_status(res)
+    for k in range(4):
+        _close(res[0]["expect"][:, k].real, g["expect"][k])
 
 
 def _jc_problem(n_items, seeds, dtype="c64"):
