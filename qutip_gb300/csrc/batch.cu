@@ -66,6 +66,10 @@ constexpr int WARP_MAX_N = 2048;
 constexpr int WARP_BLOCK = 128;   // 4 warps (4 items) per CTA in warp mode
 constexpr int CTA_BLOCK = 256;    // threads per item in CTA mode (per CTA in cluster mode)
 constexpr int CLUSTER_CTAS = 8;   // CTAs per item in cluster mode (portable cluster size)
+// Stage inputs (ytmp, 2 x max_n entries per item) live in shared memory when all
+// items of a CTA fit in this many bytes: the matvec gathers of x then hit shared
+// memory instead of L1/L2.
+constexpr int64_t STAGE_SMEM_CAP = 96 * 1024;
 // Iterations of the trajectory loop within one output interval (each advances
 // time by one accepted step) before the item stops with QG_TOO_MUCH_WORK.
 constexpr int MC_MAX_ITER = 1 << 22;
@@ -87,6 +91,13 @@ __host__ __device__ inline SlotLayout slot_layout(int64_t n, int dt) {
   L.ctmp = L.ytmp + align256(2 * n * es);   // 2 complex128 temporaries (MC)
   L.total = L.ctmp + align256(2 * n * 16);
   return L;
+}
+
+// Dynamic shared memory of a CTA holding `groups` items' stage inputs, or 0.
+__host__ __device__ inline int64_t stage_smem_bytes(int64_t max_n, int dt, int groups) {
+  const int64_t per = align256(2 * max_n * (dt == QG_C128 ? 16 : 8));
+  const int64_t b = groups * per;
+  return b <= STAGE_SMEM_CAP ? b : 0;
 }
 
 // ----------------------------------------------------------------- groups ----
@@ -986,12 +997,16 @@ __device__ __forceinline__ void finish_queue(const qg_batch& B, unsigned int n_g
 // One warp per item; slot = global warp index (n_slots warps own slots).
 template <int DT>
 __global__ void __launch_bounds__(WARP_BLOCK) batch_warp_kernel(qg_batch B) {
+  extern __shared__ __align__(256) unsigned char stage_smem[];
   const int64_t slot = (int64_t)blockIdx.x * (WARP_BLOCK / 32) + (threadIdx.x >> 5);
   WarpGroup g{(int)(threadIdx.x & 31), slot};
   const unsigned int n_groups = gridDim.x * (WARP_BLOCK / 32);
   if (slot < B.n_slots) {
     Ctx<DT> X;
     bind_slot(X, B, slot);
+    if (stage_smem_bytes(B.max_n, DT, WARP_BLOCK / 32) > 0)
+      X.ytmp = reinterpret_cast<typename elem<DT>::T*>(
+          stage_smem + (threadIdx.x >> 5) * (stage_smem_bytes(B.max_n, DT, 1)));
     while (true) {
       int it = 0;
       if (g.rank == 0) {
@@ -1011,9 +1026,12 @@ template <int DT>
 __global__ void __launch_bounds__(CTA_BLOCK) batch_cta_kernel(qg_batch B) {
   __shared__ double red[CTA_BLOCK / 32];
   __shared__ int ibuf;
+  extern __shared__ __align__(256) unsigned char stage_smem[];
   CtaGroup<CTA_BLOCK> g{(int)threadIdx.x, (int64_t)blockIdx.x, red, &ibuf};
   Ctx<DT> X;
   bind_slot(X, B, blockIdx.x);
+  if (stage_smem_bytes(B.max_n, DT, 1) > 0)
+    X.ytmp = reinterpret_cast<typename elem<DT>::T*>(stage_smem);
   while (true) {
     int it = 0;
     if (g.rank == 0) {
@@ -1054,6 +1072,14 @@ __global__ void __launch_bounds__(CTA_BLOCK) batch_cluster_kernel(qg_batch B) {
 
 static bool warp_mode(int64_t max_n, int group) {
   return group == QG_GROUP_WARP || (group == QG_GROUP_AUTO && max_n <= WARP_MAX_N);
+}
+
+// Opt a kernel into `bytes` of dynamic shared memory (above the 48 KB default).
+template <typename K>
+static bool allow_smem(K kernel, int64_t bytes) {
+  if (bytes <= 48 * 1024) return true;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) ==
+         cudaSuccess;
 }
 
 static bool valid_group(int group) {
@@ -1174,16 +1200,24 @@ extern "C" int qg_batch_group_slots(int64_t max_n, int dtype, int group) {
     return clusters;
   }
   const bool warp = warp_mode(max_n, group);
-  if (dtype == QG_C64)
+  const int64_t smem = stage_smem_bytes(max_n, dtype, warp ? WARP_BLOCK / 32 : 1);
+  bool ok;
+  if (dtype == QG_C64) {
+    ok = warp ? allow_smem(batch_warp_kernel<QG_C64>, smem)
+              : allow_smem(batch_cta_kernel<QG_C64>, smem);
     e = warp ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_warp_kernel<QG_C64>,
-                                                             WARP_BLOCK, 0)
+                                                             WARP_BLOCK, smem)
              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_cta_kernel<QG_C64>,
-                                                             CTA_BLOCK, 0);
-  else
+                                                             CTA_BLOCK, smem);
+  } else {
+    ok = warp ? allow_smem(batch_warp_kernel<QG_C128>, smem)
+              : allow_smem(batch_cta_kernel<QG_C128>, smem);
     e = warp ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_warp_kernel<QG_C128>,
-                                                             WARP_BLOCK, 0)
+                                                             WARP_BLOCK, smem)
              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_cta_kernel<QG_C128>,
-                                                             CTA_BLOCK, 0);
+                                                             CTA_BLOCK, smem);
+  }
+  if (!ok) return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
   if (e != cudaSuccess || per_sm <= 0) return set_error(QG_ERR_CUDA, "occupancy query failed");
   // slots are warps in warp mode, CTAs otherwise
   return sm_count() * per_sm * (warp ? WARP_BLOCK / 32 : 1);
@@ -1220,11 +1254,27 @@ extern "C" int qg_batch_vern7(const qg_batch* B, void* stream) {
   if (warp_mode(B->max_n, B->group)) {
     const int per = WARP_BLOCK / 32;
     const int grid = (B->n_slots + per - 1) / per;
-    if (B->dtype == QG_C64) batch_warp_kernel<QG_C64><<<grid, WARP_BLOCK, 0, st>>>(*B);
-    else batch_warp_kernel<QG_C128><<<grid, WARP_BLOCK, 0, st>>>(*B);
+    const int64_t smem = stage_smem_bytes(B->max_n, B->dtype, per);
+    if (B->dtype == QG_C64) {
+      if (!allow_smem(batch_warp_kernel<QG_C64>, smem))
+        return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
+      batch_warp_kernel<QG_C64><<<grid, WARP_BLOCK, smem, st>>>(*B);
+    } else {
+      if (!allow_smem(batch_warp_kernel<QG_C128>, smem))
+        return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
+      batch_warp_kernel<QG_C128><<<grid, WARP_BLOCK, smem, st>>>(*B);
+    }
     return check_launch("batch_warp_kernel");
   }
-  if (B->dtype == QG_C64) batch_cta_kernel<QG_C64><<<B->n_slots, CTA_BLOCK, 0, st>>>(*B);
-  else batch_cta_kernel<QG_C128><<<B->n_slots, CTA_BLOCK, 0, st>>>(*B);
+  const int64_t smem = stage_smem_bytes(B->max_n, B->dtype, 1);
+  if (B->dtype == QG_C64) {
+    if (!allow_smem(batch_cta_kernel<QG_C64>, smem))
+      return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
+    batch_cta_kernel<QG_C64><<<B->n_slots, CTA_BLOCK, smem, st>>>(*B);
+  } else {
+    if (!allow_smem(batch_cta_kernel<QG_C128>, smem))
+      return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
+    batch_cta_kernel<QG_C128><<<B->n_slots, CTA_BLOCK, smem, st>>>(*B);
+  }
   return check_launch("batch_cta_kernel");
 }
