@@ -480,9 +480,17 @@ __global__ void __launch_bounds__(BLOCK)
 // every row in the slice is adjacent in memory, so each load instruction reads
 // 32 consecutive values / column indices (256 B / 128 B), and with entries
 // ordered by (col XOR row) the gathered x entries of a warp fall in the same few
-// lines.  Four entries per thread are kept in flight.
-template <int DT, int YDT, int EPI>
-__global__ void __launch_bounds__(SPMV_BLOCK, SLICED_MIN_BLOCKS)
+// lines.  UNR entries per thread are in flight: chunks of UNR loads, the last
+// chunk of a group predicated on the (warp-uniform) slice width.
+// Resident blocks per SM: complex64 (HBM-bound) at 40 registers; complex128
+// (FP64-bound, twice the live values) at 64.
+template <int DT, int UNR>
+struct SlicedBounds {
+  static constexpr int MIN_BLOCKS = DT == QG_C64 ? SLICED_MIN_BLOCKS : 4;
+};
+
+template <int DT, int YDT, int EPI, int UNR>
+__global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, UNR>::MIN_BLOCKS)
     spmv_sliced_kernel(qg_csr_groups A, double t, const typename elem<DT>::T* __restrict__ x,
                        AxpbyArgs ax, RkArgs rk) {
   using ST = typename elem<DT>::T;
@@ -500,30 +508,44 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SLICED_MIN_BLOCKS)
   const int* __restrict__ col = A.col;
   R err_acc = 0;
   for (int sl = warp; sl < A.n_tiles; sl += nwarps) {
-    int off = __ldg(A.row_ptr + sl) + lane;
+    int goff = __ldg(A.row_ptr + sl) + lane;  // this lane's first entry of the group
     const int row = sl * 32 + lane;
     cx<R> acc{0, 0};
     for (int g = 0; g < G; ++g) {
       const int w = __ldg(A.tile_row + sl * G + g);
       R ar = 0, ai = 0;
       int j = 0;
-      for (; j + 4 <= w; j += 4) {
-        const ST v0 = ld_stream(val + off), v1 = ld_stream(val + off + 32),
-                 v2 = ld_stream(val + off + 64), v3 = ld_stream(val + off + 96);
-        const int c0 = ld_stream(col + off), c1 = ld_stream(col + off + 32),
-                  c2 = ld_stream(col + off + 64), c3 = ld_stream(col + off + 96);
-        const ST x0 = ld_gather(x + c0), x1 = ld_gather(x + c1), x2 = ld_gather(x + c2),
-                 x3 = ld_gather(x + c3);
-        cmac_any(ar, ai, v0, x0);
-        cmac_any(ar, ai, v1, x1);
-        cmac_any(ar, ai, v2, x2);
-        cmac_any(ar, ai, v3, x3);
-        off += 128;
+      for (; j + UNR <= w; j += UNR) {
+        ST v[UNR], xv[UNR];
+        int c[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+          v[u] = ld_stream(val + goff + 32 * (j + u));
+          c[u] = ld_stream(col + goff + 32 * (j + u));
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) xv[u] = ld_gather(x + c[u]);
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) cmac_any(ar, ai, v[u], xv[u]);
       }
-      for (; j < w; ++j) {
-        cmac_any(ar, ai, ld_stream(val + off), ld_gather(x + ld_stream(col + off)));
-        off += 32;
+      if (j < w) {  // tail chunk: up to UNR - 1 entries, still all in flight
+        ST v[UNR], xv[UNR];
+        int c[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR - 1; ++u) {
+          if (j + u < w) {
+            v[u] = ld_stream(val + goff + 32 * (j + u));
+            c[u] = ld_stream(col + goff + 32 * (j + u));
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < UNR - 1; ++u)
+          if (j + u < w) xv[u] = ld_gather(x + c[u]);
+#pragma unroll
+        for (int u = 0; u < UNR - 1; ++u)
+          if (j + u < w) cmac_any(ar, ai, v[u], xv[u]);
       }
+      goff += 32 * w;
       acc = cx_add(acc, cx_mul(coef[g], cx<R>{ar, ai}));
     }
     if (row < n) epilogue<DT, YDT, EPI>(row, acc, ax, rk, err_acc);
@@ -582,8 +604,10 @@ static int launch_any(cudaStream_t st, const qg_csr_groups& A, double t, const v
   using ST = typename elem<DT>::T;
   const int lanes = A.lanes > 0 ? A.lanes : 4;
   if (A.layout == QG_LAYOUT_SLICED) {
-    // one wave: every block resident at once, warps striding over the slices
-    auto kern = spmv_sliced_kernel<DT, YDT, EPI>;
+    // one wave: every block resident at once, warps striding over the slices.  (8
+    // entries in flight at 64 registers measured slower than 4 at 40: 73 vs 68 us
+    // per fused stage on the L=10 Liouvillian, so only the 4-entry variant is built.)
+    auto kern = spmv_sliced_kernel<DT, YDT, EPI, 4>;
     static OccCache cache;  // one per instantiation
     const int per_sm = staged_occupancy(kern, SPMV_BLOCK, 0, cache);
     if (per_sm <= 0) return set_error(QG_ERR_CUDA, "occupancy query failed");
