@@ -272,13 +272,22 @@ typedef struct qg_batch {
   int32_t max_jumps;
   int32_t n_slots;        /* groups (warps or CTAs, see `group`); each owns one slot */
   void* work;             /* n_slots * qg_batch_slot_bytes(max_n, dtype) bytes */
-  unsigned int* queue;    /* two words, zero before the launch; left zero */
+  unsigned int* queue;    /* four words, zero before the launch; words 0-1 are left zero;
+                             word 2 becomes non-zero if an operator-staging wait gave up
+                             (the launch then read the operator from global memory) */
   const volatile int32_t* cancel; /* optional host-visible flag; non-zero stops all items */
   int64_t* progress;      /* optional [n_slots]: (item << 32) | output index of each slot */
   double* debug;          /* optional [n_slots * 64]: last trajectory-loop states per slot */
   int32_t norm_steps;     /* MC options (qutip/solver/mcsolve.py:449-466) */
   int32_t group;          /* QG_GROUP_*: threads per item */
   double norm_t_tol, norm_tol, norm_min_step, mc_corr_eps;
+  /* Operator staging: when the launch has one system, its generator's row
+   * pointers (stage_op_rp words) and entries (stage_op_entries) can be copied once
+   * per CTA into shared memory (bulk async copies, mbarrier completion) and read
+   * from there; 0 = read from global memory.  Warp and CTA groups only. */
+  int64_t stage_op_entries;
+  int32_t stage_op_rp;
+  int32_t pad2_;
 } qg_batch;
 
 /* Threads per item of the batched solver: one warp, one 256-thread CTA, a
@@ -298,6 +307,12 @@ int qg_batch_max_slots(int64_t max_n, int dtype);
  * QG_GROUP_CLUSTER, warps or CTAs for QG_GROUP_AUTO) on the current device: the
  * useful n_slots for that group shape. */
 int qg_batch_group_slots(int64_t max_n, int dtype, int group);
+/* Resident groups for this launch description (max_n, dtype, group and operator
+ * staging of *B): the useful n_slots. */
+int qg_batch_launch_slots(const qg_batch* B);
+/* Shared-memory bytes per CTA of this launch (stage inputs and staged operator);
+ * 0 when nothing is staged. */
+int64_t qg_batch_smem_bytes(const qg_batch* B);
 
 /* Solve every item of the batch in one persistent launch: each CTA takes items
  * from an atomic queue and runs the adaptive Vern7 integration of

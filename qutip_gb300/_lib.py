@@ -75,6 +75,8 @@ _SIGS = {
     "qg_batch_slot_bytes": (C.c_int64, [C.c_int64, C.c_int]),
     "qg_batch_max_slots": (C.c_int, [C.c_int64, C.c_int]),
     "qg_batch_group_slots": (C.c_int, [C.c_int64, C.c_int, C.c_int]),
+    "qg_batch_launch_slots": (C.c_int, [C.c_void_p]),
+    "qg_batch_smem_bytes": (C.c_int64, [C.c_void_p]),
     "qg_batch_vern7": (C.c_int, [C.c_void_p, C.c_void_p]),
     "qg_batch_vern7_noalloc": (C.c_int, [C.c_void_p, C.c_void_p]),
 }

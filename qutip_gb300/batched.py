@@ -58,7 +58,8 @@ class BatchStruct(C.Structure):
                 ("progress", C.c_void_p), ("debug", C.c_void_p),
                 ("norm_steps", C.c_int32), ("group", C.c_int32), ("norm_t_tol", C.c_double),
                 ("norm_tol", C.c_double), ("norm_min_step", C.c_double),
-                ("mc_corr_eps", C.c_double)]
+                ("mc_corr_eps", C.c_double), ("stage_op_entries", C.c_int64),
+                ("stage_op_rp", C.c_int32), ("pad2_", C.c_int32)]
 
 
 MC_DEFAULTS = dict(norm_steps=25, norm_t_tol=1e-6, norm_tol=1e-4, norm_min_step=0.1,
@@ -182,7 +183,7 @@ class BatchProblem:
                              cop_rp_off, tlist_off, len(tl), 0 if kind == "me" else 1,
                              len(c_ops), int(nsteps), float(atol), float(rtol)))
         self.sys_info.append(dict(n=n, d=d, kind=kind, n_eops=len(e_ops), n_out=len(tl),
-                                  nnz=len(col), tlist=tl))
+                                  nnz=len(col), tlist=tl, rp_len=len(rp)))
         return len(self.systems) - 1
 
     def add_item(self, system: int, y0, seed=None) -> int:
@@ -210,12 +211,15 @@ class BatchProblem:
         a = np.concatenate([a, np.zeros(pad, np_dtype)])
         return torch.from_numpy(a).to(self.device, dtype)
 
-    def build(self, max_jumps=0, mc_options=None, order=None, n_slots=None, group="auto"):
+    def build(self, max_jumps=0, mc_options=None, order=None, n_slots=None, group="auto",
+              stage_operator="auto"):
         """Upload pools; ``order`` permutes the items (longest first balances the queue).
 
         ``group`` is ``"auto"``, ``"warp"``, ``"cta"`` or ``"cluster"`` (threads per
         item: 32, 256, or 8 x 256 on a thread-block cluster);
-        ``n_slots`` caps the resident groups (default: all that fit)."""
+        ``n_slots`` caps the resident groups (default: all that fit);
+        ``stage_operator``: copy the generator of a single-system launch into shared
+        memory once per CTA (``"auto"``: when it takes at most 64 KB)."""
         if not self.items:
             raise ValueError("no items")
         lib = _lib.load()
@@ -254,12 +258,14 @@ class BatchProblem:
         if group not in GROUPS:
             raise ValueError(f"group must be one of {sorted(GROUPS)}")
         self.group = group
-        slots = lib.qg_batch_group_slots(self.max_n, qdt, GROUPS[group])
-        if slots < 0:
-            _lib.check(slots, "qg_batch_group_slots")
-        self.n_slots = int(min(n_items, slots if n_slots is None else n_slots))
-        slot_bytes = int(lib.qg_batch_slot_bytes(self.max_n, qdt))
-        self.work = torch.empty(self.n_slots * slot_bytes, dtype=torch.uint8, device=self.device)
+        stage_entries = stage_rp = 0
+        if len(self.systems) == 1 and group != "cluster" and stage_operator:
+            info = self.sys_info[0]
+            es = 8 if self.dtype == "c64" else 16
+            a16 = lambda b: (b + 15) // 16 * 16  # noqa: E731
+            op_bytes = a16(4 * info["rp_len"]) + a16(4 * info["nnz"]) + a16(es * info["nnz"])
+            if stage_operator is True or op_bytes <= 64 * 1024:
+                stage_entries, stage_rp = info["nnz"], info["rp_len"]
         self.queue = torch.zeros(4, dtype=torch.int32, device=self.device)
         mc = {**MC_DEFAULTS, **(mc_options or {})}
         p = lambda t: t.data_ptr()  # noqa: E731
@@ -268,10 +274,20 @@ class BatchProblem:
             p(self.op_rp), p(self.op_col), p(self.op_val), p(self.coef_code), p(self.coef_start),
             p(self.coef_consts), p(self.eop_rp), p(self.eop_col), p(self.eop_val), p(self.cop_rp),
             p(self.cop_col), p(self.cop_val), p(self.tlist_d), p(self.y0_d), p(self.out),
-            p(self.status), p(self.jump_t), p(self.jump_which), self.max_jumps, self.n_slots,
-            p(self.work), p(self.queue), None, None, None, int(mc["norm_steps"]), GROUPS[group],
+            p(self.status), p(self.jump_t), p(self.jump_which), self.max_jumps, 1,
+            None, p(self.queue), None, None, None, int(mc["norm_steps"]), GROUPS[group],
             float(mc["norm_t_tol"]),
-            float(mc["norm_tol"]), float(mc["norm_min_step"]), float(mc["mc_corr_eps"]))
+            float(mc["norm_tol"]), float(mc["norm_min_step"]), float(mc["mc_corr_eps"]),
+            int(stage_entries), int(stage_rp), 0)
+        slots = lib.qg_batch_launch_slots(C.byref(self.struct))
+        if slots < 0:
+            _lib.check(slots, "qg_batch_launch_slots")
+        self.n_slots = int(min(n_items, slots if n_slots is None else n_slots))
+        slot_bytes = int(lib.qg_batch_slot_bytes(self.max_n, qdt))
+        self.work = torch.empty(self.n_slots * slot_bytes, dtype=torch.uint8, device=self.device)
+        self.struct.n_slots = self.n_slots
+        self.struct.work = p(self.work)
+        self.staged_operator = stage_entries > 0
         return self
 
     def set_cancel(self, host_flag_tensor):
@@ -320,6 +336,9 @@ class BatchProblem:
 
     def results(self, normalize=True):
         """Per item (original order): expect [n_out, n_eops], status row, jumps."""
+        if int(self.queue[2].item()) != 0:
+            raise RuntimeError("an operator-staging wait gave up on the device (the results "
+                               "were computed from global memory); the GPU may be unhealthy")
         out = self.out.cpu().numpy()
         status = self.status.cpu().numpy().reshape(-1, 4)
         jt = self.jump_t.cpu().numpy()

@@ -100,6 +100,44 @@ __host__ __device__ inline int64_t stage_smem_bytes(int64_t max_n, int dt, int g
   return b <= STAGE_SMEM_CAP ? b : 0;
 }
 
+__host__ __device__ inline int64_t align16(int64_t b) { return (b + 15) & ~(int64_t)15; }
+
+// Shared-memory bytes of a staged operator (row pointers, columns, values), or 0.
+__host__ __device__ inline int64_t op_smem_bytes(const qg_batch& B) {
+  if (B.stage_op_entries <= 0) return 0;
+  const int64_t es = B.dtype == QG_C128 ? 16 : 8;
+  return align16((int64_t)B.stage_op_rp * 4) + align16(B.stage_op_entries * 4) +
+         align16(B.stage_op_entries * es);
+}
+
+// Copy the single system's generator into shared memory (called by every thread
+// of the CTA, once, before the item loop): thread 0 issues three bulk async copies
+// completing on one mbarrier; all threads wait at most WAIT_CYCLES and vote.  On
+// success the Ctx reads the operator from shared memory; otherwise it keeps the
+// global pointers, the fault word queue[2] is set, and `pending` tells the caller
+// to drain the copies before the CTA exits.
+template <int DT>
+__device__ bool stage_operator(const qg_batch& B, unsigned char* smem_op, uint64_t* bar) {
+  using ST = typename elem<DT>::T;
+  const unsigned brp = (unsigned)align16((int64_t)B.stage_op_rp * 4);
+  const unsigned bcol = (unsigned)align16(B.stage_op_entries * 4);
+  const unsigned bval = (unsigned)align16(B.stage_op_entries * (int64_t)sizeof(ST));
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(bar, brp + bcol + bval);
+    bulk_g2s(smem_op, B.op_rp, brp, bar);
+    bulk_g2s(smem_op + brp, B.op_col, bcol, bar);
+    bulk_g2s(smem_op + brp + bcol, B.op_val, bval, bar);
+  }
+  const bool ok = __syncthreads_and(mbar_poll(bar, 0) ? 1 : 0) != 0;
+  if (!ok && threadIdx.x == 0) atomicOr(B.queue + 2, 1u);
+  return ok;
+}
+
 // ----------------------------------------------------------------- groups ----
 namespace cgrp = cooperative_groups;
 
@@ -203,7 +241,9 @@ struct Ctx {
   ST* k;
   ST* ytmp;
   double2* ctmp[2];
-  const ST* opval;
+  const ST* opval;        // generator entries: global pool, or the staged copy
+  const int* op_col;
+  const int* op_rp;
   double2 coef[QG_MAX_GROUPS];  // coefficients at the current stage time
   float2 coef_f[QG_MAX_GROUPS];  // the same in FP32 (mixed form)
 };
@@ -239,13 +279,13 @@ __device__ __forceinline__ void row_matvec(const Ctx<DT>& X, int r, const XT* x,
   using CT = typename elem<DT>::R;
   ar = 0;
   ai = 0;
-  const int* rp = X.B->op_rp + X.S->rp_off + (int64_t)r * X.G;
+  const int* rp = X.op_rp + X.S->rp_off + (int64_t)r * X.G;
   for (int g = 0; g < X.G; ++g) {
-    const int s = __ldg(rp + g), e = __ldg(rp + g + 1);
+    const int s = rp[g], e = rp[g + 1];
     CT gr = 0, gi = 0;
     for (int p = s; p < e; ++p) {
-      const auto v = __ldg(X.opval + p);
-      const auto xv = x[__ldg(X.B->op_col + p)];
+      const auto v = X.opval[p];
+      const auto xv = x[X.op_col[p]];
       gr = fma((CT)v.x, (CT)xv.x, gr);
       gr = fma(-(CT)v.y, (CT)xv.y, gr);
       gi = fma((CT)v.x, (CT)xv.y, gi);
@@ -967,12 +1007,24 @@ __device__ void run_item(const GT& g, const qg_batch& B, Ctx<DT>& X, int item) {
 }
 
 template <int DT>
+__device__ __forceinline__ void use_staged(Ctx<DT>& X, const qg_batch& B, unsigned char* smem_op) {
+  using ST = typename elem<DT>::T;
+  const int64_t brp = align16((int64_t)B.stage_op_rp * 4);
+  const int64_t bcol = align16(B.stage_op_entries * 4);
+  X.op_rp = reinterpret_cast<const int*>(smem_op);
+  X.op_col = reinterpret_cast<const int*>(smem_op + brp);
+  X.opval = reinterpret_cast<const ST*>(smem_op + brp + bcol);
+}
+
+template <int DT>
 __device__ __forceinline__ void bind_slot(Ctx<DT>& X, const qg_batch& B, int64_t slot_index) {
   using ST = typename elem<DT>::T;
   const SlotLayout L = slot_layout(B.max_n, DT);
   char* slot = static_cast<char*>(B.work) + slot_index * L.total;
   X.B = &B;
   X.opval = static_cast<const ST*>(B.op_val);
+  X.op_col = B.op_col;
+  X.op_rp = B.op_rp;
   X.y[0] = reinterpret_cast<double2*>(slot + L.y);
   X.y[1] = X.y[0] + B.max_n;
   X.ys[0] = reinterpret_cast<ST*>(slot + L.ys);
@@ -996,15 +1048,24 @@ __device__ __forceinline__ void finish_queue(const qg_batch& B, unsigned int n_g
 
 // One warp per item; slot = global warp index (n_slots warps own slots).
 template <int DT>
-__global__ void __launch_bounds__(WARP_BLOCK) batch_warp_kernel(qg_batch B) {
+__global__ void __launch_bounds__(WARP_BLOCK, 4) batch_warp_kernel(qg_batch B) {
   extern __shared__ __align__(256) unsigned char stage_smem[];
+  __shared__ __align__(8) uint64_t op_bar;
   const int64_t slot = (int64_t)blockIdx.x * (WARP_BLOCK / 32) + (threadIdx.x >> 5);
   WarpGroup g{(int)(threadIdx.x & 31), slot};
   const unsigned int n_groups = gridDim.x * (WARP_BLOCK / 32);
+  const int64_t in_bytes = stage_smem_bytes(B.max_n, DT, WARP_BLOCK / 32);
+  unsigned char* smem_op = stage_smem + in_bytes;
+  bool staged = false, pending = false;
+  if (B.stage_op_entries > 0) {
+    staged = stage_operator<DT>(B, smem_op, &op_bar);
+    pending = !staged;
+  }
   if (slot < B.n_slots) {
     Ctx<DT> X;
     bind_slot(X, B, slot);
-    if (stage_smem_bytes(B.max_n, DT, WARP_BLOCK / 32) > 0)
+    if (staged) use_staged(X, B, smem_op);
+    if (in_bytes > 0)
       X.ytmp = reinterpret_cast<typename elem<DT>::T*>(
           stage_smem + (threadIdx.x >> 5) * (stage_smem_bytes(B.max_n, DT, 1)));
     while (true) {
@@ -1019,6 +1080,7 @@ __global__ void __launch_bounds__(WARP_BLOCK) batch_warp_kernel(qg_batch B) {
     }
   }
   if (g.rank == 0) finish_queue(B, n_groups);
+  if (pending && threadIdx.x == 0) (void)mbar_poll(&op_bar, 0);  // drain before exit
 }
 
 // One CTA per item; slot = block index.
@@ -1027,11 +1089,18 @@ __global__ void __launch_bounds__(CTA_BLOCK) batch_cta_kernel(qg_batch B) {
   __shared__ double red[CTA_BLOCK / 32];
   __shared__ int ibuf;
   extern __shared__ __align__(256) unsigned char stage_smem[];
+  __shared__ __align__(8) uint64_t op_bar;
   CtaGroup<CTA_BLOCK> g{(int)threadIdx.x, (int64_t)blockIdx.x, red, &ibuf};
   Ctx<DT> X;
   bind_slot(X, B, blockIdx.x);
-  if (stage_smem_bytes(B.max_n, DT, 1) > 0)
-    X.ytmp = reinterpret_cast<typename elem<DT>::T*>(stage_smem);
+  const int64_t in_bytes = stage_smem_bytes(B.max_n, DT, 1);
+  if (in_bytes > 0) X.ytmp = reinterpret_cast<typename elem<DT>::T*>(stage_smem);
+  unsigned char* smem_op = stage_smem + in_bytes;
+  bool pending = false;
+  if (B.stage_op_entries > 0) {
+    if (stage_operator<DT>(B, smem_op, &op_bar)) use_staged(X, B, smem_op);
+    else pending = true;
+  }
   while (true) {
     int it = 0;
     if (g.rank == 0) {
@@ -1043,6 +1112,7 @@ __global__ void __launch_bounds__(CTA_BLOCK) batch_cta_kernel(qg_batch B) {
     run_item(g, B, X, it);
   }
   if (g.rank == 0) finish_queue(B, gridDim.x);
+  if (pending && threadIdx.x == 0) (void)mbar_poll(&op_bar, 0);  // drain before exit
 }
 
 // One cluster of CLUSTER_CTAS CTAs per item; slot = cluster index.
@@ -1162,7 +1232,7 @@ extern "C" int qg_batch_vern7_noalloc(const qg_batch* B, void* stream) {
   NoallocAddr a;
   int rc = noalloc_setup(dev, a);
   if (rc) return rc;
-  int occ = qg_batch_group_slots(B->max_n, B->dtype, B->group);
+  int occ = qg_batch_launch_slots(B);
   if (occ <= 0) return occ < 0 ? occ : set_error(QG_ERR_CUDA, "no resident CTA");
   int64_t slots = (int64_t)NOALLOC_WORK_BYTES / slot;
   if (slots > occ) slots = occ;
@@ -1182,7 +1252,16 @@ extern "C" int64_t qg_batch_slot_bytes(int64_t max_n, int dtype) {
   return slot_layout(max_n, dtype).total;
 }
 
-extern "C" int qg_batch_group_slots(int64_t max_n, int dtype, int group) {
+// Dynamic shared memory of a launch: stage inputs plus the staged operator.
+static int64_t launch_smem(const qg_batch& B) {
+  if (B.group == QG_GROUP_CLUSTER) return 0;
+  const bool warp = warp_mode(B.max_n, B.group);
+  return stage_smem_bytes(B.max_n, B.dtype, warp ? WARP_BLOCK / 32 : 1) + op_smem_bytes(B);
+}
+
+constexpr int64_t MAX_DYN_SMEM = 227 * 1024;
+
+static int group_slots(int64_t max_n, int dtype, int group, int64_t smem) {
   if (!valid_group(group))
     return set_error(QG_ERR_ARG,
                      "group must be QG_GROUP_AUTO, QG_GROUP_WARP, QG_GROUP_CTA or QG_GROUP_CLUSTER");
@@ -1199,8 +1278,8 @@ extern "C" int qg_batch_group_slots(int64_t max_n, int dtype, int group) {
       return set_error(QG_ERR_CUDA, "cluster occupancy query failed");
     return clusters;
   }
+  if (smem > MAX_DYN_SMEM) return set_error(QG_ERR_ARG, "staged data exceed shared memory");
   const bool warp = warp_mode(max_n, group);
-  const int64_t smem = stage_smem_bytes(max_n, dtype, warp ? WARP_BLOCK / 32 : 1);
   bool ok;
   if (dtype == QG_C64) {
     ok = warp ? allow_smem(batch_warp_kernel<QG_C64>, smem)
@@ -1223,6 +1302,23 @@ extern "C" int qg_batch_group_slots(int64_t max_n, int dtype, int group) {
   return sm_count() * per_sm * (warp ? WARP_BLOCK / 32 : 1);
 }
 
+extern "C" int qg_batch_group_slots(int64_t max_n, int dtype, int group) {
+  const bool warp = group != QG_GROUP_CLUSTER && warp_mode(max_n, group);
+  const int64_t smem =
+      group == QG_GROUP_CLUSTER ? 0 : stage_smem_bytes(max_n, dtype, warp ? WARP_BLOCK / 32 : 1);
+  return group_slots(max_n, dtype, group, smem);
+}
+
+extern "C" int qg_batch_launch_slots(const qg_batch* B) {
+  if (!B) return set_error(QG_ERR_ARG, "null batch pointer");
+  return group_slots(B->max_n, B->dtype, B->group, launch_smem(*B));
+}
+
+extern "C" int64_t qg_batch_smem_bytes(const qg_batch* B) {
+  if (!B) return set_error(QG_ERR_ARG, "null batch pointer");
+  return launch_smem(*B);
+}
+
 extern "C" int qg_batch_max_slots(int64_t max_n, int dtype) {
   return qg_batch_group_slots(max_n, dtype, QG_GROUP_AUTO);
 }
@@ -1240,6 +1336,12 @@ extern "C" int qg_batch_vern7(const qg_batch* B, void* stream) {
   if (!valid_group(B->group))
     return set_error(QG_ERR_ARG,
                      "group must be QG_GROUP_AUTO, QG_GROUP_WARP, QG_GROUP_CTA or QG_GROUP_CLUSTER");
+  if (B->stage_op_entries > 0 &&
+      (B->group == QG_GROUP_CLUSTER || B->n_systems != 1 || B->stage_op_rp <= 0))
+    return set_error(QG_ERR_ARG,
+                     "operator staging needs one system and a warp or CTA group");
+  if (launch_smem(*B) > MAX_DYN_SMEM)
+    return set_error(QG_ERR_ARG, "staged data exceed shared memory");
   if (B->n_items == 0) return QG_OK;
   cudaStream_t st = (cudaStream_t)stream;
   if (B->group == QG_GROUP_CLUSTER) {
@@ -1254,7 +1356,7 @@ extern "C" int qg_batch_vern7(const qg_batch* B, void* stream) {
   if (warp_mode(B->max_n, B->group)) {
     const int per = WARP_BLOCK / 32;
     const int grid = (B->n_slots + per - 1) / per;
-    const int64_t smem = stage_smem_bytes(B->max_n, B->dtype, per);
+    const int64_t smem = launch_smem(*B);
     if (B->dtype == QG_C64) {
       if (!allow_smem(batch_warp_kernel<QG_C64>, smem))
         return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
@@ -1266,7 +1368,7 @@ extern "C" int qg_batch_vern7(const qg_batch* B, void* stream) {
     }
     return check_launch("batch_warp_kernel");
   }
-  const int64_t smem = stage_smem_bytes(B->max_n, B->dtype, 1);
+  const int64_t smem = launch_smem(*B);
   if (B->dtype == QG_C64) {
     if (!allow_smem(batch_cta_kernel<QG_C64>, smem))
       return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");

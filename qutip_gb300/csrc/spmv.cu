@@ -314,49 +314,6 @@ __global__ void __launch_bounds__(SPMV_BLOCK)
 }
 
 // ------------------------------------------------------------ staged kernel --
-__device__ __forceinline__ unsigned smem_u32(const void* p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0u;
-}
-// 1-D bulk copy global -> shared; dst, src and bytes are multiples of 16.
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
-                                         uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-
-// Bounded wait: every thread polls for at most WAIT_CYCLES SM cycles (about a
-// second); a block-wide vote decides whether the wait completed.  A wait that
-// never completes (it cannot in a correct launch) sets the device fault flag
-// instead of hanging the GPU.
-constexpr long long WAIT_CYCLES = 2000000000LL;
-__device__ __forceinline__ bool mbar_poll(uint64_t* bar, unsigned parity) {
-  const long long t0 = clock64();
-  bool ok = mbar_try_wait(bar, parity);
-  while (!ok && clock64() - t0 < WAIT_CYCLES) ok = mbar_try_wait(bar, parity);
-  return ok;
-}
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
   const bool ok = mbar_poll(bar, parity);
   return __syncthreads_and(ok ? 1 : 0) != 0;

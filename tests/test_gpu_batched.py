@@ -178,3 +178,20 @@ def test_tune_batch_picks_a_valid_shape():
     best = tune_batch(lambda n: _jc_problem(n, seeds), sample_items=64, reps=1)
     assert best["group"] in ("warp", "cta") and 0 < best["slot_fraction"] <= 1
     assert best["ms"] > 0 and len(best["timings"]) >= 2
+
+
+@pytest.mark.parametrize("group", ["warp", "cta"])
+def test_staged_operator_matches_global_reads(group):
+    """The generator copied into shared memory (bulk async copies, mbarrier) gives
+    bit-identical trajectories to reading it from global memory."""
+    seeds = np.random.SeedSequence(9).spawn(64)
+    res = []
+    for stage in (False, True):
+        bp = _jc_problem(64, seeds)
+        bp.build(max_jumps=64, group=group, stage_operator=stage)
+        assert bp.staged_operator == stage
+        bp.launch()
+        res.append(bp.results())
+    for x, y in zip(*res):
+        np.testing.assert_array_equal(x["expect"], y["expect"])
+        np.testing.assert_array_equal(x["col_times"], y["col_times"])
