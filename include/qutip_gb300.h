@@ -41,7 +41,9 @@ typedef enum {
   QG_NOT_INITIATED = -4,
   QG_NORM_SEARCH_FAILED = -5, /* jump-time search exhausted (qutip/solver/mcsolve.py:363-367) */
   QG_TIMEOUT = -6,            /* cancelled through the host-visible cancel flag */
-  QG_JUMP_OVERFLOW = -7       /* more jumps than the batch's max_jumps */
+  QG_JUMP_OVERFLOW = -7,      /* more jumps than the batch's max_jumps */
+  QG_BAD_ITEM = -8            /* item not run: bad system index, state longer than max_n,
+                                 or a group count outside 1..QG_MAX_GROUPS */
 } qg_status;
 
 /* A sum of CSR matrices with time-dependent coefficients,

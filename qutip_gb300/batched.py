@@ -428,6 +428,8 @@ STATUS_TEXT = {
         "'norm_t_tol'.",
     -6: "Cancelled.",
     -7: "More jumps than max_jumps.",
+    -8: "Item not run: bad system index, state longer than max_n, or a coefficient-group "
+        "count outside 1..8.",
 }
 
 

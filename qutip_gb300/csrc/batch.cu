@@ -847,6 +847,19 @@ __device__ double cop_apply(const GT& g, Ctx<DT>& X, int i, bool store) {
 template <int DT, class GT>
 __device__ void run_item(const GT& g, const qg_batch& B, Ctx<DT>& X, int item) {
   const qg_batch_item I = B.items[item];
+  // reject an item the workspace or the kernel's fixed-size arrays cannot hold
+  // (the host builder never produces one; a raw C caller might)
+  if (I.system < 0 || I.system >= B.n_systems || B.systems[I.system].n > B.max_n ||
+      B.systems[I.system].n <= 0 || B.systems[I.system].n_groups > QG_MAX_GROUPS ||
+      B.systems[I.system].n_groups <= 0) {
+    if (g.rank == 0) {
+      int32_t* st = B.status + 4 * (int64_t)item;
+      st[0] = QG_BAD_ITEM;
+      st[1] = st[2] = st[3] = 0;
+    }
+    g.sync();
+    return;
+  }
   const qg_batch_system* S = B.systems + I.system;
   X.S = S;
   X.n = S->n;
@@ -954,17 +967,14 @@ __device__ void run_item(const GT& g, const qg_batch& B, Ctx<DT>& X, int item) {
         int which = 0;
         const int nc = S->n_cops;
         if (nc > 1) {
-          double probs[16];
+          // sum of the jump probabilities, then the reference's walk over them;
+          // each probability is recomputed (bit-identical, no per-operator array)
           double sum = 0.0;
-          const int m = nc < 16 ? nc : 16;
-          for (int i = 0; i < m; ++i) {
-            probs[i] = cop_apply(g, X, i, false);
-            sum += probs[i];
-          }
-          double tgt = sum * pcg_random(rng) - probs[0];
-          while (tgt > 0 && which < m - 1) {
+          for (int i = 0; i < nc; ++i) sum += cop_apply(g, X, i, false);
+          double tgt = sum * pcg_random(rng) - cop_apply(g, X, 0, false);
+          while (tgt > 0 && which < nc - 1) {
             ++which;
-            tgt -= probs[which];
+            tgt -= cop_apply(g, X, which, false);
           }
         }
         const double new_norm = sqrt(cop_apply(g, X, which, true));

@@ -195,3 +195,36 @@ def test_staged_operator_matches_global_reads(group):
     for x, y in zip(*res):
         np.testing.assert_array_equal(x["expect"], y["expect"])
         np.testing.assert_array_equal(x["col_times"], y["col_times"])
+
+
+def test_many_collapse_operators_match_oracle():
+    """Ising chain L=9 trajectories have 18 collapse operators (sigma-_i, sigma^z_i):
+    the device walks all of them in the reference's order (mcsolve.py:384-391)."""
+    from oracle.solvers import mc_trajectory
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import mcsolve_batch
+    s = S.ising_chain(9, gamma_minus=0.5, gamma_z=0.3, kind="mc")
+    assert len(s.c_ops) == 18
+    tl = np.linspace(0.0, 2.0, 21)
+    seeds = np.random.SeedSequence(12).spawn(3)
+    r = mcsolve_batch(s, tl, 3, seeds=seeds, precision="double", max_jumps=64)
+    total = 0
+    for tr in range(3):
+        ex, cols = mc_trajectory(s.terms, s.c_ops, s.state0, tl, s.e_ops, seeds[tr])
+        assert [w for _, w in cols] == [int(w) for w in r.col_which[tr]]
+        np.testing.assert_allclose(r.col_times[tr], [t for t, _ in cols], atol=1e-3)
+        total += len(cols)
+    assert total > 0
+
+
+def test_bad_items_are_rejected_without_touching_memory():
+    """A launch whose max_n is smaller than an item's state reports QG_BAD_ITEM for
+    that item instead of running it."""
+    seeds = np.random.SeedSequence(4).spawn(8)
+    bp = _jc_problem(8, seeds)
+    bp.build(max_jumps=16)
+    bp.struct.max_n = 4          # the JC states have 12 entries
+    bp.launch()
+    torch.cuda.synchronize()
+    st = bp.status.cpu().numpy().reshape(-1, 4)[:, 0]
+    assert np.all(st == -8)

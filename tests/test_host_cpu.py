@@ -109,3 +109,31 @@ def test_sliced_layout_host_builder():
                 y[rows[ok]] += val[idx[ok]] * x[col[idx[ok]]]
         np.testing.assert_allclose(y, mats[g] @ x, atol=1e-13)
     assert total <= 1.15 * sum(m.nnz for m in mats)
+
+
+def test_batch_argument_validation_before_any_device_call():
+    """qg_batch_vern7 rejects malformed launches on the host, before any CUDA call."""
+    import ctypes as C
+    from qutip_gb300 import _lib
+    from qutip_gb300.batched import BatchStruct
+    lib = _lib.load()
+    assert lib.qg_batch_vern7(None, None) == _lib.QG_ERR_ARG
+    fake = 256  # never dereferenced on the host
+    b = BatchStruct()
+    for f in ("systems", "items", "op_rp", "op_col", "op_val", "tlist", "y0", "out", "status",
+              "work", "queue"):
+        setattr(b, f, fake)
+    b.n_systems, b.n_items, b.dtype, b.max_n, b.n_slots = 1, 0, _lib.QG_C64, 16, 1
+    assert lib.qg_batch_vern7(C.byref(b), None) == _lib.QG_OK        # nothing to do
+    b.group = 7
+    assert lib.qg_batch_vern7(C.byref(b), None) == _lib.QG_ERR_ARG   # unknown group
+    b.group = _lib.QG_GROUP_CLUSTER
+    b.stage_op_entries, b.stage_op_rp = 100, 17
+    assert lib.qg_batch_vern7(C.byref(b), None) == _lib.QG_ERR_ARG   # staging needs warp/CTA
+    b.group, b.n_systems = _lib.QG_GROUP_CTA, 2
+    assert lib.qg_batch_vern7(C.byref(b), None) == _lib.QG_ERR_ARG   # staging needs 1 system
+    b.n_systems, b.stage_op_entries = 1, 10 ** 6
+    assert lib.qg_batch_vern7(C.byref(b), None) == _lib.QG_ERR_ARG   # exceeds shared memory
+    b.stage_op_entries, b.dtype = 0, 5
+    assert lib.qg_batch_vern7(C.byref(b), None) == _lib.QG_ERR_UNSUPPORTED
+    assert b"dtype" in lib.qg_last_error()
