@@ -23,13 +23,14 @@ from typing import Mapping
 
 import numpy as np
 
-__all__ = ["Coefficient", "coefficient", "OPCODES", "MAX_STACK", "pack_programs"]
+__all__ = ["Coefficient", "coefficient", "interpolation", "OPCODES", "MAX_STACK",
+           "pack_programs"]
 
 OPCODES = {
     "END": 0, "CONST": 1, "T": 2, "ADD": 3, "SUB": 4, "MUL": 5, "DIV": 6, "NEG": 7,
     "COS": 8, "SIN": 9, "EXP": 10, "LOG": 11, "SQRT": 12, "CONJ": 13, "REAL": 14,
     "IMAG": 15, "ABS": 16, "POW": 17, "COSH": 18, "SINH": 19, "TANH": 20, "TAN": 21,
-    "ARCTAN": 22,
+    "ARCTAN": 22, "INTERP": 23,
 }
 MAX_STACK = 16
 _FUNCS = {"cos": "COS", "sin": "SIN", "exp": "EXP", "log": "LOG", "sqrt": "SQRT",
@@ -97,7 +98,7 @@ def _shift_consts(code, shift):
     out, i = [], 0
     while i < len(code):
         out.append(code[i])
-        if code[i] == OPCODES["CONST"]:
+        if code[i] in (OPCODES["CONST"], OPCODES["INTERP"]):
             out.append(code[i + 1] + shift)
             i += 1
         i += 1
@@ -113,7 +114,7 @@ def _max_depth(code):
         op = code[i]
         if op == OPCODES["END"]:
             break
-        if op == OPCODES["CONST"]:
+        if op in (OPCODES["CONST"], OPCODES["INTERP"]):
             d += 1
             i += 1
         elif op == OPCODES["T"]:
@@ -234,6 +235,9 @@ def _run(code, consts, t):
         if op == O["CONST"]:
             i += 1
             st.append(consts[code[i]])
+        elif op == O["INTERP"]:
+            i += 1
+            st.append(_interp_eval(consts, code[i], t))
         elif op == O["T"]:
             st.append(complex(t))
         elif op in un:
@@ -245,6 +249,56 @@ def _run(code, consts, t):
                        O["POW"]: a ** b}[op])
         i += 1
     return st[-1]
+
+
+def interpolation(tlist, poly, dt=0.0) -> Coefficient:
+    """A piecewise polynomial ``poly[order+1][n]`` on breakpoints ``tlist`` (the form
+    of the reference's ``InterCoefficient``, qutip/core/cy/coefficient.pyx:412-566):
+    ``poly[order][0]`` below the first breakpoint, ``poly[order][n-1]`` from the last,
+    Horner in ``t - tlist[idx]`` inside; ``dt`` non-zero marks uniform breakpoints."""
+    tl = np.asarray(tlist, dtype=np.float64).reshape(-1)
+    pl = np.asarray(poly, dtype=np.complex128)
+    if pl.ndim != 2 or pl.shape[1] != tl.shape[0] or tl.shape[0] == 0:
+        raise ValueError("poly must have shape (order + 1, len(tlist))")
+    n, order = tl.shape[0], pl.shape[0] - 1
+    consts = [complex(n, order), complex(float(dt), 0.0)] + [complex(x) for x in tl] + \
+        [complex(z) for z in pl.reshape(-1)]
+    return Coefficient([OPCODES["INTERP"], 0, OPCODES["END"]], consts,
+                       f"interp(n={n}, order={order})")
+
+
+def _interp_eval(consts, k, t):
+    n, order = int(consts[k].real), int(consts[k].imag)
+    dt = consts[k + 1].real
+    tl = [consts[k + 2 + i].real for i in range(n)]
+    base = k + 2 + n
+
+    def p(i, j):
+        return consts[base + i * n + j]
+    if t <= tl[0]:
+        return p(order, 0)
+    if t >= tl[-1]:
+        return p(order, n - 1)
+    if dt != 0.0:
+        idx = int((t - tl[0]) / dt)
+    else:
+        lo, hi, count = 0, n, 0
+        while lo + 1 != hi and count < 64:
+            mid = (lo + hi) // 2
+            if t < tl[mid]:
+                hi = mid
+            else:
+                lo = mid
+            count += 1
+        idx = lo
+    idx = min(max(idx, 0), n - 1)
+    if order == 0:
+        return p(0, idx)
+    f = t - tl[idx]
+    out = 0j
+    for i in range(order + 1):
+        out = out * f + p(i, idx)
+    return out
 
 
 def pack_programs(coeffs):

@@ -128,7 +128,7 @@ enum : int {
   OP_END = 0, OP_CONST = 1, OP_T = 2, OP_ADD = 3, OP_SUB = 4, OP_MUL = 5, OP_DIV = 6,
   OP_NEG = 7, OP_COS = 8, OP_SIN = 9, OP_EXP = 10, OP_LOG = 11, OP_SQRT = 12, OP_CONJ = 13,
   OP_REAL = 14, OP_IMAG = 15, OP_ABS = 16, OP_POW = 17, OP_COSH = 18, OP_SINH = 19,
-  OP_TANH = 20, OP_TAN = 21, OP_ARCTAN = 22
+  OP_TANH = 20, OP_TAN = 21, OP_ARCTAN = 22, OP_INTERP = 23
 };
 constexpr int COEF_STACK = 16;
 
@@ -175,6 +175,46 @@ __device__ __forceinline__ cplx c_sinh(cplx z) {
   return cplx{sinh(z.re) * cos(z.im), cosh(z.re) * sin(z.im)};
 }
 
+// Piecewise polynomial table in the constant pool (an interpolated coefficient,
+// qutip/core/cy/coefficient.pyx:412-566): consts[k] = (n, order), consts[k+1] =
+// (dt, 0), then n breakpoints (real parts), then poly[order+1][n].  Below the first
+// breakpoint the value is poly[order][0], from the last one poly[order][n-1];
+// inside, the interval is found by dt (uniform breakpoints) or a bisection of at
+// most 64 steps, and the polynomial in (t - t_idx) is evaluated by Horner.
+__device__ __forceinline__ cplx interp_eval(const double* consts, int k, double t) {
+  const int n = (int)consts[2 * k];
+  const int order = (int)consts[2 * k + 1];
+  const double dt = consts[2 * k + 2];
+  const double* tl = consts + 2 * (k + 2);
+  const double* poly = consts + 2 * (k + 2 + n);
+  if (n <= 0 || order < 0) return cplx{0.0, 0.0};
+  const int last = order * n;
+  if (t <= tl[0]) return cplx{poly[2 * last], poly[2 * last + 1]};
+  if (t >= tl[2 * (n - 1)]) return cplx{poly[2 * (last + n - 1)], poly[2 * (last + n - 1) + 1]};
+  long long idx;
+  if (dt != 0.0) {
+    idx = (long long)((t - tl[0]) / dt);
+  } else {
+    long long lo = 0, hi = n;
+    for (int count = 0; lo + 1 != hi && count < 64; ++count) {
+      const long long mid = (lo + hi) / 2;
+      if (t < tl[2 * mid]) hi = mid;
+      else lo = mid;
+    }
+    idx = lo;
+  }
+  if (idx < 0) idx = 0;
+  if (idx > n - 1) idx = n - 1;
+  if (order == 0) return cplx{poly[2 * idx], poly[2 * idx + 1]};
+  const double f = t - tl[2 * idx];
+  double re = 0.0, im = 0.0;
+  for (int i = 0; i <= order; ++i) {
+    re = re * f + poly[2 * (i * n + idx)];
+    im = im * f + poly[2 * (i * n + idx) + 1];
+  }
+  return cplx{re, im};
+}
+
 // Evaluate one program at time t.  Programs are validated on the host (stack
 // depth <= COEF_STACK); the interpreter additionally clamps the stack index so a
 // malformed program cannot write outside its frame.
@@ -191,6 +231,11 @@ static __device__ __noinline__ cplx eval_coef(const int* code, const double* con
     }
     if (op == OP_T) {
       if (sp < COEF_STACK) st[sp++] = cplx{t, 0.0};
+      continue;
+    }
+    if (op == OP_INTERP) {
+      int k = code[++pc];
+      if (sp < COEF_STACK) st[sp++] = interp_eval(consts, k, t);
       continue;
     }
     if (sp < 1) return cplx{0.0, 0.0};

@@ -59,7 +59,7 @@ from qutip.solver.sesolve import SESolver
 from qutip.solver import parallel as _parallel
 
 from . import _lib
-from .coefficients import Coefficient, coefficient
+from .coefficients import Coefficient, coefficient, interpolation
 from .operator import DeviceOperator, stream_ptr
 from .vern7 import GpuVern7, IntegratorError
 
@@ -409,6 +409,9 @@ def _decode(c) -> Coefficient:
     if isinstance(c, _cyc.MulCoefficient):
         a, b = _members(c)
         return _decode(a) * _decode(b)
+    if isinstance(c, _cyc.InterCoefficient):
+        _, (tl, poly, dt) = c.__reduce__()
+        return interpolation(tl, poly, dt or 0.0)
     if isinstance(c, _cyc.StrFunctionCoefficient):
         base, args = c.__reduce__()[1]
         return coefficient(base, args)

@@ -206,3 +206,22 @@ def test_norm2_and_combine(dev):
     out = torch.zeros(n, dtype=torch.complex128, device="cuda")
     ig._combine(_t(x), list(f), out)
     np.testing.assert_allclose(out.cpu().numpy(), x + f @ ks, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("order,uniform", [(0, True), (1, False), (3, True), (3, False)])
+def test_device_interpolated_coefficient(dev, order, uniform):
+    """Piecewise polynomials (the reference's InterCoefficient form) on the device vs
+    the host evaluation, inside, at and outside the breakpoints."""
+    from qutip_gb300.coefficients import interpolation
+    from qutip_gb300.operator import DeviceOperator
+    rng = np.random.default_rng(order)
+    n = 9
+    tl = np.linspace(0.0, 4.0, n) if uniform else np.sort(rng.uniform(0, 4, n))
+    poly = rng.normal(size=(order + 1, n)) + 1j * rng.normal(size=(order + 1, n))
+    c = interpolation(tl, poly, (tl[1] - tl[0]) if uniform else 0.0) * 2.0 + 0.5j
+    op = DeviceOperator([(sp.identity(1, format="csr"), c)])
+    x = _t(np.ones(1))
+    for t in list(tl) + [-1.0, 0.123, 1.9, 3.999, 7.0]:
+        y = torch.zeros(1, dtype=torch.complex128, device="cuda")
+        op.matvec(t, x, y)
+        assert abs(complex(y.cpu().numpy()[0]) - c(t)) <= 1e-13 * max(1.0, abs(c(t)))

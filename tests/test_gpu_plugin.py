@@ -166,3 +166,18 @@ def test_gpudense_data_layer(qt, plugin):
     np.testing.assert_allclose(g.adjoint().to_array(), m.conj().T)
     np.testing.assert_allclose(g.transpose().to_array(), m.T)
     assert isinstance(D.zeros["gpu"](3, 4), plugin.GpuDense)
+
+
+def test_mesolve_interpolated_drive(qt, plugin):
+    """A pulse given as an array on a time grid (QuTiP's InterCoefficient) drives the
+    device solve; same result as the reference."""
+    H, c_ops, psi0, e_ops = _jc(qt, N=6)
+    a = qt.tensor(qt.destroy(6), qt.qeye(2))
+    tp = np.linspace(0, 10, 41)
+    pulse = 0.3 * np.exp(-((tp - 4.0) / 1.5) ** 2)
+    Ht = [H, [a + a.dag(), qt.coefficient(pulse, tlist=tp, order=3)]]
+    rho0 = qt.ket2dm(psi0)
+    tl = np.linspace(0, 10, 101)
+    ref = qt.mesolve(Ht, rho0, tl, c_ops, e_ops=e_ops, options={"method": "vern7"})
+    got = qt.mesolve(Ht, rho0, tl, c_ops, e_ops=e_ops, options={"method": "gpu_vern7"})
+    _assert_expect(got.expect, ref.expect)

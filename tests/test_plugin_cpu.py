@@ -87,3 +87,19 @@ def test_registrations(qt, plugin):
         D.expect[D.CSR, plugin.GpuDense] is not None
     opts = plugin.IntegratorGpuVern7.integrator_options
     assert opts["atol"] == 1e-8 and opts["rtol"] == 1e-6 and opts["nsteps"] == 1000
+
+
+@pytest.mark.parametrize("order", [0, 1, 3])
+def test_interpolated_coefficients(qt, plugin, order):
+    tl = np.linspace(0.0, 6.0, 25)
+    vals = np.exp(-((tl - 3.0) ** 2)) * np.exp(0.4j * tl)
+    c = qt.coefficient(vals, tlist=tl, order=order)
+    prog = plugin.device_coefficient(c)
+    ts = np.concatenate([np.linspace(-1.0, 7.0, 57), tl])
+    np.testing.assert_allclose([prog(t) for t in ts], [complex(c(t)) for t in ts],
+                               rtol=1e-13, atol=1e-14)
+    tn = np.sort(np.random.default_rng(1).uniform(0, 6, 20))
+    c2 = qt.coefficient(np.sin(tn) + 0j, tlist=tn, order=order)
+    prog2 = plugin.device_coefficient(c2)
+    np.testing.assert_allclose([prog2(t) for t in ts], [complex(c2(t)) for t in ts],
+                               rtol=1e-13, atol=1e-14)
