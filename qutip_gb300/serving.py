@@ -20,6 +20,7 @@ tests check bitwise.
 """
 from __future__ import annotations
 
+import gc
 import time
 from collections import deque
 from dataclasses import dataclass, field
@@ -212,7 +213,19 @@ class Server:
                 k += j.spec.ntraj
 
     def serve(self, jobs, realtime=True):
-        """Run the stream; returns (jobs with results and completion times, wall seconds)."""
+        """Run the stream; returns (jobs with results and completion times, wall seconds).
+
+        Python's cyclic garbage collector is paused while serving: with many
+        requests alive a full collection takes long enough to stall admission."""
+        gc_was_enabled = gc.isenabled()
+        gc.disable()
+        try:
+            return self._serve(jobs, realtime)
+        finally:
+            if gc_was_enabled:
+                gc.enable()
+
+    def _serve(self, jobs, realtime):
         lib = _lib.load()
         pending = deque(sorted(jobs, key=lambda j: j.spec.arrival))
         waiting = {b: deque() for b in BUCKETS}
