@@ -74,6 +74,7 @@ def parse():
     ap.add_argument("--profile-sites", type=int, default=10)
     ap.add_argument("--profile-ntraj", type=int, default=256)
     ap.add_argument("--profile-tend", type=float, default=5.0)
+    ap.add_argument("--profile-group", default="auto", choices=["auto", "warp", "cta", "cluster"])
     return ap.parse_args()
 
 
@@ -681,7 +682,7 @@ def run_profile_batch(args):
     s = S.bose_hubbard_trimer(8)
     te = args.profile_tend
     r = mcsolve_batch(s, np.linspace(0.0, te, int(round(10 * te)) + 1), args.profile_ntraj,
-                      seeds=5, precision="mixed")
+                      seeds=5, precision="mixed", group=args.profile_group)
     torch.cuda.synchronize()
     print(f"batch: {len(r.col_times)} trajectories, {sum(len(c) for c in r.col_times)} jumps")
 

@@ -9,10 +9,11 @@ Importing this module (QuTiP must be importable) registers:
   ``register_aliases`` (qutip/core/data/convert.pyx:208-331).
 * Data-layer specialisations for ``GpuDense`` operands
   (qutip/core/data/dispatch.pyx:291-294 fixes their signatures): ``matmul``
-  with a CSR or GpuDense left operand runs the library's SpMV
-  (``qg_spmv_csr`` / ``qg_spmm_csr``; the reference's
-  ``matmul_csr_dense_dense``, qutip/core/data/matmul.pyx:226-272);
-  ``expect`` / ``expect_super`` with a CSR operator run ``qg_expect_dm`` /
+  with a CSR, Dia or GpuDense left operand runs the library's SpMV
+  (``qg_spmv_csr`` / ``qg_spmm_csr`` / ``qg_spmv_dia``; the reference's
+  ``matmul_csr_dense_dense`` and ``matmul_dia_dense_dense``,
+  qutip/core/data/matmul.pyx:226-272,429-507);
+  ``expect`` / ``expect_super`` with a CSR or Dia operator run ``qg_expect_dm`` /
   ``qg_expect_ket`` (``expect_csr_dense`` and friends,
   qutip/core/data/expect.pyx:133-236); ``zeros``, ``add``, ``iadd``, ``sub``,
   ``mul``, ``imul``, ``neg``, ``trace``, ``trace_oper_ket``, ``norm.l2``,
@@ -50,7 +51,7 @@ import torch
 import qutip
 from qutip.core import data as _data
 from qutip.core.cy import coefficient as _cyc
-from qutip.core.data import CSR, Dense, Data
+from qutip.core.data import CSR, Dense, Data, Dia
 from qutip.core.data import ode as _ode
 from qutip.solver.integrator import Integrator, IntegratorException
 from qutip.solver.mcsolve import MCSolver
@@ -60,7 +61,7 @@ from qutip.solver import parallel as _parallel
 
 from . import _lib
 from .coefficients import Coefficient, coefficient, interpolation
-from .operator import DeviceOperator, stream_ptr
+from .operator import DeviceDia, DeviceOperator, stream_ptr
 from .vern7 import GpuVern7, IntegratorError
 
 __all__ = ["GpuDense", "IntegratorGpuVern7", "device_coefficient", "qobjevo_terms",
@@ -188,7 +189,28 @@ _SUPER_EOPS = _OpCache()
 def _scipy(matrix) -> sp.csr_matrix:
     if isinstance(matrix, CSR):
         return matrix.as_scipy()
+    if isinstance(matrix, Dia):
+        return sp.csr_matrix(matrix.as_scipy())
     return sp.csr_matrix(matrix.to_array())
+
+
+_DIAS = _OpCache()
+
+
+def matmul_dia_gpu(left, right, scale=1, out=None):
+    """Dia operator times a GpuDense matrix with the library's diagonal kernel
+    (``qg_spmv_dia``; the reference's ``matmul_dia_dense_dense``,
+    qutip/core/data/matmul.pyx:429-507), column by column."""
+    if left.shape[1] != right.shape[0]:
+        raise ValueError(f"incompatible matrix shapes {left.shape} and {right.shape}")
+    op = _DIAS.get(left, lambda m: DeviceDia(m.as_scipy(), dtype="c128", device=_device()))
+    rows, cols = left.shape[0], right.shape[1]
+    y = torch.empty(rows * cols, dtype=_CDT, device=right.buf.device) if out is None else out.buf
+    beta = 0.0 if out is None else 1.0
+    for j in range(cols):
+        op.matvec(right.buf[j * right.shape[0]:(j + 1) * right.shape[0]],
+                  y[j * rows:(j + 1) * rows], alpha=scale, beta=beta)
+    return out if out is not None else _wrap(y, (rows, cols))
 
 
 def _device_op(matrix) -> DeviceOperator:
@@ -659,6 +681,7 @@ def register():
     _data.zeros.add_specialisations([(GpuDense, zeros_gpu)])
     _data.matmul.add_specialisations([
         (CSR, GpuDense, GpuDense, matmul_csr_gpu),
+        (Dia, GpuDense, GpuDense, matmul_dia_gpu),
         (GpuDense, GpuDense, GpuDense, matmul_gpu),
     ])
     _data.add.add_specialisations([(GpuDense, GpuDense, GpuDense, add_gpu)])
@@ -667,8 +690,11 @@ def register():
     _data.mul.add_specialisations([(GpuDense, GpuDense, mul_gpu)])
     _data.imul.add_specialisations([(GpuDense, GpuDense, imul_gpu)])
     _data.neg.add_specialisations([(GpuDense, GpuDense, neg_gpu)])
-    _data.expect.add_specialisations([(CSR, GpuDense, expect_csr_gpu)])
-    _data.expect_super.add_specialisations([(CSR, GpuDense, expect_super_csr_gpu)])
+    # Dia operators go through the same expect kernels (converted once, cached)
+    _data.expect.add_specialisations([(CSR, GpuDense, expect_csr_gpu),
+                                      (Dia, GpuDense, expect_csr_gpu)])
+    _data.expect_super.add_specialisations([(CSR, GpuDense, expect_super_csr_gpu),
+                                            (Dia, GpuDense, expect_super_csr_gpu)])
     _data.trace.add_specialisations([(GpuDense, trace_gpu)])
     _data.trace_oper_ket.add_specialisations([(GpuDense, trace_oper_ket_gpu)])
     _data.norm.l2.add_specialisations([(GpuDense, l2_gpu)])

@@ -181,3 +181,24 @@ def test_mesolve_interpolated_drive(qt, plugin):
     ref = qt.mesolve(Ht, rho0, tl, c_ops, e_ops=e_ops, options={"method": "vern7"})
     got = qt.mesolve(Ht, rho0, tl, c_ops, e_ops=e_ops, options={"method": "gpu_vern7"})
     _assert_expect(got.expect, ref.expect)
+
+
+def test_dia_operators_on_gpudense(qt, plugin):
+    """Dia operators (the reference's diagonal format) multiply and take expectation
+    values of GpuDense states on the device."""
+    from qutip.core import data as D
+    a = qt.destroy(12).to("dia")
+    H = (a.dag() * a + 0.3 * (a + a.dag())).to("dia")
+    assert isinstance(H.data, D.Dia)
+    rng = np.random.default_rng(2)
+    psi = rng.normal(size=(12, 1)) + 1j * rng.normal(size=(12, 1))
+    g = plugin.GpuDense(psi)
+    got = D.matmul(H.data, g, 0.5 - 1j)
+    np.testing.assert_allclose(got.to_array(), (0.5 - 1j) * (H.full() @ psi), atol=1e-12)
+    np.testing.assert_allclose(D.expect(H.data, g), (psi.conj().T @ H.full() @ psi)[0, 0],
+                               rtol=1e-12)
+    res = qt.sesolve(H, qt.basis(12, 0), np.linspace(0, 3, 31), e_ops=[a.dag() * a],
+                     options={"method": "gpu_vern7"})
+    ref = qt.sesolve(H, qt.basis(12, 0), np.linspace(0, 3, 31), e_ops=[a.dag() * a],
+                     options={"method": "vern7"})
+    _assert_expect(res.expect, ref.expect)
