@@ -74,7 +74,8 @@ def parse():
     ap.add_argument("--profile-sites", type=int, default=10)
     ap.add_argument("--profile-ntraj", type=int, default=256)
     ap.add_argument("--profile-tend", type=float, default=5.0)
-    ap.add_argument("--profile-group", default="auto", choices=["auto", "warp", "cta", "cluster"])
+    ap.add_argument("--profile-group", default="auto",
+                    choices=["auto", "warp", "cta", "cta128", "cluster"])
     return ap.parse_args()
 
 
@@ -420,7 +421,7 @@ def run_mc_batch(args):
         tune_seeds = np.random.SeedSequence(7).spawn(2432)
         best = tune_batch(lambda k: make(k, dt, tl[:51], tune_seeds), sample_items=2432, reps=1)
         qdt = _lib.QG_C64 if dt == "c64" else _lib.QG_C128
-        full = lib.qg_batch_group_slots(512, qdt, {"warp": 1, "cta": 2, "cluster": 3}[best["group"]])
+        full = lib.qg_batch_group_slots(512, qdt, {"warp": 1, "cta": 2, "cluster": 3, "cta128": 4}[best["group"]])
         seeds0 = np.random.SeedSequence(20261203).spawn(n)
         bp = make(n, dt, tl, seeds0)
         bp.build(max_jumps=512, group=best["group"], n_slots=max(1, int(full * best["slot_fraction"])))

@@ -299,6 +299,7 @@ typedef struct qg_batch {
 #define QG_GROUP_WARP 1
 #define QG_GROUP_CTA 2
 #define QG_GROUP_CLUSTER 3
+#define QG_GROUP_CTA128 4 /* one 128-thread CTA per item (half the replicated control) */
 
 /* Workspace bytes of one slot. */
 int64_t qg_batch_slot_bytes(int64_t max_n, int dtype);

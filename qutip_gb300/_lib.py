@@ -19,7 +19,7 @@ QG_MAX_GROUPS, QG_MAX_EOPS = 8, 32
 
 QG_LAYOUT_GROUP_MAJOR, QG_LAYOUT_ROW_MAJOR, QG_LAYOUT_SLICED = 0, 1, 2
 QG_TILE_ROWS = 512
-QG_GROUP_AUTO, QG_GROUP_WARP, QG_GROUP_CTA, QG_GROUP_CLUSTER = 0, 1, 2, 3
+QG_GROUP_AUTO, QG_GROUP_WARP, QG_GROUP_CTA, QG_GROUP_CLUSTER, QG_GROUP_CTA128 = 0, 1, 2, 3, 4
 
 
 class CsrGroups(C.Structure):

@@ -215,8 +215,8 @@ class BatchProblem:
               stage_operator="auto"):
         """Upload pools; ``order`` permutes the items (longest first balances the queue).
 
-        ``group`` is ``"auto"``, ``"warp"``, ``"cta"`` or ``"cluster"`` (threads per
-        item: 32, 256, or 8 x 256 on a thread-block cluster);
+        ``group`` is ``"auto"``, ``"warp"``, ``"cta"``, ``"cta128"`` or ``"cluster"``
+        (threads per item: 32, 256, 128, or 8 x 256 on a thread-block cluster);
         ``n_slots`` caps the resident groups (default: all that fit);
         ``stage_operator``: copy the generator of a single-system launch into shared
         memory once per CTA (``"auto"``: when it takes at most 64 KB)."""
@@ -364,7 +364,7 @@ class BatchProblem:
 
 
 GROUPS = {"auto": _lib.QG_GROUP_AUTO, "warp": _lib.QG_GROUP_WARP, "cta": _lib.QG_GROUP_CTA,
-          "cluster": _lib.QG_GROUP_CLUSTER}
+          "cluster": _lib.QG_GROUP_CLUSTER, "cta128": _lib.QG_GROUP_CTA128}
 
 _TUNED: dict = {}
 
@@ -385,8 +385,8 @@ def tune_batch(make_problem, sample_items=256, candidates=None, reps=2):
     key = (probe.dtype, int(np.ceil(np.log2(max(max_n, 2)))), kind)
     if key in _TUNED:
         return _TUNED[key]
-    candidates = candidates or ([(g, f) for g in ("warp", "cta") for f in (1.0, 0.75, 0.5)]
-                                + [("cluster", 1.0)])
+    candidates = candidates or ([(g, f) for g in ("warp", "cta", "cta128")
+                                 for f in (1.0, 0.75, 0.5)] + [("cluster", 1.0)])
     lib = _lib.load()
     qdt = _lib.QG_C64 if probe.dtype == "c64" else _lib.QG_C128
     best = None

@@ -259,16 +259,27 @@ __device__ __forceinline__ void st2<float2>(float2* p, double re, double im) {
   *p = make_float2((float)re, (float)im);
 }
 
+// Scalar FP64 work of the replicated control is spread over the lanes of each warp
+// and shared with shuffles: lane i computes value i, every lane reads the same bits.
+// (GB300 runs FP64 at 1/64 of the FP32 rate, so 256 threads each evaluating every
+// coefficient program or dense-output polynomial kept the FP64 pipe busy.)
+__device__ __forceinline__ int lane_id() { return (int)(threadIdx.x & 31); }
+__device__ __forceinline__ double shfl_d(double v, int src) {
+  return __shfl_sync(0xffffffffu, v, src);
+}
+
+// coefficients of the system's groups at time t: lane g evaluates group g
 template <int DT>
 __device__ __forceinline__ void load_coef(Ctx<DT>& X, double t) {
+  cplx mine{1.0, 0.0};
+  if (X.S->coef_off >= 0 && lane_id() < X.G) {
+    const int st = __ldg(X.B->coef_start + X.S->coef_off + lane_id());
+    mine = eval_coef(X.B->coef_code + st, X.B->coef_consts, t);
+  }
   for (int g = 0; g < X.G; ++g) {
-    cplx c{1.0, 0.0};
-    if (X.S->coef_off >= 0) {
-      const int st = __ldg(X.B->coef_start + X.S->coef_off + g);
-      c = eval_coef(X.B->coef_code + st, X.B->coef_consts, t);
-    }
-    X.coef[g] = make_double2(c.re, c.im);
-    X.coef_f[g] = make_float2((float)c.re, (float)c.im);
+    const double re = shfl_d(mine.re, g), im = shfl_d(mine.im, g);
+    X.coef[g] = make_double2(re, im);
+    X.coef_f[g] = make_float2((float)re, (float)im);
   }
 }
 
@@ -678,17 +689,25 @@ __device__ __noinline__ void prep_dense_out(const GT& g, Ctx<DT>& X, Ctl& c) {
   c.interp_ready = 1;
 }
 
-// dense-output factors at t (Horner in tau, explicit_rk.pyx:412-430)
+// dense-output factors at t (Horner in tau, explicit_rk.pyx:412-430); lane i
+// evaluates factor i
 __device__ __forceinline__ void set_interp(Ctl& c, double t) {
   const double tau = (t - c.t_prev) / c.dt_int;
-  for (int i = 0; i < RK_EXTRA_STEP; ++i) {
+  double mine = 0.0;
+  float mh = 0.f, ml = 0.f;
+  if (lane_id() < RK_EXTRA_STEP) {
     double acc = 0.0;
     for (int j = DENSE_ORDER - 1; j >= 0; --j) {
-      acc += VERN7_BI[i][j];
+      acc += VERN7_BI[lane_id()][j];
       acc *= tau;
     }
-    c.bf[i] = c.dt_int * acc;
-    split_f(c.bf[i], c.bfh[i], c.bfl[i]);
+    mine = c.dt_int * acc;
+    split_f(mine, mh, ml);
+  }
+  for (int i = 0; i < RK_EXTRA_STEP; ++i) {
+    c.bf[i] = shfl_d(mine, i);
+    c.bfh[i] = __shfl_sync(0xffffffffu, mh, i);
+    c.bfl[i] = __shfl_sync(0xffffffffu, ml, i);
   }
   c.out_front = 0;
   c.t = t;
@@ -708,8 +727,12 @@ __device__ int step_in_err(const GT& g, Ctx<DT>& X, Ctl& c, int nsteps_left) {
     }
     c.t_front = c.t_prev + dt;
     c.dt_int = dt;
+    // _recompute_safe_step (explicit_rk.pyx:451-467); the mixed form takes the
+    // factor in FP32 (it only sets the next trial step, clamped to [0.2, 10])
     double factor;
     if (err == 0.0) factor = 10.0;
+    else if constexpr (DT == QG_C64)
+      factor = (double)fmaxf(0.2f, fminf(10.0f, 0.9f * powf((float)err, -1.0f / (RK_ORDER + 1))));
     else factor = fmax(0.2, fmin(10.0, 0.9 * pow(err, -1.0 / (RK_ORDER + 1))));
     c.dt_safe = fmax(1e-15, dt * factor);
     c.interp_ready = 0;
@@ -1093,14 +1116,14 @@ __global__ void __launch_bounds__(WARP_BLOCK, 4) batch_warp_kernel(qg_batch B) {
   if (pending && threadIdx.x == 0) (void)mbar_poll(&op_bar, 0);  // drain before exit
 }
 
-// One CTA per item; slot = block index.
-template <int DT>
-__global__ void __launch_bounds__(CTA_BLOCK) batch_cta_kernel(qg_batch B) {
-  __shared__ double red[CTA_BLOCK / 32];
+// One CTA of BB threads per item; slot = block index.
+template <int DT, int BB>
+__global__ void __launch_bounds__(BB, 65536 / (BB * 128)) batch_cta_kernel(qg_batch B) {
+  __shared__ double red[BB / 32];
   __shared__ int ibuf;
   extern __shared__ __align__(256) unsigned char stage_smem[];
   __shared__ __align__(8) uint64_t op_bar;
-  CtaGroup<CTA_BLOCK> g{(int)threadIdx.x, (int64_t)blockIdx.x, red, &ibuf};
+  CtaGroup<BB> g{(int)threadIdx.x, (int64_t)blockIdx.x, red, &ibuf};
   Ctx<DT> X;
   bind_slot(X, B, blockIdx.x);
   const int64_t in_bytes = stage_smem_bytes(B.max_n, DT, 1);
@@ -1127,7 +1150,7 @@ __global__ void __launch_bounds__(CTA_BLOCK) batch_cta_kernel(qg_batch B) {
 
 // One cluster of CLUSTER_CTAS CTAs per item; slot = cluster index.
 template <int DT>
-__global__ void __launch_bounds__(CTA_BLOCK) batch_cluster_kernel(qg_batch B) {
+__global__ void __launch_bounds__(CTA_BLOCK, 2) batch_cluster_kernel(qg_batch B) {
   __shared__ double red[CTA_BLOCK / 32];
   __shared__ int ibuf;
   cgrp::cluster_group cl = cgrp::this_cluster();
@@ -1164,7 +1187,24 @@ static bool allow_smem(K kernel, int64_t bytes) {
 
 static bool valid_group(int group) {
   return group == QG_GROUP_AUTO || group == QG_GROUP_WARP || group == QG_GROUP_CTA ||
-         group == QG_GROUP_CLUSTER;
+         group == QG_GROUP_CLUSTER || group == QG_GROUP_CTA128;
+}
+
+// Kernel, block size and items per CTA of a warp or CTA group shape.
+using BatchKernel = void (*)(qg_batch);
+struct Shape {
+  BatchKernel kernel;
+  int block, groups_per_cta;
+};
+static Shape shape_of(int64_t max_n, int dtype, int group) {
+  const bool c64 = dtype == QG_C64;
+  if (warp_mode(max_n, group))
+    return {c64 ? batch_warp_kernel<QG_C64> : batch_warp_kernel<QG_C128>, WARP_BLOCK,
+            WARP_BLOCK / 32};
+  if (group == QG_GROUP_CTA128)
+    return {c64 ? batch_cta_kernel<QG_C64, 128> : batch_cta_kernel<QG_C128, 128>, 128, 1};
+  return {c64 ? batch_cta_kernel<QG_C64, CTA_BLOCK> : batch_cta_kernel<QG_C128, CTA_BLOCK>,
+          CTA_BLOCK, 1};
 }
 
 static cudaLaunchConfig_t cluster_config(int n_clusters, cudaStream_t st, cudaLaunchAttribute* attr) {
@@ -1265,8 +1305,8 @@ extern "C" int64_t qg_batch_slot_bytes(int64_t max_n, int dtype) {
 // Dynamic shared memory of a launch: stage inputs plus the staged operator.
 static int64_t launch_smem(const qg_batch& B) {
   if (B.group == QG_GROUP_CLUSTER) return 0;
-  const bool warp = warp_mode(B.max_n, B.group);
-  return stage_smem_bytes(B.max_n, B.dtype, warp ? WARP_BLOCK / 32 : 1) + op_smem_bytes(B);
+  const Shape sh = shape_of(B.max_n, B.dtype, B.group);
+  return stage_smem_bytes(B.max_n, B.dtype, sh.groups_per_cta) + op_smem_bytes(B);
 }
 
 constexpr int64_t MAX_DYN_SMEM = 227 * 1024;
@@ -1274,7 +1314,7 @@ constexpr int64_t MAX_DYN_SMEM = 227 * 1024;
 static int group_slots(int64_t max_n, int dtype, int group, int64_t smem) {
   if (!valid_group(group))
     return set_error(QG_ERR_ARG,
-                     "group must be QG_GROUP_AUTO, QG_GROUP_WARP, QG_GROUP_CTA or QG_GROUP_CLUSTER");
+                     "group must be one of QG_GROUP_AUTO/WARP/CTA/CLUSTER/CTA128");
   int per_sm = 0;
   cudaError_t e;
   if (group == QG_GROUP_CLUSTER) {
@@ -1289,33 +1329,20 @@ static int group_slots(int64_t max_n, int dtype, int group, int64_t smem) {
     return clusters;
   }
   if (smem > MAX_DYN_SMEM) return set_error(QG_ERR_ARG, "staged data exceed shared memory");
-  const bool warp = warp_mode(max_n, group);
-  bool ok;
-  if (dtype == QG_C64) {
-    ok = warp ? allow_smem(batch_warp_kernel<QG_C64>, smem)
-              : allow_smem(batch_cta_kernel<QG_C64>, smem);
-    e = warp ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_warp_kernel<QG_C64>,
-                                                             WARP_BLOCK, smem)
-             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_cta_kernel<QG_C64>,
-                                                             CTA_BLOCK, smem);
-  } else {
-    ok = warp ? allow_smem(batch_warp_kernel<QG_C128>, smem)
-              : allow_smem(batch_cta_kernel<QG_C128>, smem);
-    e = warp ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_warp_kernel<QG_C128>,
-                                                             WARP_BLOCK, smem)
-             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_cta_kernel<QG_C128>,
-                                                             CTA_BLOCK, smem);
-  }
-  if (!ok) return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
+  const Shape sh = shape_of(max_n, dtype, group);
+  if (!allow_smem(sh.kernel, smem)) return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh.kernel, sh.block, smem);
   if (e != cudaSuccess || per_sm <= 0) return set_error(QG_ERR_CUDA, "occupancy query failed");
   // slots are warps in warp mode, CTAs otherwise
-  return sm_count() * per_sm * (warp ? WARP_BLOCK / 32 : 1);
+  return sm_count() * per_sm * sh.groups_per_cta;
 }
 
 extern "C" int qg_batch_group_slots(int64_t max_n, int dtype, int group) {
-  const bool warp = group != QG_GROUP_CLUSTER && warp_mode(max_n, group);
+  if (!valid_group(group)) return group_slots(max_n, dtype, group, 0);  // reports the error
   const int64_t smem =
-      group == QG_GROUP_CLUSTER ? 0 : stage_smem_bytes(max_n, dtype, warp ? WARP_BLOCK / 32 : 1);
+      group == QG_GROUP_CLUSTER
+          ? 0
+          : stage_smem_bytes(max_n, dtype, shape_of(max_n, dtype, group).groups_per_cta);
   return group_slots(max_n, dtype, group, smem);
 }
 
@@ -1345,7 +1372,7 @@ extern "C" int qg_batch_vern7(const qg_batch* B, void* stream) {
     return set_error(QG_ERR_ARG, "jump record buffers missing");
   if (!valid_group(B->group))
     return set_error(QG_ERR_ARG,
-                     "group must be QG_GROUP_AUTO, QG_GROUP_WARP, QG_GROUP_CTA or QG_GROUP_CLUSTER");
+                     "group must be one of QG_GROUP_AUTO/WARP/CTA/CLUSTER/CTA128");
   if (B->stage_op_entries > 0 &&
       (B->group == QG_GROUP_CLUSTER || B->n_systems != 1 || B->stage_op_rp <= 0))
     return set_error(QG_ERR_ARG,
@@ -1363,30 +1390,10 @@ extern "C" int qg_batch_vern7(const qg_batch* B, void* stream) {
     if (e != cudaSuccess) return set_error(QG_ERR_CUDA, "cluster launch failed");
     return check_launch("batch_cluster_kernel");
   }
-  if (warp_mode(B->max_n, B->group)) {
-    const int per = WARP_BLOCK / 32;
-    const int grid = (B->n_slots + per - 1) / per;
-    const int64_t smem = launch_smem(*B);
-    if (B->dtype == QG_C64) {
-      if (!allow_smem(batch_warp_kernel<QG_C64>, smem))
-        return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
-      batch_warp_kernel<QG_C64><<<grid, WARP_BLOCK, smem, st>>>(*B);
-    } else {
-      if (!allow_smem(batch_warp_kernel<QG_C128>, smem))
-        return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
-      batch_warp_kernel<QG_C128><<<grid, WARP_BLOCK, smem, st>>>(*B);
-    }
-    return check_launch("batch_warp_kernel");
-  }
+  const Shape sh = shape_of(B->max_n, B->dtype, B->group);
   const int64_t smem = launch_smem(*B);
-  if (B->dtype == QG_C64) {
-    if (!allow_smem(batch_cta_kernel<QG_C64>, smem))
-      return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
-    batch_cta_kernel<QG_C64><<<B->n_slots, CTA_BLOCK, smem, st>>>(*B);
-  } else {
-    if (!allow_smem(batch_cta_kernel<QG_C128>, smem))
-      return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
-    batch_cta_kernel<QG_C128><<<B->n_slots, CTA_BLOCK, smem, st>>>(*B);
-  }
-  return check_launch("batch_cta_kernel");
+  if (!allow_smem(sh.kernel, smem)) return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
+  const int grid = (B->n_slots + sh.groups_per_cta - 1) / sh.groups_per_cta;
+  sh.kernel<<<grid, sh.block, smem, st>>>(*B);
+  return check_launch("batch_vern7 (warp or CTA groups)");
 }

@@ -140,8 +140,8 @@ class Server:
         self.max_jobs = int(max_jobs_per_launch)
         self.max_jumps = int(max_jumps)
         self.launch_timeout = float(launch_timeout)
-        if group not in ("load", "auto", "warp", "cta", "cluster"):
-            raise ValueError("group must be 'load', 'auto', 'warp', 'cta' or 'cluster'")
+        if group not in ("load", "auto", "warp", "cta", "cta128", "cluster"):
+            raise ValueError("group must be 'load', 'auto', 'warp', 'cta', 'cta128' or 'cluster'")
         self.group = group
         self._cluster_cache = {}
         # items per launch up to which each item gets a CTA: two per SM
@@ -179,7 +179,7 @@ class Server:
             if max_n >= 1600 and n_items <= self._cluster_slots(max_n):
                 group = "cluster"     # few large items: 8 SMs each
             elif n_items <= self.cta_items:
-                group = "cta"
+                group = "cta128" if max_n <= 512 else "cta"   # small states: 128 threads
             else:
                 group = "auto"
         with torch.cuda.stream(stream):
@@ -313,5 +313,5 @@ def solve_plain(job: Job, precision="double"):
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     r = mcsolve_batch(job.system, job.tlist, job.spec.ntraj, seeds=seeds,
                       precision="double" if precision == "double" else "mixed",
-                      group="cta" if job.spec.ntraj <= 2 * sms else "auto")
+                      group="cta128" if job.spec.ntraj <= 2 * sms else "auto")
     return r.expect

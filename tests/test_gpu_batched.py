@@ -105,7 +105,7 @@ def test_mc_mixed_precision_jump_records(name):
     assert np.all(diff <= 5 * sem + 1e-3)
 
 
-@pytest.mark.parametrize("group", ["cta", "cluster"])
+@pytest.mark.parametrize("group", ["cta", "cta128", "cluster"])
 @pytest.mark.parametrize("name", sorted(MC_CASES))
 def test_mc_other_groups_match_reference(name, group):
     """The same trajectories with one 256-thread CTA, or one 8-CTA thread-block
@@ -115,7 +115,7 @@ def test_mc_other_groups_match_reference(name, group):
     assert same == ntraj
 
 
-@pytest.mark.parametrize("group", ["cta", "cluster"])
+@pytest.mark.parametrize("group", ["cta", "cta128", "cluster"])
 def test_batched_me_groups_match_reference(group):
     """Master equations (Jaynes-Cummings N=10, Ising L=4) with CTA and cluster groups."""
     from qutip_gb300 import systems as S
