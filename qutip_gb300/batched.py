@@ -67,8 +67,9 @@ MC_DEFAULTS = dict(norm_steps=25, norm_t_tol=1e-6, norm_tol=1e-4, norm_min_step=
 
 
 def pcg_state_of(seed) -> tuple[int, int]:
-    """numpy PCG64 (state, increment) of ``default_rng(seed)``."""
-    st = np.random.default_rng(seed).bit_generator.state["state"]
+    """numpy PCG64 (state, increment) of ``default_rng(seed)`` (which wraps
+    ``PCG64(seed)``; the bit generator alone is cheaper to build)."""
+    st = np.random.PCG64(seed).state["state"]
     return int(st["state"]), int(st["inc"])
 
 
@@ -205,11 +206,43 @@ class BatchProblem:
         return len(self.items) - 1
 
     # -- device upload and launch --------------------------------------------
-    def _t(self, arrs, dtype, np_dtype, pad=8):
+    @staticmethod
+    def _host(arrs, np_dtype, pad=8):
+        """Concatenated pool in its device dtype, with ``pad`` zero entries (bulk copies
+        of the pool may read up to 16 bytes past the last entry)."""
         a = np.concatenate(arrs).astype(np_dtype) if arrs and sum(len(x) for x in arrs) else \
             np.zeros(0, np_dtype)
-        a = np.concatenate([a, np.zeros(pad, np_dtype)])
-        return torch.from_numpy(a).to(self.device, dtype)
+        return np.concatenate([a, np.zeros(pad, np_dtype)])
+
+    ALIGN = 256
+
+    def _pack_upload(self, pools):
+        """Copy ``[(name, host array, torch dtype)]`` to the device in one transfer and
+        bind ``self.<name>`` to 256-byte aligned views of it."""
+        offs, total = [], 0
+        for _, a, _ in pools:
+            offs.append(total)
+            total += -(-a.nbytes // self.ALIGN) * self.ALIGN
+        host = np.zeros(max(total, self.ALIGN), dtype=np.uint8)
+        for (_, a, _), off in zip(pools, offs):
+            host[off:off + a.nbytes] = np.ascontiguousarray(a).view(np.uint8).reshape(-1)
+        dev = torch.from_numpy(host).to(self.device)
+        for (name, a, tdt), off in zip(pools, offs):
+            setattr(self, name, dev[off:off + a.nbytes].view(tdt))
+        return dev
+
+    def _pack_zeros(self, outs):
+        """One zeroed device buffer for ``[(name, count, torch dtype)]``, bound as views."""
+        offs, total = [], 0
+        for _, count, tdt in outs:
+            offs.append(total)
+            nb = count * torch.empty(0, dtype=tdt).element_size()
+            total += -(-nb // self.ALIGN) * self.ALIGN
+        dev = torch.zeros(total, dtype=torch.uint8, device=self.device)
+        for (name, count, tdt), off in zip(outs, offs):
+            nb = count * torch.empty(0, dtype=tdt).element_size()
+            setattr(self, name, dev[off:off + nb].view(tdt))
+        return dev
 
     def build(self, max_jumps=0, mc_options=None, order=None, n_slots=None, group="auto",
               stage_operator="auto"):
@@ -225,35 +258,41 @@ class BatchProblem:
         lib = _lib.load()
         cdt = torch.complex64 if self.dtype == "c64" else torch.complex128
         qdt = _lib.QG_C64 if self.dtype == "c64" else _lib.QG_C128
-        self.op_rp = self._t(self._op_rp, torch.int32, np.int64)
-        self.op_col = self._t(self._op_col, torch.int32, np.int32)
-        self.op_val = self._t(self._op_val, cdt, np.complex128)
-        self.coef_code = self._t(self._coef_code, torch.int32, np.int32)
-        self.coef_start = self._t(self._coef_start, torch.int32, np.int64)
-        self.coef_consts = self._t(self._coef_consts, torch.float64, np.float64)
-        self.eop_rp = self._t(self._eop_rp, torch.int32, np.int64)
-        self.eop_col = self._t(self._eop_col, torch.int32, np.int32)
-        self.eop_val = self._t(self._eop_val, torch.complex128, np.complex128)
-        self.cop_rp = self._t(self._cop_rp, torch.int32, np.int64)
-        self.cop_col = self._t(self._cop_col, torch.int32, np.int32)
-        self.cop_val = self._t(self._cop_val, torch.complex128, np.complex128)
-        self.tlist_d = self._t(self._tlist, torch.float64, np.float64)
-        self.y0_d = self._t(self._y0, torch.complex128, np.complex128)
+        cnp = np.complex64 if self.dtype == "c64" else np.complex128
         sys_np = np.array(self.systems, dtype=SYSTEM_DTYPE)
         items = list(self.items)
         self.order = np.arange(len(items)) if order is None else np.asarray(order)
         items = [items[i] for i in self.order]
         item_np = np.array(items, dtype=ITEM_DTYPE)
-        self.systems_d = torch.from_numpy(sys_np.view(np.uint8).copy()).to(self.device)
-        self.items_d = torch.from_numpy(item_np.view(np.uint8).copy()).to(self.device)
         n_items = len(items)
-        self.out = torch.zeros(max(self._out_len, 1), dtype=torch.complex128, device=self.device)
-        self.status = torch.zeros(4 * n_items, dtype=torch.int32, device=self.device)
         self.max_jumps = int(max_jumps)
-        self.jump_t = torch.zeros(max(n_items * self.max_jumps, 1), dtype=torch.float64,
-                                  device=self.device)
-        self.jump_which = torch.zeros(max(n_items * self.max_jumps, 1), dtype=torch.int32,
-                                      device=self.device)
+        # every input pool in one host buffer and one copy; device views by name
+        pools = [
+            ("op_rp", self._host(self._op_rp, np.int32), torch.int32),
+            ("op_col", self._host(self._op_col, np.int32), torch.int32),
+            ("op_val", self._host(self._op_val, cnp), cdt),
+            ("coef_code", self._host(self._coef_code, np.int32), torch.int32),
+            ("coef_start", self._host(self._coef_start, np.int32), torch.int32),
+            ("coef_consts", self._host(self._coef_consts, np.float64), torch.float64),
+            ("eop_rp", self._host(self._eop_rp, np.int32), torch.int32),
+            ("eop_col", self._host(self._eop_col, np.int32), torch.int32),
+            ("eop_val", self._host(self._eop_val, np.complex128), torch.complex128),
+            ("cop_rp", self._host(self._cop_rp, np.int32), torch.int32),
+            ("cop_col", self._host(self._cop_col, np.int32), torch.int32),
+            ("cop_val", self._host(self._cop_val, np.complex128), torch.complex128),
+            ("tlist_d", self._host(self._tlist, np.float64), torch.float64),
+            ("y0_d", self._host(self._y0, np.complex128), torch.complex128),
+            ("systems_d", sys_np.view(np.uint8).reshape(-1), torch.uint8),
+            ("items_d", item_np.view(np.uint8).reshape(-1), torch.uint8),
+        ]
+        self.inputs = self._pack_upload(pools)
+        # outputs (zeroed): one allocation and one fill
+        outs = [("out", max(self._out_len, 1), torch.complex128),
+                ("status", 4 * n_items, torch.int32),
+                ("jump_t", max(n_items * self.max_jumps, 1), torch.float64),
+                ("jump_which", max(n_items * self.max_jumps, 1), torch.int32),
+                ("queue", 4, torch.int32)]
+        self.outputs = self._pack_zeros(outs)
         self.max_n = max(info["n"] for info in self.sys_info)
         if group not in GROUPS:
             raise ValueError(f"group must be one of {sorted(GROUPS)}")
@@ -266,7 +305,6 @@ class BatchProblem:
             op_bytes = a16(4 * info["rp_len"]) + a16(4 * info["nnz"]) + a16(es * info["nnz"])
             if stage_operator is True or op_bytes <= 64 * 1024:
                 stage_entries, stage_rp = info["nnz"], info["rp_len"]
-        self.queue = torch.zeros(4, dtype=torch.int32, device=self.device)
         mc = {**MC_DEFAULTS, **(mc_options or {})}
         p = lambda t: t.data_ptr()  # noqa: E731
         self.struct = BatchStruct(

@@ -54,6 +54,9 @@ def row_major_layout(mats):
         m.sort_indices()
     n, m_cols = mats[0].shape
     G = len(mats)
+    if G == 1:  # one group: the row-major layout is the CSR itself
+        m = mats[0]
+        return m.indptr.astype(np.int64), m.indices.astype(np.int32), m.data.copy()
     counts = np.stack([np.diff(m.indptr) for m in mats], axis=1).reshape(-1)
     rp = np.zeros(n * G + 1, dtype=np.int64)
     np.cumsum(counts, out=rp[1:])
