@@ -228,3 +228,45 @@ def test_bad_items_are_rejected_without_touching_memory():
     torch.cuda.synchronize()
     st = bp.status.cpu().numpy().reshape(-1, 4)[:, 0]
     assert np.all(st == -8)
+
+
+def test_single_time_point_and_empty_e_ops():
+    """A tlist of one point records only the initial state; a system without e_ops still
+    reports the trace."""
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import BatchProblem, check_status
+    s = S.jaynes_cummings(5, kind="me")
+    bp = BatchProblem("c128")
+    a = bp.add_system(s.terms, s.e_ops, np.array([0.0]), "me")
+    b = bp.add_system(s.terms, [], np.linspace(0, 1, 5), "me")
+    bp.add_item(a, s.state0)
+    bp.add_item(b, s.state0)
+    bp.build()
+    bp.launch()
+    res = bp.results()
+    check_status(res)
+    assert res[0]["expect"].shape == (1, 2)
+    np.testing.assert_allclose(res[0]["expect"][0].real, [0.0, 1.0], atol=1e-14)
+    assert res[1]["expect"].shape == (5, 0)
+    np.testing.assert_allclose(res[1]["norm"].real, 1.0, atol=1e-7)
+
+
+def test_jump_overflow_is_reported():
+    """More jumps than max_jumps stops the trajectory with QG_JUMP_OVERFLOW; the host
+    raises with the reference-style message and keeps the recorded jumps."""
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import BatchProblem, check_status
+    s = S.bose_hubbard_trimer(4, F=1.0, kappa=0.5, kind="mc")
+    bp = BatchProblem("c128")
+    sid = bp.add_system(s.terms, s.e_ops, np.linspace(0, 20, 41), "mc", c_ops=s.c_ops)
+    for sd in np.random.SeedSequence(3).spawn(8):
+        bp.add_item(sid, s.state0, seed=sd)
+    bp.build(max_jumps=1)
+    bp.launch()
+    res = bp.results()
+    assert any(r["status"] == -7 for r in res)
+    for r in res:
+        if r["status"] == -7:
+            assert len(r["col_times"]) == 1
+    with pytest.raises(RuntimeError, match="max_jumps"):
+        check_status(res)

@@ -225,3 +225,40 @@ def test_device_interpolated_coefficient(dev, order, uniform):
         y = torch.zeros(1, dtype=torch.complex128, device="cuda")
         op.matvec(t, x, y)
         assert abs(complex(y.cpu().numpy()[0]) - c(t)) <= 1e-13 * max(1.0, abs(c(t)))
+
+
+@pytest.mark.parametrize("fmt", ["csr", "sliced"])
+@pytest.mark.parametrize("dtype", ["c128", "c64"])
+def test_spmv_ragged_rows_and_empty_group(dev, fmt, dtype):
+    """Rows without entries, a coefficient group that is all zero, and a row count
+    that is not a multiple of the 32-row slice."""
+    from qutip_gb300.coefficients import coefficient
+    from qutip_gb300.operator import DeviceOperator
+    rng = np.random.default_rng(5)
+    n = 1061
+    a = sp.random(n, n, density=0.01, random_state=1, format="lil", dtype=np.complex128)
+    a[::7, :] = 0                                   # every 7th row empty
+    a = sp.csr_matrix(a) + 1j * sp.random(n, n, density=0.002, random_state=2, format="csr")
+    a = sp.csr_matrix(a)
+    a[::7, :] = 0
+    a = sp.csr_matrix(a)
+    a.eliminate_zeros()
+    empty = sp.csr_matrix((n, n), dtype=np.complex128)
+    c = coefficient("cos(t)")
+    op = DeviceOperator([(a, None), (empty, c)], dtype=dtype, merge=False, fmt=fmt)
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    tdt = torch.complex128 if dtype == "c128" else torch.complex64
+    y = torch.full((n,), 7.0 + 7.0j, dtype=tdt, device="cuda")
+    op.matvec(0.4, _t(x, tdt), y)
+    want = a @ x
+    tol = 1e-12 if dtype == "c128" else 3e-6
+    np.testing.assert_allclose(y.cpu().numpy(), want, rtol=tol, atol=tol * np.abs(want).max())
+    assert np.all(y.cpu().numpy()[::7] == 0)
+
+
+def test_spmv_one_by_one(dev):
+    from qutip_gb300.operator import DeviceOperator
+    op = DeviceOperator([(sp.csr_matrix(np.array([[2.0 - 1.0j]])), None)])
+    y = torch.zeros(1, dtype=torch.complex128, device="cuda")
+    op.matvec(0.0, _t(np.array([3.0 + 0.5j])), y, alpha=2.0, beta=0.0)
+    assert complex(y.item()) == pytest.approx(2 * (2.0 - 1.0j) * (3.0 + 0.5j), abs=1e-14)
