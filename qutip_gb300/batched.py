@@ -391,7 +391,9 @@ class BatchProblem:
             raw = out[it[3]:it[3] + no * (ne + 1)].reshape(no, ne + 1)
             vals = raw[:, :ne]
             if normalize:
-                vals = vals / raw[:, ne:ne + 1]
+                # outputs a failed item never reached are zero: they become NaN here
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    vals = vals / raw[:, ne:ne + 1]
             st = status[k]
             nj = int(st[3])
             res.append(dict(expect=vals, norm=raw[:, ne], status=int(st[0]), steps=int(st[1]),

@@ -236,12 +236,11 @@ def test_spmv_ragged_rows_and_empty_group(dev, fmt, dtype):
     from qutip_gb300.operator import DeviceOperator
     rng = np.random.default_rng(5)
     n = 1061
-    a = sp.random(n, n, density=0.01, random_state=1, format="lil", dtype=np.complex128)
-    a[::7, :] = 0                                   # every 7th row empty
-    a = sp.csr_matrix(a) + 1j * sp.random(n, n, density=0.002, random_state=2, format="csr")
-    a = sp.csr_matrix(a)
-    a[::7, :] = 0
-    a = sp.csr_matrix(a)
+    a = (sp.random(n, n, density=0.01, random_state=1, format="csr", dtype=np.complex128)
+         + 1j * sp.random(n, n, density=0.002, random_state=2, format="csr"))
+    keep = np.ones(n)
+    keep[::7] = 0                                   # every 7th row empty
+    a = sp.csr_matrix(sp.diags(keep) @ a)
     a.eliminate_zeros()
     empty = sp.csr_matrix((n, n), dtype=np.complex128)
     c = coefficient("cos(t)")
