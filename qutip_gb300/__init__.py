@@ -12,7 +12,8 @@ from .coefficients import Coefficient, coefficient  # noqa: F401
 def __getattr__(name):
     # Device-side modules import torch and load the CUDA library lazily.
     import importlib
-    if name in ("operator", "vern7", "solver", "batched", "mc", "serving", "qutip_plugin", "_lib"):
+    if name in ("operator", "vern7", "solver", "batched", "serving", "superop", "qutip_plugin",
+                "_lib"):
         return importlib.import_module(f"{__name__}.{name}")
     if name in ("mesolve", "solve_system"):
         return getattr(importlib.import_module(f"{__name__}.solver"), name)
