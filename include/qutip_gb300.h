@@ -243,6 +243,11 @@ typedef struct qg_batch_item {
   int64_t y0_off;   /* initial state (complex128) in y0 */
   int64_t out_off;  /* n_out * (n_eops+1) complex128 results in out */
   uint64_t rng_state_hi, rng_state_lo, rng_inc_hi, rng_inc_lo;
+  /* improved sampling (qutip/solver/mcsolve.py:245-279): the first jump target is
+   * random() * (1 - jump_prob_floor) + jump_prob_floor, so a trajectory with a floor
+   * equal to the no-jump probability always jumps; 0 for ordinary trajectories.
+   * Later targets (after each jump) are drawn without the floor (mcsolve.py:405). */
+  double jump_prob_floor;
 } qg_batch_item;
 
 typedef struct qg_batch {

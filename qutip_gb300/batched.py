@@ -41,7 +41,8 @@ SYSTEM_DTYPE = np.dtype([("n", "<i4"), ("d", "<i4"), ("n_groups", "<i4"), ("n_eo
                          ("kind", "<i4"), ("n_cops", "<i4"), ("nsteps", "<i4"),
                          ("atol", "<f8"), ("rtol", "<f8")], align=True)
 ITEM_DTYPE = np.dtype([("system", "<i4"), ("pad", "<i4"), ("y0_off", "<i8"), ("out_off", "<i8"),
-                       ("sh", "<u8"), ("sl", "<u8"), ("ih", "<u8"), ("il", "<u8")], align=True)
+                       ("sh", "<u8"), ("sl", "<u8"), ("ih", "<u8"), ("il", "<u8"),
+                       ("floor", "<f8")], align=True)
 
 
 class BatchStruct(C.Structure):
@@ -187,7 +188,13 @@ class BatchProblem:
                                   nnz=len(col), tlist=tl, rp_len=len(rp)))
         return len(self.systems) - 1
 
-    def add_item(self, system: int, y0, seed=None) -> int:
+    def add_item(self, system: int, y0, seed=None, jump_prob_floor: float = 0.0) -> int:
+        """Queue one solve (a trajectory for ``"mc"`` systems) from ``y0``.
+
+        ``jump_prob_floor`` is improved sampling's lower bound for the first jump
+        target (mcsolve.py:245-279): the no-jump probability of ``y0``."""
+        if not 0.0 <= float(jump_prob_floor) < 1.0:
+            raise ValueError("jump_prob_floor must lie in [0, 1)")
         info = self.sys_info[system]
         y0 = np.asarray(y0, dtype=np.complex128).reshape(-1)
         if y0.shape[0] != info["n"]:
@@ -202,7 +209,7 @@ class BatchProblem:
             state, inc = seed if isinstance(seed, tuple) else pcg_state_of(seed)
             sh, sl = _split128(state)
             ih, il = _split128(inc)
-        self.items.append((system, 0, y0_off, out_off, sh, sl, ih, il))
+        self.items.append((system, 0, y0_off, out_off, sh, sl, ih, il, float(jump_prob_floor)))
         return len(self.items) - 1
 
     # -- device upload and launch --------------------------------------------

@@ -897,7 +897,10 @@ __device__ void run_item(const GT& g, const qg_batch& B, Ctx<DT>& X, int item) {
   c.rhs = 0;
   c.steps = 0;
   Pcg rng{I.rng_state_hi, I.rng_state_lo, I.rng_inc_hi, I.rng_inc_lo};
-  double target = ket ? pcg_random(rng) : 0.0;  // MCIntegrator.set_state draws first
+  // MCIntegrator.set_state draws first, above the improved-sampling floor
+  // (r * (1 - floor) + floor, rounded as the host computes it)
+  const double floor_p = I.jump_prob_floor;
+  double target = ket ? __dadd_rn(__dmul_rn(pcg_random(rng), 1.0 - floor_p), floor_p) : 0.0;
   int njumps = 0;
   set_initial(g, X, c, reinterpret_cast<const double2*>(B.y0) + I.y0_off, tl[0]);
   record(g, X, c, out, ket);

@@ -29,10 +29,10 @@ Importing this module (QuTiP must be importable) registers:
   (qutip/solver/integrator/qutip_integrator.py:51-59) plus ``precision``
   (``"double"`` or ``"mixed"``).
 * ``map="gpu"`` for ``MCSolver`` (``qutip.solver.parallel._maps``,
-  qutip/solver/parallel.py:541-559): all trajectories of a ``run`` go to one
-  persistent ``qg_batch_vern7`` launch, and each comes back to
-  ``MultiTrajResult.add`` as a trajectory result with its expectation values
-  and collapse record.
+  qutip/solver/parallel.py:541-559): all trajectories of a ``run`` -- with one
+  initial state or a mixed initial ensemble -- go to one persistent
+  ``qg_batch_vern7`` launch, and each comes back to ``MultiTrajResult.add`` as a
+  trajectory result with its expectation values, collapse record and weight.
 
 Nothing here computes on the host: a coefficient the device cannot evaluate, a
 time-dependent collapse operator in a batched run, or a missing CUDA library is
@@ -598,17 +598,86 @@ def _constant_matrix(op, what):
     return _scipy(op.data)
 
 
+def _mc_map_items(task, values, task_args, task_kwargs):
+    """Decode the trajectory task an ``MCSolver`` hands to its map.
+
+    Returns ``(solver, seeds, starts, floors, tlist, e_ops)`` where ``starts`` holds
+    ``(initial state, weight)`` per trajectory and ``floors`` the improved-sampling
+    jump-probability floor of each.  The forms follow the reference's call sites:
+
+    * ``_run_one_traj`` over seeds (multitraj.py:169-258), with
+      ``{'no_jump': False, 'jump_prob_floor': p}`` under improved sampling
+      (mcsolve.py:716-747);
+    * ``_run_one_traj_mixed`` over trajectory ids (multitraj.py:298-350);
+    * ``_unpack_arguments(_run_one_traj_mixed, ('id', 'jump_prob_floor'))`` over
+      ``(id, floor)`` pairs, improved sampling with mixed states (mcsolve.py:749-790).
+    """
+    kw = dict(task_kwargs or {})
+    if kw.pop("no_jump", False):
+        raise TypeError("map='gpu' does not run the no-jump trajectory as a map task")
+    func, names = task, None
+    if hasattr(task, "func") and hasattr(task, "argument_names"):
+        func, names = task.func, tuple(task.argument_names)
+    solver = getattr(func, "__self__", None)
+    name = getattr(func, "__name__", "")
+    if not isinstance(solver, MCSolver):
+        raise TypeError("map='gpu' runs MCSolver trajectories only")
+    if name == "_run_one_traj" and names is None:
+        state0, tlist, e_ops = task_args
+        floor = float(kw.pop("jump_prob_floor", 0.0))
+        seeds = list(values)
+        starts = [(state0, 1.0)] * len(seeds)
+        floors = [floor] * len(seeds)
+    elif name == "_run_one_traj_mixed" and names is None:
+        all_seeds, ics, tlist, e_ops = task_args
+        floor = float(kw.pop("jump_prob_floor", 0.0))
+        ids = list(values)
+        seeds = [all_seeds[i] for i in ids]
+        starts = [ics.get_state_and_weight(i) for i in ids]
+        floors = [floor] * len(ids)
+    elif name == "_run_one_traj_mixed" and names == ("id", "jump_prob_floor"):
+        all_seeds, ics, tlist, e_ops = (kw.pop(k) for k in ("seeds", "ics", "tlist", "e_ops"))
+        pairs = [tuple(v) for v in values]
+        seeds = [all_seeds[i] for i, _ in pairs]
+        starts = [ics.get_state_and_weight(i) for i, _ in pairs]
+        floors = [float(f) for _, f in pairs]
+    else:
+        raise TypeError(f"map='gpu' does not run the task {name or task!r}")
+    if kw:
+        raise TypeError(f"map='gpu' does not support the trajectory options {sorted(kw)}")
+    return solver, seeds, starts, floors, tlist, e_ops
+
+
+def _zero_trajectory(solver, e_ops, opts, tlist):
+    """The all-zero trajectory of weight 0 the reference returns when improved
+    sampling asks for a jump from a state that never jumps (mcsolve.py:544-558)."""
+    traj = solver._trajectory_resultclass(e_ops, opts)
+    traj.times = [float(t) for t in tlist]
+    for key in traj.e_data:
+        traj.e_data[key] = [0.0] * len(tlist)
+    traj.collapse = []
+    return traj
+
+
 def gpu_map(task, values, task_args=None, task_kwargs=None, reduce_func=None, map_kw=None,
             progress_bar=None, progress_bar_kwargs={}):
     """``map="gpu"``: run every trajectory of an ``MCSolver.run`` in one persistent
-    launch and hand each to ``reduce_func`` as the reference's trajectory result."""
+    launch and hand each to ``reduce_func`` as the reference's trajectory result.
+
+    The per-initial-state no-jump runs of improved sampling with mixed states
+    (``_no_jump_simulation``, mcsolve.py:756-763) are single deterministic solves: they
+    run one after another through the solver's own ``gpu_vern7`` integrator."""
+    if getattr(task, "__name__", "") == "_no_jump_simulation" and \
+            isinstance(getattr(task, "__self__", None), MCSolver):
+        out = [task(v, *(task_args or ()), **(task_kwargs or {})) for v in values]
+        if reduce_func is not None:
+            for r in out:
+                reduce_func(r)
+            return []
+        return out
     from .batched import BatchProblem, MC_DEFAULTS
-    solver = getattr(task, "__self__", None)
-    if not isinstance(solver, MCSolver) or getattr(task, "__name__", "") != "_run_one_traj":
-        raise TypeError("map='gpu' runs MCSolver trajectories only")
-    if task_kwargs:
-        raise TypeError("map='gpu' does not support improved sampling or mixed initial states")
-    state0, tlist, e_ops = task_args
+    solver, seeds, starts, floors, tlist, e_ops = _mc_map_items(
+        task, values, task_args or (), task_kwargs)
     opts = solver.options
     if opts.get("bitgenerator") not in (None, "PCG64"):
         raise TypeError("map='gpu' draws from PCG64 streams (the default bit generator)")
@@ -631,18 +700,26 @@ def gpu_map(task, values, task_args=None, task_kwargs=None, reduce_func=None, ma
     iopts = {**IntegratorGpuVern7.integrator_options,
              **{k: opts[k] for k in IntegratorGpuVern7.integrator_options if k in opts}}
     prec = iopts["precision"]
-    psi0 = np.asarray(_as_gpu(state0).to_array()).reshape(-1)
     bp = BatchProblem("c128" if prec == "double" else "c64")
     sid = bp.add_system(terms, e_mats, np.asarray(tlist, dtype=np.float64), "mc",
                         c_ops=c_mats, atol=iopts["atol"], rtol=iopts["rtol"],
                         nsteps=iopts["nsteps"])
-    seeds = list(values)
-    for s in seeds:
-        bp.add_item(sid, psi0, seed=s)
-    mc = {k: opts[k] for k in MC_DEFAULTS if k in opts}
-    bp.build(max_jumps=int((map_kw or {}).get("max_jumps", 4096)), mc_options=mc)
-    bp.launch()
-    res = bp.results()
+    # a floor at 1 - norm_tol or above: the state does not jump; the reference returns
+    # a zero trajectory of weight 0 without integrating (mcsolve.py:544-558)
+    dark = [f >= 1 - opts["norm_tol"] for f in floors]
+    host_states = {}
+    for s, (st, _), f, d in zip(seeds, starts, floors, dark):
+        if d:
+            continue
+        if id(st) not in host_states:
+            host_states[id(st)] = np.asarray(_as_gpu(st).to_array()).reshape(-1)
+        bp.add_item(sid, host_states[id(st)], seed=s, jump_prob_floor=f)
+    res = []
+    if bp.items:
+        mc = {k: opts[k] for k in MC_DEFAULTS if k in opts}
+        bp.build(max_jumps=int((map_kw or {}).get("max_jumps", 4096)), mc_options=mc)
+        bp.launch()
+        res = bp.results()
     for r in res:
         if r["status"] == -5:
             raise RuntimeError("Could not find the collapse time within desired tolerance. "
@@ -650,14 +727,22 @@ def gpu_map(task, values, task_args=None, task_kwargs=None, reduce_func=None, ma
                                "with the options 'norm_steps', 'norm_tol', 'norm_t_tol'.")
         if r["status"] < 0:
             raise IntegratorException(f"trajectory failed with status {r['status']}")
-    for seed, r in zip(seeds, res):
-        traj = solver._trajectory_resultclass(e_ops, opts)
-        traj.times = [float(t) for t in tlist]
-        for k, key in enumerate(traj.e_data):
-            traj.e_data[key] = list(r["expect"][:, k])
-        traj.collapse = [(float(t), int(w)) for t, w in zip(r["col_times"], r["col_which"])]
+    res = iter(res)
+    for seed, (_, weight), f, d in zip(seeds, starts, floors, dark):
+        if d:
+            traj, w = _zero_trajectory(solver, e_ops, opts, tlist), 0.0
+        else:
+            r = next(res)
+            traj = solver._trajectory_resultclass(e_ops, opts)
+            traj.times = [float(t) for t in tlist]
+            for k, key in enumerate(traj.e_data):
+                traj.e_data[key] = list(r["expect"][:, k])
+            traj.collapse = [(float(t), int(w)) for t, w in zip(r["col_times"], r["col_which"])]
+            # MCSolver._run_one_traj scales by (1 - floor), _run_one_traj_mixed by the
+            # initial state's weight (mcsolve.py:565, multitraj.py:297)
+            w = weight * (1 - f)
         if reduce_func is not None:
-            left = reduce_func((seed, traj, 1.0))
+            left = reduce_func((seed, traj, float(w)))
             if left is not None and left <= 0:
                 break
     return None

@@ -202,3 +202,54 @@ def test_dia_operators_on_gpudense(qt, plugin):
     ref = qt.sesolve(H, qt.basis(12, 0), np.linspace(0, 3, 31), e_ops=[a.dag() * a],
                      options={"method": "vern7"})
     _assert_expect(res.expect, ref.expect)
+
+
+def test_mcsolve_gpu_map_mixed_initial_states(qt, plugin):
+    """A mixed initial ensemble (MultiTrajSolver._run_mixed): per-trajectory states,
+    seeds and correction weights as in the reference."""
+    H, c_ops, psi0, e_ops = _jc(qt, N=6)
+    psi1 = qt.tensor(qt.basis(6, 1), qt.basis(2, 1))
+    ics = [(psi0, 0.3), (psi1, 0.7)]
+    tl = np.linspace(0, 10, 51)
+    opts = {"method": "vern7", "map": "serial", "keep_runs_results": True}
+    ref = qt.MCSolver(H, c_ops, options=opts).run(ics, tl, [8, 12], e_ops=e_ops, seeds=9)
+    got = qt.MCSolver(H, c_ops, options={**opts, "method": "gpu_vern7", "map": "gpu"}).run(
+        ics, tl, [8, 12], e_ops=e_ops, seeds=9)
+    _same_jumps(_records(got), _records(ref))
+    for g, w in zip(got.expect, ref.expect):
+        np.testing.assert_allclose(np.asarray(g), np.asarray(w), atol=2e-6)
+
+
+def test_mcsolve_gpu_map_improved_sampling(qt, plugin):
+    """Improved sampling (mcsolve.py:716-747): the no-jump run goes through the
+    gpu_vern7 integrator, every other trajectory through one batched launch whose
+    first jump target sits above the no-jump probability."""
+    H, c_ops, psi0, e_ops = _jc(qt, N=6)
+    tl = np.linspace(0, 10, 51)
+    opts = {"method": "vern7", "map": "serial", "keep_runs_results": True,
+            "improved_sampling": True}
+    ref = qt.mcsolve(H, psi0, tl, c_ops, e_ops=e_ops, ntraj=16, seeds=21, options=opts)
+    got = qt.mcsolve(H, psi0, tl, c_ops, e_ops=e_ops, ntraj=16, seeds=21,
+                     options={**opts, "method": "gpu_vern7", "map": "gpu"})
+    _same_jumps(_records(got), _records(ref))
+    recs = _records(got)
+    assert len(recs) == 16 and all(len(w) >= 1 for _, w in recs)  # every sampled run jumps
+    for g, w in zip(got.expect, ref.expect):
+        np.testing.assert_allclose(np.asarray(g), np.asarray(w), atol=2e-6)
+
+
+def test_mcsolve_gpu_map_improved_sampling_mixed_dark(qt, plugin):
+    """Improved sampling over a mixed ensemble with a dark member (mcsolve.py:749-790,
+    544-558): the dark state's trajectories are the zero trajectory of weight 0."""
+    H, c_ops, psi0, e_ops = _jc(qt, N=6)
+    dark = qt.tensor(qt.basis(6, 0), qt.basis(2, 1))
+    ics = [(psi0, 0.45), (dark, 0.55)]
+    tl = np.linspace(0, 10, 51)
+    opts = {"method": "vern7", "map": "serial", "keep_runs_results": True,
+            "improved_sampling": True}
+    ref = qt.MCSolver(H, c_ops, options=opts).run(ics, tl, [10, 4], e_ops=e_ops, seeds=4)
+    got = qt.MCSolver(H, c_ops, options={**opts, "method": "gpu_vern7", "map": "gpu"}).run(
+        ics, tl, [10, 4], e_ops=e_ops, seeds=4)
+    _same_jumps(_records(got), _records(ref))
+    for g, w in zip(got.expect, ref.expect):
+        np.testing.assert_allclose(np.asarray(g), np.asarray(w), atol=2e-6)

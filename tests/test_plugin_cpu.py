@@ -103,3 +103,61 @@ def test_interpolated_coefficients(qt, plugin, order):
     prog2 = plugin.device_coefficient(c2)
     np.testing.assert_allclose([prog2(t) for t in ts], [complex(c2(t)) for t in ts],
                                rtol=1e-13, atol=1e-14)
+
+
+def _jc_dark(qt, N=4):
+    a = qt.tensor(qt.destroy(N), qt.qeye(2))
+    sm = qt.tensor(qt.qeye(N), qt.sigmam())
+    H = 2 * np.pi * (a.dag() * a + 0.05 * (a * sm.dag() + a.dag() * sm))
+    c_ops = [np.sqrt(0.05) * a, np.sqrt(0.1) * sm]
+    bright = qt.tensor(qt.basis(N, 1), qt.basis(2, 0))
+    dark = qt.tensor(qt.basis(N, 0), qt.basis(2, 1))   # H|dark> = 0, no collapse acts on it
+    return H, c_ops, bright, dark, [a.dag() * a]
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_map_task_decoding_under_improved_sampling(qt, plugin, mixed):
+    """The trajectory tasks the reference's MCSolver hands its map (plain, mixed
+    initial states, improved sampling) decode to the seeds, initial states, weights
+    and jump-probability floors that the reference's own trajectories use."""
+    from qutip.solver import parallel
+    H, c_ops, bright, dark, e_ops = _jc_dark(qt)
+    calls = []
+
+    def recording_map(task, values, task_args=None, task_kwargs=None, reduce_func=None,
+                      **kw):
+        if getattr(task, "__name__", "") != "_no_jump_simulation":
+            calls.append(plugin._mc_map_items(task, values, task_args or (), task_kwargs))
+        return parallel.serial_map(task, values, task_args, task_kwargs, reduce_func, **kw)
+
+    parallel._maps["recording"] = recording_map
+    try:
+        state = [(bright, 0.4), (dark, 0.6)] if mixed else bright
+        ntraj = [3, 2] if mixed else 4
+        opts = {"map": "recording", "improved_sampling": True, "keep_runs_results": True}
+        res = qt.MCSolver(H, c_ops, options=opts).run(state, np.linspace(0, 2, 5), ntraj,
+                                                      e_ops=e_ops, seeds=3)
+    finally:
+        del parallel._maps["recording"]
+    assert len(calls) == 1
+    solver, seeds, starts, floors, tlist, _ = calls[0]
+    assert isinstance(solver, qt.MCSolver)
+    assert len(seeds) == len(starts) == len(floors) == sum(np.atleast_1d(ntraj))
+    assert len(tlist) == 5
+    for f in floors:
+        assert 0.0 < f <= 1.0
+    if mixed:
+        # the dark state's no-jump probability is one: the floor the reference passes
+        # marks those trajectories as the zero trajectory of weight 0
+        # correction weights: the state's weight over its share of the trajectories
+        np.testing.assert_allclose([w for _, w in starts], [0.4 * 5 / 3] * 3 + [0.6 * 5 / 2] * 2)
+        assert all(f >= 1 - 1e-9 for f in floors[3:])
+        assert all(f < 0.99 for f in floors[:3])
+    else:
+        assert len(set(floors)) == 1 and floors[0] < 0.99
+    assert res.num_trajectories == sum(np.atleast_1d(ntraj))
+
+
+def test_map_rejects_other_tasks(qt, plugin):
+    with pytest.raises(TypeError):
+        plugin.gpu_map(lambda x: x, [1, 2])
