@@ -26,6 +26,7 @@ extern "C" {
 
 #define QG_MAX_GROUPS 8   /* coefficient groups (QobjEvo terms after merging) per operator */
 #define QG_MAX_EOPS 32    /* operators per expect launch */
+#define QG_MAX_COPS 64    /* collapse operators of one matrix-free Lindblad generator */
 
 typedef enum { QG_C128 = 0, QG_C64 = 1 } qg_dtype;
 
@@ -100,6 +101,25 @@ typedef struct qg_dia {
   const int32_t* offsets;
   const void* data;
 } qg_dia;
+
+/* The Lindblad generator applied to vec(rho) without forming its d^2 x d^2
+ * superoperator (the reference's matrix form,
+ * qutip/core/cy/lindblad_matrix_form.pyx:105-204, in its full non-Hermitian branch):
+ *   L[rho] = A rho + rho A^dag + sum_i |f_i(t)|^2 C_i rho C_i^dag,
+ *   A = -i H_nh(t),  H_nh = H - (i/2) sum_i |f_i|^2 C_i^dag C_i,
+ * where vec(rho) is the column-major d*d vector (rho[r, c] at r + c*d, the F order of
+ * qutip's Dense) and the i-th collapse operator is f_i(t) C_i.
+ *   a:    A as a d x d operator, QG_LAYOUT_ROW_MAJOR, n_tiles = 0, with its coefficient
+ *         groups (at most QG_MAX_GROUPS);
+ *   cops: the C_i as a d x d operator in QG_LAYOUT_GROUP_MAJOR, group i = C_i with
+ *         coefficient f_i (NULL programs: every f_i = 1); n_groups = number of
+ *         collapse operators, 0..QG_MAX_COPS (pointers unused when 0).
+ * a and cops share dtype; d * d < 2^31. */
+typedef struct qg_lindblad {
+  int64_t d;
+  qg_csr_groups a;
+  qg_csr_groups cops;
+} qg_lindblad;
 
 /* Buffers of one explicit Runge-Kutta step.  The state (y_prev, y_front) may be
  * complex128 while the stages (k, ytmp) are complex64 ("mixed" form): the
@@ -184,6 +204,18 @@ int qg_spmv_dia(const qg_dia* A, const void* x, void* y, double alpha_re, double
  * (qutip/core/data/ode.pyx:27-52) and iadd_dense (qutip/core/data/add.pyx:203-219). */
 int qg_vern7_stage(const qg_csr_groups* A, const qg_rk_buffers* B, int stage, double t_prev,
                    double dt, double atol, double rtol, void* stream);
+
+/* y = alpha * L(t)[x] + beta * y for the matrix-free Lindblad generator; x and y
+ * are vec(rho) of length d*d in L's dtype.  Replaces LindbladMatrixForm.matmul_data
+ * (qutip/core/cy/lindblad_matrix_form.pyx:105-204). */
+int qg_lindblad_apply(const qg_lindblad* L, double t, const void* x, void* y, double alpha_re,
+                      double alpha_im, double beta_re, double beta_im, void* stream);
+
+/* qg_vern7_stage with the matrix-free Lindblad generator in place of A(t): one
+ * Vern7 stage of mesolve with options matrix_form=True (qutip/solver/mesolve.py:251-266);
+ * B->n = d*d. */
+int qg_lindblad_stage(const qg_lindblad* L, const qg_rk_buffers* B, int stage, double t_prev,
+                      double dt, double atol, double rtol, void* stream);
 
 /* Non-zero when a kernel of this library gave up a bounded wait on the current
  * device (the result of that launch is invalid); reading clears the flag. */

@@ -85,3 +85,34 @@ def wrmn_error(diff, state, atol, rtol) -> float:
     diff = np.asarray(diff).ravel()
     state = np.asarray(state).ravel()
     return float(np.sqrt(np.mean((np.abs(diff) / (atol + rtol * np.abs(state))) ** 2)))
+
+
+def lindblad_matrix_form(h_nh, c_ops, rho, scale=1.0, hermitian=False, out=None):
+    """``out += scale * L[rho]`` with rho a d x d matrix, the reference's matrix form
+    (``LindbladMatrixForm.matmul_data``, qutip/core/cy/lindblad_matrix_form.pyx:105-204).
+
+    ``h_nh`` is the non-Hermitian Hamiltonian ``H - (i/2) sum c^dag c`` at the time of
+    the call and ``c_ops`` the collapse operators at that time (d x d, sparse or dense).
+    ``hermitian=True`` takes the reference's Hermitian branch: ``A + A^dag`` with
+    ``A = -i H_nh rho + 1/2 sum c rho c^dag`` (:160-182); otherwise the full form
+    ``-i (H_nh rho - rho H_nh^dag) + sum c rho c^dag`` (:183-200).
+    """
+    rho = np.asarray(rho, dtype=np.complex128)
+    h = sp.csr_matrix(h_nh)
+    if out is None:
+        out = np.zeros_like(rho)
+    if hermitian:
+        acc = (-1j * scale) * (h @ rho)
+        for c in c_ops:
+            c = sp.csr_matrix(c)
+            tmp = (0.5 * scale) * (c @ rho)
+            acc = acc + (c.conj() @ tmp.T).T          # tmp @ c^dag
+        out += acc + acc.conj().T
+    else:
+        out += (-1j * scale) * (h @ rho)
+        out += (1j * scale) * (h.conj() @ rho.T).T    # rho @ h^dag
+        for c in c_ops:
+            c = sp.csr_matrix(c)
+            tmp = scale * (c @ rho)
+            out += (c.conj() @ tmp.T).T
+    return out

@@ -182,3 +182,41 @@ def mc_trajectory(heff_terms, c_ops, psi0, tlist, e_ops, seed, **opts):
         for k, o in enumerate(ops):
             ex[k, i] = np.vdot(psi, o @ psi)
     return ex, list(tr.collapses)
+
+
+def mesolve_matrix_form(h_terms, c_ops, rho0, tlist, e_ops, atol=1e-8, rtol=1e-6, nsteps=1000):
+    """``mesolve`` with ``matrix_form=True`` (qutip/solver/mesolve.py:251-266): the state
+    is rho itself (``_vectorize_state = False``) and the right-hand side
+    ``LindbladMatrixForm.matmul_data`` (:func:`oracle.kernels.lindblad_matrix_form`).
+
+    ``h_terms``: ``[(matrix, coefficient | None)]``; ``c_ops``: ``[(matrix, f | None)]``
+    with ``f(t)`` the collapse operator's coefficient.  H_nh is formed as the reference
+    does (lindblad_matrix_form.pyx:88-96).  Returns the e_op expectation values (traces,
+    normalised when the initial trace is 1) at ``tlist``.
+    """
+    from .kernels import lindblad_matrix_form
+    d = rho0.shape[0]
+    hs = [(sp.csr_matrix(h), _coeff_fn(c)) for h, c in h_terms]
+    cs = [(sp.csr_matrix(c), _coeff_fn(f)) for c, f in c_ops]
+
+    def deriv(t, y):
+        rho = y.reshape(d, d, order="F")
+        h_nh = sum(c(t) * h for h, c in hs)
+        for cm, f in cs:
+            h_nh = h_nh - 0.5j * abs(f(t)) ** 2 * (cm.conj().T @ cm)
+        cts = [f(t) * cm for cm, f in cs]
+        return lindblad_matrix_form(h_nh, cts, rho).reshape(-1, order="F")
+
+    ig = Vern7(deriv, atol=atol, rtol=rtol, nsteps=nsteps)
+    ig.set_initial_value(np.asarray(rho0, dtype=np.complex128).reshape(-1, order="F"), tlist[0])
+    normalize = abs(np.trace(rho0) - 1) <= 1e-12
+    out = np.zeros((len(e_ops), len(tlist)), dtype=np.complex128)
+    for i, t in enumerate(tlist):
+        if i:
+            ig.integrate(t)
+            ig.check()
+        rho = ig.y.reshape(d, d, order="F")
+        tr = np.trace(rho) if normalize else 1.0
+        for k, e in enumerate(e_ops):
+            out[k, i] = np.trace(sp.csr_matrix(e) @ rho) / tr
+    return out

@@ -14,7 +14,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libqutip_gb300.so"
 
 QG_OK, QG_ERR_ARG, QG_ERR_CUDA, QG_ERR_UNSUPPORTED = 0, -1, -2, -3
 QG_C128, QG_C64 = 0, 1
-QG_MAX_GROUPS, QG_MAX_EOPS = 8, 32
+QG_MAX_GROUPS, QG_MAX_EOPS, QG_MAX_COPS = 8, 32, 64
 
 
 QG_LAYOUT_GROUP_MAJOR, QG_LAYOUT_ROW_MAJOR, QG_LAYOUT_SLICED = 0, 1, 2
@@ -29,6 +29,10 @@ class CsrGroups(C.Structure):
                 ("col", C.c_void_p), ("val", C.c_void_p), ("tile_row", C.c_void_p),
                 ("coef_code", C.c_void_p), ("coef_start", C.c_void_p),
                 ("coef_consts", C.c_void_p)]
+
+
+class Lindblad(C.Structure):
+    _fields_ = [("d", C.c_int64), ("a", CsrGroups), ("cops", CsrGroups)]
 
 
 class Dia(C.Structure):
@@ -66,6 +70,11 @@ _SIGS = {
                               C.c_double, C.c_double, C.c_void_p]),
     "qg_vern7_stage": (C.c_int, [_P(CsrGroups), _P(RkBuffers), C.c_int, C.c_double, C.c_double,
                                  C.c_double, C.c_double, C.c_void_p]),
+    "qg_lindblad_apply": (C.c_int, [_P(Lindblad), C.c_double, C.c_void_p, C.c_void_p,
+                                    C.c_double, C.c_double, C.c_double, C.c_double,
+                                    C.c_void_p]),
+    "qg_lindblad_stage": (C.c_int, [_P(Lindblad), _P(RkBuffers), C.c_int, C.c_double,
+                                    C.c_double, C.c_double, C.c_double, C.c_void_p]),
     "qg_rk_combine": (C.c_int, [_P(StateView), C.c_void_p, C.c_int, C.c_void_p]),
     "qg_norm2": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                            C.c_void_p]),
@@ -88,6 +97,7 @@ _lib = None
 COMPUTE_ENTRY_POINTS = {
     "qg_spmv_csr", "qg_spmm_csr", "qg_spmv_dia", "qg_vern7_stage", "qg_rk_combine", "qg_norm2",
     "qg_expect_dm", "qg_expect_ket", "qg_batch_vern7", "qg_batch_vern7_noalloc",
+    "qg_lindblad_apply", "qg_lindblad_stage",
 }
 LAUNCHES = [0]
 

@@ -512,6 +512,101 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, UNR>::MIN_BLOCKS)
   }
 }
 
+// ---------------------------------------------------- matrix-free Lindblad --
+// out(r, c) = sum_j A[r,j] x[j + c d] + sum_k conj(A[c,k]) x[r + k d]
+//           + sum_i w_i sum_{j, k} C_i[r,j] conj(C_i[c,k]) x[j + k d],
+// the Lindblad generator on vec(rho) = x (column-major, rho[r, c] at r + c d) without
+// its d^2 x d^2 superoperator: A = -i H_nh and w_i = |f_i(t)|^2.  One thread per
+// element; a warp covers 32 consecutive r of one column c, so the row-c walks of A
+// and C_i are warp-uniform and every gather is a contiguous run of one column of
+// rho.  The d x d operators (a few entries per row) stay in L1 and the state (d^2
+// entries) in L2: the HBM traffic of a stage is its vectors only.
+constexpr int LB_BLOCK = 256;
+
+// acc += conj(v) * x
+__device__ __forceinline__ void cmac_conj(double& ar, double& ai, double2 v, double2 x) {
+  ar = fma(v.x, x.x, ar);
+  ar = fma(v.y, x.y, ar);
+  ai = fma(v.x, x.y, ai);
+  ai = fma(-v.y, x.x, ai);
+}
+__device__ __forceinline__ void cmac_conj(float& ar, float& ai, float2 v, float2 x) {
+  ar = fmaf(v.x, x.x, ar);
+  ar = fmaf(v.y, x.y, ar);
+  ai = fmaf(v.x, x.y, ai);
+  ai = fmaf(-v.y, x.x, ai);
+}
+
+template <int DT, int YDT, int EPI>
+__global__ void __launch_bounds__(LB_BLOCK)
+    lindblad_kernel(qg_lindblad L, double t, const typename elem<DT>::T* __restrict__ x,
+                    AxpbyArgs ax, RkArgs rk) {
+  using ST = typename elem<DT>::T;
+  using R = typename elem<DT>::R;
+  __shared__ cx<R> ca[QG_MAX_GROUPS];
+  __shared__ R wc[QG_MAX_COPS];
+  __shared__ double red[LB_BLOCK / 32];
+  load_coefs(L.a, t, ca);
+  if (threadIdx.x < L.cops.n_groups) {
+    const cplx f = group_coef(L.cops, threadIdx.x, t);
+    wc[threadIdx.x] = (R)(f.re * f.re + f.im * f.im);
+  }
+  __syncthreads();
+  const int d = (int)L.d;
+  const int n = d * d;
+  const int G = L.a.n_groups, NC = L.cops.n_groups;
+  const ST* __restrict__ aval = static_cast<const ST*>(L.a.val);
+  const int* __restrict__ acol = L.a.col;
+  const int* __restrict__ arp = L.a.row_ptr;
+  const ST* __restrict__ cval = static_cast<const ST*>(L.cops.val);
+  const int* __restrict__ ccol = L.cops.col;
+  const int* __restrict__ crp = L.cops.row_ptr;
+  R err_acc = 0;
+  for (int idx = blockIdx.x * LB_BLOCK + threadIdx.x; idx < n; idx += gridDim.x * LB_BLOCK) {
+    const int c = idx / d;
+    const int r = idx - c * d;
+    const ST* __restrict__ xc = x + (size_t)c * d;
+    cx<R> acc{0, 0};
+    for (int g = 0; g < G; ++g) {
+      // A rho: row r of A against column c of rho
+      R ar = 0, ai = 0;
+      const int s0 = __ldg(arp + r * G + g), e0 = __ldg(arp + r * G + g + 1);
+      for (int p = s0; p < e0; ++p) cmac_any(ar, ai, __ldg(aval + p), ld_gather(xc + __ldg(acol + p)));
+      // rho A^dag: row c of A, conjugated, against row r of rho
+      R br = 0, bi = 0;
+      const int s1 = __ldg(arp + c * G + g), e1 = __ldg(arp + c * G + g + 1);
+      for (int p = s1; p < e1; ++p)
+        cmac_conj(br, bi, __ldg(aval + p), ld_gather(x + r + (size_t)__ldg(acol + p) * d));
+      const cx<R> k = ca[g];
+      acc.re += k.re * ar - k.im * ai + k.re * br + k.im * bi;
+      acc.im += k.re * ai + k.im * ar + k.re * bi - k.im * br;
+    }
+    for (int i = 0; i < NC; ++i) {
+      const R w = wc[i];
+      if (w == (R)0) continue;
+      const int* __restrict__ rp = crp + (size_t)i * (d + 1);
+      const int r0 = __ldg(rp + r), r1 = __ldg(rp + r + 1);
+      const int c0 = __ldg(rp + c), c1 = __ldg(rp + c + 1);
+      if (r0 == r1 || c0 == c1) continue;
+      R sr = 0, si = 0;
+      for (int q = c0; q < c1; ++q) {
+        const ST b = __ldg(cval + q);
+        const ST* __restrict__ xk = x + (size_t)__ldg(ccol + q) * d;
+        R ir = 0, ii = 0;
+        for (int p = r0; p < r1; ++p) cmac_any(ir, ii, __ldg(cval + p), ld_gather(xk + __ldg(ccol + p)));
+        sr += b.x * ir + b.y * ii;  // conj(b) * inner
+        si += b.x * ii - b.y * ir;
+      }
+      acc.re += w * sr;
+      acc.im += w * si;
+    }
+    epilogue<DT, YDT, EPI>(idx, acc, ax, rk, err_acc);
+  }
+  if constexpr (EPI == EPI_RK) {
+    if (rk.stage == RK_STEP - 1) finish_error<LB_BLOCK>(rk, (double)err_acc, red);
+  }
+}
+
 // ------------------------------------------------------------------ launch --
 // Opt `kernel` into `smem` bytes of dynamic shared memory and return its
 // resident blocks per SM.  The caller keeps one cache per kernel instantiation.
@@ -610,6 +705,23 @@ static int launch_any(cudaStream_t st, const qg_csr_groups& A, double t, const v
   return check_launch("spmv_direct_kernel");
 }
 
+template <int DT, int YDT, int EPI>
+static int launch_lindblad(cudaStream_t st, const qg_lindblad& L, double t, const void* x,
+                           const AxpbyArgs& ax, const RkArgs& rk) {
+  using ST = typename elem<DT>::T;
+  auto kern = lindblad_kernel<DT, YDT, EPI>;
+  static OccCache cache;  // one per instantiation
+  const int per_sm = staged_occupancy(kern, LB_BLOCK, 0, cache);
+  if (per_sm <= 0) return set_error(QG_ERR_CUDA, "occupancy query failed");
+  const int64_t n = L.d * L.d;
+  const int64_t blocks = (n + LB_BLOCK - 1) / LB_BLOCK;
+  int64_t cap = (int64_t)sm_count() * per_sm;
+  if (cap > qg_scratch_doubles()) cap = qg_scratch_doubles();
+  const int grid = (int)(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
+  kern<<<grid, LB_BLOCK, 0, st>>>(L, t, (const ST*)x, ax, rk);
+  return check_launch("lindblad_kernel");
+}
+
 static int check_groups(const qg_csr_groups* A) {
   if (!A || !A->row_ptr || !A->col || !A->val) return set_error(QG_ERR_ARG, "null operator");
   if (A->n_groups < 1 || A->n_groups > QG_MAX_GROUPS)
@@ -632,6 +744,87 @@ static int check_groups(const qg_csr_groups* A) {
   }
   if (A->coef_code && (!A->coef_start || !A->coef_consts))
     return set_error(QG_ERR_ARG, "coefficient program tables incomplete");
+  return QG_OK;
+}
+
+static int check_lindblad(const qg_lindblad* L) {
+  if (!L) return set_error(QG_ERR_ARG, "null generator");
+  int rc = check_groups(&L->a);
+  if (rc) return rc;
+  const int64_t d = L->d;
+  if (d < 1 || d * d >= (int64_t)INT32_MAX)
+    return set_error(QG_ERR_ARG, "dimension out of range (need 1 <= d, d*d < 2^31)");
+  if (L->a.layout != QG_LAYOUT_ROW_MAJOR || L->a.n_tiles != 0 || L->a.n_rows != d ||
+      L->a.n_cols != d)
+    return set_error(QG_ERR_ARG, "a must be a d x d row-major operator without tiles");
+  const qg_csr_groups& C = L->cops;
+  if (C.n_groups < 0 || C.n_groups > QG_MAX_COPS)
+    return set_error(QG_ERR_ARG, "number of collapse operators out of range");
+  if (C.n_groups > 0) {
+    if (!C.row_ptr || !C.col || !C.val) return set_error(QG_ERR_ARG, "null collapse operator");
+    if (C.layout != QG_LAYOUT_GROUP_MAJOR || C.n_rows != d || C.n_cols != d)
+      return set_error(QG_ERR_ARG, "cops must be d x d in the group-major layout");
+    if (C.dtype != L->a.dtype) return set_error(QG_ERR_ARG, "cops and a must share a dtype");
+    if ((int64_t)C.n_groups * (d + 1) >= (int64_t)INT32_MAX)
+      return set_error(QG_ERR_ARG, "collapse operator row pointers exceed 2^31");
+    if (C.coef_code && (!C.coef_start || !C.coef_consts))
+      return set_error(QG_ERR_ARG, "coefficient program tables incomplete");
+  }
+  return QG_OK;
+}
+
+// Stage arguments of the fused Vern7 stage: the RK buffers, the factors dt * a_ij
+// (dt * b_j and dt * e_j at the last stage) and the stage input x.
+static int prepare_stage(const qg_rk_buffers* B, int op_dtype, int64_t n_rows, int stage,
+                         double dt, double atol, double rtol, RkArgs& rk, const void*& x) {
+  if (!B || !B->y_prev || !B->y_front || !B->k || !B->ytmp)
+    return set_error(QG_ERR_ARG, "null Runge-Kutta buffer");
+  if (stage < 0 || stage >= RK_EXTRA_STEP) return set_error(QG_ERR_ARG, "stage out of range");
+  if (B->n != n_rows) return set_error(QG_ERR_ARG, "operator must be square with n rows");
+  if (B->stage_dtype != op_dtype)
+    return set_error(QG_ERR_UNSUPPORTED, "stage dtype must equal the operator dtype");
+  const bool mixed = B->state_dtype != B->stage_dtype;
+  if (mixed && (!B->y_prev_s || !B->y_front_s))
+    return set_error(QG_ERR_ARG, "mixed form needs y_prev_s and y_front_s");
+  if (stage == RK_STEP - 1 && (!B->scratch || !B->counter || !B->result))
+    return set_error(QG_ERR_ARG, "error reduction buffers missing");
+  if (!((B->state_dtype == QG_C128 && B->stage_dtype == QG_C128) ||
+        (B->state_dtype == QG_C128 && B->stage_dtype == QG_C64) ||
+        (B->state_dtype == QG_C64 && B->stage_dtype == QG_C64)))
+    return set_error(QG_ERR_UNSUPPORTED, "unsupported state/stage dtype pair");
+  const size_t n = (size_t)B->n;
+  const size_t es = B->stage_dtype == QG_C128 ? 16 : 8;
+  rk = RkArgs{};
+  rk.y_prev = B->y_prev;
+  rk.y_front = B->y_front;
+  rk.y_prev_s = B->y_prev_s;
+  rk.y_front_s = B->y_front_s;
+  rk.k = B->k;
+  rk.ytmp_out = (char*)B->ytmp + ((stage + 1) & 1) * n * es;
+  rk.n = B->n;
+  rk.stage = stage;
+  rk.atol = atol;
+  rk.rtol = rtol;
+  rk.scratch = B->scratch;
+  rk.counter = B->counter;
+  rk.result = B->result;
+  // factors dt * tableau, formed in double and rounded once for the FP32 paths
+  for (int j = 0; j < 16; ++j) {
+    double a = 0.0, e = 0.0;
+    if (stage == RK_STEP - 1) {
+      if (j < RK_STEP) {
+        a = dt * VERN7_B_HOST[j];
+        e = dt * VERN7_E_HOST[j];
+      }
+    } else if (stage + 1 < RK_EXTRA_STEP && j <= stage) {
+      a = dt * VERN7_A_HOST[stage + 1][j];
+    }
+    rk.fa_d[j] = a;
+    rk.fe_d[j] = e;
+    rk.fa_f[j] = (float)a;
+    rk.fe_f[j] = (float)e;
+  }
+  x = stage == 0 ? (mixed ? B->y_prev_s : B->y_prev) : (const char*)B->ytmp + (stage & 1) * n * es;
   return QG_OK;
 }
 
@@ -665,61 +858,49 @@ extern "C" int qg_vern7_stage(const qg_csr_groups* A, const qg_rk_buffers* B, in
                               double t_prev, double dt, double atol, double rtol, void* stream) {
   int rc = check_groups(A);
   if (rc) return rc;
-  if (!B || !B->y_prev || !B->y_front || !B->k || !B->ytmp)
-    return set_error(QG_ERR_ARG, "null Runge-Kutta buffer");
-  if (stage < 0 || stage >= RK_EXTRA_STEP) return set_error(QG_ERR_ARG, "stage out of range");
-  if (B->n != A->n_rows || A->n_rows != A->n_cols)
-    return set_error(QG_ERR_ARG, "operator must be square with n rows");
-  if (B->stage_dtype != A->dtype)
-    return set_error(QG_ERR_UNSUPPORTED, "stage dtype must equal the operator dtype");
-  const bool mixed = B->state_dtype != B->stage_dtype;
-  if (mixed && (!B->y_prev_s || !B->y_front_s))
-    return set_error(QG_ERR_ARG, "mixed form needs y_prev_s and y_front_s");
-  if (stage == RK_STEP - 1 && (!B->scratch || !B->counter || !B->result))
-    return set_error(QG_ERR_ARG, "error reduction buffers missing");
+  if (A->n_rows != A->n_cols) return set_error(QG_ERR_ARG, "operator must be square with n rows");
+  RkArgs rk;
+  const void* x = nullptr;
+  rc = prepare_stage(B, A->dtype, A->n_rows, stage, dt, atol, rtol, rk, x);
+  if (rc) return rc;
   if (B->n == 0) return QG_OK;
-  const size_t n = (size_t)B->n;
-  const size_t es = B->stage_dtype == QG_C128 ? 16 : 8;
-  RkArgs rk{};
-  rk.y_prev = B->y_prev;
-  rk.y_front = B->y_front;
-  rk.y_prev_s = B->y_prev_s;
-  rk.y_front_s = B->y_front_s;
-  rk.k = B->k;
-  rk.ytmp_out = (char*)B->ytmp + ((stage + 1) & 1) * n * es;
-  rk.n = B->n;
-  rk.stage = stage;
-  rk.atol = atol;
-  rk.rtol = rtol;
-  rk.scratch = B->scratch;
-  rk.counter = B->counter;
-  rk.result = B->result;
-  // factors dt * tableau, formed in double and rounded once for the FP32 paths
-  for (int j = 0; j < 16; ++j) {
-    double a = 0.0, e = 0.0;
-    if (stage == RK_STEP - 1) {
-      if (j < RK_STEP) {
-        a = dt * VERN7_B_HOST[j];
-        e = dt * VERN7_E_HOST[j];
-      }
-    } else if (stage + 1 < RK_EXTRA_STEP && j <= stage) {
-      a = dt * VERN7_A_HOST[stage + 1][j];
-    }
-    rk.fa_d[j] = a;
-    rk.fe_d[j] = e;
-    rk.fa_f[j] = (float)a;
-    rk.fe_f[j] = (float)e;
-  }
   AxpbyArgs ax{};
   cudaStream_t st = (cudaStream_t)stream;
   const double t = t_prev + VERN7_C_HOST[stage] * dt;
-  const void* x = stage == 0 ? (mixed ? B->y_prev_s : B->y_prev)
-                             : (const char*)B->ytmp + (stage & 1) * n * es;
   if (B->state_dtype == QG_C128 && B->stage_dtype == QG_C128)
     return launch_any<QG_C128, QG_C128, EPI_RK>(st, *A, t, x, ax, rk);
-  if (B->state_dtype == QG_C128 && B->stage_dtype == QG_C64)
+  if (B->state_dtype == QG_C128)
     return launch_any<QG_C64, QG_C128, EPI_RK>(st, *A, t, x, ax, rk);
-  if (B->state_dtype == QG_C64 && B->stage_dtype == QG_C64)
-    return launch_any<QG_C64, QG_C64, EPI_RK>(st, *A, t, x, ax, rk);
-  return set_error(QG_ERR_UNSUPPORTED, "unsupported state/stage dtype pair");
+  return launch_any<QG_C64, QG_C64, EPI_RK>(st, *A, t, x, ax, rk);
+}
+
+extern "C" int qg_lindblad_apply(const qg_lindblad* L, double t, const void* x, void* y,
+                                 double alpha_re, double alpha_im, double beta_re, double beta_im,
+                                 void* stream) {
+  int rc = check_lindblad(L);
+  if (rc) return rc;
+  if (!x || !y) return set_error(QG_ERR_ARG, "null vector");
+  AxpbyArgs ax{y, alpha_re, alpha_im, beta_re, beta_im};
+  RkArgs rk{};
+  cudaStream_t st = (cudaStream_t)stream;
+  if (L->a.dtype == QG_C128) return launch_lindblad<QG_C128, QG_C128, EPI_AXPBY>(st, *L, t, x, ax, rk);
+  return launch_lindblad<QG_C64, QG_C64, EPI_AXPBY>(st, *L, t, x, ax, rk);
+}
+
+extern "C" int qg_lindblad_stage(const qg_lindblad* L, const qg_rk_buffers* B, int stage,
+                                 double t_prev, double dt, double atol, double rtol, void* stream) {
+  int rc = check_lindblad(L);
+  if (rc) return rc;
+  RkArgs rk;
+  const void* x = nullptr;
+  rc = prepare_stage(B, L->a.dtype, L->d * L->d, stage, dt, atol, rtol, rk, x);
+  if (rc) return rc;
+  AxpbyArgs ax{};
+  cudaStream_t st = (cudaStream_t)stream;
+  const double t = t_prev + VERN7_C_HOST[stage] * dt;
+  if (B->state_dtype == QG_C128 && B->stage_dtype == QG_C128)
+    return launch_lindblad<QG_C128, QG_C128, EPI_RK>(st, *L, t, x, ax, rk);
+  if (B->state_dtype == QG_C128)
+    return launch_lindblad<QG_C64, QG_C128, EPI_RK>(st, *L, t, x, ax, rk);
+  return launch_lindblad<QG_C64, QG_C64, EPI_RK>(st, *L, t, x, ax, rk);
 }

@@ -403,6 +403,13 @@ class DeviceOperator:
                   a.real, a.imag, b.real, b.imag, stream_ptr())
         return y
 
+    def vern7_stage(self, rk, stage: int, t_prev: float, dt: float, atol: float, rtol: float,
+                    stream: int):
+        """One fused Vern7 stage (``qg_vern7_stage``) on the buffers ``rk``."""
+        lib = _lib.load()
+        _lib.check(lib.qg_vern7_stage(C.byref(self.struct), C.byref(rk), stage, t_prev, dt,
+                                      atol, rtol, stream), "qg_vern7_stage")
+
     def matmat(self, t: float, X: torch.Tensor, Y: torch.Tensor, alpha=1.0, beta=0.0):
         """``Y = alpha A(t) X + beta Y`` for F-ordered column blocks stored as ``[n_vec, n]``."""
         if X.dtype != _TORCH[self.dtype] or Y.dtype != _TORCH[self.dtype]:

@@ -61,6 +61,7 @@ from qutip.solver import parallel as _parallel
 
 from . import _lib
 from .coefficients import Coefficient, coefficient, interpolation
+from .lindblad import LindbladOperator
 from .operator import DeviceDia, DeviceOperator, stream_ptr
 from .vern7 import GpuVern7, IntegratorError
 
@@ -485,6 +486,29 @@ def qobjevo_terms(evo):
     return out
 
 
+def _is_matrix_form(rhs) -> bool:
+    try:
+        from qutip.core.cy.lindblad_matrix_form import LindbladMatrixForm
+    except ImportError:
+        return False
+    return isinstance(rhs, LindbladMatrixForm)
+
+
+def lindblad_operator(rhs, dtype="c128"):
+    """The device generator of a ``LindbladMatrixForm`` (mesolve's ``matrix_form``
+    option, qutip/solver/mesolve.py:251-266): A = -i H_nh from its ``H_nh``
+    (lindblad_matrix_form.pyx:88-96) and one term per collapse operator."""
+    a_terms = [((-1j) * m, c) for m, c in qobjevo_terms(rhs.H_nh)]
+    c_terms = []
+    for c in rhs.c_ops:
+        terms = qobjevo_terms(c)
+        if len(terms) != 1:
+            raise TypeError("matrix_form on the GPU needs each collapse operator to be a "
+                            "single (possibly time-dependent) term")
+        c_terms.append(terms[0])
+    return LindbladOperator(a_terms, c_terms, dtype=dtype, device=_device())
+
+
 # ---------------------------------------------------------------- integrator --
 def _as_gpu(state) -> GpuDense:
     if isinstance(state, GpuDense):
@@ -532,7 +556,11 @@ class IntegratorGpuVern7(Integrator):
         if prec not in ("double", "mixed"):
             raise ValueError("precision must be 'double' or 'mixed'")
         dt = "c128" if prec == "double" else "c64"
-        self._op = DeviceOperator(qobjevo_terms(self._rhs()), dtype=dt, device=_device())
+        rhs = self._rhs()
+        if _is_matrix_form(rhs):
+            self._op = lindblad_operator(rhs, dt)
+        else:
+            self._op = DeviceOperator(qobjevo_terms(rhs), dtype=dt, device=_device())
         self._ode = GpuVern7(self._op, atol=self._options["atol"], rtol=self._options["rtol"],
                              nsteps=self._options["nsteps"],
                              first_step=self._options["first_step"],

@@ -20,6 +20,7 @@ import torch
 
 from . import _lib
 from .coefficients import Coefficient, coefficient
+from .lindblad import LindbladOperator
 from .operator import DeviceOperator, stream_ptr
 from .systems import OpenSystem, lindblad_dissipator, merge_terms, spost, spre
 from .vern7 import GpuVern7, PRECISIONS
@@ -28,7 +29,7 @@ __all__ = ["MEResult", "mesolve", "solve_system", "liouvillian_terms", "ExpectOp
 
 ME_DEFAULTS = dict(atol=1e-8, rtol=1e-6, nsteps=1000, first_step=0.0, min_step=0.0,
                    max_step=0.0, interpolate=True, precision="double", store_states=False,
-                   store_final_state=False, normalize_output=True)
+                   store_final_state=False, normalize_output=True, matrix_form=False)
 
 
 @dataclass
@@ -139,14 +140,23 @@ def _evolve(ig: GpuVern7, tlist, ex: ExpectOps, d: int, store_states, store_fina
 
 def solve_system(system: OpenSystem, tlist, options=None, op: DeviceOperator | None = None,
                  ex: ExpectOps | None = None) -> MEResult:
-    """Evolve an :class:`~qutip_gb300.systems.OpenSystem` of kind ``"me"``."""
+    """Evolve an :class:`~qutip_gb300.systems.OpenSystem` of kind ``"me"``.
+
+    ``matrix_form=True`` applies the Lindblad generator without its superoperator
+    (:class:`~qutip_gb300.lindblad.LindbladOperator`, from the system's ``h_terms`` and
+    ``c_ops``), as the reference's ``matrix_form`` option (qutip/solver/mesolve.py:251-266).
+    """
     opt = {**ME_DEFAULTS, **(options or {})}
     prec = opt["precision"]
     if prec not in PRECISIONS:
         raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
     stage_dt = PRECISIONS[prec][1]
     t0 = time.perf_counter()
-    if op is None:
+    if op is None and opt["matrix_form"]:
+        if not system.h_terms:
+            raise ValueError("matrix_form needs the system's Hamiltonian terms")
+        op = LindbladOperator.from_hamiltonian(system.h_terms, system.c_ops, dtype=stage_dt)
+    elif op is None:
         op = DeviceOperator(system.terms, dtype=stage_dt)
     if ex is None:
         ex = ExpectOps(system.e_ops)
@@ -184,6 +194,11 @@ def mesolve(H, rho0, tlist, c_ops=None, e_ops=None, args=None, options=None) -> 
         psi = rho0.reshape(-1)
         rho0 = np.outer(psi, psi.conj())
     d = rho0.shape[0]
-    system = OpenSystem("user", "me", d, liouvillian_terms(H, c_ops, args),
-                        rho0.reshape(-1, order="F").copy(), list(e_ops or []))
+    if (options or {}).get("matrix_form"):
+        system = OpenSystem("user", "me", d, None, rho0.reshape(-1, order="F").copy(),
+                            list(e_ops or []), [sp.csr_matrix(c) for c in c_ops],
+                            _as_terms(H, args))
+    else:
+        system = OpenSystem("user", "me", d, liouvillian_terms(H, c_ops, args),
+                            rho0.reshape(-1, order="F").copy(), list(e_ops or []))
     return solve_system(system, tlist, options)

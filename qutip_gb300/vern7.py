@@ -53,8 +53,9 @@ class IntegratorError(RuntimeError):
 class GpuVern7:
     """Single-system adaptive Vern7 on device buffers.
 
-    ``op`` must be a :class:`DeviceOperator` whose dtype is the stage dtype of
-    ``precision``.
+    ``op`` is a :class:`DeviceOperator` or a
+    :class:`~qutip_gb300.lindblad.LindbladOperator` whose dtype is the stage dtype
+    of ``precision``.
     """
 
     def __init__(self, op: DeviceOperator, atol=1e-8, rtol=1e-6, nsteps=1000, first_step=0.0,
@@ -274,11 +275,9 @@ class GpuVern7:
     def _compute_step(self, dt):
         # explicit_rk.pyx:358-397: ten fused stages; the last returns the error
         rk = self._rk()
-        lib = _lib.load()
         s = stream_ptr()
         for i in range(T.RK_STEP):
-            _lib.check(lib.qg_vern7_stage(C.byref(self.op.struct), C.byref(rk), i, self.t_prev, dt,
-                                          self.atol, self.rtol, s), "qg_vern7_stage")
+            self.op.vern7_stage(rk, i, self.t_prev, dt, self.atol, self.rtol, s)
         self.stats["rhs"] += T.RK_STEP
         self.t_front = self.t_prev + dt
         return self._read_result()
@@ -289,11 +288,9 @@ class GpuVern7:
         rk = self._rk()
         self._combine(self._stage_base(), [dt * self.a[T.RK_STEP, j] for j in range(T.RK_STEP)],
                       self._ytmp(T.RK_STEP & 1))
-        lib = _lib.load()
         s = stream_ptr()
         for i in range(T.RK_STEP, T.RK_EXTRA_STEP):
-            _lib.check(lib.qg_vern7_stage(C.byref(self.op.struct), C.byref(rk), i, self.t_prev, dt,
-                                          self.atol, self.rtol, s), "qg_vern7_stage")
+            self.op.vern7_stage(rk, i, self.t_prev, dt, self.atol, self.rtol, s)
         self.stats["rhs"] += T.RK_EXTRA_STEP - T.RK_STEP
 
     def dense_factors(self, t):
