@@ -106,19 +106,52 @@ typedef struct qg_dia {
  * superoperator (the reference's matrix form,
  * qutip/core/cy/lindblad_matrix_form.pyx:105-204, in its full non-Hermitian branch):
  *   L[rho] = A rho + rho A^dag + sum_i |f_i(t)|^2 C_i rho C_i^dag,
- *   A = -i H_nh(t),  H_nh = H - (i/2) sum_i |f_i|^2 C_i^dag C_i,
+ *   A(t) = sum_g a_g(t) A_g = -i H_nh(t),  H_nh = H - (i/2) sum_i |f_i|^2 C_i^dag C_i,
  * where vec(rho) is the column-major d*d vector (rho[r, c] at r + c*d, the F order of
  * qutip's Dense) and the i-th collapse operator is f_i(t) C_i.
- *   a:    A as a d x d operator, QG_LAYOUT_ROW_MAJOR, n_tiles = 0, with its coefficient
- *         groups (at most QG_MAX_GROUPS);
- *   cops: the C_i as a d x d operator in QG_LAYOUT_GROUP_MAJOR, group i = C_i with
- *         coefficient f_i (NULL programs: every f_i = 1); n_groups = number of
- *         collapse operators, 0..QG_MAX_COPS (pointers unused when 0).
- * a and cops share dtype; d * d < 2^31. */
+ * Storage ("ELL" blocks: entry j of row r of a block of width W at base + j*d + r, so
+ * that consecutive rows are consecutive in memory; padding entries have value 0 and a
+ * valid column):
+ *   A_g:  its diagonal at a_diag[g*d + r] and its off-diagonal entries in an ELL
+ *         block of width a_width[g]; the blocks of g = 0..n_groups-1 follow one
+ *         another in a_col / a_val (block g starts at d * sum_{g'<g} a_width[g']);
+ *         the widths are held in this struct (host memory);
+ *   C_i:  the first n_diag_cops are diagonal, C_i[r,r] at c_diag[i*d + r]; the other
+ *         n_cops - n_diag_cops are ELL blocks of width c_width[i - n_diag_cops] in
+ *         c_col / c_val, one after another.
+ * Constant diagonal part: d_const (d*d entries in dtype, may be NULL) holds
+ *   D0(r, c) = sum_{g in const} A_g[r,r] + conj(A_g[c,c])
+ *            + sum_{i < n_const_diag} C_i[r,r] conj(C_i[c,c])
+ * at r + c*d for the groups whose bit in a_diag_const is set (coefficient 1, folded
+ * in D0) and the first n_const_diag diagonal collapse operators (coefficient 1); the
+ * other diagonal parts are evaluated per element.  With d_const NULL, a_diag_const
+ * and n_const_diag must be 0.
+ * Coefficient programs: a_g for the groups of A, f_i for the collapse operators in
+ * the order above (NULL code: all 1).  1 <= n_groups <= QG_MAX_GROUPS,
+ * 0 <= n_diag_cops <= n_cops <= QG_MAX_COPS, d*d < 2^31, ELL blocks < 2^31 entries. */
 typedef struct qg_lindblad {
   int64_t d;
-  qg_csr_groups a;
-  qg_csr_groups cops;
+  int32_t dtype;
+  int32_t n_groups;
+  int32_t n_diag_cops;
+  int32_t n_cops;
+  int32_t a_diag_const; /* bit g: the diagonal of A_g is folded into d_const */
+  int32_t n_const_diag; /* leading diagonal collapse operators folded into d_const */
+  int32_t a_width[QG_MAX_GROUPS];
+  int32_t c_width[QG_MAX_COPS];
+  const void* d_const;
+  const void* a_diag;
+  const int32_t* a_col;
+  const void* a_val;
+  const void* c_diag;
+  const int32_t* c_col;
+  const void* c_val;
+  const int32_t* a_coef_code;
+  const int32_t* a_coef_start;
+  const double* a_coef_consts;
+  const int32_t* c_coef_code;
+  const int32_t* c_coef_start;
+  const double* c_coef_consts;
 } qg_lindblad;
 
 /* Buffers of one explicit Runge-Kutta step.  The state (y_prev, y_front) may be

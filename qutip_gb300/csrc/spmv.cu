@@ -513,14 +513,18 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, UNR>::MIN_BLOCKS)
 }
 
 // ---------------------------------------------------- matrix-free Lindblad --
-// out(r, c) = sum_j A[r,j] x[j + c d] + sum_k conj(A[c,k]) x[r + k d]
-//           + sum_i w_i sum_{j, k} C_i[r,j] conj(C_i[c,k]) x[j + k d],
-// the Lindblad generator on vec(rho) = x (column-major, rho[r, c] at r + c d) without
-// its d^2 x d^2 superoperator: A = -i H_nh and w_i = |f_i(t)|^2.  One thread per
-// element; a warp covers 32 consecutive r of one column c, so the row-c walks of A
-// and C_i are warp-uniform and every gather is a contiguous run of one column of
-// rho.  The d x d operators (a few entries per row) stay in L1 and the state (d^2
-// entries) in L2: the HBM traffic of a stage is its vectors only.
+// out(r, c) = D(r, c) x[r + c d]
+//           + sum_g a_g sum_j A_g[r,j] x[j + c d] + conj(a_g) sum_k conj(A_g[c,k]) x[r + k d]
+//           + sum_{i general} w_i sum_{j, k} C_i[r,j] conj(C_i[c,k]) x[j + k d],
+// D(r, c) = sum_g a_g A_g[r,r] + conj(a_g A_g[c,c]) + sum_{i diagonal} w_i C_i[r,r] conj(C_i[c,c]),
+// the Lindblad generator on vec(rho) = x (column-major, rho[r, c] at r + c d) without its
+// d^2 x d^2 superoperator: A = -i H_nh and w_i = |f_i(t)|^2.  One thread per element; a
+// warp covers 32 consecutive r of one column c.  Row-r operator entries are read from
+// ELL blocks laid out so that the warp's loads are one contiguous run, row-c entries
+// are warp-uniform (broadcast), and every gather is a contiguous run of one column of
+// rho.  The d x d operators stay in L1/L2 and the state (d^2 entries) in L2: the HBM
+// traffic of a stage is its vectors only.  Diagonal parts (the diagonal of A and the
+// all-diagonal collapse operators, e.g. dephasing) fold into one factor on x[r + c d].
 constexpr int LB_BLOCK = 256;
 
 // acc += conj(v) * x
@@ -537,6 +541,12 @@ __device__ __forceinline__ void cmac_conj(float& ar, float& ai, float2 v, float2
   ai = fmaf(-v.y, x.x, ai);
 }
 
+__device__ __forceinline__ cplx prog_coef(const int* code, const int* start, const double* consts,
+                                          int g, double t) {
+  if (code == nullptr) return cplx{1.0, 0.0};
+  return eval_coef(code + start[g], consts, t);
+}
+
 template <int DT, int YDT, int EPI>
 __global__ void __launch_bounds__(LB_BLOCK)
     lindblad_kernel(qg_lindblad L, double t, const typename elem<DT>::T* __restrict__ x,
@@ -546,61 +556,119 @@ __global__ void __launch_bounds__(LB_BLOCK)
   __shared__ cx<R> ca[QG_MAX_GROUPS];
   __shared__ R wc[QG_MAX_COPS];
   __shared__ double red[LB_BLOCK / 32];
-  load_coefs(L.a, t, ca);
-  if (threadIdx.x < L.cops.n_groups) {
-    const cplx f = group_coef(L.cops, threadIdx.x, t);
+  const int G = L.n_groups, ND = L.n_diag_cops, NE = L.n_cops - L.n_diag_cops;
+  if (threadIdx.x < G) {
+    const cplx k = prog_coef(L.a_coef_code, L.a_coef_start, L.a_coef_consts, threadIdx.x, t);
+    ca[threadIdx.x] = cx<R>{(R)k.re, (R)k.im};
+  }
+  if (threadIdx.x < L.n_cops) {
+    const cplx f = prog_coef(L.c_coef_code, L.c_coef_start, L.c_coef_consts, threadIdx.x, t);
     wc[threadIdx.x] = (R)(f.re * f.re + f.im * f.im);
   }
   __syncthreads();
   const int d = (int)L.d;
   const int n = d * d;
-  const int G = L.a.n_groups, NC = L.cops.n_groups;
-  const ST* __restrict__ aval = static_cast<const ST*>(L.a.val);
-  const int* __restrict__ acol = L.a.col;
-  const int* __restrict__ arp = L.a.row_ptr;
-  const ST* __restrict__ cval = static_cast<const ST*>(L.cops.val);
-  const int* __restrict__ ccol = L.cops.col;
-  const int* __restrict__ crp = L.cops.row_ptr;
+  const ST* __restrict__ dconst = static_cast<const ST*>(L.d_const);
+  const ST* __restrict__ adiag = static_cast<const ST*>(L.a_diag);
+  const int* __restrict__ acol = L.a_col;
+  const ST* __restrict__ aval = static_cast<const ST*>(L.a_val);
+  const ST* __restrict__ cdiag = static_cast<const ST*>(L.c_diag);
+  const int* __restrict__ ccol = L.c_col;
+  const ST* __restrict__ cval = static_cast<const ST*>(L.c_val);
+  const int dmask = L.a_diag_const;
+  const int nd0 = L.n_const_diag;
   R err_acc = 0;
-  for (int idx = blockIdx.x * LB_BLOCK + threadIdx.x; idx < n; idx += gridDim.x * LB_BLOCK) {
-    const int c = idx / d;
-    const int r = idx - c * d;
-    const ST* __restrict__ xc = x + (size_t)c * d;
-    cx<R> acc{0, 0};
-    for (int g = 0; g < G; ++g) {
-      // A rho: row r of A against column c of rho
-      R ar = 0, ai = 0;
-      const int s0 = __ldg(arp + r * G + g), e0 = __ldg(arp + r * G + g + 1);
-      for (int p = s0; p < e0; ++p) cmac_any(ar, ai, __ldg(aval + p), ld_gather(xc + __ldg(acol + p)));
-      // rho A^dag: row c of A, conjugated, against row r of rho
-      R br = 0, bi = 0;
-      const int s1 = __ldg(arp + c * G + g), e1 = __ldg(arp + c * G + g + 1);
-      for (int p = s1; p < e1; ++p)
-        cmac_conj(br, bi, __ldg(aval + p), ld_gather(x + r + (size_t)__ldg(acol + p) * d));
-      const cx<R> k = ca[g];
-      acc.re += k.re * ar - k.im * ai + k.re * br + k.im * bi;
-      acc.im += k.re * ai + k.im * ar + k.re * bi - k.im * br;
+  // (r, c) of idx, advanced by the grid stride without a division per element
+  const int stride = gridDim.x * LB_BLOCK;
+  const int sc = stride / d, sr = stride - (stride / d) * d;
+  int idx = blockIdx.x * LB_BLOCK + threadIdx.x;
+  int c = idx / d;
+  int r = idx - c * d;
+  for (; idx < n; idx += stride) {
+    const int cd = c * d;
+    // diagonal factor D(r, c): the precomputed constant part plus the time-dependent rest
+    R dr = 0, di = 0;
+    if (dconst) {
+      const ST p = __ldg(dconst + idx);
+      dr = p.x;
+      di = p.y;
     }
-    for (int i = 0; i < NC; ++i) {
+    for (int g = 0; g < G; ++g) {
+      if ((dmask >> g) & 1) continue;
+      const cx<R> k = ca[g];
+      const ST p = __ldg(adiag + g * d + r), q = __ldg(adiag + g * d + c);
+      dr += k.re * (p.x + q.x) - k.im * (p.y - q.y);  // k p + conj(k q)
+      di += k.re * (p.y - q.y) + k.im * (p.x + q.x);
+    }
+    for (int i = nd0; i < ND; ++i) {
       const R w = wc[i];
-      if (w == (R)0) continue;
-      const int* __restrict__ rp = crp + (size_t)i * (d + 1);
-      const int r0 = __ldg(rp + r), r1 = __ldg(rp + r + 1);
-      const int c0 = __ldg(rp + c), c1 = __ldg(rp + c + 1);
-      if (r0 == r1 || c0 == c1) continue;
-      R sr = 0, si = 0;
-      for (int q = c0; q < c1; ++q) {
-        const ST b = __ldg(cval + q);
-        const ST* __restrict__ xk = x + (size_t)__ldg(ccol + q) * d;
-        R ir = 0, ii = 0;
-        for (int p = r0; p < r1; ++p) cmac_any(ir, ii, __ldg(cval + p), ld_gather(xk + __ldg(ccol + p)));
-        sr += b.x * ir + b.y * ii;  // conj(b) * inner
-        si += b.x * ii - b.y * ir;
+      const ST p = __ldg(cdiag + i * d + r), q = __ldg(cdiag + i * d + c);
+      dr += w * (p.x * q.x + p.y * q.y);  // w p conj(q)
+      di += w * (p.y * q.x - p.x * q.y);
+    }
+    const ST xe = ld_gather(x + idx);
+    cx<R> acc{dr * xe.x - di * xe.y, dr * xe.y + di * xe.x};
+    // off-diagonal A: A rho (row r against column c) and rho A^dag (row c against row r)
+    int base = 0;
+    for (int g = 0; g < G; ++g) {
+      const int W = L.a_width[g];
+      if (W == 0) continue;
+      R lr = 0, li = 0, qr = 0, qi = 0;
+#pragma unroll 4
+      for (int j = 0; j < W; ++j) {
+        const int e = base + j * d;
+        const int cr = __ldg(acol + e + r), cc = __ldg(acol + e + c);
+        const ST vr = __ldg(aval + e + r), vc = __ldg(aval + e + c);
+        cmac_any(lr, li, vr, ld_gather(x + (cr + cd)));
+        cmac_conj(qr, qi, vc, ld_gather(x + (r + cc * d)));
       }
-      acc.re += w * sr;
-      acc.im += w * si;
+      const cx<R> k = ca[g];
+      acc.re += k.re * lr - k.im * li + k.re * qr + k.im * qi;
+      acc.im += k.re * li + k.im * lr + k.re * qi - k.im * qr;
+      base += W * d;
+    }
+    // general collapse operators: C rho C^dag
+    base = 0;
+    for (int i = 0; i < NE; ++i) {
+      const int W = L.c_width[i];
+      const R w = wc[ND + i];
+      if (W == 1) {  // one entry per row (s-, a, ...): no inner loops
+        const ST b = __ldg(cval + base + c), v = __ldg(cval + base + r);
+        if ((b.x != (R)0 || b.y != (R)0) && (v.x != (R)0 || v.y != (R)0)) {
+          const ST xv = ld_gather(x + (__ldg(ccol + base + r) + __ldg(ccol + base + c) * d));
+          // w v conj(b) x
+          const R pr = w * (v.x * b.x + v.y * b.y), pi = w * (v.y * b.x - v.x * b.y);
+          acc.re += pr * xv.x - pi * xv.y;
+          acc.im += pr * xv.y + pi * xv.x;
+        }
+      } else if (W > 1) {
+        R sr2 = 0, si2 = 0;
+        for (int q = 0; q < W; ++q) {
+          const int eq = base + q * d + c;
+          const ST b = __ldg(cval + eq);
+          if (b.x == (R)0 && b.y == (R)0) continue;  // warp-uniform: padding of row c
+          const int kd = __ldg(ccol + eq) * d;
+          R ir = 0, ii = 0;
+          for (int p = 0; p < W; ++p) {
+            const int ep = base + p * d + r;
+            const ST v = __ldg(cval + ep);
+            if (v.x != (R)0 || v.y != (R)0) cmac_any(ir, ii, v, ld_gather(x + (__ldg(ccol + ep) + kd)));
+          }
+          sr2 += b.x * ir + b.y * ii;  // conj(b) * inner
+          si2 += b.x * ii - b.y * ir;
+        }
+        acc.re += w * sr2;
+        acc.im += w * si2;
+      }
+      base += W * d;
     }
     epilogue<DT, YDT, EPI>(idx, acc, ax, rk, err_acc);
+    c += sc;
+    r += sr;
+    if (r >= d) {
+      r -= d;
+      ++c;
+    }
   }
   if constexpr (EPI == EPI_RK) {
     if (rk.stage == RK_STEP - 1) finish_error<LB_BLOCK>(rk, (double)err_acc, red);
@@ -749,27 +817,39 @@ static int check_groups(const qg_csr_groups* A) {
 
 static int check_lindblad(const qg_lindblad* L) {
   if (!L) return set_error(QG_ERR_ARG, "null generator");
-  int rc = check_groups(&L->a);
-  if (rc) return rc;
   const int64_t d = L->d;
   if (d < 1 || d * d >= (int64_t)INT32_MAX)
     return set_error(QG_ERR_ARG, "dimension out of range (need 1 <= d, d*d < 2^31)");
-  if (L->a.layout != QG_LAYOUT_ROW_MAJOR || L->a.n_tiles != 0 || L->a.n_rows != d ||
-      L->a.n_cols != d)
-    return set_error(QG_ERR_ARG, "a must be a d x d row-major operator without tiles");
-  const qg_csr_groups& C = L->cops;
-  if (C.n_groups < 0 || C.n_groups > QG_MAX_COPS)
-    return set_error(QG_ERR_ARG, "number of collapse operators out of range");
-  if (C.n_groups > 0) {
-    if (!C.row_ptr || !C.col || !C.val) return set_error(QG_ERR_ARG, "null collapse operator");
-    if (C.layout != QG_LAYOUT_GROUP_MAJOR || C.n_rows != d || C.n_cols != d)
-      return set_error(QG_ERR_ARG, "cops must be d x d in the group-major layout");
-    if (C.dtype != L->a.dtype) return set_error(QG_ERR_ARG, "cops and a must share a dtype");
-    if ((int64_t)C.n_groups * (d + 1) >= (int64_t)INT32_MAX)
-      return set_error(QG_ERR_ARG, "collapse operator row pointers exceed 2^31");
-    if (C.coef_code && (!C.coef_start || !C.coef_consts))
-      return set_error(QG_ERR_ARG, "coefficient program tables incomplete");
+  if (L->dtype != QG_C128 && L->dtype != QG_C64)
+    return set_error(QG_ERR_UNSUPPORTED, "dtype must be QG_C128 or QG_C64");
+  if (L->n_groups < 1 || L->n_groups > QG_MAX_GROUPS)
+    return set_error(QG_ERR_ARG, "n_groups out of range");
+  if (L->n_cops < 0 || L->n_cops > QG_MAX_COPS || L->n_diag_cops < 0 ||
+      L->n_diag_cops > L->n_cops)
+    return set_error(QG_ERR_ARG, "collapse operator counts out of range");
+  if (!L->a_diag) return set_error(QG_ERR_ARG, "null A storage");
+  if (!L->d_const && (L->a_diag_const != 0 || L->n_const_diag != 0))
+    return set_error(QG_ERR_ARG, "constant diagonal parts need d_const");
+  if (L->n_const_diag < 0 || L->n_const_diag > L->n_diag_cops)
+    return set_error(QG_ERR_ARG, "n_const_diag out of range");
+  if (L->n_diag_cops > 0 && !L->c_diag) return set_error(QG_ERR_ARG, "null diagonal collapse storage");
+  int64_t ta = 0, tc = 0;
+  for (int g = 0; g < L->n_groups; ++g) {
+    if (L->a_width[g] < 0) return set_error(QG_ERR_ARG, "negative ELL width");
+    ta += L->a_width[g];
   }
+  for (int i = 0; i < L->n_cops - L->n_diag_cops; ++i) {
+    if (L->c_width[i] < 0) return set_error(QG_ERR_ARG, "negative ELL width");
+    tc += L->c_width[i];
+  }
+  if (ta * d >= (int64_t)INT32_MAX || tc * d >= (int64_t)INT32_MAX)
+    return set_error(QG_ERR_ARG, "ELL storage beyond 2^31 entries");
+  if ((ta > 0 && (!L->a_col || !L->a_val)) || (tc > 0 && (!L->c_col || !L->c_val)))
+    return set_error(QG_ERR_ARG, "null ELL storage");
+  if (L->a_coef_code && (!L->a_coef_start || !L->a_coef_consts))
+    return set_error(QG_ERR_ARG, "coefficient program tables incomplete");
+  if (L->c_coef_code && (!L->c_coef_start || !L->c_coef_consts))
+    return set_error(QG_ERR_ARG, "coefficient program tables incomplete");
   return QG_OK;
 }
 
@@ -883,7 +963,7 @@ extern "C" int qg_lindblad_apply(const qg_lindblad* L, double t, const void* x, 
   AxpbyArgs ax{y, alpha_re, alpha_im, beta_re, beta_im};
   RkArgs rk{};
   cudaStream_t st = (cudaStream_t)stream;
-  if (L->a.dtype == QG_C128) return launch_lindblad<QG_C128, QG_C128, EPI_AXPBY>(st, *L, t, x, ax, rk);
+  if (L->dtype == QG_C128) return launch_lindblad<QG_C128, QG_C128, EPI_AXPBY>(st, *L, t, x, ax, rk);
   return launch_lindblad<QG_C64, QG_C64, EPI_AXPBY>(st, *L, t, x, ax, rk);
 }
 
@@ -893,7 +973,7 @@ extern "C" int qg_lindblad_stage(const qg_lindblad* L, const qg_rk_buffers* B, i
   if (rc) return rc;
   RkArgs rk;
   const void* x = nullptr;
-  rc = prepare_stage(B, L->a.dtype, L->d * L->d, stage, dt, atol, rtol, rk, x);
+  rc = prepare_stage(B, L->dtype, L->d * L->d, stage, dt, atol, rtol, rk, x);
   if (rc) return rc;
   AxpbyArgs ax{};
   cudaStream_t st = (cudaStream_t)stream;

@@ -29,17 +29,41 @@ import torch
 from . import _lib
 from .coefficients import Coefficient, pack_programs
 from .operator import DeviceOperator, _ptr, _QG, _TORCH, stream_ptr
+from .systems import merge_terms
 
-__all__ = ["LindbladOperator"]
+__all__ = ["LindbladOperator", "ell_block"]
+
+
+def ell_block(m: sp.csr_matrix):
+    """``(width, col[width*d], val[width*d])`` of a d x d CSR matrix in the ELL layout
+    the kernel reads: entry j of row r at ``j*d + r``; padding has value 0 and column r."""
+    m = sp.csr_matrix(m, dtype=np.complex128)
+    m.sort_indices()
+    d = m.shape[0]
+    lens = np.diff(m.indptr)
+    W = int(lens.max()) if m.nnz else 0
+    col = np.tile(np.arange(d, dtype=np.int32), W).reshape(W, d)
+    val = np.zeros((W, d), dtype=np.complex128)
+    if m.nnz:
+        rows = np.repeat(np.arange(d), lens)
+        pos = np.arange(m.nnz) - m.indptr[rows]
+        col[pos, rows] = m.indices
+        val[pos, rows] = m.data
+    return W, col.reshape(-1), val.reshape(-1)
+
+
+def _is_diagonal(m: sp.csr_matrix) -> bool:
+    m = sp.coo_matrix(m)
+    return bool(np.all(m.row[m.data != 0] == m.col[m.data != 0]))
 
 
 class LindbladOperator:
     """Matrix-free Lindblad generator acting on vec(rho) (length d*d).
 
-    ``a_terms``: ``[(d x d matrix, Coefficient | None)]``, the terms of A = -i H_nh.
-    ``c_terms``: ``[(d x d matrix, Coefficient | None)]``, one per collapse operator
-    f_i(t) C_i.  Exposes the interface the Vern7 driver uses (``n_rows``, ``dtype``,
-    ``device``, ``matvec``, ``vern7_stage``).
+    ``a_terms``: ``[(d x d matrix, Coefficient | None)]``, the terms of A = -i H_nh
+    (merged per coefficient).  ``c_terms``: ``[(d x d matrix, Coefficient | None)]``, one
+    per collapse operator f_i(t) C_i.  Exposes the interface the Vern7 driver uses
+    (``n_rows``, ``dtype``, ``device``, ``matvec``, ``vern7_stage``).
     """
 
     def __init__(self, a_terms, c_terms, dtype: str = "c128", device="cuda"):
@@ -57,57 +81,116 @@ class LindbladOperator:
                 raise TypeError("coefficients must be qutip_gb300.coefficients.Coefficient")
         if d * d >= 2**31:
             raise ValueError("d*d must stay below 2^31")
+        a_terms = merge_terms([(sp.csr_matrix(m, dtype=np.complex128), c) for m, c in a_terms])
+        if len(a_terms) > _lib.QG_MAX_GROUPS:
+            raise ValueError(f"at most {_lib.QG_MAX_GROUPS} coefficient groups in H_nh")
         self.d = d
         self.n_rows = self.n_cols = d * d
         self.shape = (d * d, d * d)
         self.dtype = dtype
         self.device = torch.device(device)
         self.fmt = "lindblad"
-        self.a_terms = [(sp.csr_matrix(m), c) for m, c in a_terms]
-        self.c_terms = [(sp.csr_matrix(m), c) for m, c in c_terms]
-        self.a = DeviceOperator(a_terms, dtype=dtype, device=device, fmt="csr")
-        self.coeffs = list(self.a.coeffs) + [c for _, c in c_terms]
-        mats = [sp.csr_matrix(m, dtype=np.complex128) for m, _ in c_terms]
-        for m in mats:
-            m.sort_indices()
-        self.n_cops = len(mats)
-        self.c_coeffs = [c for _, c in c_terms]
-        self.c_nnz = [int(m.nnz) for m in mats]
+        tdt = _TORCH[dtype]
+        # A: per group its diagonal and an ELL block of its off-diagonal entries
+        self.a_terms = a_terms
+        self.a_coeffs = [c for _, c in a_terms]
+        diag, widths, cols, vals = [], [], [], []
+        for m, _ in a_terms:
+            dg = m.diagonal()
+            diag.append(dg)
+            W, col, val = ell_block(m - sp.diags(dg, format="csr"))
+            widths.append(W)
+            cols.append(col)
+            vals.append(val)
+        self.a_width = widths
+        # collapse operators: the all-diagonal ones first (constant before time-dependent),
+        # then ELL blocks of the others
+        def rank(i):
+            m, f = c_terms[i]
+            return (0 if f is None else 1) if _is_diagonal(m) else 2
+        order = sorted(range(len(c_terms)), key=rank)
+        self.c_terms = [(sp.csr_matrix(c_terms[i][0], dtype=np.complex128), c_terms[i][1])
+                        for i in order]
+        self.c_order = order
+        self.n_cops = len(order)
+        self.n_diag_cops = sum(1 for m, _ in self.c_terms if _is_diagonal(m))
+        cdiag = [m.diagonal() for m, _ in self.c_terms[:self.n_diag_cops]]
+        cw, ccols, cvals = [], [], []
+        for m, _ in self.c_terms[self.n_diag_cops:]:
+            W, col, val = ell_block(m)
+            cw.append(W)
+            ccols.append(col)
+            cvals.append(val)
+        self.c_width = cw
+        if sum(widths) * d >= 2**31 or sum(cw) * d >= 2**31:
+            raise ValueError("ELL storage beyond 2^31 entries")
         P = DeviceOperator.PAD
-        if mats:
-            rps, off = [], 0
-            for m in mats:
-                rps.append(m.indptr.astype(np.int64) + off)
-                off += m.nnz
-            rp = np.concatenate(rps)
-            if rp[-1] >= 2**31 - 16:
-                raise ValueError("collapse operators beyond 2^31 entries")
-            self.c_row_ptr = torch.from_numpy(rp.astype(np.int32)).to(self.device)
-            col = np.concatenate([m.indices.astype(np.int32) for m in mats] + [np.zeros(P, np.int32)])
-            val = np.concatenate([m.data for m in mats] + [np.zeros(P, np.complex128)])
-            self.c_col = torch.from_numpy(col).to(self.device)
-            self.c_val = torch.from_numpy(val).to(self.device, _TORCH[dtype])
-        else:
-            self.c_row_ptr = self.c_col = self.c_val = None
-        if any(c is not None for c in self.c_coeffs):
-            code, starts, consts = pack_programs(self.c_coeffs)
-            self.c_code = torch.from_numpy(code).to(self.device)
-            self.c_start = torch.from_numpy(starts).to(self.device)
-            self.c_consts = torch.from_numpy(consts).to(self.device)
-        else:
-            self.c_code = self.c_start = self.c_consts = None
+        dev = self.device
+
+        def up(arrs, np_dt, t_dt):
+            a = np.concatenate(arrs + [np.zeros(P, np_dt)]) if arrs else np.zeros(P, np_dt)
+            return torch.from_numpy(a.astype(np_dt)).to(dev, t_dt)
+        self.a_diag = up(diag, np.complex128, tdt)
+        self.a_col = up(cols, np.int32, torch.int32)
+        self.a_val = up(vals, np.complex128, tdt)
+        self.c_diag = up(cdiag, np.complex128, tdt)
+        self.c_col = up(ccols, np.int32, torch.int32)
+        self.c_val = up(cvals, np.complex128, tdt)
+        self.c_coeffs = [c for _, c in self.c_terms]
+        # constant diagonal part D0(r, c) at r + c*d, precomputed once
+        self.a_diag_const = 0
+        for g, (m, c) in enumerate(a_terms):
+            if c is None and np.any(diag[g] != 0):
+                self.a_diag_const |= 1 << g
+        self.n_const_diag = sum(1 for m, c in self.c_terms[:self.n_diag_cops] if c is None)
+        self.d_const = None
+        if self.a_diag_const or self.n_const_diag:
+            self.d_const = self._constant_diagonal(diag, cdiag).to(tdt)
+        self._a_prog = self._programs(self.a_coeffs)
+        self._c_prog = self._programs(self.c_coeffs)
+        self.coeffs = self.a_coeffs + self.c_coeffs
+        self.stored = sum(widths) * d + sum(cw) * d
         self.struct = self._make_struct()
 
+    def _constant_diagonal(self, a_diag, c_diag):
+        """D0 as a (d, d) tensor M with M[c, r] = D0(r, c), i.e. vec order r + c*d."""
+        d, dev = self.d, self.device
+        a = np.zeros(d, dtype=np.complex128)
+        for g in range(len(a_diag)):
+            if (self.a_diag_const >> g) & 1:
+                a += a_diag[g]
+        av = torch.from_numpy(a).to(dev)
+        M = av[None, :] + av.conj()[:, None]
+        if self.n_const_diag:
+            V = torch.from_numpy(np.stack(c_diag[:self.n_const_diag])).to(dev)  # (m, d)
+            M = M + V.conj().T @ V     # [c, r] = sum_i conj(v_i[c]) v_i[r]
+        return M.reshape(-1)
+
+    def _programs(self, coeffs):
+        if all(c is None for c in coeffs):
+            return (None, None, None)
+        code, starts, consts = pack_programs(coeffs)
+        return tuple(torch.from_numpy(a).to(self.device) for a in (code, starts, consts))
+
     def _make_struct(self) -> _lib.Lindblad:
-        a = self.a
-        d = self.d
-        a_s = _lib.CsrGroups(d, d, a.n_groups, _QG[self.dtype], _lib.QG_LAYOUT_ROW_MAJOR,
-                             1, 0, 0, _ptr(a.row_ptr), _ptr(a.col), _ptr(a.val), None,
-                             _ptr(a.coef_code), _ptr(a.coef_start), _ptr(a.coef_consts))
-        c_s = _lib.CsrGroups(d, d, self.n_cops, _QG[self.dtype], _lib.QG_LAYOUT_GROUP_MAJOR, 1, 0,
-                             0, _ptr(self.c_row_ptr), _ptr(self.c_col), _ptr(self.c_val), None,
-                             _ptr(self.c_code), _ptr(self.c_start), _ptr(self.c_consts))
-        return _lib.Lindblad(d, a_s, c_s)
+        st = _lib.Lindblad()
+        st.d = self.d
+        st.dtype = _QG[self.dtype]
+        st.n_groups = len(self.a_terms)
+        st.n_diag_cops = self.n_diag_cops
+        st.n_cops = self.n_cops
+        st.a_diag_const = self.a_diag_const
+        st.n_const_diag = self.n_const_diag
+        st.d_const = _ptr(self.d_const)
+        for g, w in enumerate(self.a_width):
+            st.a_width[g] = w
+        for i, w in enumerate(self.c_width):
+            st.c_width[i] = w
+        st.a_diag, st.a_col, st.a_val = _ptr(self.a_diag), _ptr(self.a_col), _ptr(self.a_val)
+        st.c_diag, st.c_col, st.c_val = _ptr(self.c_diag), _ptr(self.c_col), _ptr(self.c_val)
+        st.a_coef_code, st.a_coef_start, st.a_coef_consts = (_ptr(v) for v in self._a_prog)
+        st.c_coef_code, st.c_coef_start, st.c_coef_consts = (_ptr(v) for v in self._c_prog)
+        return st
 
     # -- constructors -------------------------------------------------------
     @classmethod
@@ -126,7 +209,7 @@ class LindbladOperator:
     # -- properties ---------------------------------------------------------
     @property
     def n_groups(self) -> int:
-        return self.a.n_groups
+        return len(self.a_terms)
 
     @property
     def isconstant(self) -> bool:
@@ -145,7 +228,7 @@ class LindbladOperator:
 
     def value_bytes(self) -> int:
         es = 16 if self.dtype == "c128" else 8
-        return (self.a.stored + sum(self.c_nnz)) * (es + 4)
+        return self.stored * (es + 4) + (self.n_groups + self.n_diag_cops) * self.d * es
 
     def state_bytes(self) -> int:
         """Bytes of one vec(rho) in the stage dtype."""

@@ -47,14 +47,28 @@ def test_host_struct_layout():
     s = S.ising_chain(3)
     lop = LindbladOperator.from_hamiltonian(s.h_terms, s.c_ops, dtype="c64", device="cpu")
     st = lop.struct
-    assert st.d == 8
-    assert st.a.layout == _lib.QG_LAYOUT_ROW_MAJOR and st.a.n_tiles == 0
-    assert st.a.n_rows == st.a.n_cols == 8 and st.a.dtype == _lib.QG_C64
-    assert st.a.n_groups == 2 and st.a.coef_code  # constant group + cos(w t) group
-    assert st.cops.layout == _lib.QG_LAYOUT_GROUP_MAJOR and st.cops.n_groups == 6
-    assert not st.cops.coef_code                    # constant collapse operators
-    rp = lop.c_row_ptr.numpy()
-    assert len(rp) == 6 * 9 and rp[-1] == sum(lop.c_nnz)
+    assert st.d == 8 and st.dtype == _lib.QG_C64
+    # H_nh: a diagonal constant group (zz couplings, c^dag c) and the driven sx group
+    assert st.n_groups == 2 and sorted(st.a_width[:2]) == [0, 3]
+    assert st.a_coef_code and not st.c_coef_code
+    # sz dephasing is diagonal, s- is one entry per row
+    assert st.n_cops == 6 and st.n_diag_cops == 3 and list(st.c_width[:3]) == [1, 1, 1]
+    assert lop.a_col.numel() == 3 * 8 + 8 and lop.c_val.numel() == 3 * 8 + 8
+
+
+def test_ell_block_layout():
+    from qutip_gb300.lindblad import ell_block
+    rng = np.random.default_rng(2)
+    m = sp.random(13, 13, density=0.3, random_state=rng, format="csr")
+    m.data = m.data + 1j
+    W, col, val = ell_block(m)
+    assert W == np.diff(m.indptr).max()
+    back = np.zeros((13, 13), dtype=complex)
+    for j in range(W):
+        for r in range(13):
+            back[r, col[j * 13 + r]] += val[j * 13 + r]
+    np.testing.assert_allclose(back, m.toarray())
+    assert np.all((col >= 0) & (col < 13))
 
 
 def test_host_rejects_bad_operators():
@@ -115,3 +129,70 @@ def test_oracle_matrix_form_solver_matches_the_superoperator_solver():
     rho0 = s.state0.reshape(s.dim, s.dim, order="F")
     got = mesolve_matrix_form(s.h_terms, [(c, None) for c in s.c_ops], rho0, tl, s.e_ops)
     np.testing.assert_allclose(got, want, atol=1e-7)
+
+
+def _emulate_kernel(lop, x, t):
+    """The element formula of the matrix-free kernel, read from the arrays it reads with
+    its indexing (ELL entry j of row r at base + j*d + r)."""
+    d = lop.d
+    ca = [1.0 if c is None else c(t) for c in lop.a_coeffs]
+    wc = [1.0 if c is None else abs(c(t)) ** 2 for c in lop.c_coeffs]
+    adiag, acol, aval = lop.a_diag.numpy(), lop.a_col.numpy(), lop.a_val.numpy()
+    cdiag, ccol, cval = lop.c_diag.numpy(), lop.c_col.numpy(), lop.c_val.numpy()
+    ND = lop.n_diag_cops
+    dconst = None if lop.d_const is None else lop.d_const.numpy()
+    st = lop.struct
+    out = np.zeros(d * d, dtype=complex)
+    for idx in range(d * d):
+        c, r = divmod(idx, d)
+        D = dconst[idx] if dconst is not None else 0.0
+        D += sum(k * adiag[g * d + r] + np.conj(k * adiag[g * d + c])
+                 for g, k in enumerate(ca) if not (st.a_diag_const >> g) & 1)
+        D += sum(wc[i] * cdiag[i * d + r] * np.conj(cdiag[i * d + c])
+                 for i in range(st.n_const_diag, ND))
+        acc = D * x[idx]
+        base = 0
+        for g, k in enumerate(ca):
+            W = lop.a_width[g]
+            for j in range(W):
+                e = base + j * d
+                acc += k * aval[e + r] * x[acol[e + r] + c * d]
+                acc += np.conj(k * aval[e + c]) * x[r + acol[e + c] * d]
+            base += W * d
+        base = 0
+        for i, W in enumerate(lop.c_width):
+            for q in range(W):
+                for p in range(W):
+                    b, v = cval[base + q * d + c], cval[base + p * d + r]
+                    kc, kr = ccol[base + q * d + c], ccol[base + p * d + r]
+                    acc += wc[ND + i] * v * np.conj(b) * x[kr + kc * d]
+            base += W * d
+        out[idx] = acc
+    return out
+
+
+def test_layout_reproduces_the_generator():
+    """Walking the device arrays as the kernel does gives the superoperator's matvec:
+    a random generator with ragged rows, time-dependent groups and collapse operators,
+    diagonal and non-diagonal collapse operators and an empty one."""
+    from qutip_gb300.coefficients import coefficient
+    from qutip_gb300.lindblad import LindbladOperator
+    rng = np.random.default_rng(7)
+    d = 9
+
+    def rand(density):
+        m = sp.random(d, d, density=density, random_state=rng, format="csr")
+        m.data = rng.normal(size=m.nnz) + 1j * rng.normal(size=m.nnz)
+        return m
+    h0, h1 = rand(0.3), rand(0.2)
+    cops = [(rand(0.2), None), (sp.diags(rng.normal(size=d)).tocsr(), coefficient("0.5+0.1*t")),
+            (sp.csr_matrix((d, d), dtype=complex), None), (rand(0.1), coefficient("cos(t)"))]
+    lop = LindbladOperator.from_hamiltonian([(h0 + h0.conj().T, None),
+                                             (h1 + h1.conj().T, coefficient("sin(2*t)"))],
+                                            cops, device="cpu")
+    assert lop.n_diag_cops == 2            # the diagonal one and the empty one
+    assert lop.n_const_diag == 1 and lop.d_const is not None
+    x = rng.normal(size=d * d) + 1j * rng.normal(size=d * d)
+    for t in (0.0, 0.9):
+        want = _kron_generator(lop.a_terms, lop.c_terms, t) @ x
+        np.testing.assert_allclose(_emulate_kernel(lop, x, t), want, atol=1e-12)
