@@ -60,15 +60,18 @@ def parse():
                     help="simulated time of the CPU-baseline sample (of 10.0)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline workload only")
-    ap.add_argument("--sections", default="served,mc,large",
-                    help="extra sections after the headline (comma list of served, mc, large)")
+    ap.add_argument("--sections", default="served,mc,matrix,large",
+                    help="extra sections after the headline (comma list of served, mc, "
+                         "matrix, large)")
+    ap.add_argument("--matrix-sites", type=int, default=13,
+                    help="spins of the short matrix-form solve in the matrix section (0: skip)")
     ap.add_argument("--served-jobs", type=int, default=10000)
     ap.add_argument("--served-ntraj", type=int, default=100)
     ap.add_argument("--served-plain-sample", type=int, default=60)
     ap.add_argument("--mc-ntraj", type=int, default=4096)
     ap.add_argument("--large-sites", type=int, default=12,
                     help="Ising chain length of the large mixed-precision section (0: skip)")
-    ap.add_argument("--profile", default=None, choices=["stage", "batch"],
+    ap.add_argument("--profile", default=None, choices=["stage", "batch", "matrix"],
                     help="run the ncu profiling case only (fused stage kernel, untuned); "
                          "prints nothing to parse")
     ap.add_argument("--profile-sites", type=int, default=10)
@@ -228,14 +231,18 @@ def run_reference(args, dist):
 
 # ------------------------------------------------------------------ ours ----
 def stage_bytes(op, n, stage, mixed):
-    """Algorithmic HBM bytes of one fused Vern7 stage launch: operator entries and row
-    structure, the gathered input read once, k_s written, and the vectors the stage
-    combination reads and writes (earlier k_j, the base state, the next stage input)."""
+    """Algorithmic HBM bytes of one fused Vern7 stage launch: the operator (superoperator
+    entries and row structure, or the matrix-free generator's small operators and its
+    constant diagonal factor), the input read once, k_s written, and the vectors the
+    stage combination reads and writes (earlier k_j, the base state, the next input)."""
     from qutip_gb300 import vern7_tableau as T
     sk = op.value_bytes()                       # stage dtype (k, ytmp, x)
     base = 8 if mixed else 16                   # y_prev_s (mixed) or y_prev
-    b = op.nnz * (sk + 4) + (op.n_groups * n + 1) * 4  # operator entries + row structure
-    b += n * sk                                 # gathered x, read once
+    if getattr(op, "fmt", "") == "lindblad":
+        b = op.operator_bytes()
+    else:
+        b = op.nnz * (sk + 4) + (op.n_groups * n + 1) * 4  # operator entries + row structure
+    b += n * sk                                 # x, read once
     b += n * sk                                 # k_s written
     if stage == T.RK_STEP - 1:
         used = [j for j in range(stage) if T.B[j] != 0 or T.E[j] != 0]
@@ -276,15 +283,13 @@ def measure_stage_roofline(op, sysm, precision, reps=20):
     for _ in range(2):
         ig._compute_step(ig.dt_safe)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    lib = _lib.load()
     rk = ig._rk()
     sp_ = stream_ptr()
     torch.cuda.synchronize()
     e0.record(st)
     for _ in range(reps):
         for s in range(10):
-            _lib.check(lib.qg_vern7_stage(C.byref(op.struct), C.byref(rk), s, 0.0, ig.dt_safe,
-                                          ig.atol, ig.rtol, sp_))
+            op.vern7_stage(rk, s, 0.0, ig.dt_safe, ig.atol, ig.rtol, sp_)
     e1.record(st)
     e1.synchronize()
     ms = e0.elapsed_time(e1) / (reps * 10)
@@ -529,6 +534,66 @@ def run_large(args):
     return out
 
 
+def run_matrix_form(args, sysm, tlist, ex, ref, hbm_peak):
+    """The headline workload through mesolve's matrix form (``matrix_form=True``): the
+    Lindblad generator applied to vec(rho) without its superoperator
+    (:class:`qutip_gb300.lindblad.LindbladOperator`), mixed precision.  Reported: solves/s,
+    the error against the complex128 superoperator solve, the fused stage kernel's time
+    and algorithmic bytes, and a short solve at ``--matrix-sites`` spins (default 13,
+    67,108,864 vec(rho) entries), a size whose superoperator (about 1.9e9 entries) is
+    beyond 32-bit indices."""
+    import torch
+    from qutip_gb300 import systems as S
+    from qutip_gb300.lindblad import LindbladOperator
+    from qutip_gb300.solver import ExpectOps, solve_system
+    lop = LindbladOperator.from_hamiltonian(sysm.h_terms, sysm.c_ops, dtype="c64")
+    opts = {"precision": "mixed", "matrix_form": True}
+    solve_system(sysm, tlist, opts, op=lop, ex=ex)      # warm-up
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = solve_system(sysm, tlist, opts, op=lop, ex=ex)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    err = max(float(np.max(np.abs(res.expect[k] - ref.expect[k]))) for k in range(len(ex.ops)))
+    ms, b, gbs = measure_stage_roofline(lop, sysm, "mixed")
+    out = {"workload": f"ising_chain_L{N_SITES} mesolve matrix_form=True, mixed, tlist "
+                       f"linspace(0,{T_END:g},{N_OUT})",
+           "solves_per_sec": 1.0 / float(np.median(times)),
+           "max_abs_err_vs_fp64_superoperator": err,
+           "stage_kernel": {"kernel": "lindblad_kernel<C64,C128,RK>", "ms": ms,
+                            "algorithmic_bytes": int(b), "gbs": gbs, "frac_hbm": gbs / hbm_peak,
+                            "bound": "instruction issue (operators L1-resident, state "
+                                     "L2-resident; HBM carries only the stage vectors)"},
+           "operator_bytes": int(lop.operator_bytes()),
+           "solver_stats": {k: res.stats[k] for k in ("steps", "rejected", "rhs")}}
+    del lop
+    L = args.matrix_sites
+    if L:
+        s = S.ising_chain(L, build_terms=False)
+        tl = np.linspace(0.0, 0.05, 3)
+        t0 = time.perf_counter()
+        big = LindbladOperator.from_hamiltonian(s.h_terms, s.c_ops, dtype="c64")
+        exb = ExpectOps(s.e_ops)
+        torch.cuda.synchronize()
+        build_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        rb = solve_system(s, tl, opts, op=big, ex=exb)
+        torch.cuda.synchronize()
+        run_s = time.perf_counter() - t0
+        bms, bb, bgbs = measure_stage_roofline(big, s, "mixed", reps=2)
+        out["large"] = {"workload": f"ising_chain_L{L} mesolve matrix_form=True, mixed, "
+                                    "tlist linspace(0,0.05,3)",
+                        "vec_rho_entries": big.n_rows, "build_s": build_s, "solve_s": run_s,
+                        "rhs_calls": int(rb.stats["rhs"]), "stage_ms": bms,
+                        "stage_gbs": bgbs, "device_gb": torch.cuda.max_memory_allocated() / 1e9,
+                        "sz0_at_t_end": float(np.real(rb.expect[0][-1]))}
+        del big, exb
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args, dist):
     import torch
     from qutip_gb300 import _lib
@@ -638,6 +703,9 @@ def run_ours(args, dist):
     if dist.rank == 0 and "mc" in sections:
         log("batched mcsolve")
         out["mc_batched"] = run_mc_batch(args)
+    if dist.rank == 0 and "matrix" in sections:
+        log("matrix form")
+        out["matrix_form"] = run_matrix_form(args, sysm, tlist, ex, ref, hbm_peak)
     if dist.rank == 0 and "large" in sections and args.large_sites:
         log(f"large: Ising L={args.large_sites}")
         out["large"] = run_large(args)
@@ -672,6 +740,26 @@ def run_profile_case(args):
     print(f"c64 mixed: launch {op.launch_desc()}, {op.spmv_bytes() / 1e9:.3f} GB per matvec")
 
 
+def run_profile_matrix(args):
+    """ncu case for the matrix-free Lindblad stage kernel: the Ising chain with
+    ``--profile-sites`` spins (default 10: vec(rho) of 1,048,576 entries, stage vectors
+    larger than L2 taken together), mixed form; first-step estimate (2 applications),
+    then two Vern7 steps of 10 fused stage launches each."""
+    import torch
+    from qutip_gb300 import systems as S
+    from qutip_gb300.lindblad import LindbladOperator
+    from qutip_gb300.vern7 import GpuVern7
+    torch.cuda.set_device(0)
+    s = S.ising_chain(args.profile_sites, build_terms=False)
+    op = LindbladOperator.from_hamiltonian(s.h_terms, s.c_ops, dtype="c64")
+    ig = GpuVern7(op, precision="mixed")
+    ig.set_initial_value(torch.from_numpy(s.state0).cuda(), 0.0)
+    for _ in range(2):
+        ig.integrate(ig.t_front + 0.05, step=True)
+    torch.cuda.synchronize()
+    print(f"matrix form: {op.launch_desc()}, {op.operator_bytes() / 1e6:.1f} MB generator")
+
+
 def run_profile_batch(args):
     """ncu case for the batched trajectory kernel: ``--profile-ntraj`` Bose-Hubbard
     trajectories (default 256) over t in [0, ``--profile-tend``] (default 5, 10
@@ -695,6 +783,9 @@ def main():
         return
     if args.profile == "batch":
         run_profile_batch(args)
+        return
+    if args.profile == "matrix":
+        run_profile_matrix(args)
         return
     dist = Dist(args.gpus)
     if args.impl == "reference":

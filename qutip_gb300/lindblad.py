@@ -227,12 +227,15 @@ class LindbladOperator:
         return self.launch
 
     def value_bytes(self) -> int:
-        es = 16 if self.dtype == "c128" else 8
-        return self.stored * (es + 4) + (self.n_groups + self.n_diag_cops) * self.d * es
+        """Bytes of one value in the stage dtype."""
+        return 16 if self.dtype == "c128" else 8
 
-    def state_bytes(self) -> int:
-        """Bytes of one vec(rho) in the stage dtype."""
-        return self.n_rows * (16 if self.dtype == "c128" else 8)
+    def operator_bytes(self) -> int:
+        """Bytes of the generator's storage: ELL blocks, diagonals and the precomputed
+        constant diagonal factor (d*d values)."""
+        es = self.value_bytes()
+        b = self.stored * (es + 4) + (self.n_groups + self.n_diag_cops) * self.d * es
+        return b + (self.n_rows * es if self.d_const is not None else 0)
 
     # -- application --------------------------------------------------------
     def matvec(self, t: float, x: torch.Tensor, y: torch.Tensor, alpha=1.0, beta=0.0):
