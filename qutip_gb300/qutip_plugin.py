@@ -557,20 +557,49 @@ class IntegratorGpuVern7(Integrator):
             raise ValueError("precision must be 'double' or 'mixed'")
         dt = "c128" if prec == "double" else "c64"
         rhs = self._rhs()
+        self._terms = None
         if _is_matrix_form(rhs):
             self._op = lindblad_operator(rhs, dt)
         else:
-            self._op = DeviceOperator(qobjevo_terms(rhs), dtype=dt, device=_device())
-        self._ode = GpuVern7(self._op, atol=self._options["atol"], rtol=self._options["rtol"],
-                             nsteps=self._options["nsteps"],
-                             first_step=self._options["first_step"],
-                             min_step=self._options["min_step"],
-                             max_step=self._options["max_step"],
-                             interpolate=self._options["interpolate"], precision=prec)
+            self._terms = qobjevo_terms(rhs)
+            self._op = DeviceOperator(self._terms, dtype=dt, device=_device())
+        self._blocks = {1: self._op}
+        self._ode = self._integrator(self._op)
         self._shape = (self._op.n_rows, 1)
         self.name = f"{self.method} ({prec})"
 
+    def _integrator(self, op):
+        o = self._options
+        return GpuVern7(op, atol=o["atol"], rtol=o["rtol"], nsteps=o["nsteps"],
+                        first_step=o["first_step"], min_step=o["min_step"],
+                        max_step=o["max_step"], interpolate=o["interpolate"],
+                        precision=o["precision"])
+
+    def _block_operator(self, m):
+        """``I_m (x) A(t)``: the generator applied to each of the m columns of an
+        operator-valued state (``propagator``'s identity, qutip/solver/propagator.py:201-213,
+        evolved as ``rhs.matmul_data`` does on a matrix)."""
+        if m not in self._blocks:
+            if self._terms is None:
+                raise ValueError("operator-valued states are not supported with matrix_form")
+            eye = sp.identity(m, format="csr", dtype=np.complex128)
+            dt = "c128" if self._options["precision"] == "double" else "c64"
+            self._blocks[m] = DeviceOperator([(sp.kron(eye, a, format="csr"), c)
+                                              for a, c in self._terms], dtype=dt,
+                                             device=_device())
+        return self._blocks[m]
+
     def set_state(self, t, state0):
+        rows, cols = state0.shape
+        if rows * cols == self._op.n_rows:
+            op = self._op                      # a vector, or rho of the matrix form
+        elif rows == self._op.n_rows:
+            op = self._block_operator(cols)    # an operator-valued state, column by column
+        else:
+            raise ValueError(f"state of shape {state0.shape} for a generator of size "
+                             f"{self._op.n_rows}")
+        if self._ode.op is not op:
+            self._ode = self._integrator(op)
         self._ode.set_initial_value(_as_gpu(state0).buf, t)
         self._shape = state0.shape
         self._is_set = True

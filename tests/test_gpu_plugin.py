@@ -253,3 +253,33 @@ def test_mcsolve_gpu_map_improved_sampling_mixed_dark(qt, plugin):
     _same_jumps(_records(got), _records(ref))
     for g, w in zip(got.expect, ref.expect):
         np.testing.assert_allclose(np.asarray(g), np.asarray(w), atol=2e-6)
+
+
+def test_propagator_open_and_unitary(qt, plugin):
+    """``propagator`` (qutip/solver/propagator.py:183-213) evolves the identity as an
+    operator-valued state: the superoperator with collapse operators, and the unitary
+    (sesolve) without; the ``Propagator`` class steps it through solver.start/step."""
+    N = 4
+    a = qt.tensor(qt.destroy(N), qt.qeye(2))
+    sm = qt.tensor(qt.qeye(N), qt.sigmam())
+    H = [2 * np.pi * a.dag() * a + np.pi * sm.dag() * sm + 0.3 * (a.dag() * sm + a * sm.dag()),
+         [a + a.dag(), "0.2*cos(t)"]]
+    c_ops = [np.sqrt(0.1) * a, np.sqrt(0.05) * sm]
+    ts = [0.0, 0.5, 1.5]
+    for cops in (c_ops, None):
+        ref = qt.propagator(H, ts, cops, options={"method": "vern7"})
+        got = qt.propagator(H, ts, cops, options={"method": "gpu_vern7"})
+        assert len(got) == len(ref)
+        for g, r in zip(got, ref):
+            assert g.dims == r.dims
+            np.testing.assert_allclose(g.full(), r.full(), atol=1e-7)
+    Hevo = qt.QobjEvo(H)
+    P = qt.Propagator(Hevo, c_ops=c_ops, options={"method": "gpu_vern7"})
+    Pr = qt.Propagator(Hevo, c_ops=c_ops, options={"method": "vern7"})
+    for t in (1.2, 0.4):
+        np.testing.assert_allclose(P(t).full(), Pr(t).full(), atol=1e-7)
+    # sesolve from an operator initial state: the columns evolve independently
+    U = qt.sesolve(H, qt.qeye_like(a), [0, 1.0], options={"method": "gpu_vern7"}).states[-1]
+    psi0 = qt.tensor(qt.basis(N, 1), qt.basis(2, 0))
+    psi = qt.sesolve(H, psi0, [0, 1.0], options={"method": "gpu_vern7"}).states[-1]
+    np.testing.assert_allclose((U * psi0).full(), psi.full(), atol=1e-7)
