@@ -21,7 +21,7 @@ Importing this module (QuTiP must be importable) registers:
   ``wrmn_error``, ``adjoint``, ``conj`` and ``transpose`` stay on the device
   (torch element-wise kernels; they are not on the integration hot path).
 * :class:`IntegratorGpuVern7` as ``method="gpu_vern7"`` on ``MESolver``,
-  ``SESolver`` and ``MCSolver`` (``Solver.add_integrator``,
+  ``SESolver``, ``MCSolver`` and ``BRSolver`` (``Solver.add_integrator``,
   qutip/solver/solver_base.py:475-492).  It takes the solver
   (``rhs_format = "solver"``), turns its ``QobjEvo`` right-hand side into one
   device operator with device-evaluated coefficients, and integrates with the
@@ -54,6 +54,7 @@ from qutip.core.cy import coefficient as _cyc
 from qutip.core.data import CSR, Dense, Data, Dia
 from qutip.core.data import ode as _ode
 from qutip.solver.integrator import Integrator, IntegratorException
+from qutip.solver.brmesolve import BRSolver
 from qutip.solver.mcsolve import MCSolver
 from qutip.solver.mesolve import MESolver
 from qutip.solver.sesolve import SESolver
@@ -469,9 +470,22 @@ def device_coefficient(c) -> Coefficient:
 
 
 def qobjevo_terms(evo):
-    """``(scipy CSR, device Coefficient | None)`` terms of a QobjEvo or Qobj."""
+    """``(scipy CSR, device Coefficient | None)`` terms of a QobjEvo or Qobj.
+
+    A constant QobjEvo whose elements are not (operator, coefficient) pairs, e.g. a
+    Bloch-Redfield tensor built from special elements (qutip/solver/brmesolve.py:323-333),
+    becomes the single constant term ``evo(0)``, evaluated once by QuTiP itself."""
     if isinstance(evo, qutip.Qobj):
         return [(_scipy(evo.data), None)]
+    try:
+        return _decode_terms(evo)
+    except TypeError:
+        if evo.isconstant:
+            return [(_scipy(evo(0).data), None)]
+        raise
+
+
+def _decode_terms(evo):
     out = []
     for el in evo.to_list():
         if isinstance(el, qutip.Qobj):
@@ -848,7 +862,7 @@ def register():
     _data.adjoint.add_specialisations([(GpuDense, GpuDense, adjoint_gpu)])
     _data.conj.add_specialisations([(GpuDense, GpuDense, conj_gpu)])
     _data.transpose.add_specialisations([(GpuDense, GpuDense, transpose_gpu)])
-    for solver in (MESolver, SESolver, MCSolver):
+    for solver in (MESolver, SESolver, MCSolver, BRSolver):
         solver.add_integrator(IntegratorGpuVern7, "gpu_vern7")
     _parallel._maps["gpu"] = gpu_map
     _REGISTERED = True

@@ -283,3 +283,44 @@ def test_propagator_open_and_unitary(qt, plugin):
     psi0 = qt.tensor(qt.basis(N, 1), qt.basis(2, 0))
     psi = qt.sesolve(H, psi0, [0, 1.0], options={"method": "gpu_vern7"}).states[-1]
     np.testing.assert_allclose((U * psi0).full(), psi.full(), atol=1e-7)
+
+
+def test_brmesolve_constant_tensor(qt, plugin):
+    """brmesolve (qutip/solver/brmesolve.py:199-333) with ``method="gpu_vern7"``: the
+    Bloch-Redfield tensor of constant spectra runs as the device generator."""
+    N = 6
+    a = qt.destroy(N)
+    H = a.dag() * a + 0.25 * (a + a.dag())
+    a_ops = [[a + a.dag(), qt.coefficient("0.05 * (w > 0)", args={"w": 0})]]
+    c_ops = [np.sqrt(0.01) * a]
+    rho0 = qt.ket2dm(qt.basis(N, 3))
+    tl = np.linspace(0, 10, 41)
+    e_ops = [a.dag() * a, a + a.dag()]
+    ref = qt.brmesolve(H, rho0, tl, a_ops=a_ops, c_ops=c_ops, e_ops=e_ops,
+                       options={"method": "vern7", "progress_bar": None})
+    got = qt.brmesolve(H, rho0, tl, a_ops=a_ops, c_ops=c_ops, e_ops=e_ops,
+                       options={"method": "gpu_vern7", "progress_bar": None})
+    for g, r in zip(got.expect, ref.expect):
+        np.testing.assert_allclose(g, r, atol=1e-8, rtol=1e-6)
+
+
+def test_mcsolve_gpu_map_target_tol(qt, plugin):
+    """``target_tol`` (multitrajresult.py:320-361): the reference's reduce step estimates
+    the trajectories still needed and stops the map; the batched launch hands its
+    trajectories over in seed order and stops at the same count."""
+    N = 6
+    a = qt.tensor(qt.destroy(N), qt.qeye(2))
+    sm = qt.tensor(qt.qeye(N), qt.sigmam())
+    sz = qt.tensor(qt.qeye(N), qt.sigmaz())
+    H = 2 * np.pi * (a.dag() * a + sz / 2) + 2 * np.pi * 0.05 * (a * sm.dag() + a.dag() * sm)
+    c_ops = [np.sqrt(0.05) * a, np.sqrt(0.2) * sm]
+    psi0 = qt.tensor(qt.basis(N, 2), qt.basis(2, 0))
+    tl = np.linspace(0, 10, 51)
+    opts = {"method": "vern7", "map": "serial", "progress_bar": None}
+    kw = dict(e_ops=[a.dag() * a, sz], ntraj=300, seeds=3, target_tol=0.12)
+    ref = qt.mcsolve(H, psi0, tl, c_ops, options=opts, **kw)
+    got = qt.mcsolve(H, psi0, tl, c_ops, options={**opts, "method": "gpu_vern7", "map": "gpu"},
+                     **kw)
+    assert got.num_trajectories == ref.num_trajectories < 300
+    for g, w in zip(got.expect, ref.expect):
+        np.testing.assert_allclose(np.asarray(g), np.asarray(w), atol=2e-6)
