@@ -577,6 +577,8 @@ __global__ void __launch_bounds__(LB_BLOCK)
   const ST* __restrict__ cval = static_cast<const ST*>(L.c_val);
   const int dmask = L.a_diag_const;
   const int nd0 = L.n_const_diag;
+  int nw1 = 0;  // leading general collapse operators of width 1
+  while (nw1 < NE && L.c_width[nw1] == 1) ++nw1;
   R err_acc = 0;
   // (r, c) of idx, advanced by the grid stride without a division per element
   const int stride = gridDim.x * LB_BLOCK;
@@ -627,21 +629,33 @@ __global__ void __launch_bounds__(LB_BLOCK)
       acc.im += k.re * li + k.im * lr + k.re * qi - k.im * qr;
       base += W * d;
     }
-    // general collapse operators: C rho C^dag
+    // general collapse operators: C rho C^dag.  The leading width-1 operators (s-, a, ...)
+    // run branch-free in complex64 (a padding entry has value 0 and a valid column), so
+    // the gathers of several operators are in flight at once: 56 -> 48 us per stage at
+    // L = 10.  The FP64-bound complex128 form skips padding instead.
     base = 0;
-    for (int i = 0; i < NE; ++i) {
+    int i = 0;
+#pragma unroll 4
+    for (; i < nw1; ++i) {
+      const R w = wc[ND + i];
+      const int er = base + r, ec = base + c;
+      const ST b = __ldg(cval + ec), v = __ldg(cval + er);
+      if constexpr (DT == QG_C128) {  // FP64-bound: skip padding rather than multiply by 0
+        if ((b.x == (R)0 && b.y == (R)0) || (v.x == (R)0 && v.y == (R)0)) {
+          base += d;
+          continue;
+        }
+      }
+      const ST xv = ld_gather(x + (__ldg(ccol + er) + __ldg(ccol + ec) * d));
+      const R pr = w * (v.x * b.x + v.y * b.y), pi = w * (v.y * b.x - v.x * b.y);  // w v conj(b)
+      acc.re += pr * xv.x - pi * xv.y;
+      acc.im += pr * xv.y + pi * xv.x;
+      base += d;
+    }
+    for (; i < NE; ++i) {
       const int W = L.c_width[i];
       const R w = wc[ND + i];
-      if (W == 1) {  // one entry per row (s-, a, ...): no inner loops
-        const ST b = __ldg(cval + base + c), v = __ldg(cval + base + r);
-        if ((b.x != (R)0 || b.y != (R)0) && (v.x != (R)0 || v.y != (R)0)) {
-          const ST xv = ld_gather(x + (__ldg(ccol + base + r) + __ldg(ccol + base + c) * d));
-          // w v conj(b) x
-          const R pr = w * (v.x * b.x + v.y * b.y), pi = w * (v.y * b.x - v.x * b.y);
-          acc.re += pr * xv.x - pi * xv.y;
-          acc.im += pr * xv.y + pi * xv.x;
-        }
-      } else if (W > 1) {
+      if (W > 0) {
         R sr2 = 0, si2 = 0;
         for (int q = 0; q < W; ++q) {
           const int eq = base + q * d + c;

@@ -107,8 +107,10 @@ class LindbladOperator:
         # then ELL blocks of the others
         def rank(i):
             m, f = c_terms[i]
-            return (0 if f is None else 1) if _is_diagonal(m) else 2
-        order = sorted(range(len(c_terms)), key=rank)
+            if _is_diagonal(m):
+                return 0 if f is None else 1
+            return 2 if np.diff(sp.csr_matrix(m).indptr).max() == 1 else 3
+        order = sorted(range(len(c_terms)), key=rank)   # width-1 general operators lead
         self.c_terms = [(sp.csr_matrix(c_terms[i][0], dtype=np.complex128), c_terms[i][1])
                         for i in order]
         self.c_order = order
