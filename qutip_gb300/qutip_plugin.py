@@ -641,7 +641,11 @@ class IntegratorGpuVern7(Integrator):
     def reset(self, hard=False):
         if self._is_set:
             state = self.get_state()
-        if hard:
+        # The device coefficient programs hold the args they were decoded with, while the
+        # reference's integrators read the rhs live: Solver._argument follows
+        # rhs.arguments(args) with a soft reset (solver_base.py:457-460), so a
+        # time-dependent rhs is decoded again.
+        if hard or not getattr(self._rhs(), "isconstant", True):
             self._prepare()
         if self._is_set:
             self.set_state(*state)

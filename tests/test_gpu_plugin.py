@@ -324,3 +324,22 @@ def test_mcsolve_gpu_map_target_tol(qt, plugin):
     assert got.num_trajectories == ref.num_trajectories < 300
     for g, w in zip(got.expect, ref.expect):
         np.testing.assert_allclose(np.asarray(g), np.asarray(w), atol=2e-6)
+
+
+def test_new_args_reach_the_device_coefficients(qt, plugin):
+    """Solver.run(..., args=...) updates the rhs arguments and resets the integrator
+    (solver_base.py:457-460); the device coefficients follow the new args."""
+    N = 6
+    a = qt.destroy(N)
+    H = [a.dag() * a, [a + a.dag(), "amp * cos(2 * t)"]]
+    c_ops = [np.sqrt(0.1) * a]
+    rho0 = qt.ket2dm(qt.basis(N, 0))
+    tl = np.linspace(0, 3, 13)
+    e_ops = [a.dag() * a]
+    ref = qt.MESolver(qt.QobjEvo(H, args={"amp": 0.2}), c_ops, options={"method": "vern7"})
+    got = qt.MESolver(qt.QobjEvo(H, args={"amp": 0.2}), c_ops,
+                      options={"method": "gpu_vern7"})
+    for amp in (0.2, 0.7, 0.0):
+        r = ref.run(rho0, tl, args={"amp": amp}, e_ops=e_ops)
+        g = got.run(rho0, tl, args={"amp": amp}, e_ops=e_ops)
+        np.testing.assert_allclose(g.expect[0], r.expect[0], atol=1e-8, rtol=1e-6)
