@@ -238,10 +238,7 @@ def stage_bytes(op, n, stage, mixed):
     from qutip_gb300 import vern7_tableau as T
     sk = op.value_bytes()                       # stage dtype (k, ytmp, x)
     base = 8 if mixed else 16                   # y_prev_s (mixed) or y_prev
-    if getattr(op, "fmt", "") == "lindblad":
-        b = op.operator_bytes()
-    else:
-        b = op.nnz * (sk + 4) + (op.n_groups * n + 1) * 4  # operator entries + row structure
+    b = op.operator_bytes()                     # operator stream (entries, codes, tables)
     b += n * sk                                 # x, read once
     b += n * sk                                 # k_s written
     if stage == T.RK_STEP - 1:

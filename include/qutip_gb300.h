@@ -67,11 +67,24 @@ typedef enum {
  *   slice; entry j of group g of the row at lane l sits at
  *   row_ptr[s] + 32 * (sum_{g'<g} width_g') + 32 j + l.  Padding entries have
  *   value 0 and a valid column.  One thread per row; lanes and tile_nnz unused.
+ * QG_LAYOUT_SLICED_DICT (dictionary-coded sliced ELLPACK, for operators whose entries
+ *   repeat a few (column - row, value) pairs, as Kronecker-structured Liouvillians do):
+ *   32-row slices as above, but every stored entry is a code into its group's table:
+ *   code k of group g stands for column row + dict_off[dict_start[g] + k] and value
+ *   val[dict_start[g] + k] (val holds the tables, lanes = their total length, at most
+ *   QG_DICT_MAX); code 0 of every group is padding (offset 0, value 0).  col points to
+ *   the codes, tile_nnz bytes each (1 or 2).  Each group has its own code section:
+ *   row_ptr[g*(n_tiles+1) + s] is the code offset of slice s of group g (a multiple of
+ *   128), tile_row[s*G + g] its width (a multiple of 4), and codes are stored four per
+ *   lane: entries 4q..4q+3 of lane l of the slice at row_ptr[...] + 128 q + 4 l + (0..3).
+ *   Columns are clamped into [0, n_cols), so no code can address outside x.
  * Coefficient programs are the bytecode of qutip_gb300/coefficients.py;
  * coef_code == NULL means every c_g = 1. */
 #define QG_LAYOUT_GROUP_MAJOR 0
 #define QG_LAYOUT_ROW_MAJOR 1
 #define QG_LAYOUT_SLICED 2
+#define QG_LAYOUT_SLICED_DICT 3
+#define QG_DICT_MAX 4096
 #define QG_TILE_ROWS 512
 typedef struct qg_csr_groups {
   int64_t n_rows;
@@ -89,6 +102,8 @@ typedef struct qg_csr_groups {
   const int32_t* coef_code;
   const int32_t* coef_start; /* [n_groups+1] */
   const double* coef_consts; /* complex constants as (re, im) pairs */
+  const int32_t* dict_off;   /* QG_LAYOUT_SLICED_DICT: column - row of each table entry */
+  const int32_t* dict_start; /* QG_LAYOUT_SLICED_DICT: [n_groups+1] table bounds */
 } qg_csr_groups;
 
 /* Dia matrix in the reference's layout (qutip/core/data/dia.pxd:17-38):

@@ -17,7 +17,8 @@ QG_C128, QG_C64 = 0, 1
 QG_MAX_GROUPS, QG_MAX_EOPS, QG_MAX_COPS = 8, 32, 64
 
 
-QG_LAYOUT_GROUP_MAJOR, QG_LAYOUT_ROW_MAJOR, QG_LAYOUT_SLICED = 0, 1, 2
+QG_LAYOUT_GROUP_MAJOR, QG_LAYOUT_ROW_MAJOR, QG_LAYOUT_SLICED, QG_LAYOUT_SLICED_DICT = 0, 1, 2, 3
+QG_DICT_MAX = 4096
 QG_TILE_ROWS = 512
 QG_GROUP_AUTO, QG_GROUP_WARP, QG_GROUP_CTA, QG_GROUP_CLUSTER, QG_GROUP_CTA128 = 0, 1, 2, 3, 4
 
@@ -28,7 +29,8 @@ class CsrGroups(C.Structure):
                 ("n_tiles", C.c_int32), ("tile_nnz", C.c_int32), ("row_ptr", C.c_void_p),
                 ("col", C.c_void_p), ("val", C.c_void_p), ("tile_row", C.c_void_p),
                 ("coef_code", C.c_void_p), ("coef_start", C.c_void_p),
-                ("coef_consts", C.c_void_p)]
+                ("coef_consts", C.c_void_p), ("dict_off", C.c_void_p),
+                ("dict_start", C.c_void_p)]
 
 
 class Lindblad(C.Structure):

@@ -219,6 +219,19 @@ def coefficient(base, args: Mapping | None = None) -> Coefficient:
     raise TypeError(f"cannot evaluate a coefficient of type {type(base).__name__} on the device")
 
 
+def _cpow(a: complex, b: complex) -> complex:
+    """a ** b as the device interpreter evaluates it (``eval_coef``): real pow for a real
+    base and exponent when the base is positive or the exponent an integer (0 ** -k is
+    inf), 0 for any other zero base, exp(b log a) otherwise."""
+    if a.imag == 0.0 and b.imag == 0.0 and (a.real > 0.0 or b.real == math.floor(b.real)):
+        if a.real == 0.0 and b.real < 0.0:
+            return complex(math.inf)
+        return complex(a.real ** b.real)
+    if a == 0:
+        return 0j
+    return cmath.exp(b * cmath.log(a))
+
+
 def _run(code, consts, t):
     st: list[complex] = []
     i = 0
@@ -244,9 +257,18 @@ def _run(code, consts, t):
             st.append(complex(un[op](st.pop())))
         else:
             b, a = st.pop(), st.pop()
-            st.append({O["ADD"]: a + b, O["SUB"]: a - b, O["MUL"]: a * b,
-                       O["DIV"]: a / b if b != 0 else complex("nan"),
-                       O["POW"]: a ** b}[op])
+            if op == O["ADD"]:
+                st.append(a + b)
+            elif op == O["SUB"]:
+                st.append(a - b)
+            elif op == O["MUL"]:
+                st.append(a * b)
+            elif op == O["DIV"]:
+                st.append(a / b if b != 0 else complex("nan"))
+            elif op == O["POW"]:
+                st.append(_cpow(a, b))
+            else:
+                raise ValueError(f"unknown opcode {op}")
         i += 1
     return st[-1]
 

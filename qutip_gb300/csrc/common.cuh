@@ -53,6 +53,8 @@ __device__ __forceinline__ float2 from_c<float2>(cplx v) {
 __device__ __forceinline__ double2 ld_stream(const double2* p) { return __ldcs(p); }
 __device__ __forceinline__ float2 ld_stream(const float2* p) { return __ldcs(p); }
 __device__ __forceinline__ int ld_stream(const int* p) { return __ldcs(p); }
+__device__ __forceinline__ unsigned int ld_stream(const unsigned int* p) { return __ldcs(p); }
+__device__ __forceinline__ uint2 ld_stream(const uint2* p) { return __ldcs(p); }
 // Gathered vector: read-only path.
 __device__ __forceinline__ double2 ld_gather(const double2* p) { return __ldg(p); }
 __device__ __forceinline__ float2 ld_gather(const float2* p) { return __ldg(p); }

@@ -512,6 +512,89 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, UNR>::MIN_BLOCKS)
   }
 }
 
+// ------------------------------------------------ dictionary-coded sliced --
+// The sliced kernel with every stored entry replaced by a 1- or 2-byte code into its
+// group's table of (column - row, value) pairs, staged in shared memory per block.  A
+// Kronecker-structured Liouvillian repeats a few such pairs (the Ising L = 10 one: 20
+// in the driven group, about 700 in the constant one), so the operator stream shrinks
+// from 12 bytes per entry (complex64 value, int32 column) to 1-2 bytes, and a stage is
+// bound by the shared-memory lookups and the L2 gathers of x instead of by HBM.
+template <int CB>
+struct Codes4;
+template <>
+struct Codes4<1> {
+  using T = unsigned int;
+  __device__ static int at(T c, int u) { return (int)((c >> (8 * u)) & 0xffu); }
+};
+template <>
+struct Codes4<2> {
+  using T = uint2;
+  __device__ static int at(T c, int u) {
+    const unsigned w = u < 2 ? c.x : c.y;
+    return (int)((w >> (16 * (u & 1))) & 0xffffu);
+  }
+};
+
+template <int DT, int YDT, int EPI, int CB>
+__global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, 4>::MIN_BLOCKS)
+    spmv_dict_kernel(qg_csr_groups A, double t, const typename elem<DT>::T* __restrict__ x,
+                     AxpbyArgs ax, RkArgs rk) {
+  using ST = typename elem<DT>::T;
+  using R = typename elem<DT>::R;
+  using C4 = typename Codes4<CB>::T;
+  extern __shared__ __align__(16) unsigned char dict_smem[];
+  __shared__ cx<R> coef[QG_MAX_GROUPS];
+  __shared__ int tstart[QG_MAX_GROUPS + 1];
+  __shared__ double red[SPMV_BLOCK / 32];
+  const int D = A.lanes;
+  ST* tval = reinterpret_cast<ST*>(dict_smem);
+  int* toff = reinterpret_cast<int*>(dict_smem + (size_t)D * sizeof(ST));
+  load_coefs(A, t, coef);
+  for (int i = threadIdx.x; i < D; i += SPMV_BLOCK) {
+    tval[i] = __ldg(static_cast<const ST*>(A.val) + i);
+    toff[i] = __ldg(A.dict_off + i);
+  }
+  if (threadIdx.x <= (unsigned)A.n_groups) tstart[threadIdx.x] = __ldg(A.dict_start + threadIdx.x);
+  __syncthreads();
+  const int G = A.n_groups;
+  const int n = (int)A.n_rows;
+  const int S = A.n_tiles;
+  const int last_col = (int)A.n_cols - 1;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * SPMV_BLOCK + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * SPMV_BLOCK) >> 5;
+  const unsigned char* __restrict__ codes = reinterpret_cast<const unsigned char*>(A.col);
+  R err_acc = 0;
+  for (int sl = warp; sl < S; sl += nwarps) {
+    const int row = sl * 32 + lane;
+    cx<R> acc{0, 0};
+    for (int g = 0; g < G; ++g) {
+      const int w4 = __ldg(A.tile_row + sl * G + g) >> 2;  // chunks of four entries
+      const int t0 = tstart[g], tn = tstart[g + 1] - t0;
+      const C4* __restrict__ cp =
+          reinterpret_cast<const C4*>(codes + (size_t)CB * __ldg(A.row_ptr + g * (S + 1) + sl)) +
+          lane;
+      R ar = 0, ai = 0;
+#pragma unroll 2
+      for (int q = 0; q < w4; ++q) {
+        const C4 c4 = ld_stream(cp + 32 * q);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          int k = Codes4<CB>::at(c4, u);
+          k = t0 + (k < tn ? k : 0);  // a table index of this group whatever the code
+          const int col = min(max(row + toff[k], 0), last_col);
+          cmac_any(ar, ai, tval[k], ld_gather(x + col));
+        }
+      }
+      acc = cx_add(acc, cx_mul(coef[g], cx<R>{ar, ai}));
+    }
+    if (row < n) epilogue<DT, YDT, EPI>(row, acc, ax, rk, err_acc);
+  }
+  if constexpr (EPI == EPI_RK) {
+    if (rk.stage == RK_STEP - 1) finish_error<SPMV_BLOCK>(rk, (double)err_acc, red);
+  }
+}
+
 // ---------------------------------------------------- matrix-free Lindblad --
 // out(r, c) = D(r, c) x[r + c d]
 //           + sum_g a_g sum_j A_g[r,j] x[j + c d] + conj(a_g) sum_k conj(A_g[c,k]) x[r + k d]
@@ -732,11 +815,31 @@ static int launch_staged(cudaStream_t st, const qg_csr_groups& A, double t, cons
   return check_launch("spmv_staged_kernel");
 }
 
+template <int DT, int YDT, int EPI, int CB>
+static int launch_dict(cudaStream_t st, const qg_csr_groups& A, double t, const void* x,
+                       const AxpbyArgs& ax, const RkArgs& rk) {
+  using ST = typename elem<DT>::T;
+  auto kern = spmv_dict_kernel<DT, YDT, EPI, CB>;
+  const size_t smem = ((size_t)A.lanes * (sizeof(ST) + sizeof(int)) + 15) & ~(size_t)15;
+  static OccCache cache;  // one per instantiation
+  const int per_sm = staged_occupancy(kern, SPMV_BLOCK, smem, cache);
+  if (per_sm <= 0) return set_error(QG_ERR_ARG, "dictionary does not fit in shared memory");
+  const int64_t blocks = ((int64_t)A.n_tiles * 32 + SPMV_BLOCK - 1) / SPMV_BLOCK;
+  int64_t cap = (int64_t)sm_count() * per_sm;
+  if (cap > qg_scratch_doubles()) cap = qg_scratch_doubles();
+  const int grid = (int)(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
+  kern<<<grid, SPMV_BLOCK, smem, st>>>(A, t, (const ST*)x, ax, rk);
+  return check_launch("spmv_dict_kernel");
+}
+
 template <int DT, int YDT, int EPI>
 static int launch_any(cudaStream_t st, const qg_csr_groups& A, double t, const void* x,
                       const AxpbyArgs& ax, const RkArgs& rk) {
   using ST = typename elem<DT>::T;
   const int lanes = A.lanes > 0 ? A.lanes : 4;
+  if (A.layout == QG_LAYOUT_SLICED_DICT)
+    return A.tile_nnz == 1 ? launch_dict<DT, YDT, EPI, 1>(st, A, t, x, ax, rk)
+                           : launch_dict<DT, YDT, EPI, 2>(st, A, t, x, ax, rk);
   if (A.layout == QG_LAYOUT_SLICED) {
     // one wave: every block resident at once, warps striding over the slices.  (8
     // entries in flight at 64 registers measured slower than 4 at 40: 73 vs 68 us
@@ -813,9 +916,19 @@ static int check_groups(const qg_csr_groups* A) {
   if (A->dtype != QG_C128 && A->dtype != QG_C64)
     return set_error(QG_ERR_UNSUPPORTED, "operator dtype must be QG_C128 or QG_C64");
   if (A->layout != QG_LAYOUT_GROUP_MAJOR && A->layout != QG_LAYOUT_ROW_MAJOR &&
-      A->layout != QG_LAYOUT_SLICED)
+      A->layout != QG_LAYOUT_SLICED && A->layout != QG_LAYOUT_SLICED_DICT)
     return set_error(QG_ERR_ARG, "unknown row-pointer layout");
-  if (A->layout == QG_LAYOUT_SLICED) {
+  if (A->layout == QG_LAYOUT_SLICED_DICT) {
+    if (!A->tile_row || !A->dict_off || !A->dict_start || A->n_tiles != (A->n_rows + 31) / 32)
+      return set_error(QG_ERR_ARG,
+                       "dictionary layout needs n_tiles = ceil(n_rows/32), widths and tables");
+    if (A->tile_nnz != 1 && A->tile_nnz != 2)
+      return set_error(QG_ERR_ARG, "dictionary codes must be 1 or 2 bytes");
+    if (A->lanes < A->n_groups || A->lanes > QG_DICT_MAX)
+      return set_error(QG_ERR_ARG, "dictionary size out of range");
+    if ((int64_t)A->n_groups * (A->n_tiles + 1) >= (int64_t)INT32_MAX)
+      return set_error(QG_ERR_ARG, "too many slices");
+  } else if (A->layout == QG_LAYOUT_SLICED) {
     if (!A->tile_row || A->n_tiles != (A->n_rows + 31) / 32)
       return set_error(QG_ERR_ARG, "sliced layout needs n_tiles = ceil(n_rows/32) and widths");
   } else if (A->n_tiles > 0) {

@@ -280,6 +280,8 @@ static int expect_launch(const qg_csr_groups* ops, int64_t d, const qg_state_vie
   if (!ops || !v || !out || !v->base) return set_error(QG_ERR_ARG, "null pointer");
   if (ops->n_groups < 1 || ops->n_groups > QG_MAX_EOPS)
     return set_error(QG_ERR_ARG, "number of operators out of range");
+  if (ops->layout != QG_LAYOUT_GROUP_MAJOR && ops->layout != QG_LAYOUT_ROW_MAJOR)
+    return set_error(QG_ERR_UNSUPPORTED, "expect needs a CSR (group- or row-major) layout");
   if (!dt_ok(v->base_dtype) || !dt_ok(v->k_dtype) || !dt_ok(ops->dtype))
     return set_error(QG_ERR_UNSUPPORTED, "dtype");
   if (KET ? (ops->n_rows != v->n || ops->n_cols != v->n)
@@ -332,6 +334,8 @@ extern "C" int qg_spmm_csr(const qg_csr_groups* A, double t, const void* X, void
     return set_error(QG_ERR_ARG, "null pointer");
   if (A->n_groups < 1 || A->n_groups > QG_MAX_GROUPS) return set_error(QG_ERR_ARG, "n_groups");
   if (!dt_ok(A->dtype)) return set_error(QG_ERR_UNSUPPORTED, "dtype");
+  if (A->layout != QG_LAYOUT_GROUP_MAJOR && A->layout != QG_LAYOUT_ROW_MAJOR)
+    return set_error(QG_ERR_UNSUPPORTED, "spmm needs a CSR (group- or row-major) layout");
   if (n_vec < 0 || ld < A->n_rows || ld < A->n_cols) return set_error(QG_ERR_ARG, "bad n_vec/ld");
   if (A->n_rows == 0 || n_vec == 0) return QG_OK;
   cudaStream_t st = (cudaStream_t)stream;

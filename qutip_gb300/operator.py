@@ -111,6 +111,71 @@ def sliced_layout(mats, n_cols):
     return slice_ptr, widths.reshape(-1).astype(np.int32), col, val, total
 
 
+def dict_sliced_layout(mats, n_cols, dtype: str, max_table: int = _lib.QG_DICT_MAX):
+    """Dictionary-coded sliced ELLPACK of coefficient groups, or ``None`` when the groups'
+    (column - row, value) pairs do not fit ``max_table`` table entries.
+
+    Rows are grouped in 32-row slices as in :func:`sliced_layout` (entries of a row ordered
+    by ``col XOR row``); each group has its own code section, widths rounded up to a
+    multiple of 4, and the codes of lane l are stored four at a time (entries 4q..4q+3 at
+    ``base + 128 q + 4 l``).  Code 0 of every group is padding (offset 0, value 0).
+    Values are deduplicated in the operator's dtype.  Returns ``(row_ptr[G*(S+1)],
+    widths[S*G], codes, code_bytes, table_off, table_val, table_start[G+1], stored)``.
+    """
+    mats = [sp.csr_matrix(m, dtype=np.complex128) for m in mats]
+    n = mats[0].shape[0]
+    G = len(mats)
+    S = (n + 31) // 32
+    vdt = np.complex64 if dtype == "c64" else np.complex128
+    widths = np.zeros((S, G), dtype=np.int64)
+    for g, m in enumerate(mats):
+        c = np.zeros(S * 32, dtype=np.int64)
+        c[:n] = np.diff(m.indptr)
+        widths[:, g] = (c.reshape(S, 32).max(axis=1) + 3) // 4 * 4
+    sect = 32 * widths                                   # codes per (slice, group)
+    gsize = sect.sum(axis=0)                             # codes per group
+    gbase = np.concatenate([[0], np.cumsum(gsize)[:-1]])
+    row_ptr = np.zeros((G, S + 1), dtype=np.int64)
+    for g in range(G):
+        row_ptr[g, 1:] = np.cumsum(sect[:, g])
+        row_ptr[g] += gbase[g]
+    total = int(gsize.sum())
+    if total >= 2**31 - 16:
+        return None
+    codes = np.zeros(total, dtype=np.int32)
+    t_off, t_val, t_start = [], [], [0]
+    for g, m in enumerate(mats):
+        rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(m.indptr))
+        order = np.lexsort((m.indices.astype(np.int64) ^ rows, rows))
+        ci = m.indices[order].astype(np.int64)
+        dv = m.data[order].astype(vdt)
+        off = ci - rows
+        nz = dv != 0
+        vals, vcode = np.unique(dv[nz], return_inverse=True)
+        key = off[nz] * max(len(vals), 1) + vcode.reshape(-1)
+        ukey, kcode = np.unique(key, return_inverse=True)
+        if len(ukey) + 1 > max_table:
+            return None
+        voff = ukey // max(len(vals), 1)
+        t_off.append(np.concatenate([[0], voff]).astype(np.int32))
+        t_val.append(np.concatenate([np.zeros(1, vdt), vals[ukey - voff * max(len(vals), 1)]]))
+        t_start.append(t_start[-1] + len(ukey) + 1)
+        code = np.zeros(m.nnz, dtype=np.int32)
+        code[nz] = kcode.reshape(-1) + 1
+        q = np.arange(m.nnz, dtype=np.int64) - m.indptr[rows]
+        sl = rows // 32
+        dst = row_ptr[g, sl] + 128 * (q // 4) + 4 * (rows % 32) + q % 4
+        codes[dst] = code
+    if t_start[-1] > max_table:
+        return None
+    cb = 1 if max(b - a for a, b in zip(t_start[:-1], t_start[1:])) <= 256 else 2
+    if cb == 2 and max(b - a for a, b in zip(t_start[:-1], t_start[1:])) > 65536:
+        return None
+    return (row_ptr.reshape(-1), widths.reshape(-1).astype(np.int32),
+            codes.astype(np.uint8 if cb == 1 else np.uint16), cb,
+            np.concatenate(t_off), np.concatenate(t_val), np.asarray(t_start, np.int32), total)
+
+
 def row_tiles(row_start, tile_nnz, max_rows):
     """Greedy row tiles holding at most ``tile_nnz - 8`` entries and ``max_rows`` rows.
 
@@ -167,13 +232,35 @@ class DeviceOperator:
         mats = [sp.csr_matrix(op) for op, _ in terms]
         self.group_nnz = [int(m.nnz) for m in mats]
         self.nnz = sum(self.group_nnz)
+        lay = None
         if fmt == "auto":
             fmt = self._choose_format(mats)
-        if fmt not in ("csr", "sliced"):
-            raise ValueError("fmt must be 'auto', 'csr' or 'sliced'")
+            if fmt == "sliced":  # prefer the dictionary-coded form when the tables fit
+                lay = dict_sliced_layout(mats, self.n_cols, dtype)
+                fmt = "dict" if lay is not None else "sliced"
+        elif fmt == "dict":
+            lay = dict_sliced_layout(mats, self.n_cols, dtype)
+            if lay is None:
+                raise ValueError("the (column - row, value) pairs exceed the dictionary size")
+        if fmt not in ("csr", "sliced", "dict"):
+            raise ValueError("fmt must be 'auto', 'csr', 'sliced' or 'dict'")
         self.fmt = fmt
         P = self.PAD
         self._tiles = {}
+        self.dict_off = self.dict_start = None
+        self.code_bytes = 0
+        if fmt == "dict":
+            rp, widths, codes, cb, t_off, t_val, t_start, total = lay
+            self.stored = total
+            self.code_bytes = cb
+            self.slice_width = torch.from_numpy(widths).to(self.device)
+            self.row_ptr = torch.from_numpy(rp.astype(np.int32)).to(self.device)
+            self.col = torch.from_numpy(codes if cb == 1 else codes.view(np.int16)).to(self.device)
+            self.val = torch.from_numpy(t_val).to(self.device, _TORCH[dtype])
+            self.dict_off = torch.from_numpy(t_off).to(self.device)
+            self.dict_start = torch.from_numpy(t_start).to(self.device)
+            self._finish(G)
+            return
         if fmt == "sliced":
             rp, widths, col, val, total = sliced_layout(mats, self.n_cols)
             self.stored = total
@@ -223,6 +310,8 @@ class DeviceOperator:
         self.nnz = sum(self.group_nnz)
         self.fmt = "sliced"
         self._tiles = {}
+        self.dict_off = self.dict_start = None
+        self.code_bytes = 0
         P = self.PAD
         rp, widths, col, val, total = device_sliced_layout(groups, n)
         if total >= 2**31 - 16 or n * len(groups) >= 2**31 - 16:
@@ -260,11 +349,13 @@ class DeviceOperator:
             self.coef_code = torch.from_numpy(code).to(self.device)
             self.coef_start = torch.from_numpy(starts).to(self.device)
             self.coef_consts = torch.from_numpy(consts).to(self.device)
-        layout = _lib.QG_LAYOUT_SLICED if fmt == "sliced" else _lib.QG_LAYOUT_ROW_MAJOR
+        layout = {"sliced": _lib.QG_LAYOUT_SLICED, "dict": _lib.QG_LAYOUT_SLICED_DICT}.get(
+            fmt, _lib.QG_LAYOUT_ROW_MAJOR)
         self.struct = _lib.CsrGroups(
             self.n_rows, self.n_cols, G, _QG[dtype], layout, 4, 0, 0,
             _ptr(self.row_ptr), _ptr(self.col), _ptr(self.val), None, _ptr(self.coef_code),
-            _ptr(self.coef_start), _ptr(self.coef_consts))
+            _ptr(self.coef_start), _ptr(self.coef_consts), _ptr(self.dict_off),
+            _ptr(self.dict_start))
         self.set_launch(self.default_launch())
 
     def _choose_format(self, mats) -> str:
@@ -285,6 +376,8 @@ class DeviceOperator:
         """Staged tiles for short rows, a sub-warp per row otherwise (before tuning)."""
         if self.fmt == "sliced":
             return ("sliced", 0, 1)
+        if self.fmt == "dict":
+            return ("dict", 0, 1)
         mean = self.nnz / max(self.n_rows, 1)
         tn = 4096 if self.dtype == "c64" else 2048
         if tn in self._tiles and mean <= 64:
@@ -296,8 +389,15 @@ class DeviceOperator:
 
     def set_launch(self, launch):
         kind, tile_nnz, lanes = launch
-        if (kind == "sliced") != (self.fmt == "sliced"):
+        if (kind in ("sliced", "dict") or self.fmt in ("sliced", "dict")) and kind != self.fmt:
             raise ValueError(f"launch {kind!r} does not match the {self.fmt!r} storage")
+        if kind == "dict":
+            self.struct.n_tiles = (self.n_rows + 31) // 32
+            self.struct.tile_nnz = self.code_bytes
+            self.struct.tile_row = self.slice_width.data_ptr()
+            self.struct.lanes = int(self.val.numel())
+            self.launch = launch
+            return
         if kind == "sliced":
             self.struct.n_tiles = (self.n_rows + 31) // 32
             self.struct.tile_nnz = 0
@@ -318,13 +418,17 @@ class DeviceOperator:
 
     def launch_desc(self) -> str:
         kind, tn, lanes = self.launch
+        if kind == "dict":
+            return (f"dict(32-row slices, {self.code_bytes}-byte codes, "
+                    f"{self.val.numel()} table entries, {self.stored / max(self.nnz, 1):.3f}x "
+                    "stored/nnz)")
         if kind == "sliced":
             return f"sliced(32-row slices, {self.stored / max(self.nnz, 1):.3f}x stored/nnz)"
         return f"{kind}(lanes={lanes}" + (f", tile_nnz={tn})" if kind == "staged" else ")")
 
     def candidates(self):
-        if self.fmt == "sliced":
-            return [("sliced", 0, 1)]
+        if self.fmt in ("sliced", "dict"):
+            return [(self.fmt, 0, 1)]
         out = [("direct", 0, l) for l in (1, 2, 4, 8, 16, 32)]
         for tn in sorted(self._tiles):
             out += [("staged", tn, l) for l in (1, 2, 4, 8, 16)]
@@ -354,7 +458,8 @@ class DeviceOperator:
 
     def device_arrays(self):
         return [t for t in (self.row_ptr, self.col, self.val, self.slice_width, self.coef_code,
-                            self.coef_start, self.coef_consts) if t is not None]
+                            self.coef_start, self.coef_consts, self.dict_off, self.dict_start)
+                if t is not None]
 
     def host_copy(self, pinned: bool = True):
         """Host copies of the device arrays (pinned), for end-to-end transfer timing."""
@@ -384,10 +489,21 @@ class DeviceOperator:
     def value_bytes(self) -> int:
         return 16 if self.dtype == "c128" else 8
 
-    def spmv_bytes(self, accumulate: bool = False) -> int:
-        """Algorithmic HBM bytes of one matvec: values + indices + row pointers + x + y."""
+    def operator_bytes(self) -> int:
+        """Algorithmic HBM bytes of the operator stream of one application: values and
+        int32 indices plus row pointers, or for the dictionary form its codes (padding
+        included), slice pointers and widths, and the tables."""
         sv = self.value_bytes()
-        return (self.nnz * (sv + 4) + (self.n_groups * self.n_rows + 1) * 4 + self.n_cols * sv
+        if self.fmt == "dict":
+            S = (self.n_rows + 31) // 32
+            return (self.stored * self.code_bytes + 8 * self.n_groups * (S + 1)
+                    + int(self.val.numel()) * (sv + 4))
+        return self.nnz * (sv + 4) + (self.n_groups * self.n_rows + 1) * 4
+
+    def spmv_bytes(self, accumulate: bool = False) -> int:
+        """Algorithmic HBM bytes of one matvec: the operator stream + x + y."""
+        sv = self.value_bytes()
+        return (self.operator_bytes() + self.n_cols * sv
                 + self.n_rows * sv * (2 if accumulate else 1))
 
     def matvec(self, t: float, x: torch.Tensor, y: torch.Tensor, alpha=1.0, beta=0.0):

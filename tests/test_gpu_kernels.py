@@ -91,22 +91,24 @@ def test_sliced_layout_matches_scipy(dev, L):
     rng = np.random.default_rng(L)
     x = rng.normal(size=4 ** L) + 1j * rng.normal(size=4 ** L)
     want = sum((m * (1 if c is None else c(1.7))) @ x for m, c in s.terms)
-    for dt, tol in (("c128", 1e-12), ("c64", 2e-5)):
-        op = DeviceOperator(s.terms, dtype=dt, fmt="sliced")
-        assert op.launch[0] == "sliced" and op.stored >= op.nnz
-        xt = _t(x, torch.complex128 if dt == "c128" else torch.complex64)
-        y = _t(np.ones(op.n_rows), xt.dtype)
-        op.matvec(1.7, xt, y, alpha=2.0, beta=-1.0)
-        np.testing.assert_allclose(y.cpu().numpy(), 2 * want - 1, rtol=tol,
-                                   atol=tol * np.abs(want).max())
+    for fmt in ("sliced", "dict"):
+        for dt, tol in (("c128", 1e-12), ("c64", 2e-5)):
+            op = DeviceOperator(s.terms, dtype=dt, fmt=fmt)
+            assert op.launch[0] == fmt and op.stored >= op.nnz
+            xt = _t(x, torch.complex128 if dt == "c128" else torch.complex64)
+            y = _t(np.ones(op.n_rows), xt.dtype)
+            op.matvec(1.7, xt, y, alpha=2.0, beta=-1.0)
+            np.testing.assert_allclose(y.cpu().numpy(), 2 * want - 1, rtol=tol,
+                                       atol=tol * np.abs(want).max(), err_msg=f"{fmt} {dt}")
     outs = []
-    for fmt in ("sliced", "csr"):
+    for fmt in ("sliced", "csr", "dict"):
         op = DeviceOperator(s.terms, dtype="c128", fmt=fmt)
         ig = GpuVern7(op)
         ig.set_initial_value(torch.from_numpy(s.state0).cuda(), 0.0)
         ig.integrate(0.7)
         outs.append(ig.get_state().cpu().numpy())
     np.testing.assert_allclose(outs[0], outs[1], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(outs[2], outs[1], rtol=1e-12, atol=1e-14)
 
 
 def test_grouped_coefficients_match_scipy(dev):
@@ -261,3 +263,47 @@ def test_spmv_one_by_one(dev):
     y = torch.zeros(1, dtype=torch.complex128, device="cuda")
     op.matvec(0.0, _t(np.array([3.0 + 0.5j])), y, alpha=2.0, beta=0.0)
     assert complex(y.item()) == pytest.approx(2 * (2.0 - 1.0j) * (3.0 + 0.5j), abs=1e-14)
+
+
+@pytest.mark.parametrize("dtype", ["c128", "c64"])
+def test_spmv_dict_ragged_rows_and_empty_group(dev, dtype):
+    """Dictionary-coded storage: entries on a few diagonals with values from a small
+    set, every 7th row empty, a row count that is not a multiple of 32, an all-zero
+    coefficient group, columns near both edges, and both Vern7 epilogues."""
+    from qutip_gb300.coefficients import coefficient
+    from qutip_gb300.operator import DeviceOperator
+    from qutip_gb300.vern7 import GpuVern7
+    rng = np.random.default_rng(9)
+    n = 1061
+    rows, cols, vals = [], [], []
+    choices = [1.0, -0.5j, 0.25 + 1j, -2.0]
+    for r in range(n):
+        if r % 7 == 0:
+            continue
+        for o in (-40, -1, 0, 3, 33):
+            if 0 <= r + o < n and rng.random() < 0.8:
+                rows.append(r)
+                cols.append(r + o)
+                vals.append(choices[rng.integers(4)])
+    a = sp.csr_matrix((vals, (rows, cols)), shape=(n, n), dtype=np.complex128)
+    empty = sp.csr_matrix((n, n), dtype=np.complex128)
+    c = coefficient("cos(t)")
+    op = DeviceOperator([(a, None), (empty, c)], dtype=dtype, merge=False, fmt="dict")
+    assert op.launch[0] == "dict" and op.code_bytes == 1
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    tdt = torch.complex128 if dtype == "c128" else torch.complex64
+    y = torch.full((n,), 7.0 + 7.0j, dtype=tdt, device="cuda")
+    op.matvec(0.4, _t(x, tdt), y)
+    want = a @ x
+    tol = 1e-12 if dtype == "c128" else 3e-6
+    np.testing.assert_allclose(y.cpu().numpy(), want, rtol=tol, atol=tol * np.abs(want).max())
+    assert np.all(y.cpu().numpy()[::7] == 0)
+    # a Vern7 integration through the fused stages agrees with the CSR storage
+    gen = [((-0.1j) * (a + a.conj().T), None), (empty, c)]
+    outs = []
+    for fmt in ("csr", "dict"):
+        ig = GpuVern7(DeviceOperator(gen, dtype="c128", merge=False, fmt=fmt))
+        ig.set_initial_value(_t(x / np.linalg.norm(x)), 0.0)
+        ig.integrate(0.5)
+        outs.append(ig.get_state().cpu().numpy())
+    np.testing.assert_allclose(outs[1], outs[0], rtol=1e-12, atol=1e-14)

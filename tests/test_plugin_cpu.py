@@ -37,6 +37,7 @@ def _close(prog, c):
     ("t**2", {}),
     ("sin(w*t)**2 - 0.5*cos(2*t)", {"w": 0.7}),
     ("sqrt(1 + t) * exp(1j*w*t)", {"w": 2.0}),
+    ("amp * cos(2 * t)", {"amp": 0.0}),          # a zero factor (no 0 ** b on the host)
 ])
 def test_string_coefficients(qt, plugin, expr, args):
     c = qt.coefficient(expr, args=args)
