@@ -75,6 +75,8 @@ def parse():
                     help="run the ncu profiling case only (fused stage kernel, untuned); "
                          "prints nothing to parse")
     ap.add_argument("--profile-sites", type=int, default=10)
+    ap.add_argument("--profile-fmt", default="auto", choices=["auto", "sliced", "dict", "csr"],
+                    help="operator storage of the stage profiling case")
     ap.add_argument("--profile-ntraj", type=int, default=256)
     ap.add_argument("--profile-tend", type=float, default=5.0)
     ap.add_argument("--profile-group", default="auto",
@@ -250,13 +252,14 @@ def stage_bytes(op, n, stage, mixed):
     return b
 
 
-TRAFFIC_PROFILE = "profiles/spmv_sliced_ising_L10_stage.md"
+TRAFFIC_PROFILE = "profiles/spmv_dict_ising_L10_stage.md"
+SLICED_PROFILE = "profiles/spmv_sliced_ising_L10_stage.md"
 
 
-def profiled_traffic():
-    """DRAM bytes per fused stage launch from the committed ncu summary, or None."""
+def profiled_traffic(path=TRAFFIC_PROFILE):
+    """DRAM bytes per fused stage launch from a committed ncu summary, or None."""
     try:
-        with open(os.path.join(ROOT, TRAFFIC_PROFILE)) as f:
+        with open(os.path.join(ROOT, path)) as f:
             for line in f:
                 if line.startswith("traffic_bytes_per_launch:"):
                     return int(line.split(":")[1])
@@ -659,6 +662,10 @@ def run_ours(args, dist):
 
     log("roofline measurements")
     stage_ms, stage_b, stage_gbs = measure_stage_roofline(op64, sysm, "mixed")
+    # the same stage with the uncompressed sliced operator (12 bytes per entry)
+    op_sl = DeviceOperator(sysm.terms, dtype="c64", fmt="sliced")
+    sl_ms, sl_b, sl_gbs = measure_stage_roofline(op_sl, sysm, "mixed")
+    del op_sl
     stage128_ms, stage128_b, stage128_gbs = measure_stage_roofline(op, sysm, "double")
     spmv_ms, spmv_b, spmv_gbs = measure_spmv(op)
     spmv64_ms, spmv64_b, spmv64_gbs = measure_spmv(op64)
@@ -681,9 +688,21 @@ def run_ours(args, dist):
                      "traffic_source": f"{TRAFFIC_PROFILE} (ncu dram__bytes_read.sum + "
                                        "dram__bytes_write.sum, mean over the 10 stage launches "
                                        "of a step, same operator)",
-                     "kernel": "spmv_sliced_kernel<C64,C128,RK> (fused Vern7 stage, mixed)",
+                     "kernel": (f"spmv_dict_kernel<C64,C128,RK,{op64.code_bytes}> (fused Vern7 "
+                                "stage, mixed, dictionary-coded operator)" if op64.fmt == "dict"
+                                else "spmv_sliced_kernel<C64,C128,RK> (fused Vern7 stage, mixed)"),
                      "bytes_per_launch": stage_b, "ms_per_launch": stage_ms,
-                     "peak_source": f"{peak_src} hbm_gbs (of {peak_src})"},
+                     "peak_source": f"{peak_src} hbm_gbs (of {peak_src})",
+                     "note": "the dictionary codes cut the operator stream from 12 to 2 bytes "
+                             "per entry, so HBM no longer bounds this kernel: shared-memory "
+                             "table lookups and L2 gathers of x do; see roofline_uncompressed "
+                             "for the same stage with the 12-byte entries"},
+        "roofline_uncompressed": {"kernel": "spmv_sliced_kernel<C64,C128,RK>",
+                                  "bound": "hbm", "achieved": sl_gbs, "peak": hbm_peak,
+                                  "unit": "GB/s", "frac": sl_gbs / hbm_peak,
+                                  "bytes_per_launch": sl_b, "ms_per_launch": sl_ms,
+                                  "traffic": profiled_traffic(SLICED_PROFILE),
+                                  "traffic_source": SLICED_PROFILE},
         "double_precision": {"value": double_v, "unit": UNIT,
                              "stage_kernel_gbs": stage128_gbs, "stage_kernel_ms": stage128_ms,
                              "bound": "FP64 throughput (about 4 DFMA per stored entry)"},
@@ -728,7 +747,7 @@ def run_profile_case(args):
     from qutip_gb300.vern7 import GpuVern7
     torch.cuda.set_device(0)
     s = S.ising_chain(args.profile_sites)
-    op = DeviceOperator(s.terms, dtype="c64")
+    op = DeviceOperator(s.terms, dtype="c64", fmt=args.profile_fmt)
     ig = GpuVern7(op, precision="mixed")
     ig.set_initial_value(torch.from_numpy(s.state0).cuda(), 0.0)
     for _ in range(2):
