@@ -286,11 +286,15 @@ class DeviceOperator:
         self._finish(G)
 
     @classmethod
-    def from_device_groups(cls, groups, dtype: str = "c64"):
-        """Sliced-ELLPACK operator from device CSR groups
-        ``[(indptr, indices, data, Coefficient | None), ...]`` (for example from
-        :func:`qutip_gb300.superop.liouvillian_groups`), laid out on the device."""
-        from .superop import device_sliced_layout
+    def from_device_groups(cls, groups, dtype: str = "c64", fmt: str = "auto"):
+        """Sliced operator from device CSR groups ``[(indptr, indices, data,
+        Coefficient | None), ...]`` (for example from
+        :func:`qutip_gb300.superop.liouvillian_groups`), laid out on the device:
+        dictionary-coded when the groups' (column - row, value) pairs fit the tables
+        (``fmt="auto"`` or ``"dict"``), plain sliced ELLPACK otherwise (or ``"sliced"``)."""
+        from .superop import device_dict_layout, device_sliced_layout
+        if fmt not in ("auto", "dict", "sliced"):
+            raise ValueError("fmt must be 'auto', 'dict' or 'sliced'")
         if dtype not in _TORCH:
             raise TypeError(f"unsupported dtype {dtype!r}")
         if not groups or len(groups) > _lib.QG_MAX_GROUPS:
@@ -308,10 +312,23 @@ class DeviceOperator:
         self.device = indptr0.device
         self.group_nnz = [int(ix.numel()) for _, ix, _, _ in groups]
         self.nnz = sum(self.group_nnz)
-        self.fmt = "sliced"
         self._tiles = {}
         self.dict_off = self.dict_start = None
         self.code_bytes = 0
+        lay = device_dict_layout(groups, n, dtype) if fmt != "sliced" else None
+        if lay is None and fmt == "dict":
+            raise ValueError("the (column - row, value) pairs exceed the dictionary size")
+        if lay is not None:
+            rp, widths, codes, cb, t_off, t_val, t_start, total = lay
+            self.fmt = "dict"
+            self.stored = total
+            self.code_bytes = cb
+            self.slice_width = widths
+            self.row_ptr, self.col, self.val = rp, codes, t_val.to(_TORCH[dtype])
+            self.dict_off, self.dict_start = t_off, t_start
+            self._finish(len(groups))
+            return self
+        self.fmt = "sliced"
         P = self.PAD
         rp, widths, col, val, total = device_sliced_layout(groups, n)
         if total >= 2**31 - 16 or n * len(groups) >= 2**31 - 16:

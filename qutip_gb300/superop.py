@@ -167,3 +167,91 @@ def device_sliced_layout(groups, n_cols):
         val[dst] = dv
         del dst, ci, dv, rows
     return slice_ptr, widths.reshape(-1).to(torch.int32), col, val, total
+
+
+def device_dict_layout(groups, n_cols, dtype: str, max_table: int = 4096):
+    """Dictionary-coded sliced layout of device CSR groups: the layout of
+    :func:`qutip_gb300.operator.dict_sliced_layout` computed with device sorts, uniques
+    and scatters (tables in a different but equivalent order).  Returns
+    ``(row_ptr, widths, codes, code_bytes, table_off, table_val, table_start, stored)``
+    as device tensors, or ``None`` when the (column - row, value) pairs do not fit
+    ``max_table`` table entries."""
+    indptr0 = groups[0][0]
+    device = indptr0.device
+    n = indptr0.numel() - 1
+    G = len(groups)
+    S = (n + 31) // 32
+    vdt = torch.complex64 if dtype == "c64" else torch.complex128
+    counts = torch.zeros((G, S * 32), dtype=torch.int64, device=device)
+    for g, (indptr, _, _, _) in enumerate(groups):
+        counts[g, :n] = indptr[1:] - indptr[:-1]
+    widths = (counts.view(G, S, 32).amax(dim=2) + 3) // 4 * 4      # [G, S]
+    del counts
+    sect = 32 * widths
+    gsize = sect.sum(dim=1)
+    gbase = torch.cumsum(gsize, 0) - gsize
+    row_ptr = torch.zeros((G, S + 1), dtype=torch.int64, device=device)
+    row_ptr[:, 1:] = torch.cumsum(sect, dim=1)
+    row_ptr += gbase[:, None]
+    total = int(gsize.sum().item())
+    if total >= 2**31 - 16:
+        return None
+    codes = torch.zeros(total, dtype=torch.int32, device=device)
+    t_off, t_val, t_start = [], [], [0]
+    for g, (indptr, indices, data, _) in enumerate(groups):
+        nnz = indices.numel()
+        cnt = indptr[1:] - indptr[:-1]
+        rows = torch.repeat_interleave(torch.arange(n, device=device), cnt)
+        idx = indices.to(torch.int64)
+        key = (rows << 32) | (idx ^ rows)              # rows stay grouped, (col XOR row) within
+        _, perm = torch.sort(key)
+        del key
+        off = idx[perm] - rows
+        dv = data[perm].to(vdt)
+        del perm, idx
+        nz = dv != 0
+        # distinct values by their bit patterns, with one-dimensional uniques only
+        parts = torch.view_as_real(dv[nz]).contiguous()
+        if dtype == "c64":
+            vbits, vcode = torch.unique(parts.view(torch.int64).view(-1), return_inverse=True)
+        else:
+            pb = parts.view(torch.int64)                 # [m, 2]: real and imaginary bits
+            ure, ire = torch.unique(pb[:, 0], return_inverse=True)
+            uim, iim = torch.unique(pb[:, 1], return_inverse=True)
+            del pb
+            vkey, vcode = torch.unique(ire * uim.numel() + iim, return_inverse=True)
+            del ire, iim
+            q_re = torch.div(vkey, uim.numel(), rounding_mode="floor")
+            vbits = torch.stack([ure[q_re], uim[vkey - q_re * uim.numel()]], dim=1)
+            del ure, uim, vkey, q_re
+        del parts
+        V = max(int(vbits.shape[0]), 1)
+        ukey, kcode = torch.unique(off[nz] * V + vcode, return_inverse=True)
+        del vcode
+        if ukey.numel() + 1 > max_table:
+            return None
+        voff = torch.div(ukey, V, rounding_mode="floor")
+        vals = vbits[ukey - voff * V].contiguous()
+        if dtype == "c64":
+            vals = vals.view(torch.complex64)
+        else:
+            vals = torch.view_as_complex(vals.view(torch.float64))
+        t_off.append(torch.cat([torch.zeros(1, dtype=torch.int64, device=device), voff]))
+        t_val.append(torch.cat([torch.zeros(1, dtype=vdt, device=device), vals.reshape(-1)]))
+        t_start.append(t_start[-1] + ukey.numel() + 1)
+        code = torch.zeros(nnz, dtype=torch.int32, device=device)
+        code[nz] = kcode.to(torch.int32) + 1
+        del kcode, nz, off, dv
+        q = torch.arange(nnz, device=device) - indptr[rows]
+        sl = torch.div(rows, 32, rounding_mode="floor")
+        dst = row_ptr[g, sl] + 128 * torch.div(q, 4, rounding_mode="floor") + 4 * (rows % 32) + q % 4
+        codes[dst] = code
+        del q, sl, dst, code, rows
+    if t_start[-1] > max_table:
+        return None
+    longest = max(b - a for a, b in zip(t_start[:-1], t_start[1:]))
+    cb = 1 if longest <= 256 else 2
+    codes = codes.to(torch.uint8) if cb == 1 else codes.to(torch.int16)
+    return (row_ptr.reshape(-1).to(torch.int32), widths.t().reshape(-1).to(torch.int32), codes,
+            cb, torch.cat(t_off).to(torch.int32), torch.cat(t_val),
+            torch.tensor(t_start, dtype=torch.int32, device=device), total)

@@ -217,3 +217,50 @@ def test_dict_layout_declines_incompressible_operators():
     from qutip_gb300.operator import dict_sliced_layout
     m = sp.random(3000, 3000, density=0.01, random_state=3, format="csr")
     assert dict_sliced_layout([m], 3000, "c128") is None
+
+
+@pytest.mark.parametrize("dtype", ["c128", "c64"])
+def test_device_dict_layout_reproduces_the_matvec(dtype):
+    """The device-side dictionary builder (torch, run here on CPU tensors) gives a layout
+    whose kernel walk reproduces the Liouvillian matvec, as the host builder does."""
+    import torch
+    from qutip_gb300 import systems as S
+    from qutip_gb300.superop import device_dict_layout, liouvillian_groups
+    s = S.ising_chain(3, build_terms=False)
+    groups = liouvillian_groups(s.h_terms, s.c_ops, device="cpu")
+    n = groups[0][0].numel() - 1
+    lay = device_dict_layout(groups, n, dtype)
+    assert lay is not None
+    host = tuple(v.numpy() if isinstance(v, torch.Tensor) else v for v in lay)
+    rng = np.random.default_rng(4)
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    coefs = [1.0 if c is None else c(0.8) for _, _, _, c in groups]
+    mats = [sp_from(g, n) for g in groups]
+    want = sum(c * (m @ x) for c, m in zip(coefs, mats))
+    tol = 1e-12 if dtype == "c128" else 1e-6
+    np.testing.assert_allclose(_emulate_dict(host, n, x, coefs), want, atol=tol * np.abs(want).max())
+
+
+def sp_from(group, n):
+    import scipy.sparse as sp
+    indptr, indices, data, _ = group
+    return sp.csr_matrix((data.numpy(), indices.numpy(), indptr.numpy()), shape=(n, n))
+
+
+def test_device_groups_operator_prefers_the_dictionary():
+    """``DeviceOperator.from_device_groups`` (device assembly path, run on CPU tensors)
+    builds the dictionary-coded storage and its struct, and keeps sliced on request."""
+    from qutip_gb300 import _lib
+    from qutip_gb300 import systems as S
+    from qutip_gb300.operator import DeviceOperator
+    from qutip_gb300.superop import liouvillian_groups
+    s = S.ising_chain(3, build_terms=False)
+    groups = liouvillian_groups(s.h_terms, s.c_ops, device="cpu")
+    op = DeviceOperator.from_device_groups(groups, "c128")
+    assert op.fmt == "dict" and op.struct.layout == _lib.QG_LAYOUT_SLICED_DICT
+    assert op.struct.tile_nnz == op.code_bytes == 1 and op.struct.lanes == op.val.numel()
+    assert op.struct.dict_off and op.struct.dict_start
+    op64 = op.astype("c64")
+    assert op64.fmt == "dict" and op64.val.dtype.is_complex and op64.struct.lanes == op.struct.lanes
+    sl = DeviceOperator.from_device_groups(groups, "c64", fmt="sliced")
+    assert sl.fmt == "sliced" and sl.struct.layout == _lib.QG_LAYOUT_SLICED
