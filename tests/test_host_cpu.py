@@ -264,3 +264,69 @@ def test_device_groups_operator_prefers_the_dictionary():
     assert op64.fmt == "dict" and op64.val.dtype.is_complex and op64.struct.lanes == op.struct.lanes
     sl = DeviceOperator.from_device_groups(groups, "c64", fmt="sliced")
     assert sl.fmt == "sliced" and sl.struct.layout == _lib.QG_LAYOUT_SLICED
+
+
+def _groups(layout, **kw):
+    from qutip_gb300 import _lib
+    g = _lib.CsrGroups(64, 64, 1, _lib.QG_C64, layout, 1, 0, 0, 8, 8, 8, None, None, None, None,
+                       None, None)
+    for k, v in kw.items():
+        setattr(g, k, v)
+    return g
+
+
+def test_layout_validation_before_any_device_call():
+    """The entry points reject storage they cannot read before touching the device:
+    spmm and expect need a CSR layout; the dictionary layout needs its tables, 1- or
+    2-byte codes and a table size within QG_DICT_MAX."""
+    import ctypes as C
+    from qutip_gb300 import _lib
+    lib = _lib.load()
+    x = C.c_void_p(8)
+    for layout in (_lib.QG_LAYOUT_SLICED, _lib.QG_LAYOUT_SLICED_DICT):
+        g = _groups(layout)
+        assert lib.qg_spmm_csr(C.byref(g), 0.0, x, x, 1, 64, 1.0, 0.0, 0.0, 0.0,
+                               None) == _lib.QG_ERR_UNSUPPORTED
+        v = _lib.StateView(64 * 64, 0, 0, 8, 8, 0, 0)
+        assert lib.qg_expect_dm(C.byref(g), 64, C.byref(v), x, None) == _lib.QG_ERR_UNSUPPORTED
+    base = dict(n_tiles=2, tile_row=8, dict_off=8, dict_start=8, tile_nnz=1)
+    bad = [dict(dict_off=None), dict(dict_start=None), dict(tile_row=None), dict(n_tiles=1),
+           dict(tile_nnz=4), dict(lanes=0), dict(lanes=_lib.QG_DICT_MAX + 1)]
+    for change in bad:
+        g = _groups(_lib.QG_LAYOUT_SLICED_DICT, **{**base, **change})
+        assert lib.qg_spmv_csr(C.byref(g), 0.0, x, x, 1.0, 0.0, 0.0, 0.0, None) == \
+            _lib.QG_ERR_ARG, change
+
+
+def test_lindblad_validation_before_any_device_call():
+    import ctypes as C
+    from qutip_gb300 import _lib
+    lib = _lib.load()
+    x = C.c_void_p(8)
+
+    def make(**kw):
+        L = _lib.Lindblad()
+        L.d, L.dtype, L.n_groups, L.n_diag_cops, L.n_cops = 4, _lib.QG_C64, 1, 0, 1
+        L.a_width[0], L.c_width[0] = 1, 1
+        L.a_diag = L.a_col = L.a_val = L.c_col = L.c_val = 8
+        for k, v in kw.items():
+            setattr(L, k, v)
+        return L
+    assert lib.qg_lindblad_apply(None, 0.0, x, x, 1.0, 0.0, 0.0, 0.0, None) == _lib.QG_ERR_ARG
+    bad = [dict(d=0), dict(d=46341), dict(dtype=7), dict(n_groups=0), dict(n_groups=9),
+           dict(n_cops=65), dict(n_diag_cops=2), dict(a_diag=None), dict(a_diag_const=1),
+           dict(n_const_diag=1), dict(a_col=None), dict(c_val=None)]
+    for change in bad:
+        L = make(**change)
+        rc = lib.qg_lindblad_apply(C.byref(L), 0.0, x, x, 1.0, 0.0, 0.0, 0.0, None)
+        assert rc in (_lib.QG_ERR_ARG, _lib.QG_ERR_UNSUPPORTED), change
+    L = make()
+    L.a_width[0] = -1
+    assert lib.qg_lindblad_apply(C.byref(L), 0.0, x, x, 1.0, 0.0, 0.0, 0.0, None) == _lib.QG_ERR_ARG
+    rk = _lib.RkBuffers(16, 0, 1, 8, 8, None, None, 8, 8, 8, 8, 8)
+    L = make()
+    assert lib.qg_lindblad_stage(C.byref(L), C.byref(rk), 0, 0.0, 0.1, 1e-8, 1e-6, None) == \
+        _lib.QG_ERR_ARG          # mixed form without its complex64 shadows
+    rk = _lib.RkBuffers(15, 1, 1, 8, 8, None, None, 8, 8, 8, 8, 8)
+    assert lib.qg_lindblad_stage(C.byref(L), C.byref(rk), 0, 0.0, 0.1, 1e-8, 1e-6, None) == \
+        _lib.QG_ERR_ARG          # n != d*d
