@@ -162,3 +162,24 @@ def test_map_task_decoding_under_improved_sampling(qt, plugin, mixed):
 def test_map_rejects_other_tasks(qt, plugin):
     with pytest.raises(TypeError):
         plugin.gpu_map(lambda x: x, [1, 2])
+
+
+def test_map_task_decoding_rejects_what_it_cannot_batch(qt, plugin):
+    """The batched map refuses, with TypeError, the no-jump run as a map task, trajectory
+    options it does not know, and tasks that are not an MCSolver's trajectories."""
+    H, c_ops, bright, dark, e_ops = _jc_dark(qt)
+    solver = qt.MCSolver(H, c_ops, options={"map": "serial"})
+    tl = np.linspace(0, 1, 3)
+    with pytest.raises(TypeError):
+        plugin._mc_map_items(solver._run_one_traj, [1], (bright, tl, e_ops), {"no_jump": True})
+    with pytest.raises(TypeError):
+        plugin._mc_map_items(solver._run_one_traj, [1], (bright, tl, e_ops), {"unknown": 1})
+    with pytest.raises(TypeError):
+        plugin._mc_map_items(solver._no_jump_simulation, [bright], (tl, e_ops), None)
+    me = qt.MESolver(H, c_ops, options={})
+    with pytest.raises(TypeError):
+        plugin._mc_map_items(me.run, [bright], (tl,), None)
+    seeds, starts, floors = plugin._mc_map_items(
+        solver._run_one_traj, [4, 5], (bright, tl, e_ops),
+        {"no_jump": False, "jump_prob_floor": 0.25})[1:4]
+    assert seeds == [4, 5] and floors == [0.25, 0.25] and [w for _, w in starts] == [1.0, 1.0]
