@@ -1,20 +1,25 @@
 #!/usr/bin/env python
 """Benchmark: time-dependent Lindblad solve of the dissipative transverse-field
 Ising chain, L = 10 spins (Hilbert dim 1024, Liouvillian dim 1,048,576,
-24.6 M stored entries in two coefficient groups), Vern7 atol 1e-8 / rtol 1e-6,
-tlist = linspace(0, 10, 101), 10 e_ops.
+24.6 M stored entries), Vern7 atol 1e-8 / rtol 1e-6, tlist = linspace(0, 10, 101),
+10 e_ops, through QuTiP's own solver API with the GPU integrator plugged in.
 
-One step = one complete solve in the mixed form (complex64 generator and stages
-with FP32 accumulation; FP64 state, step control and expectation values), whose
-error against the complex128 solve is reported with it.  ``value`` is solves/s
-with the operator already resident in HBM (0.3 GB, larger than L2, so no flush
-is needed); ``e2e`` repeats the solve through the host API with the operator and
-initial state copied from pinned host memory every step and the expectation
-values read back.  ``roofline`` is that of the fused Vern7 stage kernel (sliced
-ELLPACK matvec + stage combination), timed with CUDA events on its stream.
-Also reported: the complex128 form, the served mixed-size Jaynes-Cummings stream
-(continuous batching vs the plain complex128 per-request drop-in) and the
-batched 4096-trajectory Bose-Hubbard mcsolve.
+One step = one complete solve in complex128, the reference's own arithmetic:
+``MESolver(H, c_ops, options={"method": "gpu_vern7"}).run(rho0, tlist, e_ops)``
+with QuTiP's Liouvillian already on the device (the solver built once, the initial
+state resident).  ``e2e`` is the whole user call ``qutip.mesolve(H, rho0, tlist,
+c_ops, e_ops, options={"method": "gpu_vern7"})`` from host Qobjs: QuTiP's Liouvillian
+construction, the integrator's device build from host memory, the solve and the
+expectation values read back.  The mixed form (complex64 stages, FP64 state and
+step control) is reported beside it with its relative error against the
+reference's FP64 result.  ``roofline`` is that of the complex128 fused Vern7 stage
+kernel, timed with CUDA events on its stream.  Also reported: the served
+mixed-size Jaynes-Cummings stream, the batched 4096-trajectory Bose-Hubbard
+mcsolve, the matrix-free form and the L = 12 chain.
+
+``--impl reference`` times one complete solve of the same workload with the
+reference QuTiP (compiled from its sources into oracle/_ref) on the host cores,
+split into ``--steps`` chunks of output times; nothing is extrapolated.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -42,7 +47,10 @@ WORKLOAD = f"ising_chain_L{N_SITES}_mesolve_vern7"
 CONFIG = {"workload": WORKLOAD, "n_sites": N_SITES, "hilbert_dim": 2 ** N_SITES,
           "liouvillian_dim": 4 ** N_SITES, "tlist": f"linspace(0,{T_END:g},{N_OUT})",
           "atol": 1e-8, "rtol": 1e-6, "e_ops": N_SITES, "h_seed": 1234,
-          "l2": "per-step working set larger than L2 (129 MB): operator 0.06 GB (dictionary-coded; 0.3 GB uncompressed) + 16 complex64 stage vectors 0.13 GB + complex128 state 0.03 GB; no flush"}
+          "api": "qutip MESolver / mesolve (QuTiP's Liouvillian, vern7 step control)",
+          "l2": "per-step working set larger than L2 (129 MB): complex128 operator and 16 "
+                "complex128 stage vectors of 16.8 MB each; no flush"}
+GOLDEN = os.path.join(ROOT, "tests", "golden", "ising_L10_expect.npz")
 
 
 def log(msg):
@@ -56,8 +64,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample", type=float, default=0.3,
-                    help="simulated time of the CPU-baseline sample (of 10.0)")
+    ap.add_argument("--cpu-sample", type=int, default=10,
+                    help="output intervals of the CPU-baseline sample (of 100)")
+    ap.add_argument("--e2e-reps", type=int, default=2,
+                    help="whole mesolve calls timed for e2e (at most --steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline workload only")
     ap.add_argument("--sections", default="served,mc,matrix,large",
@@ -77,11 +87,39 @@ def parse():
     ap.add_argument("--profile-sites", type=int, default=10)
     ap.add_argument("--profile-fmt", default="auto", choices=["auto", "sliced", "dict", "csr"],
                     help="operator storage of the stage profiling case")
+    ap.add_argument("--profile-dtype", default="c64", choices=["c64", "c128"],
+                    help="operator dtype of the stage profiling case")
     ap.add_argument("--profile-ntraj", type=int, default=256)
     ap.add_argument("--profile-tend", type=float, default=5.0)
     ap.add_argument("--profile-group", default="auto",
                     choices=["auto", "warp", "cta", "cta128", "cluster"])
     return ap.parse_args()
+
+
+def host_qutip():
+    """QuTiP, the host framework the plugin registers into, and the workload's Qobjs.
+
+    On machines without an installed QuTiP this is the build of the reference's own
+    sources in oracle/_ref; both arms build their inputs with the same constructors
+    (``oracle.ref_workloads.ising_qobjs``).  QuTiP contributes the solver shell (option
+    handling, Liouvillian construction, the output loop); in our arm every kernel of
+    the integration runs from ``libqutip_gb300.so``."""
+    from oracle import ref_workloads as RW
+    qt = RW.import_reference()
+    return qt, RW
+
+
+def rel_err(got, want):
+    """max over e_ops of max_t |got - want| / max_t |want| (norm-wise relative error of
+    each expectation-value trajectory), and whether every point is within the
+    reference's own tolerance atol 1e-8 + rtol 1e-6 |want|."""
+    got = np.real(np.asarray(got, dtype=np.complex128))
+    want = np.asarray(want, dtype=np.float64)
+    rel = max(float(np.max(np.abs(g - w)) / max(np.max(np.abs(w)), 1e-300))
+              for g, w in zip(got, want))
+    absmax = float(np.max(np.abs(got - want)))
+    within = bool(np.all(np.abs(got - want) <= 1e-8 + 1e-6 * np.abs(want)))
+    return rel, absmax, within
 
 
 # ------------------------------------------------------------------ clocks --
@@ -191,43 +229,130 @@ class Dist:
 
 
 # ----------------------------------------------------------- cpu baseline --
-def cpu_baseline(sample_t: float):
-    """Reference vern7 mesolve (compiled from source into oracle/_ref) on the host,
-    over the first ``sample_t`` of simulated time, scaled to solves/s."""
-    from oracle import ref_workloads as RW
+def coefficient_path(qt, solver, rhs_s):
+    """How the reference evaluates the string coefficient ``cos(w*t)``: compiled by
+    Cython (``StrCoefficient``) or through Python ``eval`` (``StrFunctionCoefficient``,
+    the fallback when Cython, setuptools or filelock is missing), with its measured cost
+    per evaluation against one right-hand-side call (two evaluations per call)."""
+    coeffs = [el[1] for el in solver.rhs.to_list() if isinstance(el, list)]
+    if not coeffs:
+        return {"path": "none"}
+    c = coeffs[0]
+    name = type(c).__name__
+    path = ("eval (StrFunctionCoefficient)" if name == "StrFunctionCoefficient"
+            else "compiled (StrCoefficient)" if name == "StrCoefficient" else name)
+    reps = 2000
+    t0 = time.perf_counter()
+    for i in range(reps):
+        c(0.001 * i)
+    us = 1e6 * (time.perf_counter() - t0) / reps
+    return {"path": path, "us_per_eval": us, "evals_per_rhs": len(coeffs),
+            "share_of_rhs": len(coeffs) * us * 1e-6 / rhs_s}
+
+
+def reference_rhs_seconds(qt, solver, rho0, reps=2):
+    """Seconds per right-hand-side call of the reference (``QobjEvo.matmul_data`` of the
+    Liouvillian on vec(rho0))."""
+    from qutip.core import data as _data
+    y = _data.to(_data.Dense, qt.operator_to_vector(rho0).data)
+    solver.rhs.matmul_data(0.1, y)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        solver.rhs.matmul_data(0.1, y)
+    return (time.perf_counter() - t0) / reps
+
+
+def cpu_baseline(n_sample: int, rhs_sample: int, rhs_full: int):
+    """Reference vern7 mesolve (oracle/_ref) on the host over the first ``n_sample`` output
+    intervals, scaled to one solve by right-hand-side calls: the reference and the
+    complex128 GPU integrator take the same step sequence (tested), so the GPU solve's
+    RHS counts of the window (``rhs_sample``) and of the whole solve (``rhs_full``) scale
+    the window's time."""
+    qt, RW = host_qutip()
     cores = os.cpu_count() or 1
-    if RW.reference_available():
-        secs, frac = RW.reference_mesolve_sample(N_SITES, T_END, N_OUT, sample_t)
-        kind = "reference"
-        what = "QuTiP reference (oracle/_ref) mesolve vern7, CSR complex128, 1-thread SpMV"
-    else:
-        from qutip_gb300 import systems as S
-        s = S.ising_chain(N_SITES)
-        secs, frac = RW.port_mesolve_sample(s.terms, s.state0, s.e_ops, T_END, N_OUT, sample_t)
-        kind = "port"
-        what = "oracle numpy/scipy restatement of vern7 mesolve, complex128"
-    value = frac / secs
-    return {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
-            "sample": f"{what}; integrated t in [0,{sample_t:g}] of [0,{T_END:g}] "
-                      f"({secs:.2f} s), scaled by simulated time; BLAS threads = host cores"}
+    H, c_ops, rho0, e_ops = RW.ising_qobjs(N_SITES)
+    tlist = np.linspace(0.0, T_END, N_OUT)
+    opts = {"method": "vern7", "atol": 1e-8, "rtol": 1e-6, "progress_bar": False}
+    solver = qt.MESolver(H, c_ops, options=opts)
+    solver.run(rho0, tlist[:2], e_ops=e_ops)          # first-call setup out of the timing
+    t0 = time.perf_counter()
+    solver.run(rho0, tlist[:n_sample + 1], e_ops=e_ops)
+    secs = time.perf_counter() - t0
+    rhs_s = reference_rhs_seconds(qt, solver, rho0)
+    full_s = secs * rhs_full / max(rhs_sample, 1)
+    return {"value": 1.0 / full_s, "unit": UNIT, "cores": cores, "kind": "reference",
+            "sample": (f"QuTiP reference (oracle/_ref) MESolver.run vern7, CSR complex128 "
+                       f"(single-thread matvec, OpenBLAS vector ops on {cores} threads); "
+                       f"outputs 0..{n_sample} of {N_OUT - 1} in {secs:.2f} s = {rhs_sample} "
+                       f"RHS calls, scaled to the {rhs_full} RHS calls of the whole solve "
+                       f"(counts from the complex128 GPU solve, which takes the reference's "
+                       f"step sequence); {1e3 * rhs_s:.1f} ms per reference RHS call"),
+            "rhs_sample": rhs_sample, "rhs_full": rhs_full, "sample_s": secs,
+            "coefficient": coefficient_path(qt, solver, rhs_s)}
+
+
+def reference_solve(steps: int, warmup: int) -> dict:
+    """One complete reference solve of the workload, timed in ``steps`` chunks.
+
+    The solver is built inside the first chunk, as ``qutip.mesolve`` builds it
+    (QuTiP's Liouvillian construction included); the chunks then step through the output
+    times with ``MESolver.step`` and evaluate the e_ops with ``qutip.expect`` at every
+    output, the work ``MESolver.run`` does.  Warm-up steps are short solves of the first
+    output interval.  Returns the chunk times, the expectation values, the seconds per
+    right-hand-side call and the coefficient path."""
+    qt, RW = host_qutip()
+    H, c_ops, rho0, e_ops = RW.ising_qobjs(N_SITES)
+    tlist = np.linspace(0.0, T_END, N_OUT)
+    opts = {"method": "vern7", "atol": 1e-8, "rtol": 1e-6, "progress_bar": False}
+    warm = qt.MESolver(H, c_ops, options=opts)
+    for _ in range(warmup):
+        warm.run(rho0, tlist[:2], e_ops=e_ops)
+    K = max(1, min(steps, N_OUT - 1))
+    chunks = np.array_split(np.arange(1, N_OUT), K)
+    times = []
+    expect = np.zeros((len(e_ops), N_OUT))
+    solver = None
+    for ci, chunk in enumerate(chunks):
+        t0 = time.perf_counter()
+        if ci == 0:
+            solver = qt.MESolver(H, c_ops, options=opts)
+            solver.start(rho0, tlist[0])
+            expect[:, 0] = [qt.expect(e, rho0) for e in e_ops]
+        for i in chunk:
+            st = solver.step(tlist[i], copy=False)
+            expect[:, i] = [qt.expect(e, st) for e in e_ops]
+        times.append(time.perf_counter() - t0)
+    rhs_s = reference_rhs_seconds(qt, solver, rho0)
+    return {"times": times, "expect": expect, "rhs_s": rhs_s,
+            "coefficient": coefficient_path(qt, solver, rhs_s)}
 
 
 def run_reference(args, dist):
+    """``--impl reference``: rank 0 times one complete reference solve (``value`` = 1 /
+    the sum of its chunk times); other ranks exit without work."""
     if dist.rank != 0:
         return
-    steps = []
-    for i in range(args.warmup + args.steps):
-        b = cpu_baseline(args.cpu_sample)
-        if i >= args.warmup:
-            steps.append(b)
-    vals = [s["value"] for s in steps]
-    v = float(np.median(vals))
+    cores = os.cpu_count() or 1
+    r = reference_solve(args.steps, args.warmup)
+    times = r["times"]
+    K = len(times)
+    total = float(sum(times))
+    v = 1.0 / total
+    want = np.load(GOLDEN)["expect"]
+    sample = (f"one complete QuTiP reference mesolve (oracle/_ref, vern7, CSR complex128, "
+              f"single-thread matvec, OpenBLAS vector ops on {cores} threads) of the workload, "
+              f"Liouvillian construction included, timed in {K} chunks of output times "
+              f"({total:.1f} s); nothing extrapolated")
     out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
+           "steps": K, "warmup": args.warmup, "ms_per_step": 1e3 * total / K,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-           "data": "synthetic (seeded h_i ~ U[0.5,1.5])", "config": CONFIG,
-           "cpu_baseline": {**steps[-1], "value": v},
-           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "data": "synthetic (seeded h_i ~ U[0.5,1.5], default_rng(1234))", "config": CONFIG,
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "reference",
+                            "sample": sample},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "chunk_s": [round(x, 3) for x in times],
+           "rhs_call_s": r["rhs_s"], "coefficient": r["coefficient"],
+           "max_abs_diff_vs_golden": float(np.max(np.abs(r["expect"] - want)))}
     print(json.dumps(out))
 
 
@@ -252,7 +377,7 @@ def stage_bytes(op, n, stage, mixed):
     return b
 
 
-TRAFFIC_PROFILE = "profiles/spmv_dict_ising_L10_stage.md"
+TRAFFIC_PROFILE = "profiles/spmv_dict_c128_ising_L10_stage.md"
 SLICED_PROFILE = "profiles/spmv_sliced_ising_L10_stage.md"
 
 
@@ -268,15 +393,16 @@ def profiled_traffic(path=TRAFFIC_PROFILE):
     return None
 
 
-def measure_stage_roofline(op, sysm, precision, reps=20):
-    """Average duration and algorithmic GB/s of the fused stage kernel (events on its stream)."""
+def measure_stage_roofline(op, state0, precision, reps=20):
+    """Average duration and algorithmic GB/s of the fused stage kernel (events on its stream),
+    from the initial state ``state0`` (host vector)."""
     import ctypes as C
     import torch
     from qutip_gb300 import _lib
     from qutip_gb300.operator import stream_ptr
     from qutip_gb300.vern7 import GpuVern7
     ig = GpuVern7(op, precision=precision)
-    ig.set_initial_value(torch.from_numpy(sysm.state0).cuda(), 0.0)
+    ig.set_initial_value(torch.from_numpy(np.asarray(state0)).cuda(), 0.0)
     ig.integrate(0.05, step=True)
     total_bytes = sum(stage_bytes(op, ig.n, s, ig.mixed) for s in range(10))
     st = torch.cuda.current_stream()
@@ -518,7 +644,7 @@ def run_large(args):
         times.append(time.perf_counter() - t1)
     err = max(float(np.max(np.abs(np.real(a) - np.real(b)))) for a, b in zip(r64.expect, r128.expect))
     spmv_ms, spmv_b, spmv_gbs = measure_spmv(op64, reps=10)
-    stage_ms, stage_b, stage_gbs = measure_stage_roofline(op64, s, "mixed", reps=3)
+    stage_ms, stage_b, stage_gbs = measure_stage_roofline(op64, s.state0, "mixed", reps=3)
     peak, _ = hbm_peak_gbs()
     out = {"workload": f"ising_chain_L{L}_mesolve_vern7 mixed, tlist linspace(0,5,51)",
            "liouvillian_rows": op64.n_rows, "entries": int(op64.nnz),
@@ -537,11 +663,11 @@ def run_large(args):
     return out
 
 
-def run_matrix_form(args, sysm, tlist, ex, ref, hbm_peak):
+def run_matrix_form(args, sysm, tlist, ex, want, hbm_peak):
     """The headline workload through mesolve's matrix form (``matrix_form=True``): the
     Lindblad generator applied to vec(rho) without its superoperator
     (:class:`qutip_gb300.lindblad.LindbladOperator`), mixed precision.  Reported: solves/s,
-    the error against the complex128 superoperator solve, the fused stage kernel's time
+    the relative error against the reference's FP64 result, the fused stage kernel's time
     and algorithmic bytes, and a short solve at ``--matrix-sites`` spins (default 13,
     67,108,864 vec(rho) entries), a size whose superoperator (about 1.9e9 entries) is
     beyond 32-bit indices."""
@@ -559,12 +685,13 @@ def run_matrix_form(args, sysm, tlist, ex, ref, hbm_peak):
         res = solve_system(sysm, tlist, opts, op=lop, ex=ex)
         torch.cuda.synchronize()
         times.append(time.perf_counter() - t0)
-    err = max(float(np.max(np.abs(res.expect[k] - ref.expect[k]))) for k in range(len(ex.ops)))
-    ms, b, gbs = measure_stage_roofline(lop, sysm, "mixed")
+    rel, absmax, within = rel_err(res.expect, want)
+    ms, b, gbs = measure_stage_roofline(lop, sysm.state0, "mixed")
     out = {"workload": f"ising_chain_L{N_SITES} mesolve matrix_form=True, mixed, tlist "
                        f"linspace(0,{T_END:g},{N_OUT})",
            "solves_per_sec": 1.0 / float(np.median(times)),
-           "max_abs_err_vs_fp64_superoperator": err,
+           "rel_err_vs_reference_fp64": rel, "max_abs_err_vs_reference_fp64": absmax,
+           "within_reference_tolerance": within,
            "stage_kernel": {"kernel": "lindblad_kernel<C64,C128,RK>", "ms": ms,
                             "algorithmic_bytes": int(b), "gbs": gbs, "frac_hbm": gbs / hbm_peak,
                             "bound": "instruction issue (operators L1-resident, state "
@@ -585,7 +712,7 @@ def run_matrix_form(args, sysm, tlist, ex, ref, hbm_peak):
         rb = solve_system(s, tl, opts, op=big, ex=exb)
         torch.cuda.synchronize()
         run_s = time.perf_counter() - t0
-        bms, bb, bgbs = measure_stage_roofline(big, s, "mixed", reps=2)
+        bms, bb, bgbs = measure_stage_roofline(big, s.state0, "mixed", reps=2)
         out["large"] = {"workload": f"ising_chain_L{L} mesolve matrix_form=True, mixed, "
                                     "tlist linspace(0,0.05,3)",
                         "vec_rho_entries": big.n_rows, "build_s": build_s, "solve_s": run_s,
@@ -597,37 +724,58 @@ def run_matrix_form(args, sysm, tlist, ex, ref, hbm_peak):
     return out
 
 
+def mesolve_opts(precision):
+    return {"method": "gpu_vern7", "atol": 1e-8, "rtol": 1e-6, "progress_bar": False,
+            "precision": precision}
+
+
+def operator_upload_bytes(rhs, rho0) -> int:
+    """Host-to-device bytes of one mesolve call: each Liouvillian element's CSR arrays as
+    stored (32-bit indices and row pointers, complex128 values) and the initial state."""
+    import scipy.sparse as sp
+    b = 0
+    for el in rhs.to_list():
+        q = el[0] if isinstance(el, list) else el
+        m = sp.csr_matrix(q.data.as_scipy())
+        b += m.data.nbytes + m.indices.nbytes + m.indptr.nbytes
+    n = rho0.shape[0]
+    return b + 16 * n * n
+
+
 def run_ours(args, dist):
     import torch
     from qutip_gb300 import _lib
     from qutip_gb300 import systems as S
-    from qutip_gb300.operator import DeviceOperator
-    from qutip_gb300.solver import ExpectOps, solve_system
+    from qutip_gb300.solver import ExpectOps
 
     dist.init()
     hbm_peak, peak_src = hbm_peak_gbs()
-
-    log("building the Ising L=10 Liouvillian")
-    sysm = S.ising_chain(N_SITES)
+    qt, RW = host_qutip()
+    from qutip_gb300 import qutip_plugin  # noqa: F401  (registers gpu_vern7, GpuDense)
+    H, c_ops, rho0, e_ops = RW.ising_qobjs(N_SITES)
     tlist = np.linspace(0.0, T_END, N_OUT)
-    op64 = DeviceOperator(sysm.terms, dtype="c64")
-    op64.tune()
-    op = DeviceOperator(sysm.terms, dtype="c128")
-    op.tune()
-    ex = ExpectOps(sysm.e_ops)
+    want = np.load(GOLDEN)["expect"]             # the reference's FP64 result
 
-    def solve(o=op64, prec="mixed"):
-        return solve_system(sysm, tlist, {"precision": prec}, op=o, ex=ex)
+    log("building the complex128 solver (QuTiP's Liouvillian, device operator)")
+    t0 = time.perf_counter()
+    solver = qt.MESolver(H, c_ops, options=mesolve_opts("double"))
+    build_s = time.perf_counter() - t0
+    ig = solver._integrator
+    op = ig._op
+    rho_dev = rho0.to("gpu")
 
-    log("FP64 reference solve")
-    ref = solve(op, "double")  # FP64 result the mixed form is checked against
-    log("warm-up")
+    def solve(s=solver):
+        return s.run(rho_dev, tlist, e_ops=e_ops)
+
+    log(f"warm-up ({op.launch_desc()})")
     for _ in range(args.warmup):
-        solve()
+        res = solve()
     dist.barrier()
     clocks = ClockSampler(dist.local)
     clocks.start()
     n0 = _lib.LAUNCHES[0]
+    rhs0 = ig._ode.stats["rhs"]
+    steps0 = ig._ode.stats["steps"]
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(args.steps):
@@ -636,83 +784,99 @@ def run_ours(args, dist):
     dist.barrier()
     ms = e0.elapsed_time(e1)
     launches = _lib.LAUNCHES[0] - n0
+    rhs_full = (ig._ode.stats["rhs"] - rhs0) // args.steps
+    steps_full = (ig._ode.stats["steps"] - steps0) // args.steps
     clk = clocks.stop()
     ms_max = dist.max(ms)
     value = args.steps * dist.world / (ms_max / 1000.0)
-    err_m = max(float(np.max(np.abs(res.expect[k] - ref.expect[k]))) for k in range(N_SITES))
+    rel, absmax, within = rel_err(res.expect, want)
+    log(f"headline {value:.3f} solves/s complex128, rel err {rel:.2e} vs the reference")
 
-    log(f"headline {value:.3f} solves/s; end-to-end")
-    # end to end: operator + initial state from pinned host memory every step, expect read back
-    host = op64.host_copy()
-    h2d = sum(h.numel() * h.element_size() for h in host) + sysm.state0.nbytes
-    d2h = N_OUT * 2 * (len(sysm.e_ops) + 1) * 8
+    # end to end: the whole user call from host Qobjs, every step
+    n_e2e = max(1, min(args.steps, args.e2e_reps))
     dist.barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        op64.upload(host)
-        solve()
+    for _ in range(n_e2e):
+        r_e2e = qt.mesolve(H, rho0, tlist, c_ops, e_ops=e_ops, options=mesolve_opts("double"))
     dist.barrier()
-    e2e = args.steps * dist.world / dist.max(time.perf_counter() - t0)
-
-    # complex128 form (the plain drop-in precision)
-    nd = max(1, args.steps // 2)
+    e2e = n_e2e * dist.world / dist.max(time.perf_counter() - t0)
+    rel_e2e, _, within_e2e = rel_err(r_e2e.expect, want)
+    h2d = operator_upload_bytes(solver.rhs, rho0)
+    d2h = N_OUT * (32 * len(e_ops) + 16) + 8 * steps_full
+    # where the end-to-end time goes: QuTiP's host Liouvillian, the device build
+    t0 = time.perf_counter()
+    ref_solver = qt.MESolver(H, c_ops, options={"method": "vern7"})
+    liou_s = time.perf_counter() - t0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(nd):
-        solve(op, "double")
+    qutip_plugin.IntegratorGpuVern7(ref_solver, mesolve_opts("double"))
     torch.cuda.synchronize()
-    double_v = nd / (time.perf_counter() - t0)
+    dev_build_s = time.perf_counter() - t0
+    del ref_solver
+    log(f"e2e {e2e:.3f} solves/s (Liouvillian {liou_s:.2f} s, device build {dev_build_s:.2f} s)")
+
+    # the mixed form through the same API
+    solver_m = qt.MESolver(H, c_ops, options=mesolve_opts("mixed"))
+    solve(solver_m)
+    nm = max(2, args.steps // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(nm):
+        res_m = solve(solver_m)
+    torch.cuda.synchronize()
+    mixed_v = nm / (time.perf_counter() - t0)
+    rel_m, abs_m, within_m = rel_err(res_m.expect, want)
+    op64 = solver_m._integrator._op
 
     log("roofline measurements")
-    stage_ms, stage_b, stage_gbs = measure_stage_roofline(op64, sysm, "mixed")
-    # the same stage with the uncompressed sliced operator (12 bytes per entry)
-    op_sl = DeviceOperator(sysm.terms, dtype="c64", fmt="sliced")
-    sl_ms, sl_b, sl_gbs = measure_stage_roofline(op_sl, sysm, "mixed")
-    del op_sl
-    stage128_ms, stage128_b, stage128_gbs = measure_stage_roofline(op, sysm, "double")
+    state0 = rho0.full().reshape(-1, order="F")
+    stage_ms, stage_b, stage_gbs = measure_stage_roofline(op, state0, "double")
     spmv_ms, spmv_b, spmv_gbs = measure_spmv(op)
+    st64_ms, st64_b, st64_gbs = measure_stage_roofline(op64, state0, "mixed")
     spmv64_ms, spmv64_b, spmv64_gbs = measure_spmv(op64)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c64 stages / f64 state (mixed)",
-        "accuracy": {"max_abs_err_vs_fp64_expect": err_m, "bound": 1e-6,
-                     "fp64_reference": "the same solve in complex128 on the GPU, which matches "
-                                       "the reference QuTiP within atol 1e-8 / rtol 1e-6"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "accuracy": {"rel_err_vs_reference_fp64": rel, "max_abs_err": absmax,
+                     "within_reference_tolerance": within,
+                     "reference": "the reference QuTiP's own vern7 mesolve of the same inputs "
+                                  "(tests/golden/ising_L10_expect.npz); rel = max over e_ops of "
+                                  "max_t |d| / max_t |want|; tolerance atol 1e-8 + rtol 1e-6 |want|"},
         "data": "synthetic (seeded h_i ~ U[0.5,1.5], default_rng(1234))",
-        "config": {**CONFIG, "parallelism": "replicas" if dist.world > 1 else "single",
-                   "spmv_launch": op64.launch_desc()},
+        "config": CONFIG,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h),
+                "call": "qutip.mesolve(H, rho0, tlist, c_ops, e_ops, options={'method': "
+                        "'gpu_vern7'}) from host Qobjs",
+                "reps": n_e2e, "rel_err_vs_reference_fp64": rel_e2e,
+                "within_reference_tolerance": within_e2e,
+                "breakdown_s": {"qutip_liouvillian_host": liou_s, "device_build": dev_build_s,
+                                "solve": 1.0 / value}},
         "gpu_launches": int(launches),
+        "solver_stats": {"steps": int(steps_full), "rhs": int(rhs_full),
+                         "build_s": build_s, "launch": op.launch_desc()},
         "roofline": {"bound": "hbm", "achieved": stage_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": stage_gbs / hbm_peak, "traffic": profiled_traffic(),
+                     "frac": stage_gbs / hbm_peak, "traffic": profiled_traffic(TRAFFIC_PROFILE),
                      "traffic_source": f"{TRAFFIC_PROFILE} (ncu dram__bytes_read.sum + "
-                                       "dram__bytes_write.sum, mean over the 10 stage launches "
-                                       "of a step, same operator)",
-                     "kernel": (f"spmv_dict_kernel<C64,C128,RK,{op64.code_bytes}> (fused Vern7 "
-                                "stage, mixed, dictionary-coded operator)" if op64.fmt == "dict"
-                                else "spmv_sliced_kernel<C64,C128,RK> (fused Vern7 stage, mixed)"),
+                                       "dram__bytes_write.sum per launch)",
+                     "kernel": (f"spmv_dict_kernel<C128,C128,RK,{op.code_bytes}> (fused Vern7 "
+                                "stage, complex128, dictionary-coded operator)"
+                                if op.fmt == "dict" else
+                                "spmv_sliced_kernel<C128,C128,RK> (fused Vern7 stage)"),
                      "bytes_per_launch": stage_b, "ms_per_launch": stage_ms,
-                     "peak_source": f"{peak_src} hbm_gbs (of {peak_src})",
-                     "note": "the dictionary codes cut the operator stream from 12 to 2 bytes "
-                             "per entry, so HBM no longer bounds this kernel: shared-memory "
-                             "table lookups and L2 gathers of x do; see roofline_uncompressed "
-                             "for the same stage with the 12-byte entries"},
-        "roofline_uncompressed": {"kernel": "spmv_sliced_kernel<C64,C128,RK>",
-                                  "bound": "hbm", "achieved": sl_gbs, "peak": hbm_peak,
-                                  "unit": "GB/s", "frac": sl_gbs / hbm_peak,
-                                  "bytes_per_launch": sl_b, "ms_per_launch": sl_ms,
-                                  "traffic": profiled_traffic(SLICED_PROFILE),
-                                  "traffic_source": SLICED_PROFILE},
-        "double_precision": {"value": double_v, "unit": UNIT,
-                             "stage_kernel_gbs": stage128_gbs, "stage_kernel_ms": stage128_ms,
-                             "bound": "FP64 throughput (about 4 DFMA per stored entry)"},
-        "spmv": {"c64_gbs": spmv64_gbs, "c64_ms": spmv64_ms, "c64_bytes": spmv64_b,
-                 "frac_c64": spmv64_gbs / hbm_peak, "c128_gbs": spmv_gbs, "c128_ms": spmv_ms,
-                 "c128_bytes": spmv_b, "frac_c128": spmv_gbs / hbm_peak},
-        "solver_stats": {k: res.stats[k] for k in ("steps", "rejected", "rhs")},
+                     "peak_source": f"{peak_src} hbm_gbs (of {peak_src})"},
+        "spmv": {"c128_gbs": spmv_gbs, "c128_ms": spmv_ms, "c128_bytes": spmv_b,
+                 "frac_c128": spmv_gbs / hbm_peak, "c64_gbs": spmv64_gbs, "c64_ms": spmv64_ms,
+                 "c64_bytes": spmv64_b, "frac_c64": spmv64_gbs / hbm_peak},
+        "mixed": {"value": mixed_v, "unit": UNIT, "dtype": "c64 stages / f64 state and step control",
+                  "rel_err_vs_reference_fp64": rel_m, "max_abs_err": abs_m,
+                  "within_reference_tolerance": within_m, "bound_rel": 1e-6,
+                  "stage_kernel": {"kernel": f"spmv_dict_kernel<C64,C128,RK,{op64.code_bytes}>"
+                                   if op64.fmt == "dict" else op64.launch_desc(),
+                                   "ms": st64_ms, "bytes": st64_b, "gbs": st64_gbs,
+                                   "frac_hbm": st64_gbs / hbm_peak}},
         "clocks": clk,
     }
     sections = set() if args.quick else set(args.sections.split(","))
@@ -724,14 +888,20 @@ def run_ours(args, dist):
         out["mc_batched"] = run_mc_batch(args)
     if dist.rank == 0 and "matrix" in sections:
         log("matrix form")
-        out["matrix_form"] = run_matrix_form(args, sysm, tlist, ex, ref, hbm_peak)
+        sysm = S.ising_chain(N_SITES, build_terms=False)
+        out["matrix_form"] = run_matrix_form(args, sysm, tlist, ExpectOps(sysm.e_ops), want,
+                                             hbm_peak)
     if dist.rank == 0 and "large" in sections and args.large_sites:
         log(f"large: Ising L={args.large_sites}")
         out["large"] = run_large(args)
     if dist.rank == 0 and not args.no_cpu_baseline:
         log("CPU baseline")
         try:
-            out["cpu_baseline"] = cpu_baseline(args.cpu_sample)
+            k = max(1, min(args.cpu_sample, N_OUT - 1))
+            ig._ode.stats["rhs"] = 0
+            solver.run(rho_dev, tlist[:k + 1], e_ops=e_ops)
+            rhs_sample = int(ig._ode.stats["rhs"])
+            out["cpu_baseline"] = cpu_baseline(k, rhs_sample, int(rhs_full))
         except Exception as exc:  # noqa: BLE001
             out["cpu_baseline"] = {"value": None, "error": repr(exc)[:300]}
     if dist.rank == 0:
@@ -750,13 +920,13 @@ def run_profile_case(args):
     from qutip_gb300.vern7 import GpuVern7
     torch.cuda.set_device(0)
     s = S.ising_chain(args.profile_sites)
-    op = DeviceOperator(s.terms, dtype="c64", fmt=args.profile_fmt)
-    ig = GpuVern7(op, precision="mixed")
+    op = DeviceOperator(s.terms, dtype=args.profile_dtype, fmt=args.profile_fmt)
+    ig = GpuVern7(op, precision="mixed" if args.profile_dtype == "c64" else "double")
     ig.set_initial_value(torch.from_numpy(s.state0).cuda(), 0.0)
     for _ in range(2):
         ig.integrate(ig.t_front + 0.05, step=True)
     torch.cuda.synchronize()
-    print(f"c64 mixed: launch {op.launch_desc()}, {op.spmv_bytes() / 1e9:.3f} GB per matvec")
+    print(f"{args.profile_dtype}: launch {op.launch_desc()}, {op.spmv_bytes() / 1e9:.3f} GB per matvec")
 
 
 def run_profile_matrix(args):

@@ -75,15 +75,24 @@ typedef enum {
  *   QG_DICT_MAX); code 0 of every group is padding (offset 0, value 0).  col points to
  *   the codes, tile_nnz bytes each (1 or 2).  Each group has its own code section:
  *   row_ptr[g*(n_tiles+1) + s] is the code offset of slice s of group g (a multiple of
- *   128), tile_row[s*G + g] its width (a multiple of 4), and codes are stored four per
- *   lane: entries 4q..4q+3 of lane l of the slice at row_ptr[...] + 128 q + 4 l + (0..3).
- *   Columns are clamped into [0, n_cols), so no code can address outside x.
+ *   128), tile_row[s*G + g] its width w (the longest row; the section holds 4*ceil(w/4)
+ *   codes per lane), and codes are stored four per lane: entries 4q..4q+3 of lane l of
+ *   the slice at row_ptr[...] + 128 q + 4 l + (0..3).  Columns are clamped into
+ *   [0, n_cols), so no code can address outside x.
+ * QG_LAYOUT_SLICED_DICT_RI (complex128 only): QG_LAYOUT_SLICED_DICT with the real and the
+ *   imaginary part of every entry coded separately, so that a code costs two FP64
+ *   multiply-adds instead of four.  Table entry t stands for column
+ *   row + (dict_off[t] >> 1); with the low bit of dict_off[t] clear it is the real part a
+ *   of an entry and val[t] = (a, a), with it set an imaginary part i a and
+ *   val[t] = (-a, a).  The product is (val.re * p, val.im * q) with (p, q) = (x.re, x.im),
+ *   or (x.im, x.re) for an imaginary part.  A complex entry occupies two codes.
  * Coefficient programs are the bytecode of qutip_gb300/coefficients.py;
  * coef_code == NULL means every c_g = 1. */
 #define QG_LAYOUT_GROUP_MAJOR 0
 #define QG_LAYOUT_ROW_MAJOR 1
 #define QG_LAYOUT_SLICED 2
 #define QG_LAYOUT_SLICED_DICT 3
+#define QG_LAYOUT_SLICED_DICT_RI 4
 #define QG_DICT_MAX 4096
 #define QG_TILE_ROWS 512
 typedef struct qg_csr_groups {
@@ -102,8 +111,8 @@ typedef struct qg_csr_groups {
   const int32_t* coef_code;
   const int32_t* coef_start; /* [n_groups+1] */
   const double* coef_consts; /* complex constants as (re, im) pairs */
-  const int32_t* dict_off;   /* QG_LAYOUT_SLICED_DICT: column - row of each table entry */
-  const int32_t* dict_start; /* QG_LAYOUT_SLICED_DICT: [n_groups+1] table bounds */
+  const int32_t* dict_off;   /* dictionary layouts: column - row of each table entry */
+  const int32_t* dict_start; /* dictionary layouts: [n_groups+1] table bounds */
 } qg_csr_groups;
 
 /* Dia matrix in the reference's layout (qutip/core/data/dia.pxd:17-38):

@@ -18,6 +18,7 @@ QG_MAX_GROUPS, QG_MAX_EOPS, QG_MAX_COPS = 8, 32, 64
 
 
 QG_LAYOUT_GROUP_MAJOR, QG_LAYOUT_ROW_MAJOR, QG_LAYOUT_SLICED, QG_LAYOUT_SLICED_DICT = 0, 1, 2, 3
+QG_LAYOUT_SLICED_DICT_RI = 4
 QG_DICT_MAX = 4096
 QG_TILE_ROWS = 512
 QG_GROUP_AUTO, QG_GROUP_WARP, QG_GROUP_CTA, QG_GROUP_CLUSTER, QG_GROUP_CTA128 = 0, 1, 2, 3, 4

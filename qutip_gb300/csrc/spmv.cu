@@ -188,6 +188,9 @@ __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
     st_cx(k + (size_t)s * n64 + row, acc);
     const cx<CT> ks = ld_cx<CT>(k + (size_t)s * n64 + row);  // the stored (rounded) k_s
     constexpr bool MIXED = (DT != YDT);
+    // The factor loops are unrolled over compile-time indices (the bound s is a runtime
+    // value): indexed at run time, the factor arrays of the kernel parameters would be
+    // copied to local memory by every thread.
     if (s != RK_STEP - 1 && s != RK_EXTRA_STEP - 1) {
       // next stage input: base + sum_{j<=s} fa_j k_j, in the reference's order
       cx<CT> v;
@@ -195,7 +198,9 @@ __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
         v = ld_cx<CT>(static_cast<const ST*>(rk.y_prev_s) + row);
       else
         v = ld_cx<CT>(static_cast<const YT*>(rk.y_prev) + row);
-      for (int j = 0; j <= s; ++j) {
+#pragma unroll
+      for (int j = 0; j < RK_EXTRA_STEP - 1; ++j) {
+        if (j > s) break;
         const CT f = fa<CT>(rk, j);
         if (f != (CT)0) cx_axpy(v, f, j == s ? ks : ld_cx<CT>(k + (size_t)j * n64 + row));
       }
@@ -205,6 +210,7 @@ __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
       CT ymag;
       if constexpr (MIXED) {
         cx<CT> inc{0, 0};
+#pragma unroll
         for (int j = 0; j < RK_STEP; ++j) {
           const CT fb = fa<CT>(rk, j), fq = fe<CT>(rk, j);
           if (fb == (CT)0 && fq == (CT)0) continue;
@@ -222,6 +228,7 @@ __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
       } else {
         // reference order: y_front = y_prev, then += fb_j k_j term by term
         cx<CT> y = ld_cx<CT>(static_cast<const YT*>(rk.y_prev) + row);
+#pragma unroll
         for (int j = 0; j < RK_STEP; ++j) {
           const CT fb = fa<CT>(rk, j), fq = fe<CT>(rk, j);
           if (fb == (CT)0 && fq == (CT)0) continue;
@@ -535,7 +542,46 @@ struct Codes4<2> {
   }
 };
 
-template <int DT, int YDT, int EPI, int CB>
+// One stored code: the table pair k applied to x[row + offset].  Whole complex values
+// (QG_LAYOUT_SLICED_DICT) cost four multiply-adds.  With the real/imaginary split
+// (QG_LAYOUT_SLICED_DICT_RI, complex128) a table entry is one real factor: toff holds
+// (offset << 1) | imag and tval the pair (c1, c2) = (a, a) for a real part or (-a, a) for
+// an imaginary part, applied as (c1 p, c2 q) with (p, q) = x, or x's parts exchanged for
+// an imaginary part -- two FP64 multiply-adds, GB300's scarce FP64 rate being the bound.
+template <bool RI, typename ST, typename R>
+__device__ __forceinline__ void dict_mac(const ST* __restrict__ tval, const int* __restrict__ toff,
+                                         const ST* __restrict__ x, int k, int row, int last_col,
+                                         R& ar, R& ai) {
+  if constexpr (RI) {
+    const int oc = toff[k];
+    const int col = min(max(row + (oc >> 1), 0), last_col);
+    const ST v = tval[k];
+    const ST xv = ld_gather(x + col);
+    const bool sw = (oc & 1) != 0;
+    ar = fma(v.x, sw ? xv.y : xv.x, ar);
+    ai = fma(v.y, sw ? xv.x : xv.y, ai);
+  } else {
+    const int col = min(max(row + toff[k], 0), last_col);
+    cmac_any(ar, ai, tval[k], ld_gather(x + col));
+  }
+}
+
+// acc += c * (ar, ai).  In FP64 a real coefficient (every group of a Liouvillian with a
+// real time dependence, and the constant group) takes two multiply-adds, not four; the
+// branch is uniform (one coefficient per group).  FP32 keeps the plain product.
+template <typename R>
+__device__ __forceinline__ void coef_mac(cx<R>& acc, cx<R> c, R ar, R ai) {
+  if constexpr (sizeof(R) == 8) {
+    if (c.im == (R)0) {
+      acc.re = fma(c.re, ar, acc.re);
+      acc.im = fma(c.re, ai, acc.im);
+      return;
+    }
+  }
+  acc = cx_add(acc, cx_mul(c, cx<R>{ar, ai}));
+}
+
+template <int DT, int YDT, int EPI, int CB, bool RI>
 __global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, 4>::MIN_BLOCKS)
     spmv_dict_kernel(qg_csr_groups A, double t, const typename elem<DT>::T* __restrict__ x,
                      AxpbyArgs ax, RkArgs rk) {
@@ -569,24 +615,42 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, 4>::MIN_BLOCKS)
     const int row = sl * 32 + lane;
     cx<R> acc{0, 0};
     for (int g = 0; g < G; ++g) {
-      const int w4 = __ldg(A.tile_row + sl * G + g) >> 2;  // chunks of four entries
+      // exact width (uniform over the warp): whole chunks of four codes, then a tail
+      const int w = __ldg(A.tile_row + sl * G + g);
+      const int wq = w >> 2, wr = w & 3;
       const int t0 = tstart[g], tn = tstart[g + 1] - t0;
       const C4* __restrict__ cp =
           reinterpret_cast<const C4*>(codes + (size_t)CB * __ldg(A.row_ptr + g * (S + 1) + sl)) +
           lane;
       R ar = 0, ai = 0;
 #pragma unroll 2
-      for (int q = 0; q < w4; ++q) {
+      for (int q = 0; q < wq; ++q) {
         const C4 c4 = ld_stream(cp + 32 * q);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           int k = Codes4<CB>::at(c4, u);
+          if constexpr (RI) {  // FP64-bound: skip a position that is padding in every row
+            if (!__any_sync(0xffffffffu, k != 0)) continue;
+          }
           k = t0 + (k < tn ? k : 0);  // a table index of this group whatever the code
-          const int col = min(max(row + toff[k], 0), last_col);
-          cmac_any(ar, ai, tval[k], ld_gather(x + col));
+          dict_mac<RI>(tval, toff, x, k, row, last_col, ar, ai);
         }
       }
-      acc = cx_add(acc, cx_mul(coef[g], cx<R>{ar, ai}));
+      if (wr) {
+        const C4 c4 = ld_stream(cp + 32 * wq);
+#pragma unroll
+        for (int u = 0; u < 3; ++u) {
+          if (u < wr) {
+            int k = Codes4<CB>::at(c4, u);
+            if constexpr (RI) {
+              if (!__any_sync(0xffffffffu, k != 0)) continue;
+            }
+            k = t0 + (k < tn ? k : 0);
+            dict_mac<RI>(tval, toff, x, k, row, last_col, ar, ai);
+          }
+        }
+      }
+      coef_mac(acc, coef[g], ar, ai);
     }
     if (row < n) epilogue<DT, YDT, EPI>(row, acc, ax, rk, err_acc);
   }
@@ -815,11 +879,11 @@ static int launch_staged(cudaStream_t st, const qg_csr_groups& A, double t, cons
   return check_launch("spmv_staged_kernel");
 }
 
-template <int DT, int YDT, int EPI, int CB>
+template <int DT, int YDT, int EPI, int CB, bool RI>
 static int launch_dict(cudaStream_t st, const qg_csr_groups& A, double t, const void* x,
                        const AxpbyArgs& ax, const RkArgs& rk) {
   using ST = typename elem<DT>::T;
-  auto kern = spmv_dict_kernel<DT, YDT, EPI, CB>;
+  auto kern = spmv_dict_kernel<DT, YDT, EPI, CB, RI>;
   const size_t smem = ((size_t)A.lanes * (sizeof(ST) + sizeof(int)) + 15) & ~(size_t)15;
   static OccCache cache;  // one per instantiation
   const int per_sm = staged_occupancy(kern, SPMV_BLOCK, smem, cache);
@@ -838,8 +902,14 @@ static int launch_any(cudaStream_t st, const qg_csr_groups& A, double t, const v
   using ST = typename elem<DT>::T;
   const int lanes = A.lanes > 0 ? A.lanes : 4;
   if (A.layout == QG_LAYOUT_SLICED_DICT)
-    return A.tile_nnz == 1 ? launch_dict<DT, YDT, EPI, 1>(st, A, t, x, ax, rk)
-                           : launch_dict<DT, YDT, EPI, 2>(st, A, t, x, ax, rk);
+    return A.tile_nnz == 1 ? launch_dict<DT, YDT, EPI, 1, false>(st, A, t, x, ax, rk)
+                           : launch_dict<DT, YDT, EPI, 2, false>(st, A, t, x, ax, rk);
+  if (A.layout == QG_LAYOUT_SLICED_DICT_RI) {
+    if constexpr (DT == QG_C128)
+      return A.tile_nnz == 1 ? launch_dict<DT, YDT, EPI, 1, true>(st, A, t, x, ax, rk)
+                             : launch_dict<DT, YDT, EPI, 2, true>(st, A, t, x, ax, rk);
+    return set_error(QG_ERR_UNSUPPORTED, "the real/imaginary split dictionary is complex128 only");
+  }
   if (A.layout == QG_LAYOUT_SLICED) {
     // one wave: every block resident at once, warps striding over the slices.  (8
     // entries in flight at 64 registers measured slower than 4 at 40: 73 vs 68 us
@@ -916,9 +986,12 @@ static int check_groups(const qg_csr_groups* A) {
   if (A->dtype != QG_C128 && A->dtype != QG_C64)
     return set_error(QG_ERR_UNSUPPORTED, "operator dtype must be QG_C128 or QG_C64");
   if (A->layout != QG_LAYOUT_GROUP_MAJOR && A->layout != QG_LAYOUT_ROW_MAJOR &&
-      A->layout != QG_LAYOUT_SLICED && A->layout != QG_LAYOUT_SLICED_DICT)
+      A->layout != QG_LAYOUT_SLICED && A->layout != QG_LAYOUT_SLICED_DICT &&
+      A->layout != QG_LAYOUT_SLICED_DICT_RI)
     return set_error(QG_ERR_ARG, "unknown row-pointer layout");
-  if (A->layout == QG_LAYOUT_SLICED_DICT) {
+  if (A->layout == QG_LAYOUT_SLICED_DICT_RI && A->dtype != QG_C128)
+    return set_error(QG_ERR_UNSUPPORTED, "the real/imaginary split dictionary is complex128 only");
+  if (A->layout == QG_LAYOUT_SLICED_DICT || A->layout == QG_LAYOUT_SLICED_DICT_RI) {
     if (!A->tile_row || !A->dict_off || !A->dict_start || A->n_tiles != (A->n_rows + 31) / 32)
       return set_error(QG_ERR_ARG,
                        "dictionary layout needs n_tiles = ceil(n_rows/32), widths and tables");

@@ -111,7 +111,34 @@ def sliced_layout(mats, n_cols):
     return slice_ptr, widths.reshape(-1).astype(np.int32), col, val, total
 
 
-def dict_sliced_layout(mats, n_cols, dtype: str, max_table: int = _lib.QG_DICT_MAX):
+def split_entries(m):
+    """The real/imaginary split of a CSR matrix's entries: every entry becomes its nonzero
+    real part ``(off << 1, a)`` and its nonzero imaginary part ``((off << 1) | 1, a)``, in
+    row order, then ``col XOR row`` order, real part first.  ``off`` is column - row.
+    Returns ``(rows, off2, a)``: int64, int64, float64."""
+    m = sp.csr_matrix(m, dtype=np.complex128)
+    n = m.shape[0]
+    rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(m.indptr))
+    order = np.lexsort((m.indices.astype(np.int64) ^ rows, rows))
+    ci = m.indices[order].astype(np.int64)
+    dv = m.data[order]
+    r2 = np.repeat(rows, 2)
+    off2 = np.repeat(ci - rows, 2) * 2 + np.tile(np.array([0, 1], np.int64), len(dv))
+    a = np.stack([dv.real, dv.imag], axis=1).reshape(-1)
+    keep = a != 0
+    return r2[keep], off2[keep], a[keep]
+
+
+def split_table_values(off2, a):
+    """Table values of split entries: ``(a, a)`` for a real part (the product is
+    ``a x``), ``(-a, a)`` for an imaginary part, whose product ``i a x`` is formed from x
+    with its real and imaginary parts exchanged."""
+    imag = (off2 & 1) == 1
+    return np.where(imag, -a, a) + 1j * a
+
+
+def dict_sliced_layout(mats, n_cols, dtype: str, max_table: int = _lib.QG_DICT_MAX,
+                       split: bool = False):
     """Dictionary-coded sliced ELLPACK of coefficient groups, or ``None`` when the groups'
     (column - row, value) pairs do not fit ``max_table`` table entries.
 
@@ -121,7 +148,14 @@ def dict_sliced_layout(mats, n_cols, dtype: str, max_table: int = _lib.QG_DICT_M
     ``base + 128 q + 4 l``).  Code 0 of every group is padding (offset 0, value 0).
     Values are deduplicated in the operator's dtype.  Returns ``(row_ptr[G*(S+1)],
     widths[S*G], codes, code_bytes, table_off, table_val, table_start[G+1], stored)``.
+
+    ``split=True`` (complex128, ``QG_LAYOUT_SLICED_DICT_RI``) codes the real and the
+    imaginary part of every entry separately (:func:`split_entries`), so that each code
+    costs two FP64 multiply-adds instead of four; table offsets are then ``off << 1``
+    with the low bit set for an imaginary part.
     """
+    if split:
+        return _dict_split_layout(mats, n_cols, max_table)
     mats = [sp.csr_matrix(m, dtype=np.complex128) for m in mats]
     n = mats[0].shape[0]
     G = len(mats)
@@ -131,8 +165,8 @@ def dict_sliced_layout(mats, n_cols, dtype: str, max_table: int = _lib.QG_DICT_M
     for g, m in enumerate(mats):
         c = np.zeros(S * 32, dtype=np.int64)
         c[:n] = np.diff(m.indptr)
-        widths[:, g] = (c.reshape(S, 32).max(axis=1) + 3) // 4 * 4
-    sect = 32 * widths                                   # codes per (slice, group)
+        widths[:, g] = c.reshape(S, 32).max(axis=1)      # exact: the kernel skips the rest
+    sect = 32 * ((widths + 3) // 4 * 4)                  # codes per (slice, group)
     gsize = sect.sum(axis=0)                             # codes per group
     gbase = np.concatenate([[0], np.cumsum(gsize)[:-1]])
     row_ptr = np.zeros((G, S + 1), dtype=np.int64)
@@ -171,6 +205,57 @@ def dict_sliced_layout(mats, n_cols, dtype: str, max_table: int = _lib.QG_DICT_M
     cb = 1 if max(b - a for a, b in zip(t_start[:-1], t_start[1:])) <= 256 else 2
     if cb == 2 and max(b - a for a, b in zip(t_start[:-1], t_start[1:])) > 65536:
         return None
+    return (row_ptr.reshape(-1), widths.reshape(-1).astype(np.int32),
+            codes.astype(np.uint8 if cb == 1 else np.uint16), cb,
+            np.concatenate(t_off), np.concatenate(t_val), np.asarray(t_start, np.int32), total)
+
+
+def _dict_split_layout(mats, n_cols, max_table):
+    """:func:`dict_sliced_layout` of the real/imaginary split entries (complex128)."""
+    n = mats[0].shape[0]
+    G = len(mats)
+    S = (n + 31) // 32
+    ents = [split_entries(m) for m in mats]
+    widths = np.zeros((S, G), dtype=np.int64)
+    for g, (r, _, _) in enumerate(ents):
+        c = np.zeros(S * 32, dtype=np.int64)
+        c[:n] = np.bincount(r, minlength=n)
+        widths[:, g] = c.reshape(S, 32).max(axis=1)
+    sect = 32 * ((widths + 3) // 4 * 4)
+    gsize = sect.sum(axis=0)
+    gbase = np.concatenate([[0], np.cumsum(gsize)[:-1]])
+    row_ptr = np.zeros((G, S + 1), dtype=np.int64)
+    for g in range(G):
+        row_ptr[g, 1:] = np.cumsum(sect[:, g])
+        row_ptr[g] += gbase[g]
+    total = int(gsize.sum())
+    if total >= 2**31 - 16:
+        return None
+    codes = np.zeros(total, dtype=np.int32)
+    t_off, t_val, t_start = [], [], [0]
+    for g, (r, off2, a) in enumerate(ents):
+        vals, vcode = np.unique(a, return_inverse=True)
+        V = max(len(vals), 1)
+        ukey, kcode = np.unique(off2 * V + vcode.reshape(-1), return_inverse=True)
+        if len(ukey) + 1 > max_table:
+            return None
+        uoff = np.floor_divide(ukey, V)
+        ua = vals[ukey - uoff * V]
+        t_off.append(np.concatenate([[0], uoff]).astype(np.int32))
+        t_val.append(np.concatenate([np.zeros(1, np.complex128), split_table_values(uoff, ua)]))
+        t_start.append(t_start[-1] + len(ukey) + 1)
+        start = np.zeros(n + 1, dtype=np.int64)
+        np.cumsum(np.bincount(r, minlength=n), out=start[1:])
+        q = np.arange(len(r), dtype=np.int64) - start[r]
+        sl = r // 32
+        dst = row_ptr[g, sl] + 128 * (q // 4) + 4 * (r % 32) + q % 4
+        codes[dst] = kcode.reshape(-1) + 1
+    if t_start[-1] > max_table:
+        return None
+    longest = max(b - a for a, b in zip(t_start[:-1], t_start[1:]))
+    if longest > 65536:
+        return None
+    cb = 1 if longest <= 256 else 2
     return (row_ptr.reshape(-1), widths.reshape(-1).astype(np.int32),
             codes.astype(np.uint8 if cb == 1 else np.uint16), cb,
             np.concatenate(t_off), np.concatenate(t_val), np.asarray(t_start, np.int32), total)
@@ -233,13 +318,14 @@ class DeviceOperator:
         self.group_nnz = [int(m.nnz) for m in mats]
         self.nnz = sum(self.group_nnz)
         lay = None
+        self.dict_split = False
         if fmt == "auto":
             fmt = self._choose_format(mats)
             if fmt == "sliced":  # prefer the dictionary-coded form when the tables fit
-                lay = dict_sliced_layout(mats, self.n_cols, dtype)
+                lay, self.dict_split = self._dict_layout(mats, dtype)
                 fmt = "dict" if lay is not None else "sliced"
         elif fmt == "dict":
-            lay = dict_sliced_layout(mats, self.n_cols, dtype)
+            lay, self.dict_split = self._dict_layout(mats, dtype)
             if lay is None:
                 raise ValueError("the (column - row, value) pairs exceed the dictionary size")
         if fmt not in ("csr", "sliced", "dict"):
@@ -285,6 +371,16 @@ class DeviceOperator:
                     self._tiles[tn] = torch.from_numpy(t).to(self.device)
         self._finish(G)
 
+    def _dict_layout(self, mats, dtype):
+        """Dictionary layout of host groups: real/imaginary split for complex128 (two FP64
+        multiply-adds per code instead of four), falling back to whole complex values when
+        the split tables do not fit.  Returns ``(layout or None, split)``."""
+        if dtype == "c128":
+            lay = dict_sliced_layout(mats, self.n_cols, dtype, split=True)
+            if lay is not None:
+                return lay, True
+        return dict_sliced_layout(mats, self.n_cols, dtype), False
+
     @classmethod
     def from_device_groups(cls, groups, dtype: str = "c64", fmt: str = "auto"):
         """Sliced operator from device CSR groups ``[(indptr, indices, data,
@@ -315,7 +411,13 @@ class DeviceOperator:
         self._tiles = {}
         self.dict_off = self.dict_start = None
         self.code_bytes = 0
-        lay = device_dict_layout(groups, n, dtype) if fmt != "sliced" else None
+        self.dict_split = False
+        lay = None
+        if fmt != "sliced" and dtype == "c128":
+            lay = device_dict_layout(groups, n, dtype, split=True)
+            self.dict_split = lay is not None
+        if lay is None and fmt != "sliced":
+            lay = device_dict_layout(groups, n, dtype)
         if lay is None and fmt == "dict":
             raise ValueError("the (column - row, value) pairs exceed the dictionary size")
         if lay is not None:
@@ -347,7 +449,11 @@ class DeviceOperator:
         return self
 
     def astype(self, dtype: str):
-        """The same operator and layout with values in ``dtype`` (device copy)."""
+        """The same operator and layout with values in ``dtype`` (device copy).  The
+        real/imaginary split tables exist for complex128 only."""
+        if getattr(self, "dict_split", False) and dtype != "c128":
+            raise TypeError("the real/imaginary split dictionary is a complex128 layout; "
+                            "build the complex64 operator from the terms")
         other = self.__class__.__new__(self.__class__)
         other.__dict__.update(self.__dict__)
         other.dtype = dtype
@@ -368,6 +474,8 @@ class DeviceOperator:
             self.coef_consts = torch.from_numpy(consts).to(self.device)
         layout = {"sliced": _lib.QG_LAYOUT_SLICED, "dict": _lib.QG_LAYOUT_SLICED_DICT}.get(
             fmt, _lib.QG_LAYOUT_ROW_MAJOR)
+        if fmt == "dict" and getattr(self, "dict_split", False):
+            layout = _lib.QG_LAYOUT_SLICED_DICT_RI
         self.struct = _lib.CsrGroups(
             self.n_rows, self.n_cols, G, _QG[dtype], layout, 4, 0, 0,
             _ptr(self.row_ptr), _ptr(self.col), _ptr(self.val), None, _ptr(self.coef_code),
@@ -436,9 +544,10 @@ class DeviceOperator:
     def launch_desc(self) -> str:
         kind, tn, lanes = self.launch
         if kind == "dict":
+            split = ", real/imaginary split" if getattr(self, "dict_split", False) else ""
             return (f"dict(32-row slices, {self.code_bytes}-byte codes, "
-                    f"{self.val.numel()} table entries, {self.stored / max(self.nnz, 1):.3f}x "
-                    "stored/nnz)")
+                    f"{self.val.numel()} table entries{split}, "
+                    f"{self.stored / max(self.nnz, 1):.3f}x stored/nnz)")
         if kind == "sliced":
             return f"sliced(32-row slices, {self.stored / max(self.nnz, 1):.3f}x stored/nnz)"
         return f"{kind}(lanes={lanes}" + (f", tile_nnz={tn})" if kind == "staged" else ")")

@@ -330,6 +330,19 @@ def wrmn_error_gpu(diff, state, atol, rtol):
     return float(torch.sqrt(torch.mean(w * w)).item())
 
 
+def isherm_gpu(matrix, tol=-1):
+    """Hermitian up to an element-wise absolute tolerance: every pair satisfies
+    ``|a_rc - conj(a_cr)|^2 < tol^2`` (isherm_dense and _conj_feq,
+    qutip/core/data/properties.pyx:25-33,218-246), tested on the device."""
+    rows, cols = matrix.shape
+    if rows != cols:
+        return False
+    tol = float(tol) if tol >= 0 else float(qutip.settings.core["atol"])
+    m = matrix.matrix()
+    d = m - m.transpose(0, 1).conj()
+    return bool(((d.real * d.real + d.imag * d.imag) < tol * tol).all().item())
+
+
 def adjoint_gpu(matrix):
     return matrix.adjoint()
 
@@ -365,22 +378,129 @@ def _view(buf: torch.Tensor) -> _lib.StateView:
                           (C.c_double * 16)())
 
 
-def expect_csr_gpu(op, state):
-    """``<psi|op|psi>`` for a ket, ``tr(op rho)`` for a square state."""
-    e = _EOPS.get(op, lambda o: _ExpectOp(_scipy(o)))
+def _check_expect_shapes(op, state):
     if state.shape[1] == 1:
         if op.shape[1] != state.shape[0]:
             raise ValueError(f"incompatible shapes {op.shape} and {state.shape}")
-        _lib.call("qg_expect_ket", C.byref(e.struct), C.byref(_view(state.buf)),
-                  e.out.data_ptr(), stream_ptr())
     else:
         d = state.shape[0]
         if state.shape != (d, d) or op.shape != (d, d):
             raise ValueError(f"incompatible shapes {op.shape} and {state.shape}")
-        _lib.call("qg_expect_dm", C.byref(e.struct), d, C.byref(_view(state.buf)),
-                  e.out.data_ptr(), stream_ptr())
-    v = e.out.cpu()
-    return complex(float(v[0]), float(v[1]))
+
+
+def _launch_expect(op, state, out_ptr):
+    """``<psi|op|psi>`` (ket) or ``tr(op rho)`` (square state) into ``out_ptr[0:2]``
+    (the kernel also writes the norm or trace to ``out_ptr[2:4]``)."""
+    e = _EOPS.get(op, lambda o: _ExpectOp(_scipy(o)))
+    if state.shape[1] == 1:
+        _lib.call("qg_expect_ket", C.byref(e.struct), C.byref(_view(state.buf)),
+                  out_ptr, stream_ptr())
+    else:
+        _lib.call("qg_expect_dm", C.byref(e.struct), state.shape[0],
+                  C.byref(_view(state.buf)), out_ptr, stream_ptr())
+
+
+def _super_row(op, d):
+    def build(o):
+        rows = _scipy(o)[np.arange(d) * (d + 1)]
+        return _ExpectOp(sp.csr_matrix(np.ones((1, d))) @ rows)   # 1 x n summed row
+    return _SUPER_EOPS.get(op, build)
+
+
+def _launch_expect_super(op, state, out_ptr):
+    """``tr(unvec(op @ vec(rho)))`` into ``out_ptr[0:2]``: the rows of ``op`` on the
+    diagonal of rho, summed into one row, times the state (a matvec with one row)."""
+    d = int(math.isqrt(state.shape[0]))
+    e = _super_row(op, d)
+    _lib.call("qg_spmv_csr", C.byref(e.struct), 0.0, state.buf.data_ptr(), out_ptr,
+              1.0, 0.0, 0.0, 0.0, stream_ptr())
+
+
+def _fits(kind, op, state) -> bool:
+    """Whether ``op`` can be evaluated against ``state`` as an e_op of this ``kind``."""
+    n, m = state.shape
+    if kind == "super":
+        d = int(math.isqrt(n))
+        return m == 1 and d * d == n and op.shape[1] == n
+    return op.shape[1] == n if m == 1 else (n == m and op.shape == (n, n))
+
+
+class _ExpectBatch:
+    """Expectation values of one state against several operators with one read-back.
+
+    ``Result.add`` asks for the e_ops of an output time one at a time, and each answer
+    must be a host number, so computed one by one every e_op costs a launch and a
+    blocking device-to-host read.  Here the first request against a new state launches
+    the kernels of every operator asked for against the previous state (the e_ops of
+    the previous output time) into one device buffer and reads it back once; the other
+    requests against the same state are answered from that read.
+
+    An answer is reused only while nothing can have changed the state: the same
+    ``GpuDense`` object, the same torch version counter of its buffer, and no launch of
+    the library since the read (every kernel that writes device memory counts)."""
+
+    def __init__(self):
+        self.state = None
+        self.version = -1
+        self.launch_mark = -1
+        self.values = {}          # (kind, id(op)) -> complex
+        self.keep = []            # the operators of ``values`` (their ids stay valid)
+        self.prev = []            # (kind, op) asked for against the previous state
+        self.cur = []
+        self.buf = None
+        self.host = None
+
+    def _valid(self, state):
+        return (state is self.state and state.buf._version == self.version
+                and _lib.LAUNCHES[0] == self.launch_mark)
+
+    def _buffers(self, k, device):
+        if self.buf is None or self.buf.numel() < 4 * k or self.buf.device != device:
+            self.buf = torch.zeros(4 * max(k, 16), dtype=torch.float64, device=device)
+            self.host = torch.zeros(4 * max(k, 16), dtype=torch.float64).pin_memory()
+
+    def get(self, kind, op, state):
+        key = (kind, id(op))
+        if self._valid(state):
+            if key in self.values:
+                self.cur.append((kind, op))
+                return self.values[key]
+            batch = [(kind, op)]
+        else:
+            if self.state is not None:
+                self.prev = self.cur
+            self.cur = []
+            self.values = {}
+            self.keep = []
+            batch = [(kind, op)]
+            for k2, o2 in self.prev:
+                if (k2, id(o2)) != key and _fits(k2, o2, state):
+                    batch.append((k2, o2))
+        self._buffers(len(batch), state.buf.device)
+        base = self.buf.data_ptr()
+        for i, (k2, o) in enumerate(batch):
+            (_launch_expect if k2 == "expect" else _launch_expect_super)(o, state, base + 32 * i)
+        h = self.host[:4 * len(batch)]
+        h.copy_(self.buf[:4 * len(batch)], non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        v = h.numpy()
+        for i, (k2, o) in enumerate(batch):
+            self.values[(k2, id(o))] = complex(float(v[4 * i]), float(v[4 * i + 1]))
+            self.keep.append(o)
+        self.state = state
+        self.version = state.buf._version
+        self.launch_mark = _lib.LAUNCHES[0]
+        self.cur.append((kind, op))
+        return self.values[key]
+
+
+_BATCH = _ExpectBatch()
+
+
+def expect_csr_gpu(op, state):
+    """``<psi|op|psi>`` for a ket, ``tr(op rho)`` for a square state."""
+    _check_expect_shapes(op, state)
+    return _BATCH.get("expect", op, state)
 
 
 def expect_super_csr_gpu(op, state):
@@ -390,16 +510,7 @@ def expect_super_csr_gpu(op, state):
     d = int(math.isqrt(n))
     if d * d != n or state.shape[1] != 1 or op.shape[1] != n:
         raise ValueError(f"incompatible shapes {op.shape} and {state.shape}")
-
-    def build(o):
-        rows = _scipy(o)[np.arange(d) * (d + 1)]
-        return _ExpectOp(sp.csr_matrix(np.ones((1, d))) @ rows)   # 1 x n summed row
-    e = _SUPER_EOPS.get(op, build)
-    y = torch.zeros(1, dtype=_CDT, device=state.buf.device)
-    # one-row operator times the state: a matvec with n_rows = 1
-    _lib.call("qg_spmv_csr", C.byref(e.struct), 0.0, state.buf.data_ptr(), y.data_ptr(),
-              1.0, 0.0, 0.0, 0.0, stream_ptr())
-    return complex(y.item())
+    return _BATCH.get("super", op, state)
 
 
 # ---------------------------------------------------------- coefficients ------
@@ -500,6 +611,30 @@ def _decode_terms(evo):
     return out
 
 
+#: generators with at least this many rows are merged and laid out on the device
+DEVICE_BUILD_ROWS = 1024
+
+
+def device_operator(terms, dtype="c128") -> DeviceOperator:
+    """The device operator of ``(scipy matrix, Coefficient | None)`` terms.
+
+    Square generators of ``DEVICE_BUILD_ROWS`` rows or more -- every Liouvillian of a
+    system of Hilbert dimension 32 or more -- are copied to the device term by term,
+    merged per coefficient and laid out there (dictionary-coded sliced ELLPACK when the
+    (column - row, value) pairs fit its tables, else sliced ELLPACK when its padding
+    costs at most 15 %).  The host layouts of the same operator take seconds at a
+    million rows (10 s for the L = 10 Ising Liouvillian).  Smaller or irregular
+    generators keep the host layouts (row-major CSR with staged tiles)."""
+    from .superop import device_term_groups, sliced_padding
+    n_rows, n_cols = terms[0][0].shape
+    if n_rows == n_cols and n_rows >= DEVICE_BUILD_ROWS and len(terms) <= _lib.QG_MAX_GROUPS * 4:
+        groups = device_term_groups(terms, _device())
+        if len(groups) <= _lib.QG_MAX_GROUPS and sliced_padding(groups) <= 1.15:
+            return DeviceOperator.from_device_groups(groups, dtype, fmt="auto")
+        del groups
+    return DeviceOperator(terms, dtype=dtype, device=_device())
+
+
 def _is_matrix_form(rhs) -> bool:
     try:
         from qutip.core.cy.lindblad_matrix_form import LindbladMatrixForm
@@ -576,7 +711,7 @@ class IntegratorGpuVern7(Integrator):
             self._op = lindblad_operator(rhs, dt)
         else:
             self._terms = qobjevo_terms(rhs)
-            self._op = DeviceOperator(self._terms, dtype=dt, device=_device())
+            self._op = device_operator(self._terms, dt)
         self._blocks = {1: self._op}
         self._ode = self._integrator(self._op)
         self._shape = (self._op.n_rows, 1)
@@ -863,6 +998,7 @@ def register():
     _data.column_unstack.add_specialisations([(GpuDense, GpuDense, column_unstack_gpu)])
     _data.inner.add_specialisations([(GpuDense, GpuDense, inner_gpu)])
     _ode.wrmn_error.add_specialisations([(GpuDense, GpuDense, wrmn_error_gpu)])
+    _data.isherm.add_specialisations([(GpuDense, isherm_gpu)])
     _data.adjoint.add_specialisations([(GpuDense, GpuDense, adjoint_gpu)])
     _data.conj.add_specialisations([(GpuDense, GpuDense, conj_gpu)])
     _data.transpose.add_specialisations([(GpuDense, GpuDense, transpose_gpu)])

@@ -22,7 +22,8 @@ import numpy as np
 import scipy.sparse as sp
 import torch
 
-__all__ = ["kron_coo", "coalesce", "liouvillian_groups", "device_sliced_layout"]
+__all__ = ["kron_coo", "coalesce", "liouvillian_groups", "device_sliced_layout",
+           "device_term_groups", "sliced_padding"]
 
 
 def _coo(m, device):
@@ -124,6 +125,99 @@ def liouvillian_groups(h_terms, c_ops=(), device="cuda"):
     return out
 
 
+def _upload_csr(m, device):
+    """Device copies of a CSR matrix's arrays, indices widened on the device (the host
+    arrays are sent as stored: 32-bit indices, complex128 values)."""
+    m = sp.csr_matrix(m)
+
+    def idx(a):
+        a = np.asarray(a)
+        if a.dtype not in (np.int32, np.int64):
+            a = a.astype(np.int64)
+        return torch.from_numpy(np.ascontiguousarray(a)).to(device).to(torch.int64)
+    return (idx(m.indptr), idx(m.indices),
+            torch.from_numpy(np.ascontiguousarray(m.data, dtype=np.complex128)).to(device))
+
+
+def _sum_in_order(parts, n):
+    """Sum of device CSR matrices ``parts`` (same shape) with each position summed
+    left to right in list order, as chained scipy ``+`` does, and exact zeros dropped.
+    The order is fixed, so equal inputs give equal bits (a dictionary of the values
+    then deduplicates them)."""
+    keys = torch.cat([torch.repeat_interleave(torch.arange(n, device=ip.device), ip[1:] - ip[:-1])
+                      * n + ix for ip, ix, _ in parts])
+    vals = torch.cat([v for _, _, v in parts])
+    keys, perm = torch.sort(keys, stable=True)        # stable: list order within a position
+    vals = vals[perm]
+    del perm
+    first = torch.ones_like(keys, dtype=torch.bool)
+    first[1:] = keys[1:] != keys[:-1]
+    seg = torch.cumsum(first, 0) - 1
+    starts = torch.nonzero(first).reshape(-1)
+    rank = torch.arange(keys.numel(), device=keys.device) - starts[seg]
+    uniq = keys[first]
+    del keys, first
+    summed = vals[starts].clone()
+    for r in range(1, len(parts)):
+        m = rank == r
+        if not bool(m.any()):
+            break
+        summed[seg[m]] += vals[m]                     # one entry per position: no races
+    keep = summed != 0
+    uniq, summed = uniq[keep], summed[keep]
+    rows = torch.div(uniq, n, rounding_mode="floor")
+    counts = torch.bincount(rows, minlength=n)
+    indptr = torch.zeros(n + 1, dtype=torch.int64, device=uniq.device)
+    torch.cumsum(counts, 0, out=indptr[1:])
+    return indptr, uniq - rows * n, summed
+
+
+def device_term_groups(terms, device="cuda"):
+    """Coefficient groups of ``(scipy matrix, Coefficient | None)`` terms as device CSR
+    ``[(indptr, indices, data, coefficient), ...]``: each term's arrays are copied to the
+    device once and the terms sharing a coefficient are summed there, in the group order
+    of :func:`qutip_gb300.systems.merge_terms` (``QobjEvo.compress``,
+    qutip/core/cy/qobjevo.pyx:816).  This is the device twin of the host merge that
+    :class:`~qutip_gb300.operator.DeviceOperator` runs before its layouts, for generators
+    too large to lay out on the host in reasonable time."""
+    n = terms[0][0].shape[0]
+    keyed: dict = {}
+    order = []
+    for m, c in terms:
+        key = None if c is None else c.key()
+        if key not in keyed:
+            keyed[key] = (c, [])
+            order.append(key)
+        keyed[key][1].append(m)
+    out = []
+    for key in order:
+        c, mats = keyed[key]
+        parts = [_upload_csr(m, device) for m in mats]
+        if len(parts) == 1:
+            ip, ix, v = parts[0]
+            if bool((v == 0).any()):                 # drop stored zeros, as the host merge does
+                ip, ix, v = _sum_in_order(parts, n)
+        else:
+            ip, ix, v = _sum_in_order(parts, n)
+        out.append((ip, ix, v, c))
+    return out
+
+
+def sliced_padding(groups) -> float:
+    """Entries the sliced layout of device CSR ``groups`` stores (32-row slices padded to
+    their longest row) per structural entry."""
+    n = groups[0][0].numel() - 1
+    S = (n + 31) // 32
+    padded = 0
+    nnz = 0
+    for indptr, ix, _, _ in groups:
+        c = torch.zeros(S * 32, dtype=torch.int64, device=indptr.device)
+        c[:n] = indptr[1:] - indptr[:-1]
+        padded += 32 * int(c.view(S, 32).amax(dim=1).sum().item())
+        nnz += ix.numel()
+    return padded / max(nnz, 1)
+
+
 def device_sliced_layout(groups, n_cols):
     """Sliced ELLPACK of device CSR groups: the layout of
     :func:`qutip_gb300.operator.sliced_layout` computed with device sorts and
@@ -169,13 +263,86 @@ def device_sliced_layout(groups, n_cols):
     return slice_ptr, widths.reshape(-1).to(torch.int32), col, val, total
 
 
-def device_dict_layout(groups, n_cols, dtype: str, max_table: int = 4096):
+def _device_split_entries(indptr, indices, data, n):
+    """Device twin of :func:`qutip_gb300.operator.split_entries`: ``(rows, off2, a)``."""
+    device = indptr.device
+    cnt = indptr[1:] - indptr[:-1]
+    rows = torch.repeat_interleave(torch.arange(n, device=device), cnt)
+    idx = indices.to(torch.int64)
+    _, perm = torch.sort((rows << 32) | (idx ^ rows))
+    off = idx[perm] - rows
+    dv = data[perm].to(torch.complex128)
+    del perm, idx
+    r2 = rows.repeat_interleave(2)
+    off2 = off.repeat_interleave(2) * 2 + torch.tensor([0, 1], device=device).repeat(dv.numel())
+    a = torch.view_as_real(dv).reshape(-1)
+    keep = a != 0
+    return r2[keep], off2[keep], a[keep]
+
+
+def _device_dict_split_layout(groups, n, max_table):
+    """Device twin of the real/imaginary split dictionary layout (complex128)."""
+    device = groups[0][0].device
+    G = len(groups)
+    S = (n + 31) // 32
+    ents = [_device_split_entries(ip, ix, v, n) for ip, ix, v, _ in groups]
+    counts = torch.zeros((G, S * 32), dtype=torch.int64, device=device)
+    for g, (r, _, _) in enumerate(ents):
+        counts[g, :n] = torch.bincount(r, minlength=n)
+    widths = counts.view(G, S, 32).amax(dim=2)          # exact: the kernel skips the rest
+    sect = 32 * ((widths + 3) // 4 * 4)
+    gsize = sect.sum(dim=1)
+    gbase = torch.cumsum(gsize, 0) - gsize
+    row_ptr = torch.zeros((G, S + 1), dtype=torch.int64, device=device)
+    row_ptr[:, 1:] = torch.cumsum(sect, dim=1)
+    row_ptr += gbase[:, None]
+    total = int(gsize.sum().item())
+    if total >= 2**31 - 16:
+        return None
+    codes = torch.zeros(total, dtype=torch.int32, device=device)
+    t_off, t_val, t_start = [], [], [0]
+    for g, (r, off2, a) in enumerate(ents):
+        vbits, vcode = torch.unique(a.view(torch.int64), return_inverse=True)
+        V = max(int(vbits.numel()), 1)
+        ukey, kcode = torch.unique(off2 * V + vcode, return_inverse=True)
+        del vcode
+        if ukey.numel() + 1 > max_table:
+            return None
+        uoff = torch.div(ukey, V, rounding_mode="floor")
+        ua = vbits[ukey - uoff * V].view(torch.float64)
+        tv = torch.complex(torch.where((uoff & 1) == 1, -ua, ua), ua)
+        t_off.append(torch.cat([torch.zeros(1, dtype=torch.int64, device=device), uoff]))
+        t_val.append(torch.cat([torch.zeros(1, dtype=torch.complex128, device=device), tv]))
+        t_start.append(t_start[-1] + ukey.numel() + 1)
+        start = torch.zeros(n + 1, dtype=torch.int64, device=device)
+        torch.cumsum(counts[g, :n], 0, out=start[1:])
+        q = torch.arange(r.numel(), device=device) - start[r]
+        sl = torch.div(r, 32, rounding_mode="floor")
+        dst = row_ptr[g, sl] + 128 * torch.div(q, 4, rounding_mode="floor") + 4 * (r % 32) + q % 4
+        codes[dst] = kcode.to(torch.int32) + 1
+        del q, sl, dst, kcode, start
+    if t_start[-1] > max_table:
+        return None
+    longest = max(b - a for a, b in zip(t_start[:-1], t_start[1:]))
+    if longest > 65536:
+        return None
+    cb = 1 if longest <= 256 else 2
+    codes = codes.to(torch.uint8) if cb == 1 else codes.to(torch.int16)
+    return (row_ptr.reshape(-1).to(torch.int32), widths.t().reshape(-1).to(torch.int32), codes,
+            cb, torch.cat(t_off).to(torch.int32), torch.cat(t_val),
+            torch.tensor(t_start, dtype=torch.int32, device=device), total)
+
+
+def device_dict_layout(groups, n_cols, dtype: str, max_table: int = 4096, split: bool = False):
     """Dictionary-coded sliced layout of device CSR groups: the layout of
     :func:`qutip_gb300.operator.dict_sliced_layout` computed with device sorts, uniques
     and scatters (tables in a different but equivalent order).  Returns
     ``(row_ptr, widths, codes, code_bytes, table_off, table_val, table_start, stored)``
     as device tensors, or ``None`` when the (column - row, value) pairs do not fit
-    ``max_table`` table entries."""
+    ``max_table`` table entries.  ``split=True``: the real/imaginary split of complex128
+    entries (``QG_LAYOUT_SLICED_DICT_RI``)."""
+    if split:
+        return _device_dict_split_layout(groups, groups[0][0].numel() - 1, max_table)
     indptr0 = groups[0][0]
     device = indptr0.device
     n = indptr0.numel() - 1
@@ -185,9 +352,9 @@ def device_dict_layout(groups, n_cols, dtype: str, max_table: int = 4096):
     counts = torch.zeros((G, S * 32), dtype=torch.int64, device=device)
     for g, (indptr, _, _, _) in enumerate(groups):
         counts[g, :n] = indptr[1:] - indptr[:-1]
-    widths = (counts.view(G, S, 32).amax(dim=2) + 3) // 4 * 4      # [G, S]
+    widths = counts.view(G, S, 32).amax(dim=2)                    # [G, S], exact
     del counts
-    sect = 32 * widths
+    sect = 32 * ((widths + 3) // 4 * 4)
     gsize = sect.sum(dim=1)
     gbase = torch.cumsum(gsize, 0) - gsize
     row_ptr = torch.zeros((G, S + 1), dtype=torch.int64, device=device)

@@ -6,6 +6,7 @@ import os
 import socket
 import sys
 
+import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
@@ -54,11 +55,13 @@ def _ref_rank(rank, world, port, out):
     sys.path.insert(0, ROOT)
     import bench
     called = []
-    bench.cpu_baseline = lambda sample: called.append(sample) or {"value": 1.0}
+    want = np.load(bench.GOLDEN)["expect"]
+    bench.reference_solve = lambda steps, warmup: called.append(steps) or {
+        "times": [0.5] * steps, "expect": want, "rhs_s": 0.1, "coefficient": {}}
     d = bench.Dist(world, backend="gloo")
 
     class A:
-        steps, warmup, gpus, cpu_sample = 1, 0, world, 0.01
+        steps, warmup, gpus = 2, 0, world
     buf = io.StringIO()
     with contextlib.redirect_stdout(buf):
         bench.run_reference(A, d)

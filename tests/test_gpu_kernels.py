@@ -103,11 +103,51 @@ def test_sliced_layout_matches_scipy(dev, L):
     outs = []
     for fmt in ("sliced", "csr", "dict"):
         op = DeviceOperator(s.terms, dtype="c128", fmt=fmt)
+        assert fmt != "dict" or op.dict_split      # complex128: real/imaginary split tables
         ig = GpuVern7(op)
         ig.set_initial_value(torch.from_numpy(s.state0).cuda(), 0.0)
         ig.integrate(0.7)
         outs.append(ig.get_state().cpu().numpy())
     np.testing.assert_allclose(outs[0], outs[1], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(outs[2], outs[1], rtol=1e-12, atol=1e-14)
+
+
+def test_split_dictionary_with_complex_coefficients_and_entries(dev):
+    """The complex128 real/imaginary split dictionary: complex, real and imaginary
+    entries (a banded matrix and the Ising Liouvillian, whose diagonal is complex), a
+    complex time-dependent coefficient (the general coefficient product) and a real one
+    (its two-multiply-add path), a row count that is not a multiple of 32; matvec and a
+    Vern7 step against the CSR storage."""
+    from qutip_gb300 import _lib
+    from qutip_gb300.coefficients import coefficient
+    from qutip_gb300.operator import DeviceOperator
+    from qutip_gb300.vern7 import GpuVern7
+    n = 1100
+    rng = np.random.default_rng(11)
+    diags = {-33: 0.5, -1: -0.25j, 0: 0.3 + 0.7j, 2: 1.1, 31: -0.2 - 0.4j}
+    band = sp.diags([np.full(n - abs(k), v) for k, v in diags.items()], list(diags), shape=(n, n),
+                    format="csr", dtype=np.complex128)
+    other = sp.diags([np.full(n - 5, 0.9j), np.full(n, -0.1)], [5, 0], shape=(n, n), format="csr",
+                     dtype=np.complex128)
+    terms = [(band, None), (other, coefficient("exp(1j*w*t)", args={"w": 0.8})),
+             (band.T.tocsr() * 0.5, coefficient("cos(w*t)", args={"w": 1.3}))]
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    t = 0.77
+    want = sum((m * (1 if c is None else c(t))) @ x for m, c in terms)
+    op = DeviceOperator(terms, dtype="c128", fmt="dict")
+    assert op.dict_split and op.struct.layout == _lib.QG_LAYOUT_SLICED_DICT_RI
+    y = _t(np.ones(n))
+    op.matvec(t, _t(x), y, alpha=1.5 - 0.5j, beta=0.25)
+    np.testing.assert_allclose(y.cpu().numpy(), (1.5 - 0.5j) * want + 0.25, rtol=1e-12,
+                               atol=1e-12 * np.abs(want).max())
+    outs = []
+    for fmt in ("csr", "dict"):
+        o = DeviceOperator(terms, dtype="c128", fmt=fmt)
+        ig = GpuVern7(o, atol=1e-10, rtol=1e-9)
+        ig.set_initial_value(_t(x / np.linalg.norm(x)), 0.0)
+        ig.integrate(0.4)
+        outs.append(ig.get_state().cpu().numpy())
+    np.testing.assert_allclose(outs[1], outs[0], rtol=1e-12, atol=1e-14)
     np.testing.assert_allclose(outs[2], outs[1], rtol=1e-12, atol=1e-14)
 
 

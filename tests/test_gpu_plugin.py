@@ -85,6 +85,47 @@ def test_mesolve_time_dependent_ising(qt, plugin):
     _assert_expect(got.expect, ref.expect)
 
 
+def test_mesolve_device_built_liouvillian(qt, plugin):
+    """L = 5 (1024-row Liouvillian): the integrator merges and lays out QuTiP's Liouvillian
+    on the device (dictionary with the real/imaginary split in complex128); results equal
+    the reference's, through MESolver.run with a device-resident initial state, a second
+    run on the same solver, and the batched expectation values."""
+    H, c_ops, psi0, e_ops = _ising(qt, L=5)
+    rho0 = qt.ket2dm(psi0)
+    tl = np.linspace(0, 4, 41)
+    ref = qt.mesolve(H, rho0, tl, c_ops, e_ops=e_ops, options={"method": "vern7"})
+    solver = qt.MESolver(H, c_ops, options={"method": "gpu_vern7"})
+    op = solver._integrator._op
+    assert op.fmt == "dict" and op.dict_split and op.n_rows == 1024
+    for state in (rho0, rho0.to("gpu")):
+        got = solver.run(state, tl, e_ops=e_ops)
+        _assert_expect(got.expect, ref.expect)
+    # e_ops asked for in another order, and a single e_op, against the cached batch
+    got = solver.run(rho0, tl, e_ops=e_ops[::-1])
+    _assert_expect(got.expect, ref.expect[::-1])
+    got = solver.run(rho0, tl, e_ops=[e_ops[2]])
+    _assert_expect(got.expect, [ref.expect[2]])
+
+
+def test_expect_batch_never_reuses_a_changed_state(qt, plugin):
+    """The batched expectation values of one state are not reused once the state's
+    buffer changed in place or a kernel of the library ran."""
+    d = 16
+    rng = np.random.default_rng(3)
+    ops = [qt.rand_herm(d, seed=i).to("csr") for i in range(3)]
+    m = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    rho = qt.Qobj(m @ m.conj().T).unit().to("gpu")
+    want = [qt.expect(o, rho.to("dense")) for o in ops]
+    for _ in range(2):
+        np.testing.assert_allclose([qt.expect(o, rho) for o in ops], want, rtol=1e-12)
+    rho.data.buf.mul_(2.0)                      # in place: torch bumps the version
+    np.testing.assert_allclose([qt.expect(o, rho) for o in ops], [2 * w for w in want], rtol=1e-12)
+    # a library kernel writing the state through a raw pointer (torch sees no change):
+    # rho <- I rho + rho
+    plugin.matmul_csr_gpu(qt.qeye(d).to("csr").data, rho.data, scale=1.0, out=rho.data)
+    np.testing.assert_allclose([qt.expect(o, rho) for o in ops], [4 * w for w in want], rtol=1e-12)
+
+
 def test_mesolve_mixed_precision_error_stated(qt, plugin):
     H, c_ops, psi0, e_ops = _ising(qt, L=4)
     rho0 = qt.ket2dm(psi0)

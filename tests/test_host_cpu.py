@@ -157,9 +157,12 @@ def _banded(n, offsets, values, empty_every=7, seed=5):
     return sp.csr_matrix((vals, (rows, cols)), shape=(n, n), dtype=np.complex128)
 
 
-def _emulate_dict(lay, n, x, coefs):
+def _emulate_dict(lay, n, x, coefs, split=False):
     """The dictionary kernel's indexing on the host: codes of lane l, chunk q of slice s
-    and group g at row_ptr[g*(S+1)+s] + 128 q + 4 l + u."""
+    and group g at row_ptr[g*(S+1)+s] + 128 q + 4 l + u.  ``split``: the real/imaginary
+    split tables (offset << 1 with the low bit marking an imaginary part, value pair
+    (c1, c2) applied as (c1 p, c2 q) to x with real and imaginary parts exchanged for an
+    imaginary part)."""
     rp, widths, codes, cb, t_off, t_val, t_start, total = lay
     G = len(t_start) - 1
     S = (n + 31) // 32
@@ -172,10 +175,17 @@ def _emulate_dict(lay, n, x, coefs):
                 w = widths[s * G + g]
                 base = rp[g * (S + 1) + s]
                 part = 0j
-                for q in range(w // 4):
-                    for u in range(4):
+                for q in range((w + 3) // 4):
+                    for u in range(min(4, w - 4 * q)):
                         k = int(codes[base + 128 * q + 4 * lane + u])
                         k = t_start[g] + (k if k < t_start[g + 1] - t_start[g] else 0)
+                        if split:
+                            oc = int(t_off[k])
+                            col = min(max(row + (oc >> 1), 0), n - 1)
+                            xv = x[col]
+                            p, r = (xv.imag, xv.real) if oc & 1 else (xv.real, xv.imag)
+                            part += complex(t_val[k].real * p, t_val[k].imag * r)
+                            continue
                         col = min(max(row + t_off[k], 0), n - 1)
                         part += t_val[k] * x[col]
                 acc += coefs[g] * part
@@ -207,7 +217,7 @@ def test_dict_layout_reproduces_the_matvec():
     rp, widths, codes, cb, t_off, t_val, t_start, total = lay
     assert list(np.diff(t_start)) == [len(set(zip(b.tocoo().col - b.tocoo().row,
                                                     b.tocoo().data))) + 1, 1]
-    assert all(w % 4 == 0 for w in widths) and all(r % 128 == 0 for r in rp)
+    assert all(r % 128 == 0 for r in rp)
     x = rng.normal(size=n) + 1j * rng.normal(size=n)
     np.testing.assert_allclose(_emulate_dict(lay, n, x, [1.0, 5.0]), b @ x, atol=1e-6)
 
@@ -241,6 +251,50 @@ def test_device_dict_layout_reproduces_the_matvec(dtype):
     np.testing.assert_allclose(_emulate_dict(host, n, x, coefs), want, atol=tol * np.abs(want).max())
 
 
+def test_split_dict_layout_reproduces_the_matvec():
+    """The real/imaginary split tables (complex128): the Ising chain's Liouvillian, whose
+    diagonal entries are complex and split in two codes, and a banded matrix with real,
+    imaginary and complex entries; host and device builders agree with A @ x."""
+    import scipy.sparse as sp
+    import torch
+    from qutip_gb300 import systems as S
+    from qutip_gb300.operator import dict_sliced_layout
+    from qutip_gb300.superop import device_dict_layout
+    rng = np.random.default_rng(2)
+    s = S.ising_chain(3)
+    mats = [sp.csr_matrix(m) for m, _ in s.terms]
+    n = mats[0].shape[0]
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    coefs = [1.0, 0.3 - 0.2j]
+    want = mats[0] @ x + coefs[1] * (mats[1] @ x)
+    lay = dict_sliced_layout(mats, n, "c128", split=True)
+    assert lay is not None
+    rp, widths, codes, cb, t_off, t_val, t_start, total = lay
+    pad = np.zeros(len(t_val), dtype=bool)
+    pad[t_start[:-1]] = True                       # code 0 of each group
+    imag = ((t_off & 1) == 1) & ~pad
+    real = ((t_off & 1) == 0) & ~pad
+    assert np.all(t_val.imag[~pad] != 0) and np.all(t_val[pad] == 0)
+    assert np.all(t_val.real[imag] == -t_val.imag[imag])
+    assert np.all(t_val.real[real] == t_val.imag[real])
+    n_parts = sum(int(np.count_nonzero(m.data.real) + np.count_nonzero(m.data.imag)) for m in mats)
+    assert int(np.count_nonzero(codes)) == n_parts
+    np.testing.assert_allclose(_emulate_dict(lay, n, x, coefs, split=True), want, atol=1e-12)
+    groups = [(torch.from_numpy(m.indptr.astype(np.int64)), torch.from_numpy(m.indices.astype(np.int64)),
+               torch.from_numpy(m.data), None) for m in mats]
+    dl = device_dict_layout(groups, n, "c128", split=True)
+    dh = tuple(v.numpy() if isinstance(v, torch.Tensor) else v for v in dl)
+    assert dh[-1] == total and list(dh[6]) == list(t_start)
+    np.testing.assert_allclose(_emulate_dict(dh, n, x, coefs, split=True), want, atol=1e-12)
+    n = 101
+    b = _banded(n, [-5, -1, 0, 2, 31], [1.0, -0.5j, 0.25 + 1j])
+    z = sp.csr_matrix((n, n), dtype=complex)
+    lay = dict_sliced_layout([b, z], n, "c128", split=True)
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    np.testing.assert_allclose(_emulate_dict(lay, n, x, [1.0, 5.0], split=True), b @ x,
+                               atol=1e-12)
+
+
 def sp_from(group, n):
     import scipy.sparse as sp
     indptr, indices, data, _ = group
@@ -257,11 +311,16 @@ def test_device_groups_operator_prefers_the_dictionary():
     s = S.ising_chain(3, build_terms=False)
     groups = liouvillian_groups(s.h_terms, s.c_ops, device="cpu")
     op = DeviceOperator.from_device_groups(groups, "c128")
-    assert op.fmt == "dict" and op.struct.layout == _lib.QG_LAYOUT_SLICED_DICT
+    assert op.fmt == "dict" and op.struct.layout == _lib.QG_LAYOUT_SLICED_DICT_RI
+    assert op.dict_split
     assert op.struct.tile_nnz == op.code_bytes == 1 and op.struct.lanes == op.val.numel()
     assert op.struct.dict_off and op.struct.dict_start
-    op64 = op.astype("c64")
-    assert op64.fmt == "dict" and op64.val.dtype.is_complex and op64.struct.lanes == op.struct.lanes
+    with pytest.raises(TypeError):
+        op.astype("c64")                            # the split tables are complex128 only
+    op64 = DeviceOperator.from_device_groups(groups, "c64")
+    assert op64.fmt == "dict" and op64.struct.layout == _lib.QG_LAYOUT_SLICED_DICT
+    op128 = op64.astype("c128")
+    assert op128.val.dtype.is_complex and op128.struct.lanes == op64.struct.lanes
     sl = DeviceOperator.from_device_groups(groups, "c64", fmt="sliced")
     assert sl.fmt == "sliced" and sl.struct.layout == _lib.QG_LAYOUT_SLICED
 

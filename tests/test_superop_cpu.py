@@ -56,3 +56,54 @@ def test_jaynes_cummings_groups():
     got = sum(sp.csr_matrix((d.numpy(), i.numpy(), p.numpy()), shape=(n, n)) for p, i, d, _ in groups)
     want = sum(sp.csr_matrix(m) for m, _ in s.terms)
     assert abs(got - want).max() <= 1e-13
+
+
+def _split_terms(L):
+    """The Ising Liouvillian as separate terms, two of them sharing the constant group and
+    two sharing one coefficient, so that merging has to sum overlapping entries."""
+    from qutip_gb300 import systems as S
+    s = S.ising_chain(L)
+    (m0, c0), (m1, c1) = s.terms[0], s.terms[1]
+    m0 = sp.csr_matrix(m0)
+    half = sp.csr_matrix(m0.multiply(sp.random(m0.shape[0], m0.shape[1], density=0.3,
+                                               random_state=3, format="csr") != 0))
+    rest = sp.csr_matrix(m0 - half)
+    m1 = sp.csr_matrix(m1)
+    return [(rest, None), (m1 * 0.25, c1), (half, None), (m1 * 0.75, c1), (sp.diags(m0.diagonal()).tocsr(), None)]
+
+
+def test_device_term_groups_equal_the_host_merge_bit_for_bit():
+    from qutip_gb300.superop import device_term_groups
+    from qutip_gb300.systems import merge_terms
+    terms = _split_terms(4)
+    host = merge_terms(terms)
+    dev = device_term_groups(terms, device="cpu")
+    assert len(dev) == len(host)
+    n = terms[0][0].shape[0]
+    for (ip, ix, v, c), (m, ch) in zip(dev, host):
+        assert (c is None) == (ch is None)
+        m = sp.csr_matrix(m)
+        m.sort_indices()
+        m.eliminate_zeros()
+        np.testing.assert_array_equal(ip.numpy(), m.indptr)
+        np.testing.assert_array_equal(ix.numpy(), m.indices)
+        np.testing.assert_array_equal(v.numpy(), m.data)   # same summation order: same bits
+        assert ip.numel() == n + 1
+
+
+def test_device_term_groups_dictionary_layout_deduplicates_complex128():
+    """Summed in a fixed order, equal complex128 entries keep equal bits, so the
+    dictionary of (column - row, value) pairs is as small as the host one."""
+    from qutip_gb300.operator import dict_sliced_layout
+    from qutip_gb300.superop import device_dict_layout, device_term_groups, sliced_padding
+    from qutip_gb300.systems import merge_terms
+    terms = _split_terms(5)
+    dev = device_term_groups(terms, device="cpu")
+    assert sliced_padding(dev) <= 1.15
+    n = terms[0][0].shape[0]
+    lay_d = device_dict_layout(dev, n, "c128")
+    lay_h = dict_sliced_layout([m for m, _ in merge_terms(terms)], n, "c128")
+    assert lay_d is not None and lay_h is not None
+    assert lay_d[-1] == lay_h[-1]                                  # stored entries
+    assert int(lay_d[5].numel()) == len(lay_h[5])                  # table entries
+    np.testing.assert_array_equal(lay_d[6].numpy(), lay_h[6])      # table starts per group
