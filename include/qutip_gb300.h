@@ -439,8 +439,18 @@ int qg_batch_vern7(const qg_batch* B, void* stream);
  * before any stream capture.  All calls share the array and its queue words:
  * calls that overlap on the GPU (different streams, or different host threads)
  * race and corrupt each other; serialise them.  No cudaMalloc, cudaFree or
- * allocating library routine is called. */
+ * allocating library routine is called.  The device address is kept for the life
+ * of the process: resetting the device (cudaDeviceReset) after the first call on it
+ * is not supported. */
 int qg_batch_vern7_noalloc(const qg_batch* B, void* stream);
+
+/* After qg_batch_vern7_noalloc on this device and stream: 1 if a CTA gave up its
+ * bounded wait for the bulk copy of the staged operator (it then read the operator
+ * from global memory, so results stay correct but the launch ran slower than
+ * planned), 0 if not, negative on error.  The flag lives in the static queue words
+ * that the next call clears, so read it before the next call.  Synchronises the
+ * stream; allocates nothing. */
+int qg_batch_noalloc_staging_fault(void* stream);
 
 #ifdef __cplusplus
 }

@@ -99,6 +99,7 @@ _SIGS = {
     "qg_batch_smem_bytes": (C.c_int64, [C.c_void_p]),
     "qg_batch_vern7": (C.c_int, [C.c_void_p, C.c_void_p]),
     "qg_batch_vern7_noalloc": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "qg_batch_noalloc_staging_fault": (C.c_int, [C.c_void_p]),
 }
 
 _lib = None

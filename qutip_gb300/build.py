@@ -66,6 +66,7 @@ static __constant__ float VERN7_AL[16][16] = {fa2([lo(r) for r in a])};
 static __constant__ float VERN7_BH[10] = {fa1(hi(T.B))};
 static __constant__ float VERN7_BL[10] = {fa1(lo(T.B))};
 static __constant__ float VERN7_EF[10] = {fa1(hi(T.E))};
+static __constant__ float VERN7_EL[10] = {fa1(lo(T.E))};
 static const double VERN7_A_HOST[16][16] = {arr2(a)};
 static const double VERN7_B_HOST[10] = {arr1(T.B)};
 static const double VERN7_C_HOST[16] = {arr1(T.C)};

@@ -330,49 +330,6 @@ __device__ void matvec_to_k(const GT& g, Ctx<DT>& X, Ctl& c, double t,
   g.sync();
 }
 
-// Float-float accumulation for the mixed form: hi + lo += (fh + fl) * k with the
-// product error from one FMA (TwoProduct) and the addition error from Knuth's
-// TwoSum (Ogita, Rump & Oishi, "Accurate sum and dot product", SIAM J. Sci.
-// Comput. 26 (2005)).  The _rn intrinsics keep the compiler from contracting
-// the product into the sum.  Vern7's stage weights are large and of both signs,
-// so a plain FP32 sum of f_j k_j loses several bits of the stage input; this
-// keeps it to the final rounding to FP32.
-__device__ __forceinline__ void ff_acc(float& hi, float& lo, float fh, float fl, float k) {
-  const float p = __fmul_rn(fh, k);
-  float pe = fmaf(fh, k, -p);
-  pe = fmaf(fl, k, pe);
-  const float sum = __fadd_rn(hi, p);
-  const float bp = __fsub_rn(sum, hi);
-  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bp)), __fsub_rn(p, bp));
-  hi = sum;
-  lo = __fadd_rn(lo, __fadd_rn(e, pe));
-}
-
-// dt * a as a float pair from dt = dh + dl and a = ah + al (tableau hi/lo):
-// hi = fl(dh ah), lo = the product's rounding error plus the cross terms.
-__device__ __forceinline__ void ff_factor(float dh, float dl, float ah, float al, float& fh,
-                                          float& fl) {
-  fh = __fmul_rn(dh, ah);
-  float e = fmaf(dh, ah, -fh);
-  e = fmaf(dh, al, e);
-  fl = fmaf(dl, ah, e);
-}
-
-// fl32(bh + bl + ih + il): TwoSum of the high parts, the low parts added to its
-// error, one final rounding.
-__device__ __forceinline__ float ff_round4(float bh, float bl, float ih, float il) {
-  const float sum = __fadd_rn(bh, ih);
-  const float bp = __fsub_rn(sum, bh);
-  float e = __fadd_rn(__fsub_rn(bh, __fsub_rn(sum, bp)), __fsub_rn(ih, bp));
-  e = __fadd_rn(e, __fadd_rn(bl, il));
-  return __fadd_rn(sum, e);
-}
-
-__device__ __forceinline__ void split_f(double v, float& h, float& l) {
-  h = (float)v;
-  l = (float)(v - (double)h);
-}
-
 // One fused stage: k_s = A(t_prev + c_s dt) x_s and the next stage input, or at
 // s == 9 y_front and the WRMS error (returned).  In the mixed form the stage
 // input x_{s+1} = y_prev + sum_j dt a_{s+1,j} k_j is accumulated in float-float
@@ -389,25 +346,26 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
   // factors: FP64 for the double form; float pairs from the hi/lo tableau for the
   // mixed form (no FP64 work per stage)
   CT fa[16], fe[16];
-  float fl[16];
+  float fl[16], fel[16];
   if constexpr (MIXED) {
     float dh, dl;
     split_f(dt, dh, dl);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      float ah = 0.f, al = 0.f, e = 0.f;
+      float ah = 0.f, al = 0.f, eh = 0.f, el = 0.f;
       if (j < nk) {
         if (last) {
           ah = VERN7_BH[j];
           al = VERN7_BL[j];
-          e = VERN7_EF[j];
+          eh = VERN7_EF[j];
+          el = VERN7_EL[j];
         } else if (forms_input) {
           ah = VERN7_AH[s + 1][j];
           al = VERN7_AL[s + 1][j];
         }
       }
       ff_factor(dh, dl, ah, al, fa[j], fl[j]);
-      fe[j] = dh * e;
+      ff_factor(dh, dl, eh, el, fe[j], fel[j]);
     }
   } else {
 #pragma unroll
@@ -424,6 +382,7 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
       fa[j] = (CT)a;
       fe[j] = (CT)e;
       fl[j] = 0.f;
+      fel[j] = 0.f;
     }
   }
   load_coef(X, c.t_prev + VERN7_C[s] * dt);
@@ -438,8 +397,6 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
   ST* out = X.ytmp + (int64_t)((s + 1) & 1) * X.n;
   const int64_t n = X.n;
   double err_acc = 0.0;
-  float err_accf = 0.f;
-  const float atol_f = (float)X.S->atol, rtol_f = (float)X.S->rtol;
   for (int r = g.rank; r < X.n; r += GT::SIZE) {
     CT ar, ai;
     row_matvec(X, r, x, ar, ai);
@@ -471,14 +428,15 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
       }
     } else if (last) {
       if constexpr (MIXED) {
-        float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f, er = 0.f, ei = 0.f;
+        float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;
+        float erh = 0.f, erl = 0.f, eih = 0.f, eil = 0.f;
         for (int j = 0; j < RK_STEP; ++j) {
-          if (fa[j] == 0.f && fl[j] == 0.f && fe[j] == 0.f) continue;
+          if (fa[j] == 0.f && fl[j] == 0.f && fe[j] == 0.f && fel[j] == 0.f) continue;
           const ST kj = (j == s) ? ks : X.k[j * n + r];
           ff_acc(hr, lr, fa[j], fl[j], kj.x);
           ff_acc(hi, li, fa[j], fl[j], kj.y);
-          er = fmaf(fe[j], kj.x, er);
-          ei = fmaf(fe[j], kj.y, ei);
+          ff_acc(erh, erl, fe[j], fel[j], kj.x);   // error estimate in float-float
+          ff_acc(eih, eil, fe[j], fel[j], kj.y);
         }
         // the once-per-step FP64 state update, then its float-pair shadow
         const double yr = X.y[cur][r].x + ((double)hr + (double)lr);
@@ -489,9 +447,11 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
         split_f(yi, shi, sli);
         X.ys[cur ^ 1][r] = make_float2(shr, shi);
         X.yl[cur ^ 1][r] = make_float2(slr, sli);
-        // WRMS error terms in FP32 (the sum over rows is FP64)
-        const float w = sqrtf(er * er + ei * ei) / (atol_f + rtol_f * sqrtf(shr * shr + shi * shi));
-        err_accf = fmaf(w, w, err_accf);
+        // WRMS error term in FP64 against the FP64 state (wrmn_error_dense,
+        // qutip/core/data/ode.pyx:27-52), written as |e|^2 / (atol + rtol |y|)^2
+        const double er = (double)erh + (double)erl, ei = (double)eih + (double)eil;
+        const double sc = X.S->atol + X.S->rtol * sqrt(yr * yr + yi * yi);
+        err_acc += (er * er + ei * ei) / (sc * sc);
       } else {
         CT er = 0, ei = 0;
         double yr = X.y[cur][r].x, yi = X.y[cur][r].y;
@@ -517,7 +477,7 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
   }
   c.rhs += 1;
   double err = 0.0;
-  if (last) err = sqrt(g.sum(MIXED ? (double)err_accf : err_acc) / (double)X.n);
+  if (last) err = sqrt(g.sum(err_acc) / (double)X.n);
   g.sync();
   return err;
 }
@@ -727,13 +687,17 @@ __device__ int step_in_err(const GT& g, Ctx<DT>& X, Ctl& c, int nsteps_left) {
     }
     c.t_front = c.t_prev + dt;
     c.dt_int = dt;
-    // _recompute_safe_step (explicit_rk.pyx:451-467); the mixed form takes the
-    // factor in FP32 (it only sets the next trial step, clamped to [0.2, 10])
+    // _recompute_safe_step (explicit_rk.pyx:451-467) in FP64 for both forms.  Every
+    // thread holds the same err; lane 0 of each warp takes the pow and shares it, so
+    // the FP64 pipe sees one pow per warp, not one per thread.
     double factor;
-    if (err == 0.0) factor = 10.0;
-    else if constexpr (DT == QG_C64)
-      factor = (double)fmaxf(0.2f, fminf(10.0f, 0.9f * powf((float)err, -1.0f / (RK_ORDER + 1))));
-    else factor = fmax(0.2, fmin(10.0, 0.9 * pow(err, -1.0 / (RK_ORDER + 1))));
+    if (err == 0.0) {
+      factor = 10.0;
+    } else {
+      double mine = 0.0;
+      if (lane_id() == 0) mine = fmax(0.2, fmin(10.0, 0.9 * pow(err, -1.0 / (RK_ORDER + 1))));
+      factor = shfl_d(mine, 0);
+    }
     c.dt_safe = fmax(1e-15, dt * factor);
     c.interp_ready = 0;
     c.steps += 1;
@@ -1299,6 +1263,22 @@ extern "C" int qg_batch_vern7_noalloc(const qg_batch* B, void* stream) {
   if (cudaMemsetAsync(a.queue, 0, 4 * sizeof(unsigned int), st) != cudaSuccess)
     return set_error(QG_ERR_CUDA, "clearing the static queue words failed");
   return qg_batch_vern7(&b, stream);
+}
+
+extern "C" int qg_batch_noalloc_staging_fault(void* stream) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return set_error(QG_ERR_CUDA, "no current CUDA device");
+  NoallocAddr a;
+  int rc = noalloc_setup(dev, a);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned int v = 0;
+  if (cudaMemcpyFromSymbolAsync(&v, g_noalloc_queue, sizeof(v), 2 * sizeof(unsigned int),
+                                cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return set_error(QG_ERR_CUDA, "reading the static queue words failed");
+  return v != 0 ? 1 : 0;
 }
 
 extern "C" int64_t qg_batch_slot_bytes(int64_t max_n, int dtype) {

@@ -307,4 +307,47 @@ __device__ __forceinline__ cplx group_coef(const qg_csr_groups& A, int g, double
   return eval_coef(A.coef_code + A.coef_start[g], A.coef_consts, t);
 }
 
+// Float-float accumulation for the mixed form: hi + lo += (fh + fl) * k with the
+// product error from one FMA (TwoProduct) and the addition error from Knuth's
+// TwoSum (Ogita, Rump & Oishi, "Accurate sum and dot product", SIAM J. Sci.
+// Comput. 26 (2005)).  The _rn intrinsics keep the compiler from contracting
+// the product into the sum.  Vern7's stage weights are large and of both signs,
+// so a plain FP32 sum of f_j k_j loses several bits of the stage input; this
+// keeps it to the final rounding to FP32.
+__device__ __forceinline__ void ff_acc(float& hi, float& lo, float fh, float fl, float k) {
+  const float p = __fmul_rn(fh, k);
+  float pe = fmaf(fh, k, -p);
+  pe = fmaf(fl, k, pe);
+  const float sum = __fadd_rn(hi, p);
+  const float bp = __fsub_rn(sum, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bp)), __fsub_rn(p, bp));
+  hi = sum;
+  lo = __fadd_rn(lo, __fadd_rn(e, pe));
+}
+
+// dt * a as a float pair from dt = dh + dl and a = ah + al (tableau hi/lo):
+// hi = fl(dh ah), lo = the product's rounding error plus the cross terms.
+__device__ __forceinline__ void ff_factor(float dh, float dl, float ah, float al, float& fh,
+                                          float& fl) {
+  fh = __fmul_rn(dh, ah);
+  float e = fmaf(dh, ah, -fh);
+  e = fmaf(dh, al, e);
+  fl = fmaf(dl, ah, e);
+}
+
+// fl32(bh + bl + ih + il): TwoSum of the high parts, the low parts added to its
+// error, one final rounding.
+__device__ __forceinline__ float ff_round4(float bh, float bl, float ih, float il) {
+  const float sum = __fadd_rn(bh, ih);
+  const float bp = __fsub_rn(sum, bh);
+  float e = __fadd_rn(__fsub_rn(bh, __fsub_rn(sum, bp)), __fsub_rn(ih, bp));
+  e = __fadd_rn(e, __fadd_rn(bl, il));
+  return __fadd_rn(sum, e);
+}
+
+__device__ __forceinline__ void split_f(double v, float& h, float& l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
 }  // namespace qg

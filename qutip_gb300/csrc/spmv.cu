@@ -20,6 +20,8 @@
 // formed once on the host.  FP64 remains where it carries the result: the
 // complex128 path throughout, and in the mixed form the once-per-step state
 // update y_front = y_prev + increment and the WRMS error reduction.
+#include <mutex>
+
 #include "capi_internal.h"
 #include "common.cuh"
 
@@ -92,6 +94,7 @@ struct RkArgs {
   double* result;
   double fa_d[16], fe_d[16];
   float fa_f[16], fe_f[16];
+  float fe_l[16];  // fe_d - fe_f: the error weights as float pairs (mixed form)
 };
 
 __device__ unsigned int g_fault = 0u;
@@ -170,8 +173,7 @@ __device__ __forceinline__ void lane_dot(const int* __restrict__ col, const VT* 
 // DT: stage dtype (operator, k, ytmp); YDT: state dtype.  CT = elem<DT>::R.
 template <int DT, int YDT, int EPI>
 __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
-                                         const AxpbyArgs& ax, const RkArgs& rk,
-                                         typename elem<DT>::R& err_acc) {
+                                         const AxpbyArgs& ax, const RkArgs& rk, double& err_acc) {
   using ST = typename elem<DT>::T;
   using YT = typename elem<YDT>::T;
   using CT = typename elem<DT>::R;
@@ -210,21 +212,29 @@ __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
       CT ymag;
       if constexpr (MIXED) {
         cx<CT> inc{0, 0};
+        float erh = 0.f, erl = 0.f, eih = 0.f, eil = 0.f;
 #pragma unroll
         for (int j = 0; j < RK_STEP; ++j) {
           const CT fb = fa<CT>(rk, j), fq = fe<CT>(rk, j);
           if (fb == (CT)0 && fq == (CT)0) continue;
           const cx<CT> kj = (j == s) ? ks : ld_cx<CT>(k + (size_t)j * n64 + row);
           if (fb != (CT)0) cx_axpy(inc, fb, kj);
-          if (fq != (CT)0) cx_axpy(e, fq, kj);
+          if (fq != (CT)0) {  // the error estimate in float-float
+            ff_acc(erh, erl, (float)fq, rk.fe_l[j], (float)kj.re);
+            ff_acc(eih, eil, (float)fq, rk.fe_l[j], (float)kj.im);
+          }
         }
         // FP64 state update of the step; FP32 shadow for the next stages
         const double2 yp = static_cast<const double2*>(rk.y_prev)[row];
         const double2 yf = make_double2(yp.x + (double)inc.re, yp.y + (double)inc.im);
         static_cast<double2*>(rk.y_front)[row] = yf;
-        const float2 yf32 = make_float2((float)yf.x, (float)yf.y);
-        static_cast<float2*>(rk.y_front_s)[row] = yf32;
-        ymag = (CT)sqrtf(yf32.x * yf32.x + yf32.y * yf32.y);
+        static_cast<float2*>(rk.y_front_s)[row] = make_float2((float)yf.x, (float)yf.y);
+        // WRMS error term in FP64 against the FP64 state (wrmn_error_dense,
+        // qutip/core/data/ode.pyx:27-52), written as |e|^2 / (atol + rtol |y|)^2
+        const double er = (double)erh + (double)erl, ei = (double)eih + (double)eil;
+        const double sc = rk.atol + rk.rtol * sqrt(yf.x * yf.x + yf.y * yf.y);
+        err_acc += (er * er + ei * ei) / (sc * sc);
+        return;
       } else {
         // reference order: y_front = y_prev, then += fb_j k_j term by term
         cx<CT> y = ld_cx<CT>(static_cast<const YT*>(rk.y_prev) + row);
@@ -240,7 +250,8 @@ __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
         const cx<CT> ys = ld_cx<CT>(static_cast<const YT*>(rk.y_front) + row);
         ymag = sqrt(ys.re * ys.re + ys.im * ys.im);
       }
-      const CT w = sqrt(e.re * e.re + e.im * e.im) / ((CT)rk.atol + (CT)rk.rtol * ymag);
+      const double w = sqrt((double)e.re * e.re + (double)e.im * e.im) /
+                       (rk.atol + rk.rtol * (double)ymag);
       err_acc += w * w;
     }
   }
@@ -296,7 +307,7 @@ __global__ void __launch_bounds__(SPMV_BLOCK)
   const int sub = threadIdx.x / LANES, lane = threadIdx.x % LANES;
   constexpr int RPB = SPMV_BLOCK / LANES;
   const ST* __restrict__ val = static_cast<const ST*>(A.val);
-  R err_acc = 0;
+  double err_acc = 0.0;
 
   for (int base = blockIdx.x * RPB; base < n; base += gridDim.x * RPB) {
     const int row = base + sub;
@@ -316,7 +327,7 @@ __global__ void __launch_bounds__(SPMV_BLOCK)
     if (valid && lane == 0) epilogue<DT, YDT, EPI>(row, acc, ax, rk, err_acc);
   }
   if constexpr (EPI == EPI_RK) {
-    if (rk.stage == RK_STEP - 1) finish_error<SPMV_BLOCK>(rk, (double)err_acc, red);
+    if (rk.stage == RK_STEP - 1) finish_error<SPMV_BLOCK>(rk, err_acc, red);
   }
 }
 
@@ -369,7 +380,7 @@ __global__ void __launch_bounds__(BLOCK)
 
   const int sub = threadIdx.x / LANES, lane = threadIdx.x % LANES;
   constexpr int NSUB = BLOCK / LANES;
-  R err_acc = 0;
+  double err_acc = 0.0;
 
   auto issue = [&](int tile, int stage) {
     TileGeom g = tile_geom(A, tile);
@@ -435,7 +446,7 @@ __global__ void __launch_bounds__(BLOCK)
     return;
   }
   if constexpr (EPI == EPI_RK) {
-    if (rk.stage == RK_STEP - 1) finish_error<BLOCK>(rk, (double)err_acc, red);
+    if (rk.stage == RK_STEP - 1) finish_error<BLOCK>(rk, err_acc, red);
   }
 }
 
@@ -470,7 +481,7 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, UNR>::MIN_BLOCKS)
   const int nwarps = (gridDim.x * SPMV_BLOCK) >> 5;
   const ST* __restrict__ val = static_cast<const ST*>(A.val);
   const int* __restrict__ col = A.col;
-  R err_acc = 0;
+  double err_acc = 0.0;
   for (int sl = warp; sl < A.n_tiles; sl += nwarps) {
     int goff = __ldg(A.row_ptr + sl) + lane;  // this lane's first entry of the group
     const int row = sl * 32 + lane;
@@ -515,7 +526,7 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, UNR>::MIN_BLOCKS)
     if (row < n) epilogue<DT, YDT, EPI>(row, acc, ax, rk, err_acc);
   }
   if constexpr (EPI == EPI_RK) {
-    if (rk.stage == RK_STEP - 1) finish_error<SPMV_BLOCK>(rk, (double)err_acc, red);
+    if (rk.stage == RK_STEP - 1) finish_error<SPMV_BLOCK>(rk, err_acc, red);
   }
 }
 
@@ -610,7 +621,7 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, 4>::MIN_BLOCKS)
   const int warp = (blockIdx.x * SPMV_BLOCK + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * SPMV_BLOCK) >> 5;
   const unsigned char* __restrict__ codes = reinterpret_cast<const unsigned char*>(A.col);
-  R err_acc = 0;
+  double err_acc = 0.0;
   for (int sl = warp; sl < S; sl += nwarps) {
     const int row = sl * 32 + lane;
     cx<R> acc{0, 0};
@@ -655,7 +666,7 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, 4>::MIN_BLOCKS)
     if (row < n) epilogue<DT, YDT, EPI>(row, acc, ax, rk, err_acc);
   }
   if constexpr (EPI == EPI_RK) {
-    if (rk.stage == RK_STEP - 1) finish_error<SPMV_BLOCK>(rk, (double)err_acc, red);
+    if (rk.stage == RK_STEP - 1) finish_error<SPMV_BLOCK>(rk, err_acc, red);
   }
 }
 
@@ -726,7 +737,7 @@ __global__ void __launch_bounds__(LB_BLOCK)
   const int nd0 = L.n_const_diag;
   int nw1 = 0;  // leading general collapse operators of width 1
   while (nw1 < NE && L.c_width[nw1] == 1) ++nw1;
-  R err_acc = 0;
+  double err_acc = 0.0;
   // (r, c) of idx, advanced by the grid stride without a division per element
   const int stride = gridDim.x * LB_BLOCK;
   const int sc = stride / d, sr = stride - (stride / d) * d;
@@ -832,31 +843,35 @@ __global__ void __launch_bounds__(LB_BLOCK)
     }
   }
   if constexpr (EPI == EPI_RK) {
-    if (rk.stage == RK_STEP - 1) finish_error<LB_BLOCK>(rk, (double)err_acc, red);
+    if (rk.stage == RK_STEP - 1) finish_error<LB_BLOCK>(rk, err_acc, red);
   }
 }
 
 // ------------------------------------------------------------------ launch --
 // Opt `kernel` into `smem` bytes of dynamic shared memory and return its
-// resident blocks per SM.  The caller keeps one cache per kernel instantiation.
+// resident blocks per SM.  The caller keeps one cache per kernel instantiation; it
+// holds one entry per device (the attribute is set with that device current) and is
+// shared by host threads under its mutex.
+constexpr int OCC_MAX_DEVICES = 64;
 struct OccCache {
-  int dev = -1, occ = 0;
-  size_t smem = 0;
+  std::mutex mu;
+  int occ[OCC_MAX_DEVICES] = {};
+  size_t smem[OCC_MAX_DEVICES] = {};
 };
 template <typename K>
 static int staged_occupancy(K kernel, int block, size_t smem, OccCache& c) {
   int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev == c.dev && smem == c.smem) return c.occ;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= OCC_MAX_DEVICES) return -1;
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (c.occ[dev] > 0 && c.smem[dev] == smem) return c.occ[dev];
   if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return -1;
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem) != cudaSuccess)
     return -1;
-  c.dev = dev;
-  c.smem = smem;
-  c.occ = per_sm;
+  c.smem[dev] = smem;
+  c.occ[dev] = per_sm;
   return per_sm;
 }
 
@@ -1103,6 +1118,7 @@ static int prepare_stage(const qg_rk_buffers* B, int op_dtype, int64_t n_rows, i
     rk.fe_d[j] = e;
     rk.fa_f[j] = (float)a;
     rk.fe_f[j] = (float)e;
+    rk.fe_l[j] = (float)(e - (double)rk.fe_f[j]);
   }
   x = stage == 0 ? (mixed ? B->y_prev_s : B->y_prev) : (const char*)B->ytmp + (stage & 1) * n * es;
   return QG_OK;

@@ -462,9 +462,7 @@ class DeviceOperator:
         other.set_launch(self.launch)
         return other
 
-    def _finish(self, G):
-        fmt = self.fmt
-        dtype = self.dtype
+    def _pack_coefficients(self):
         if all(c is None for c in self.coeffs):
             self.coef_code = self.coef_start = self.coef_consts = None
         else:
@@ -472,6 +470,23 @@ class DeviceOperator:
             self.coef_code = torch.from_numpy(code).to(self.device)
             self.coef_start = torch.from_numpy(starts).to(self.device)
             self.coef_consts = torch.from_numpy(consts).to(self.device)
+
+    def set_coefficients(self, coeffs):
+        """Replace the groups' coefficient programs (new args), keeping the storage."""
+        if len(coeffs) != self.n_groups:
+            raise ValueError(f"{len(coeffs)} coefficients for {self.n_groups} groups")
+        if [c is None for c in coeffs] != [c is None for c in self.coeffs]:
+            raise ValueError("constant and time-dependent groups cannot swap places")
+        self.coeffs = list(coeffs)
+        self._pack_coefficients()
+        self.struct.coef_code = _ptr(self.coef_code)
+        self.struct.coef_start = _ptr(self.coef_start)
+        self.struct.coef_consts = _ptr(self.coef_consts)
+
+    def _finish(self, G):
+        fmt = self.fmt
+        dtype = self.dtype
+        self._pack_coefficients()
         layout = {"sliced": _lib.QG_LAYOUT_SLICED, "dict": _lib.QG_LAYOUT_SLICED_DICT}.get(
             fmt, _lib.QG_LAYOUT_ROW_MAJOR)
         if fmt == "dict" and getattr(self, "dict_split", False):

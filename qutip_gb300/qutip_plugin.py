@@ -635,6 +635,19 @@ def device_operator(terms, dtype="c128") -> DeviceOperator:
     return DeviceOperator(terms, dtype=dtype, device=_device())
 
 
+def _coefficient_groups(terms):
+    """Term indices per coefficient group, in the order the operators merge them
+    (:func:`qutip_gb300.systems.merge_terms`), with each group's coefficient."""
+    keyed, out = {}, []
+    for i, (_, c) in enumerate(terms):
+        key = None if c is None else c.key()
+        if key not in keyed:
+            keyed[key] = len(out)
+            out.append(([], c))
+        out[keyed[key]][0].append(i)
+    return [(tuple(idx), c) for idx, c in out]
+
+
 def _is_matrix_form(rhs) -> bool:
     try:
         from qutip.core.cy.lindblad_matrix_form import LindbladMatrixForm
@@ -707,10 +720,12 @@ class IntegratorGpuVern7(Integrator):
         dt = "c128" if prec == "double" else "c64"
         rhs = self._rhs()
         self._terms = None
+        self._groups = None
         if _is_matrix_form(rhs):
             self._op = lindblad_operator(rhs, dt)
         else:
             self._terms = qobjevo_terms(rhs)
+            self._groups = _coefficient_groups(self._terms)
             self._op = device_operator(self._terms, dt)
         self._blocks = {1: self._op}
         self._ode = self._integrator(self._op)
@@ -778,12 +793,31 @@ class IntegratorGpuVern7(Integrator):
             state = self.get_state()
         # The device coefficient programs hold the args they were decoded with, while the
         # reference's integrators read the rhs live: Solver._argument follows
-        # rhs.arguments(args) with a soft reset (solver_base.py:457-460), so a
-        # time-dependent rhs is decoded again.
-        if hard or not getattr(self._rhs(), "isconstant", True):
+        # rhs.arguments(args) with a soft reset (solver_base.py:457-460), so the
+        # coefficients of a time-dependent rhs are decoded again.  The operator storage
+        # stays: only the programs depend on the args.
+        if hard:
             self._prepare()
+        elif not getattr(self._rhs(), "isconstant", True):
+            self._update_coefficients()
         if self._is_set:
             self.set_state(*state)
+
+    def _update_coefficients(self):
+        """New device coefficient programs for the same operator storage, or a full
+        rebuild when the args regroup the terms (two coefficients become equal)."""
+        if self._terms is None:                       # matrix form: rebuild
+            self._prepare()
+            return
+        terms = qobjevo_terms(self._rhs())
+        groups = _coefficient_groups(terms)
+        if [idx for idx, _ in groups] != [idx for idx, _ in self._groups]:
+            self._prepare()
+            return
+        coeffs = [c for _, c in groups]
+        for op in self._blocks.values():
+            op.set_coefficients(coeffs)
+        self._terms, self._groups = terms, groups
 
     @property
     def options(self):
@@ -889,6 +923,10 @@ def gpu_map(task, values, task_args=None, task_kwargs=None, reduce_func=None, ma
     solver, seeds, starts, floors, tlist, e_ops = _mc_map_items(
         task, values, task_args or (), task_kwargs)
     opts = solver.options
+    if opts.get("method") not in ("vern7", "gpu_vern7"):
+        raise TypeError(f"map='gpu' integrates with Vern7 on the device; method="
+                        f"{opts.get('method')!r} is not available there (use 'vern7' or "
+                        "'gpu_vern7')")
     if opts.get("bitgenerator") not in (None, "PCG64"):
         raise TypeError("map='gpu' draws from PCG64 streams (the default bit generator)")
     if opts.get("store_states") or opts.get("store_final_state"):

@@ -380,7 +380,19 @@ def test_new_args_reach_the_device_coefficients(qt, plugin):
     ref = qt.MESolver(qt.QobjEvo(H, args={"amp": 0.2}), c_ops, options={"method": "vern7"})
     got = qt.MESolver(qt.QobjEvo(H, args={"amp": 0.2}), c_ops,
                       options={"method": "gpu_vern7"})
+    op0 = got._integrator._op
     for amp in (0.2, 0.7, 0.0):
         r = ref.run(rho0, tl, args={"amp": amp}, e_ops=e_ops)
         g = got.run(rho0, tl, args={"amp": amp}, e_ops=e_ops)
         np.testing.assert_allclose(g.expect[0], r.expect[0], atol=1e-8, rtol=1e-6)
+        assert got._integrator._op is op0     # new programs, the same operator storage
+
+
+def test_gpu_map_refuses_other_methods(qt, plugin):
+    """map='gpu' integrates with Vern7 on the device; another method is an error, not a
+    silent change of integrator."""
+    H, c_ops, psi0, e_ops = _jc(qt, N=4)
+    for method in ("adams", "dop853"):
+        with pytest.raises(TypeError, match="map='gpu'"):
+            qt.mcsolve(H, psi0, np.linspace(0, 1, 5), c_ops, e_ops=e_ops, ntraj=2, seeds=1,
+                       options={"method": method, "map": "gpu"})

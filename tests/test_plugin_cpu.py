@@ -183,3 +183,14 @@ def test_map_task_decoding_rejects_what_it_cannot_batch(qt, plugin):
         solver._run_one_traj, [4, 5], (bright, tl, e_ops),
         {"no_jump": False, "jump_prob_floor": 0.25})[1:4]
     assert seeds == [4, 5] and floors == [0.25, 0.25] and [w for _, w in starts] == [1.0, 1.0]
+
+
+def test_map_refuses_integration_methods_it_does_not_run(qt, plugin):
+    """map='gpu' runs Vern7 on the device: an MCSolver set to another method is refused
+    with TypeError before anything reaches the device."""
+    H, c_ops, bright, dark, e_ops = _jc_dark(qt)
+    tl = np.linspace(0, 1, 3)
+    for method in ("adams", "dop853", "lsoda"):
+        solver = qt.MCSolver(H, c_ops, options={"map": "serial", "method": method})
+        with pytest.raises(TypeError, match="map='gpu'"):
+            plugin.gpu_map(solver._run_one_traj, [1, 2], (bright, tl, e_ops), {})

@@ -61,6 +61,8 @@ def test_noalloc_matches_allocating_entry_point_twice(dtype):
         bp.jump_which.zero_()
         rc = lib.qg_batch_vern7_noalloc(C.byref(bp.struct), stream_ptr())
         _lib.check(rc, "qg_batch_vern7_noalloc")
+        # the staging-timeout flag of this call, read before the next call clears it
+        assert lib.qg_batch_noalloc_staging_fault(stream_ptr()) == 0
         got = _snapshot(bp)
         np.testing.assert_allclose(got[0], want[0], rtol=1e-12, atol=1e-14)
         np.testing.assert_array_equal(got[1].reshape(-1, 4)[:, [0, 3]],
