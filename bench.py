@@ -625,10 +625,15 @@ def run_large(args):
     # values (complex128 values summed on the device in varying order differ in their last
     # bits and do not deduplicate)
     op64 = DeviceOperator.from_device_groups(groups, "c64")
-    del groups
-    torch.cuda.empty_cache()
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
+    host_groups = None
+    if not args.no_cpu_baseline:
+        # the generator's CSR groups on the host, for the reference's matvec timing below
+        host_groups = [(p.cpu().numpy(), i.to(torch.int32).cpu().numpy(), d.cpu().numpy(), c)
+                       for p, i, d, c in groups]
+    del groups
+    torch.cuda.empty_cache()
     log(f"large: L={L} operator assembled on the device in {build_s:.1f} s, "
         f"{op64.nnz} entries ({op64.launch_desc()})")
     ex = ExpectOps(s.e_ops)
@@ -643,6 +648,8 @@ def run_large(args):
         torch.cuda.synchronize()
         times.append(time.perf_counter() - t1)
     err = max(float(np.max(np.abs(np.real(a) - np.real(b)))) for a, b in zip(r64.expect, r128.expect))
+    rel = max(float(np.max(np.abs(np.real(a) - np.real(b))) / np.max(np.abs(np.real(b))))
+              for a, b in zip(r64.expect, r128.expect))
     spmv_ms, spmv_b, spmv_gbs = measure_spmv(op64, reps=10)
     stage_ms, stage_b, stage_gbs = measure_stage_roofline(op64, s.state0, "mixed", reps=3)
     peak, _ = hbm_peak_gbs()
@@ -650,17 +657,56 @@ def run_large(args):
            "liouvillian_rows": op64.n_rows, "entries": int(op64.nnz),
            "device_assembly_s": build_s, "solves_per_sec": 1.0 / float(np.median(times)),
            "s_per_solve": float(np.median(times)), "rhs_calls": int(r64.stats.get("rhs", 0)),
-           "max_abs_err_vs_fp64_gpu": err,
+           "max_abs_err_vs_fp64_gpu": err, "rel_err_vs_fp64_gpu": rel,
+           "steps_mixed_vs_fp64": [int(r64.stats["steps"]), int(r128.stats["steps"])],
            "spmv_c64": {"gbs": spmv_gbs, "ms": spmv_ms, "bytes": int(spmv_b), "frac": spmv_gbs / peak},
            "stage_c64": {"gbs": stage_gbs, "ms": stage_ms, "bytes": int(stage_b),
                          "frac": stage_gbs / peak},
-           "cpu_baseline": None,
-           "cpu_baseline_note": "not run at this size: the reference's host Liouvillian "
-                                "construction alone takes minutes (the CPU baseline of the "
-                                "headline line is at L = 10)"}
+           "cpu_baseline": None}
     del op64, op128
     torch.cuda.empty_cache()
+    if host_groups is not None:
+        try:
+            out["cpu_baseline"] = large_cpu_baseline(host_groups, s.state0,
+                                                     int(r128.stats.get("rhs", 0)))
+        except Exception as exc:  # noqa: BLE001
+            out["cpu_baseline"] = {"value": None, "error": repr(exc)[:300]}
     return out
+
+
+def large_cpu_baseline(host_groups, state0, rhs_full, reps=2):
+    """The reference's right-hand side at L = 12 on the host: its ``QobjEvo.matmul_data``
+    (the compiled CSR matvec of every term, with the term's coefficient) on the same
+    generator -- downloaded from the device, because building it with QuTiP's Kronecker
+    products takes minutes and tens of GB -- timed over ``reps`` calls and scaled by the
+    RHS calls of the whole solve.  The reference's Vern7 vector operations are not
+    included, so this bounds the reference's speed from above."""
+    qt, _ = host_qutip()
+    from qutip.core import data as _data
+    n = host_groups[0][0].size - 1
+    d = int(round(np.sqrt(n)))
+    dims = [[[d], [d]], [[d], [d]]]
+    def as_function(c):
+        return lambda t: c(t)          # the coefficient's value, evaluated on the host
+
+    elems = []
+    for indptr, indices, data, c in host_groups:
+        m = _data.CSR((data, indices, indptr.astype(np.int32)), shape=(n, n), copy=False)
+        q = qt.Qobj(m, dims=dims, superrep="super", copy=False)
+        elems.append(q if c is None else [q, as_function(c)])
+    evo = qt.QobjEvo(elems)
+    x = _data.Dense(np.asarray(state0, dtype=np.complex128).reshape(-1, 1))
+    evo.matmul_data(0.1, x)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        evo.matmul_data(0.1, x)
+    rhs_s = (time.perf_counter() - t0) / reps
+    return {"value": 1.0 / (rhs_s * rhs_full), "unit": UNIT, "cores": 1, "kind": "reference",
+            "sample": (f"the reference's QobjEvo.matmul_data (compiled single-thread CSR matvec) "
+                       f"on the L=12 generator, {rhs_s:.2f} s per call over {reps} calls, scaled "
+                       f"by the {rhs_full} RHS calls of the whole solve; Vern7 vector operations "
+                       "not included (an upper bound on the reference's solves/s)"),
+            "rhs_call_s": rhs_s, "rhs_full": rhs_full}
 
 
 def run_matrix_form(args, sysm, tlist, ex, want, hbm_peak):

@@ -68,7 +68,55 @@ class Coefficient:
                            self.consts + other.consts, f"({self.expr}){sym}({other.expr})")
 
     def conj(self) -> "Coefficient":
+        """``conj(c)``; a program that is real for every real t is its own conjugate, so
+        it comes back unchanged (the reference's ConjCoefficient of a real function --
+        the spost part of every Liouvillian with a real time dependence -- then shares
+        the original's coefficient group)."""
+        if self.is_real():
+            return self
         return Coefficient(self._body() + [OPCODES["CONJ"]], self.consts, f"conj({self.expr})")
+
+    def is_real(self) -> bool:
+        """Whether the program returns a real number for every real t: a static pass over
+        the stack that tracks, per slot, whether the value is provably real.  Real
+        constants and t are real; +, -, *, /, negation, cos, sin, exp, cosh, sinh, tanh,
+        tan, arctan and conj keep realness; real, imag and abs always give a real value;
+        log, sqrt, pow (a negative real argument gives a complex result) and
+        interpolation are treated as possibly complex."""
+        keep = {OPCODES[k] for k in ("NEG", "COS", "SIN", "EXP", "COSH", "SINH", "TANH", "TAN",
+                                     "ARCTAN", "CONJ")}
+        make = {OPCODES[k] for k in ("REAL", "IMAG", "ABS")}
+        binary = {OPCODES[k] for k in ("ADD", "SUB", "MUL", "DIV")}
+        stack: list[bool] = []
+        i = 0
+        code = self.code
+        while i < len(code):
+            op = code[i]
+            if op == OPCODES["END"]:
+                break
+            if op == OPCODES["CONST"]:
+                stack.append(self.consts[code[i + 1]].imag == 0)
+                i += 2
+                continue
+            if op == OPCODES["INTERP"]:
+                stack.append(False)
+                i += 2
+                continue
+            if op == OPCODES["T"]:
+                stack.append(True)
+            elif op in keep:
+                pass
+            elif op in make:
+                stack[-1] = True
+            elif op in binary:
+                b = stack.pop()
+                stack[-1] = stack[-1] and b
+            else:                       # LOG, SQRT, POW and anything unknown
+                if op == OPCODES["POW"]:
+                    stack.pop()
+                stack[-1] = False
+            i += 1
+        return len(stack) == 1 and stack[0]
 
     def __add__(self, other):
         return self._combine(_as_coeff(other), "ADD", "+")

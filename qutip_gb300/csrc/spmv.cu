@@ -95,6 +95,9 @@ struct RkArgs {
   double fa_d[16], fe_d[16];
   float fa_f[16], fe_f[16];
   float fe_l[16];  // fe_d - fe_f: the error weights as float pairs (mixed form)
+  // bit j set where fa_d[j] / fe_d[j] is nonzero: the factor loops test these integer
+  // masks, not the factors (a floating-point compare per row would run on the FP64 pipe)
+  unsigned int nz_a, nz_e;
 };
 
 __device__ unsigned int g_fault = 0u;
@@ -203,25 +206,25 @@ __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
 #pragma unroll
       for (int j = 0; j < RK_EXTRA_STEP - 1; ++j) {
         if (j > s) break;
-        const CT f = fa<CT>(rk, j);
-        if (f != (CT)0) cx_axpy(v, f, j == s ? ks : ld_cx<CT>(k + (size_t)j * n64 + row));
+        if ((rk.nz_a >> j) & 1u)
+          cx_axpy(v, fa<CT>(rk, j), j == s ? ks : ld_cx<CT>(k + (size_t)j * n64 + row));
       }
       st_cx(static_cast<ST*>(rk.ytmp_out) + row, v);
     } else if (s == RK_STEP - 1) {
       cx<CT> e{0, 0};
-      CT ymag;
+      double ymag2;
       if constexpr (MIXED) {
         cx<CT> inc{0, 0};
         float erh = 0.f, erl = 0.f, eih = 0.f, eil = 0.f;
 #pragma unroll
         for (int j = 0; j < RK_STEP; ++j) {
-          const CT fb = fa<CT>(rk, j), fq = fe<CT>(rk, j);
-          if (fb == (CT)0 && fq == (CT)0) continue;
+          const bool ub = (rk.nz_a >> j) & 1u, uq = (rk.nz_e >> j) & 1u;
+          if (!ub && !uq) continue;
           const cx<CT> kj = (j == s) ? ks : ld_cx<CT>(k + (size_t)j * n64 + row);
-          if (fb != (CT)0) cx_axpy(inc, fb, kj);
-          if (fq != (CT)0) {  // the error estimate in float-float
-            ff_acc(erh, erl, (float)fq, rk.fe_l[j], (float)kj.re);
-            ff_acc(eih, eil, (float)fq, rk.fe_l[j], (float)kj.im);
+          if (ub) cx_axpy(inc, fa<CT>(rk, j), kj);
+          if (uq) {  // the error estimate in float-float
+            ff_acc(erh, erl, fe<CT>(rk, j), rk.fe_l[j], (float)kj.re);
+            ff_acc(eih, eil, fe<CT>(rk, j), rk.fe_l[j], (float)kj.im);
           }
         }
         // FP64 state update of the step; FP32 shadow for the next stages
@@ -240,19 +243,19 @@ __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
         cx<CT> y = ld_cx<CT>(static_cast<const YT*>(rk.y_prev) + row);
 #pragma unroll
         for (int j = 0; j < RK_STEP; ++j) {
-          const CT fb = fa<CT>(rk, j), fq = fe<CT>(rk, j);
-          if (fb == (CT)0 && fq == (CT)0) continue;
+          const bool ub = (rk.nz_a >> j) & 1u, uq = (rk.nz_e >> j) & 1u;
+          if (!ub && !uq) continue;
           const cx<CT> kj = (j == s) ? ks : ld_cx<CT>(k + (size_t)j * n64 + row);
-          if (fb != (CT)0) cx_axpy(y, fb, kj);
-          if (fq != (CT)0) cx_axpy(e, fq, kj);
+          if (ub) cx_axpy(y, fa<CT>(rk, j), kj);
+          if (uq) cx_axpy(e, fe<CT>(rk, j), kj);
         }
         st_cx(static_cast<YT*>(rk.y_front) + row, y);
         const cx<CT> ys = ld_cx<CT>(static_cast<const YT*>(rk.y_front) + row);
-        ymag = sqrt(ys.re * ys.re + ys.im * ys.im);
+        ymag2 = (double)ys.re * ys.re + (double)ys.im * ys.im;
       }
-      const double w = sqrt((double)e.re * e.re + (double)e.im * e.im) /
-                       (rk.atol + rk.rtol * (double)ymag);
-      err_acc += w * w;
+      // wrmn_error_dense (qutip/core/data/ode.pyx:27-52) as |e|^2 / (atol + rtol |y|)^2
+      const double sc = rk.atol + rk.rtol * sqrt(ymag2);
+      err_acc += ((double)e.re * e.re + (double)e.im * e.im) / (sc * sc);
     }
   }
 }
@@ -287,6 +290,16 @@ __device__ __forceinline__ void load_coefs(const qg_csr_groups& A, double t, cx<
   if (threadIdx.x < A.n_groups) {
     cplx c = group_coef(A, threadIdx.x, t);
     coef[threadIdx.x] = cx<CT>{(CT)c.re, (CT)c.im};
+  }
+}
+
+// Class of each group's coefficient, decided once per block: 0 = exactly one (the
+// group's sum goes straight into the row's), 1 = real, 2 = complex.
+template <typename CT>
+__device__ __forceinline__ void coef_classes(const qg_csr_groups& A, const cx<CT>* coef, int* cls) {
+  if (threadIdx.x < A.n_groups) {
+    const cx<CT> c = coef[threadIdx.x];
+    cls[threadIdx.x] = (c.re == (CT)1 && c.im == (CT)0) ? 0 : (c.im == (CT)0 ? 1 : 2);
   }
 }
 
@@ -601,12 +614,14 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, 4>::MIN_BLOCKS)
   using C4 = typename Codes4<CB>::T;
   extern __shared__ __align__(16) unsigned char dict_smem[];
   __shared__ cx<R> coef[QG_MAX_GROUPS];
+  __shared__ int ccls[QG_MAX_GROUPS];
   __shared__ int tstart[QG_MAX_GROUPS + 1];
   __shared__ double red[SPMV_BLOCK / 32];
   const int D = A.lanes;
   ST* tval = reinterpret_cast<ST*>(dict_smem);
   int* toff = reinterpret_cast<int*>(dict_smem + (size_t)D * sizeof(ST));
   load_coefs(A, t, coef);
+  coef_classes(A, coef, ccls);
   for (int i = threadIdx.x; i < D; i += SPMV_BLOCK) {
     tval[i] = __ldg(static_cast<const ST*>(A.val) + i);
     toff[i] = __ldg(A.dict_off + i);
@@ -633,7 +648,9 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, 4>::MIN_BLOCKS)
       const C4* __restrict__ cp =
           reinterpret_cast<const C4*>(codes + (size_t)CB * __ldg(A.row_ptr + g * (S + 1) + sl)) +
           lane;
-      R ar = 0, ai = 0;
+      // FP64: a group whose coefficient is one accumulates into the row's sum directly
+      const bool direct = sizeof(R) == 8 && ccls[g] == 0;
+      R ar = direct ? acc.re : (R)0, ai = direct ? acc.im : (R)0;
 #pragma unroll 2
       for (int q = 0; q < wq; ++q) {
         const C4 c4 = ld_stream(cp + 32 * q);
@@ -661,7 +678,10 @@ __global__ void __launch_bounds__(SPMV_BLOCK, SlicedBounds<DT, 4>::MIN_BLOCKS)
           }
         }
       }
-      coef_mac(acc, coef[g], ar, ai);
+      if (direct)
+        acc = cx<R>{ar, ai};
+      else
+        coef_mac(acc, coef[g], ar, ai);
     }
     if (row < n) epilogue<DT, YDT, EPI>(row, acc, ax, rk, err_acc);
   }
@@ -1119,6 +1139,8 @@ static int prepare_stage(const qg_rk_buffers* B, int op_dtype, int64_t n_rows, i
     rk.fa_f[j] = (float)a;
     rk.fe_f[j] = (float)e;
     rk.fe_l[j] = (float)(e - (double)rk.fe_f[j]);
+    if (a != 0.0) rk.nz_a |= 1u << j;
+    if (e != 0.0) rk.nz_e |= 1u << j;
   }
   x = stage == 0 ? (mixed ? B->y_prev_s : B->y_prev) : (const char*)B->ytmp + (stage & 1) * n * es;
   return QG_OK;

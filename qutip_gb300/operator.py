@@ -38,7 +38,17 @@ def _ptr(t: torch.Tensor | None) -> int | None:
     return None if t is None else t.data_ptr()
 
 
+try:  # the raw current stream without torch.cuda.current_stream()'s Python overhead
+    _raw_stream = torch._C._cuda_getCurrentRawStream
+    _cur_device = torch._C._cuda_getDevice
+except AttributeError:  # pragma: no cover - older or newer torch without these bindings
+    _raw_stream = _cur_device = None
+
+
 def stream_ptr() -> int:
+    """``cudaStream_t`` of torch's current stream on the current device, as an int."""
+    if _raw_stream is not None:
+        return _raw_stream(_cur_device())
     return torch.cuda.current_stream().cuda_stream
 
 

@@ -184,7 +184,6 @@ class _OpCache:
 
 
 _OPS = _OpCache()
-_EOPS = _OpCache()
 _SUPER_EOPS = _OpCache()
 
 
@@ -388,32 +387,70 @@ def _check_expect_shapes(op, state):
             raise ValueError(f"incompatible shapes {op.shape} and {state.shape}")
 
 
-def _launch_expect(op, state, out_ptr):
-    """``<psi|op|psi>`` (ket) or ``tr(op rho)`` (square state) into ``out_ptr[0:2]``
-    (the kernel also writes the norm or trace to ``out_ptr[2:4]``)."""
-    e = _EOPS.get(op, lambda o: _ExpectOp(_scipy(o)))
-    if state.shape[1] == 1:
-        _lib.call("qg_expect_ket", C.byref(e.struct), C.byref(_view(state.buf)),
-                  out_ptr, stream_ptr())
-    else:
-        _lib.call("qg_expect_dm", C.byref(e.struct), state.shape[0],
-                  C.byref(_view(state.buf)), out_ptr, stream_ptr())
+_MULTI = _OpCache(size=16)
 
 
-def _super_row(op, d):
-    def build(o):
-        rows = _scipy(o)[np.arange(d) * (d + 1)]
-        return _ExpectOp(sp.csr_matrix(np.ones((1, d))) @ rows)   # 1 x n summed row
-    return _SUPER_EOPS.get(op, build)
+class _MultiExpect:
+    """Several e_ops as one operator with one coefficient group each, so that one
+    ``qg_expect_dm`` / ``qg_expect_ket`` launch evaluates all of them."""
+
+    def __init__(self, ops):
+        from .solver import _wide_groups
+        self.ops = ops                                   # keeps the ids below valid
+        self.dev = _wide_groups([_scipy(o) for o in ops], "c128", _device())
+        self.G = len(ops)
 
 
-def _launch_expect_super(op, state, out_ptr):
-    """``tr(unvec(op @ vec(rho)))`` into ``out_ptr[0:2]``: the rows of ``op`` on the
-    diagonal of rho, summed into one row, times the state (a matvec with one row)."""
-    d = int(math.isqrt(state.shape[0]))
-    e = _super_row(op, d)
-    _lib.call("qg_spmv_csr", C.byref(e.struct), 0.0, state.buf.data_ptr(), out_ptr,
-              1.0, 0.0, 0.0, 0.0, stream_ptr())
+class _SuperRows:
+    """Several super-operator e_ops as one operator whose row k is the sum of the
+    diagonal-position rows of op k: one matvec gives every ``expect_super`` value."""
+
+    def __init__(self, ops, d):
+        self.ops = ops
+        rows = [sp.csr_matrix(np.ones((1, d))) @ _scipy(o)[np.arange(d) * (d + 1)] for o in ops]
+        self.e = _ExpectOp(sp.vstack(rows, format="csr"))
+
+
+def _group_get(cache, ops, build):
+    key = tuple(id(o) for o in ops)
+    hit = cache._d.get(key)
+    if hit is not None and all(a is b for a, b in zip(hit[1].ops, ops)):
+        cache._d.move_to_end(key)
+        return hit[1]
+    val = build(tuple(ops))
+    cache._d[key] = (None, val)
+    if len(cache._d) > cache.size:
+        cache._d.popitem(last=False)
+    return val
+
+
+def _launch_batch(batch, state, base_ptr):
+    """Launch the kernels of every ``(kind, op)`` of ``batch`` against ``state``: the
+    ``expect`` operators in launches of up to QG_MAX_EOPS groups, the ``super`` ones as
+    one multi-row matvec.  Returns ``(kind, op, double offset)`` per operator."""
+    place = []
+    off = 0
+    ex = [o for k, o in batch if k == "expect"]
+    for i in range(0, len(ex), _lib.QG_MAX_EOPS):
+        chunk = ex[i:i + _lib.QG_MAX_EOPS]
+        m = _group_get(_MULTI, chunk, _MultiExpect)
+        if state.shape[1] == 1:
+            _lib.call("qg_expect_ket", C.byref(m.dev.struct), C.byref(_view(state.buf)),
+                      base_ptr + 8 * off, stream_ptr())
+        else:
+            _lib.call("qg_expect_dm", C.byref(m.dev.struct), state.shape[0],
+                      C.byref(_view(state.buf)), base_ptr + 8 * off, stream_ptr())
+        place += [("expect", o, off + 2 * g) for g, o in enumerate(chunk)]
+        off += 2 * (len(chunk) + 1)
+    su = [o for k, o in batch if k == "super"]
+    if su:
+        d = int(math.isqrt(state.shape[0]))
+        m = _group_get(_SUPER_EOPS, su, lambda ops: _SuperRows(ops, d))
+        _lib.call("qg_spmv_csr", C.byref(m.e.struct), 0.0, state.buf.data_ptr(),
+                  base_ptr + 8 * off, 1.0, 0.0, 0.0, 0.0, stream_ptr())
+        place += [("super", o, off + 2 * g) for g, o in enumerate(su)]
+        off += 2 * len(su)
+    return place, off
 
 
 def _fits(kind, op, state) -> bool:
@@ -455,9 +492,10 @@ class _ExpectBatch:
                 and _lib.LAUNCHES[0] == self.launch_mark)
 
     def _buffers(self, k, device):
-        if self.buf is None or self.buf.numel() < 4 * k or self.buf.device != device:
-            self.buf = torch.zeros(4 * max(k, 16), dtype=torch.float64, device=device)
-            self.host = torch.zeros(4 * max(k, 16), dtype=torch.float64).pin_memory()
+        size = 4 * k + 2 * (k // _lib.QG_MAX_EOPS + 2)    # values, traces / norms
+        if self.buf is None or self.buf.numel() < size or self.buf.device != device:
+            self.buf = torch.zeros(max(size, 64), dtype=torch.float64, device=device)
+            self.host = torch.zeros(max(size, 64), dtype=torch.float64).pin_memory()
 
     def get(self, kind, op, state):
         key = (kind, id(op))
@@ -477,15 +515,13 @@ class _ExpectBatch:
                 if (k2, id(o2)) != key and _fits(k2, o2, state):
                     batch.append((k2, o2))
         self._buffers(len(batch), state.buf.device)
-        base = self.buf.data_ptr()
-        for i, (k2, o) in enumerate(batch):
-            (_launch_expect if k2 == "expect" else _launch_expect_super)(o, state, base + 32 * i)
-        h = self.host[:4 * len(batch)]
-        h.copy_(self.buf[:4 * len(batch)], non_blocking=True)
+        place, used = _launch_batch(batch, state, self.buf.data_ptr())
+        h = self.host[:used]
+        h.copy_(self.buf[:used], non_blocking=True)
         torch.cuda.current_stream().synchronize()
         v = h.numpy()
-        for i, (k2, o) in enumerate(batch):
-            self.values[(k2, id(o))] = complex(float(v[4 * i]), float(v[4 * i + 1]))
+        for k2, o, at in place:
+            self.values[(k2, id(o))] = complex(float(v[at]), float(v[at + 1]))
             self.keep.append(o)
         self.state = state
         self.version = state.buf._version

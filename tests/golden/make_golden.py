@@ -4,6 +4,7 @@ Run in a checkout that has the compiled reference (``python oracle/build_ref.py 
 
     python tests/golden/make_golden.py            # small fixtures (about a minute)
     python tests/golden/make_golden.py --large    # + Ising L=10 complex128 mesolve (minutes)
+    python tests/golden/make_golden.py --only bh4096   # 4096-trajectory BH mcsolve (minutes)
 
 Every number stored here comes from the reference's own public API
 (``qutip.mesolve``, ``qutip.MCSolver``, ``qutip.core.data``) on seeded inputs;
@@ -246,6 +247,33 @@ def mc_fixtures():
     _mc_fixture("bh_jumpy_mcsolve.npz", H, c_ops, psi0, n, np.linspace(0, 10, 101), 32, 777)
 
 
+def bh_full_mcsolve(ntraj=4096, seed=20261203):
+    """The Bose-Hubbard trimer (cutoff 8, ring) mcsolve at full size: 4096 trajectories
+    over tlist linspace(0, 50, 501), seeds SeedSequence(seed).spawn(4096), the
+    reference's vern7 with map="parallel" on every host core.  Stored: the averaged
+    expectation values, their spread over the trajectories (for the statistical error of
+    the mean) and every trajectory's jump record -- not the per-trajectory runs."""
+    H, c_ops, psi0, n = _bh_qobjs(8)
+    tlist = np.linspace(0, 50, 501)
+    seeds = np.random.SeedSequence(seed).spawn(ntraj)
+    t0 = time.time()
+    res = qutip.mcsolve(H, psi0, tlist, c_ops, e_ops=n, ntraj=ntraj, seeds=seeds,
+                        options={"method": "vern7", "progress_bar": False, "map": "parallel",
+                                 "num_cpus": os.cpu_count() or 1})
+    wall = time.time() - t0
+    col_t, col_w, col_off = [], [], [0]
+    for tr in range(ntraj):
+        col_t += list(res.col_times[tr])
+        col_w += list(res.col_which[tr])
+        col_off.append(len(col_t))
+    np.savez_compressed(os.path.join(HERE, "bh_full_mcsolve.npz"), tlist=tlist, seed=seed,
+                        ntraj=ntraj, avg_expect=np.array([np.asarray(e) for e in res.expect]),
+                        std_expect=np.array([np.asarray(e) for e in res.std_expect]),
+                        col_times=np.array(col_t), col_which=np.array(col_w, dtype=np.int8),
+                        col_off=np.array(col_off, dtype=np.int32), wall=wall,
+                        cores=os.cpu_count() or 1)
+
+
 def pcg64():
     out = {}
     for i, seed in enumerate([0, 1, 12345, 2**63 + 7]):
@@ -266,6 +294,8 @@ if __name__ == "__main__":
     a = ap.parse_args()
     jobs = {"tableau": tableau, "kernels": kernels, "jc": jc_mesolve,
             "ising3": lambda: ising(3), "ising4": lambda: ising(4), "mc": mc_fixtures, "pcg": pcg64}
+    if a.only and "bh4096" in a.only.split(","):
+        jobs["bh4096"] = bh_full_mcsolve
     for name, fn in jobs.items():
         if a.only and name not in a.only.split(","):
             continue

@@ -94,12 +94,14 @@ def test_mc_jump_records_identical_double(name):
 
 @pytest.mark.parametrize("name", sorted(MC_CASES))
 def test_mc_mixed_precision_jump_records(name):
-    """complex64 stages: jump records match for the vast majority of trajectories;
-    the averaged expectations agree within statistical error."""
+    """complex64 stages: jump records match the reference's (observed: every trajectory
+    of every fixture).  The slack is one trajectory per fixture: a complex64 trajectory
+    may legitimately end its jump-time bisection across the edge of the reference's
+    window.  The averaged expectations agree within statistical error."""
     from qutip_gb300 import systems as S
     g, r, same, ntraj = _mc_golden(name, lambda: MC_CASES[name](S), "mixed")
     print(f"\n{name} mixed: {same}/{ntraj} identical jump records")
-    assert same >= int(0.75 * ntraj)
+    assert same >= ntraj - 1
     sem = g["runs_expect"].std(axis=1) / np.sqrt(ntraj)
     diff = np.abs(r.runs_expect.real.mean(axis=1) - g["runs_expect"].mean(axis=1))
     assert np.all(diff <= 5 * sem + 1e-3)

@@ -57,6 +57,30 @@ def test_jc_step_sequence_is_the_reference():
     np.testing.assert_allclose(ends, g["step_ends"], rtol=1e-8)
 
 
+def test_jc_mixed_step_sequence_follows_the_reference():
+    """The mixed form keeps the step-size control in FP64: the error estimate is summed
+    in float-float from the complex64 stage vectors and the WRMS norm and step factor
+    are FP64.  Its steps are the reference's, one for one; the step ends differ only by
+    the complex64 rounding of the stage vectors that reaches the error estimate (about
+    1e-7 of err, 1e-8 of the step size), bounded here at 1e-6."""
+    from qutip_gb300 import systems as S
+    from qutip_gb300.operator import DeviceOperator
+    from qutip_gb300.vern7 import GpuVern7
+    g = golden("jc_mesolve.npz")
+    s = S.jaynes_cummings()
+    ig = GpuVern7(DeviceOperator(s.terms, dtype="c64"), precision="mixed")
+    ig.set_initial_value(torch.from_numpy(g["rho0"]).cuda(), 0.0)
+    ends = []
+    while ig.t_front < 20.0:
+        ig.integrate(20.0, step=True)
+        ig.check()
+        ends.append(ig.t_front)
+    rel = np.max(np.abs(np.asarray(ends) - g["step_ends"]) / g["step_ends"])
+    print(f"\nmixed step ends vs the reference: {len(ends)} steps, max rel diff {rel:.2e}")
+    assert len(ends) == len(g["step_ends"])
+    assert rel <= 1e-6
+
+
 @pytest.mark.parametrize("L", [3, 4])
 def test_ising_td_mesolve_double_matches_reference(L):
     from qutip_gb300 import systems as S
@@ -120,3 +144,34 @@ def test_ising_L10_full_size_matches_reference():
     err = max(np.abs(resm.expect[k].real - g["expect"][k]).max() for k in range(10))
     print(f"\nIsing L=10 mixed: max |<sz_i> - FP64 reference| = {err:.3e}")
     assert err < 1e-5
+
+
+def test_ising_L12_mixed_against_complex128_gpu():
+    """Config 5 at full size: the L = 12 chain (Liouvillian 16,777,216 rows, 469,762,047
+    entries assembled on the device), tlist linspace(0, 5, 51).  The mixed form (complex64
+    matvec and stages, FP64 state, step control and expectation values) against the
+    complex128 solve of the same generator: relative error of every sigma_z trajectory
+    (max_t |diff| / max_t |want|) at most 1e-6, the stated bound of the mixed form."""
+    from qutip_gb300 import systems as S
+    from qutip_gb300.operator import DeviceOperator
+    from qutip_gb300.solver import ExpectOps, solve_system
+    from qutip_gb300.superop import liouvillian_groups
+    s = S.ising_chain(12, build_terms=False)
+    groups = liouvillian_groups(s.h_terms, s.c_ops)
+    op64 = DeviceOperator.from_device_groups(groups, "c64")
+    op128 = DeviceOperator.from_device_groups(groups, "c128")
+    del groups
+    torch.cuda.empty_cache()
+    assert op64.n_rows == 4 ** 12 and op64.nnz == 469762047
+    ex = ExpectOps(s.e_ops)
+    tl = np.linspace(0.0, 5.0, 51)
+    r128 = solve_system(s, tl, {"precision": "double"}, op=op128, ex=ex)
+    r64 = solve_system(s, tl, {"precision": "mixed"}, op=op64, ex=ex)
+    rel = max(float(np.max(np.abs(a.real - b.real)) / np.max(np.abs(b.real)))
+              for a, b in zip(r64.expect, r128.expect))
+    print(f"\nIsing L=12 mixed vs complex128 GPU: max relative error {rel:.2e}, "
+          f"{r64.stats['steps']} / {r128.stats['steps']} steps")
+    assert r64.stats["steps"] == r128.stats["steps"]
+    assert rel <= 1e-6
+    del op64, op128
+    torch.cuda.empty_cache()

@@ -396,3 +396,57 @@ def test_gpu_map_refuses_other_methods(qt, plugin):
         with pytest.raises(TypeError, match="map='gpu'"):
             qt.mcsolve(H, psi0, np.linspace(0, 1, 5), c_ops, e_ops=e_ops, ntraj=2, seeds=1,
                        options={"method": method, "map": "gpu"})
+
+
+def _bh(qt, cutoff=8, J=1.0, U=0.5, F=0.3, kappa=0.1):
+    a = [qt.tensor(*[qt.destroy(cutoff) if k == i else qt.qeye(cutoff) for k in range(3)])
+         for i in range(3)]
+    n = [x.dag() * x for x in a]
+    H = 0
+    for i, j in [(0, 1), (1, 2), (2, 0)]:
+        H += -J * (a[i].dag() * a[j] + a[j].dag() * a[i])
+    for i in range(3):
+        H += U / 2 * n[i] * (n[i] - 1)
+    H += F * (a[0] + a[0].dag())
+    return H, [np.sqrt(kappa) * x for x in a], qt.tensor(*[qt.basis(cutoff, 0)] * 3), n
+
+
+@pytest.mark.parametrize("prec", ["double", "mixed"])
+def test_bh_trimer_4096_trajectories_match_the_reference(qt, plugin, prec):
+    """The batched mcsolve workload at full size through qutip.mcsolve with map='gpu':
+    4096 trajectories of the Bose-Hubbard trimer (dim 512) over t in [0, 50], seeded as the
+    reference's own map='parallel' run in tests/golden/bh_full_mcsolve.npz.
+
+    Jump records (count, channels, times within 1e-3): all 4096 identical in complex128;
+    the mixed form may let a trajectory cross a bisection window edge, so at most 1 in
+    500 may differ there.  Averages: within 5 standard errors of the reference's mean
+    (the statistical error of 4096 trajectories), and in complex128 within 1e-6."""
+    import os
+    from conftest import GOLDEN, golden
+    path = os.path.join(GOLDEN, "bh_full_mcsolve.npz")
+    if not os.path.exists(path):
+        pytest.skip("full-size mcsolve golden not generated")
+    g = golden("bh_full_mcsolve.npz")
+    ntraj = int(g["ntraj"])
+    H, c_ops, psi0, n = _bh(qt)
+    seeds = np.random.SeedSequence(int(g["seed"])).spawn(ntraj)
+    res = qt.mcsolve(H, psi0, g["tlist"], c_ops, e_ops=n, ntraj=ntraj, seeds=seeds,
+                     options={"method": "gpu_vern7", "map": "gpu", "precision": prec,
+                              "progress_bar": False})
+    same = 0
+    for tr in range(ntraj):
+        o0, o1 = int(g["col_off"][tr]), int(g["col_off"][tr + 1])
+        wt, ww = g["col_times"][o0:o1], g["col_which"][o0:o1]
+        gt, gw = np.asarray(res.col_times[tr]), np.asarray(res.col_which[tr])
+        if len(gt) == len(wt) and np.all(gw == ww) and np.all(np.abs(gt - wt) <= 1e-3):
+            same += 1
+    sem = g["std_expect"] / np.sqrt(ntraj)
+    diff = np.abs(np.array([np.asarray(e) for e in res.expect]).real - g["avg_expect"])
+    print(f"\nBH 4096 {prec}: {same}/{ntraj} identical jump records, max |avg diff| "
+          f"{diff.max():.2e}, max diff/SEM {np.max(diff / np.maximum(sem, 1e-300)):.2f}")
+    if prec == "double":
+        assert same == ntraj
+        assert diff.max() <= 1e-6
+    else:
+        assert same >= ntraj - ntraj // 500
+    assert np.all(diff <= 5 * sem + 1e-8)

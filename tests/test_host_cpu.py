@@ -389,3 +389,23 @@ def test_lindblad_validation_before_any_device_call():
     rk = _lib.RkBuffers(15, 1, 1, 8, 8, None, None, 8, 8, 8, 8, 8)
     assert lib.qg_lindblad_stage(C.byref(L), C.byref(rk), 0, 0.0, 0.1, 1e-8, 1e-6, None) == \
         _lib.QG_ERR_ARG          # n != d*d
+
+
+def test_conj_of_a_real_coefficient_is_itself():
+    """A coefficient program that is real for every real t is its own conjugate, so the
+    reference's ConjCoefficient of it (the spost part of a Liouvillian) shares its group;
+    programs that can turn complex keep an explicit conj."""
+    from qutip_gb300.coefficients import coefficient
+    real = ["cos(w*t)", "amp * sin(2*t) + exp(-t)", "abs(sqrt(t - 1))", "real(exp(1j*t)) * t",
+            "tanh(t) / (1 + t)"]
+    maybe = ["exp(1j*w*t)", "sqrt(t)", "t**2", "log(t)", "1j * cos(t)"]
+    for e in real:
+        c = coefficient(e, args={"w": 1.3, "amp": 0.5})
+        assert c.is_real() and c.conj() is c, e
+        for t in (0.0, 0.7, 3.1):
+            assert abs(c(t).imag) == 0.0
+    for e in maybe:
+        c = coefficient(e, args={"w": 1.3})
+        assert not c.is_real() and c.conj().key() != c.key(), e
+        for t in (0.3, 2.2):
+            assert c.conj()(t) == c(t).conjugate()
