@@ -984,52 +984,86 @@ def gpu_map(task, values, task_args=None, task_kwargs=None, reduce_func=None, ma
     iopts = {**IntegratorGpuVern7.integrator_options,
              **{k: opts[k] for k in IntegratorGpuVern7.integrator_options if k in opts}}
     prec = iopts["precision"]
-    bp = BatchProblem("c128" if prec == "double" else "c64")
-    sid = bp.add_system(terms, e_mats, np.asarray(tlist, dtype=np.float64), "mc",
-                        c_ops=c_mats, atol=iopts["atol"], rtol=iopts["rtol"],
-                        nsteps=iopts["nsteps"])
+    tl = np.asarray(tlist, dtype=np.float64)
+    mc = {k: opts[k] for k in MC_DEFAULTS if k in opts}
+    max_jumps = int((map_kw or {}).get("max_jumps", 4096))
     # a floor at 1 - norm_tol or above: the state does not jump; the reference returns
     # a zero trajectory of weight 0 without integrating (mcsolve.py:544-558)
     dark = [f >= 1 - opts["norm_tol"] for f in floors]
     host_states = {}
-    for s, (st, _), f, d in zip(seeds, starts, floors, dark):
-        if d:
-            continue
-        if id(st) not in host_states:
-            host_states[id(st)] = np.asarray(_as_gpu(st).to_array()).reshape(-1)
-        bp.add_item(sid, host_states[id(st)], seed=s, jump_prob_floor=f)
-    res = []
-    if bp.items:
-        mc = {k: opts[k] for k in MC_DEFAULTS if k in opts}
-        bp.build(max_jumps=int((map_kw or {}).get("max_jumps", 4096)), mc_options=mc)
+
+    def launch(idx):
+        """One persistent launch over the trajectories ``idx`` (dark ones skipped)."""
+        bp = BatchProblem("c128" if prec == "double" else "c64")
+        sid = bp.add_system(terms, e_mats, tl, "mc", c_ops=c_mats, atol=iopts["atol"],
+                            rtol=iopts["rtol"], nsteps=iopts["nsteps"])
+        for i in idx:
+            if dark[i]:
+                continue
+            st = starts[i][0]
+            if id(st) not in host_states:
+                host_states[id(st)] = np.asarray(_as_gpu(st).to_array()).reshape(-1)
+            bp.add_item(sid, host_states[id(st)], seed=seeds[i], jump_prob_floor=floors[i])
+        if not bp.items:
+            return iter(())
+        bp.build(max_jumps=max_jumps, mc_options=mc)
         bp.launch()
         res = bp.results()
-    for r in res:
-        if r["status"] == -5:
-            raise RuntimeError("Could not find the collapse time within desired tolerance. "
-                               "Increase accuracy of the ODE solver or lower the tolerance "
-                               "with the options 'norm_steps', 'norm_tol', 'norm_t_tol'.")
-        if r["status"] < 0:
-            raise IntegratorException(f"trajectory failed with status {r['status']}")
-    res = iter(res)
-    for seed, (_, weight), f, d in zip(seeds, starts, floors, dark):
-        if d:
-            traj, w = _zero_trajectory(solver, e_ops, opts, tlist), 0.0
-        else:
-            r = next(res)
-            traj = solver._trajectory_resultclass(e_ops, opts)
-            traj.times = [float(t) for t in tlist]
-            for k, key in enumerate(traj.e_data):
-                traj.e_data[key] = list(r["expect"][:, k])
-            traj.collapse = [(float(t), int(w)) for t, w in zip(r["col_times"], r["col_which"])]
-            # MCSolver._run_one_traj scales by (1 - floor), _run_one_traj_mixed by the
-            # initial state's weight (mcsolve.py:565, multitraj.py:297)
-            w = weight * (1 - f)
-        if reduce_func is not None:
-            left = reduce_func((seed, traj, float(w)))
-            if left is not None and left <= 0:
-                break
+        gpu_map.launched_items += len(res)
+        for r in res:
+            if r["status"] == -5:
+                raise RuntimeError("Could not find the collapse time within desired tolerance. "
+                                   "Increase accuracy of the ODE solver or lower the tolerance "
+                                   "with the options 'norm_steps', 'norm_tol', 'norm_t_tol'.")
+            if r["status"] < 0:
+                raise IntegratorException(f"trajectory failed with status {r['status']}")
+        return iter(res)
+
+    # With a target tolerance (multitrajresult.py:320-361) the reference stops the map as
+    # soon as its reduce step estimates that no more trajectories are needed.  The
+    # trajectories are then admitted in chunks: a first chunk, then as many as the
+    # reduce step's own estimate asks for (at least ``min_chunk``), so no more are
+    # integrated than the estimate needs.  Without one, every trajectory goes to one
+    # launch.
+    result = getattr(reduce_func, "__self__", None)
+    early = getattr(result, "_target_tols", None) is not None
+    total = len(seeds)
+    min_chunk = int((map_kw or {}).get("min_chunk", 64))
+    chunk = min(total, int((map_kw or {}).get("first_chunk", 256))) if early else total
+    gpu_map.launched_items = 0
+    pos = 0
+    while pos < total:
+        idx = range(pos, min(total, pos + max(chunk, 1)))
+        res = launch(idx)
+        left = None
+        for i in idx:
+            seed, (_, weight), f, d = seeds[i], starts[i], floors[i], dark[i]
+            if d:
+                traj, w = _zero_trajectory(solver, e_ops, opts, tlist), 0.0
+            else:
+                r = next(res)
+                traj = solver._trajectory_resultclass(e_ops, opts)
+                traj.times = [float(t) for t in tlist]
+                for k, key in enumerate(traj.e_data):
+                    traj.e_data[key] = list(r["expect"][:, k])
+                traj.collapse = [(float(t), int(w)) for t, w in zip(r["col_times"],
+                                                                      r["col_which"])]
+                # MCSolver._run_one_traj scales by (1 - floor), _run_one_traj_mixed by the
+                # initial state's weight (mcsolve.py:565, multitraj.py:297)
+                w = weight * (1 - f)
+            if reduce_func is not None:
+                left = reduce_func((seed, traj, float(w)))
+                if left is not None and left <= 0:
+                    return None
+        pos = idx.stop
+        if early and left is not None and np.isfinite(left):
+            chunk = max(min_chunk, int(math.ceil(left)))
+        elif early:
+            chunk = max(min_chunk, chunk)
     return None
+
+
+gpu_map.launched_items = 0
 
 
 # ---------------------------------------------------------------- register ----

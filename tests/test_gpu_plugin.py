@@ -365,6 +365,11 @@ def test_mcsolve_gpu_map_target_tol(qt, plugin):
     assert got.num_trajectories == ref.num_trajectories < 300
     for g, w in zip(got.expect, ref.expect):
         np.testing.assert_allclose(np.asarray(g), np.asarray(w), atol=2e-6)
+    # trajectories are admitted in chunks sized by the reference's own estimate: no more
+    # are integrated than a first chunk (256) or the estimate's last chunk needs
+    launched = plugin.gpu_map.launched_items
+    print(f"\ntarget_tol: {got.num_trajectories} trajectories used, {launched} integrated")
+    assert got.num_trajectories <= launched <= max(256, got.num_trajectories + 64)
 
 
 def test_new_args_reach_the_device_coefficients(qt, plugin):
