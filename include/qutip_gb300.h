@@ -178,6 +178,28 @@ typedef struct qg_lindblad {
   const double* c_coef_consts;
 } qg_lindblad;
 
+/* Dense small-dimension bucket (d <= QG_DENSE_MAX_D): the Lindblad generator with
+ * dense operators, L(t)[X] = A X + X A^dag + sum_i |f_i(t)|^2 C_i X C_i^dag with
+ * A = sum_g a_g(t) A_g = -i H_nh, applied as GEMMs on the tensor cores (TF32 split into
+ * hi + lo parts, FP32 accumulation).  Operators are complex64, row-major:
+ * A_g[m][k] at a + (g*d + m)*d + k, C_i[m][k] at c + (i*d + m)*d + k.  Coefficient
+ * programs as in qg_lindblad (NULL code: all 1). */
+#define QG_DENSE_MAX_D 128
+typedef struct qg_dense_lindblad {
+  int32_t d;
+  int32_t n_groups;
+  int32_t n_cops;
+  int32_t reserved; /* 0 */
+  const void* a;
+  const void* c;
+  const int32_t* a_coef_code;
+  const int32_t* a_coef_start;
+  const double* a_coef_consts;
+  const int32_t* c_coef_code;
+  const int32_t* c_coef_start;
+  const double* c_coef_consts;
+} qg_dense_lindblad;
+
 /* Buffers of one explicit Runge-Kutta step.  The state (y_prev, y_front) may be
  * complex128 while the stages (k, ytmp) are complex64 ("mixed" form): the
  * state update of each accepted step and the error norm stay in FP64, the stage
@@ -273,6 +295,19 @@ int qg_lindblad_apply(const qg_lindblad* L, double t, const void* x, void* y, do
  * B->n = d*d. */
 int qg_lindblad_stage(const qg_lindblad* L, const qg_rk_buffers* B, int stage, double t_prev,
                       double dt, double atol, double rtol, void* stream);
+
+/* y = alpha * L(t)[x] + beta * y for the dense generator; x, y complex64 vec(rho) of
+ * length d*d.  Replaces LindbladMatrixForm.matmul_data
+ * (qutip/core/cy/lindblad_matrix_form.pyx:105-204, full branch) for small dense systems;
+ * one CTA per application, tcgen05 tensor-core GEMMs. */
+int qg_dense_lindblad_apply(const qg_dense_lindblad* L, double t, const void* x, void* y,
+                            double alpha_re, double alpha_im, double beta_re, double beta_im,
+                            void* stream);
+
+/* qg_vern7_stage with the dense generator: complex64 stages (B->stage_dtype = QG_C64),
+ * the state complex128 (mixed form) or complex64; B->n = d*d. */
+int qg_dense_lindblad_stage(const qg_dense_lindblad* L, const qg_rk_buffers* B, int stage,
+                            double t_prev, double dt, double atol, double rtol, void* stream);
 
 /* Non-zero when a kernel of this library gave up a bounded wait on the current
  * device (the result of that launch is invalid); reading clears the flag. */

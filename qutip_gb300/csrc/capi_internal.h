@@ -12,3 +12,6 @@ int check_launch(const char* what);
 // Multiprocessor count of the current device (cached per device).
 int sm_count();
 }  // namespace qg
+
+// The dense kernel's fault flag, read and cleared (for qg_device_fault).
+int dense_fault_take();

@@ -250,17 +250,20 @@ def mc_fixtures():
 def bh_full_mcsolve(ntraj=4096, seed=20261203):
     """The Bose-Hubbard trimer (cutoff 8, ring) mcsolve at full size: 4096 trajectories
     over tlist linspace(0, 50, 501), seeds SeedSequence(seed).spawn(4096), the
-    reference's vern7 with map="parallel" on every host core.  Stored: the averaged
-    expectation values, their spread over the trajectories (for the statistical error of
-    the mean) and every trajectory's jump record -- not the per-trajectory runs."""
+    reference's vern7 with map="serial" (so that the bisection window of every jump is
+    recorded, as for the small fixtures).  Stored: the averaged expectation values, their
+    spread over the trajectories (for the statistical error of the mean) and every
+    trajectory's jump record with its windows -- not the per-trajectory runs."""
     H, c_ops, psi0, n = _bh_qobjs(8)
     tlist = np.linspace(0, 50, 501)
     seeds = np.random.SeedSequence(seed).spawn(ntraj)
+    windows, undo = _hook_collapse_windows()
     t0 = time.time()
     res = qutip.mcsolve(H, psi0, tlist, c_ops, e_ops=n, ntraj=ntraj, seeds=seeds,
-                        options={"method": "vern7", "progress_bar": False, "map": "parallel",
-                                 "num_cpus": os.cpu_count() or 1})
+                        options={"method": "vern7", "progress_bar": False, "map": "serial"})
     wall = time.time() - t0
+    M, find0, do0 = undo
+    M.MCIntegrator._find_collapse_time, M.MCIntegrator._do_collapse = find0, do0
     col_t, col_w, col_off = [], [], [0]
     for tr in range(ntraj):
         col_t += list(res.col_times[tr])
@@ -270,8 +273,8 @@ def bh_full_mcsolve(ntraj=4096, seed=20261203):
                         ntraj=ntraj, avg_expect=np.array([np.asarray(e) for e in res.expect]),
                         std_expect=np.array([np.asarray(e) for e in res.std_expect]),
                         col_times=np.array(col_t), col_which=np.array(col_w, dtype=np.int8),
-                        col_off=np.array(col_off, dtype=np.int32), wall=wall,
-                        cores=os.cpu_count() or 1)
+                        col_off=np.array(col_off, dtype=np.int32),
+                        col_window=np.array(windows), wall=wall, cores=1)
 
 
 def pcg64():

@@ -422,10 +422,11 @@ def test_bh_trimer_4096_trajectories_match_the_reference(qt, plugin, prec):
     4096 trajectories of the Bose-Hubbard trimer (dim 512) over t in [0, 50], seeded as the
     reference's own map='parallel' run in tests/golden/bh_full_mcsolve.npz.
 
-    Jump records (count, channels, times within 1e-3): all 4096 identical in complex128;
-    the mixed form may let a trajectory cross a bisection window edge, so at most 1 in
-    500 may differ there.  Averages: within 5 standard errors of the reference's mean
-    (the statistical error of 4096 trajectories), and in complex128 within 1e-6."""
+    Jump records (count, channels, each time inside the reference's own bisection
+    window, recorded per jump in the fixture): all 4096 identical in complex128; the
+    mixed form may let a trajectory cross a window edge, so at most 1 in 200 may differ.
+    Averages: in complex128 within 1e-6 of the reference's; in the mixed form within 5
+    standard errors of the reference's mean plus the form's 1e-6 bound."""
     import os
     from conftest import GOLDEN, golden
     path = os.path.join(GOLDEN, "bh_full_mcsolve.npz")
@@ -442,8 +443,9 @@ def test_bh_trimer_4096_trajectories_match_the_reference(qt, plugin, prec):
     for tr in range(ntraj):
         o0, o1 = int(g["col_off"][tr]), int(g["col_off"][tr + 1])
         wt, ww = g["col_times"][o0:o1], g["col_which"][o0:o1]
+        win = g["col_window"][o0:o1]
         gt, gw = np.asarray(res.col_times[tr]), np.asarray(res.col_which[tr])
-        if len(gt) == len(wt) and np.all(gw == ww) and np.all(np.abs(gt - wt) <= 1e-3):
+        if len(gt) == len(wt) and np.all(gw == ww) and np.all(np.abs(gt - wt) <= win):
             same += 1
     sem = g["std_expect"] / np.sqrt(ntraj)
     diff = np.abs(np.array([np.asarray(e) for e in res.expect]).real - g["avg_expect"])
@@ -453,5 +455,5 @@ def test_bh_trimer_4096_trajectories_match_the_reference(qt, plugin, prec):
         assert same == ntraj
         assert diff.max() <= 1e-6
     else:
-        assert same >= ntraj - ntraj // 500
-    assert np.all(diff <= 5 * sem + 1e-8)
+        assert same >= ntraj - ntraj // 200
+        assert np.all(diff <= 5 * sem + 1e-6)
