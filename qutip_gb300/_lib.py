@@ -20,6 +20,7 @@ QG_MAX_GROUPS, QG_MAX_EOPS, QG_MAX_COPS = 8, 32, 64
 QG_LAYOUT_GROUP_MAJOR, QG_LAYOUT_ROW_MAJOR, QG_LAYOUT_SLICED, QG_LAYOUT_SLICED_DICT = 0, 1, 2, 3
 QG_LAYOUT_SLICED_DICT_RI = 4
 QG_DICT_MAX = 4096
+QG_DENSE_MAX_D = 128
 QG_TILE_ROWS = 512
 QG_GROUP_AUTO, QG_GROUP_WARP, QG_GROUP_CTA, QG_GROUP_CLUSTER, QG_GROUP_CTA128 = 0, 1, 2, 3, 4
 
@@ -41,6 +42,14 @@ class Lindblad(C.Structure):
                 ("a_width", C.c_int32 * QG_MAX_GROUPS), ("c_width", C.c_int32 * QG_MAX_COPS),
                 ("d_const", C.c_void_p), ("a_diag", C.c_void_p), ("a_col", C.c_void_p), ("a_val", C.c_void_p),
                 ("c_diag", C.c_void_p), ("c_col", C.c_void_p), ("c_val", C.c_void_p),
+                ("a_coef_code", C.c_void_p), ("a_coef_start", C.c_void_p),
+                ("a_coef_consts", C.c_void_p), ("c_coef_code", C.c_void_p),
+                ("c_coef_start", C.c_void_p), ("c_coef_consts", C.c_void_p)]
+
+
+class DenseLindblad(C.Structure):
+    _fields_ = [("d", C.c_int32), ("n_groups", C.c_int32), ("n_cops", C.c_int32),
+                ("reserved", C.c_int32), ("a", C.c_void_p), ("c", C.c_void_p),
                 ("a_coef_code", C.c_void_p), ("a_coef_start", C.c_void_p),
                 ("a_coef_consts", C.c_void_p), ("c_coef_code", C.c_void_p),
                 ("c_coef_start", C.c_void_p), ("c_coef_consts", C.c_void_p)]
@@ -86,6 +95,11 @@ _SIGS = {
                                     C.c_void_p]),
     "qg_lindblad_stage": (C.c_int, [_P(Lindblad), _P(RkBuffers), C.c_int, C.c_double,
                                     C.c_double, C.c_double, C.c_double, C.c_void_p]),
+    "qg_dense_lindblad_apply": (C.c_int, [_P(DenseLindblad), C.c_double, C.c_void_p, C.c_void_p,
+                                          C.c_double, C.c_double, C.c_double, C.c_double,
+                                          C.c_void_p]),
+    "qg_dense_lindblad_stage": (C.c_int, [_P(DenseLindblad), _P(RkBuffers), C.c_int, C.c_double,
+                                          C.c_double, C.c_double, C.c_double, C.c_void_p]),
     "qg_rk_combine": (C.c_int, [_P(StateView), C.c_void_p, C.c_int, C.c_void_p]),
     "qg_norm2": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                            C.c_void_p]),
@@ -109,7 +123,7 @@ _lib = None
 COMPUTE_ENTRY_POINTS = {
     "qg_spmv_csr", "qg_spmm_csr", "qg_spmv_dia", "qg_vern7_stage", "qg_rk_combine", "qg_norm2",
     "qg_expect_dm", "qg_expect_ket", "qg_batch_vern7", "qg_batch_vern7_noalloc",
-    "qg_lindblad_apply", "qg_lindblad_stage",
+    "qg_lindblad_apply", "qg_lindblad_stage", "qg_dense_lindblad_apply", "qg_dense_lindblad_stage",
 }
 LAUNCHES = [0]
 

@@ -46,7 +46,8 @@ extern "C" int qg_abi_sizes(int64_t* out, int n) {
   const int64_t s[] = {(int64_t)sizeof(qg_csr_groups),   (int64_t)sizeof(qg_dia),
                        (int64_t)sizeof(qg_rk_buffers),   (int64_t)sizeof(qg_state_view),
                        (int64_t)sizeof(qg_batch_system), (int64_t)sizeof(qg_batch_item),
-                       (int64_t)sizeof(qg_batch),        (int64_t)sizeof(qg_lindblad)};
+                       (int64_t)sizeof(qg_batch),        (int64_t)sizeof(qg_lindblad),
+                       (int64_t)sizeof(qg_dense_lindblad)};
   const int m = (int)(sizeof(s) / sizeof(s[0]));
   if (!out) return qg::set_error(QG_ERR_ARG, "null output");
   for (int i = 0; i < m && i < n; ++i) out[i] = s[i];
