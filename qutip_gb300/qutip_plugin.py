@@ -692,10 +692,16 @@ def _is_matrix_form(rhs) -> bool:
     return isinstance(rhs, LindbladMatrixForm)
 
 
-def lindblad_operator(rhs, dtype="c128"):
+def lindblad_operator(rhs, dtype="c128", dense="auto"):
     """The device generator of a ``LindbladMatrixForm`` (mesolve's ``matrix_form``
     option, qutip/solver/mesolve.py:251-266): A = -i H_nh from its ``H_nh``
-    (lindblad_matrix_form.pyx:88-96) and one term per collapse operator."""
+    (lindblad_matrix_form.pyx:88-96) and one term per collapse operator.
+
+    The dense small-dimension bucket (:class:`~qutip_gb300.dense.DenseLindbladOperator`,
+    tensor-core GEMMs) takes the mixed form (complex64 stages) of a system with
+    ``d <= 128`` whose operators are at least ``DENSE_FILL`` filled, or whenever
+    ``dense=True``; sparse systems keep the matrix-free sparse kernel."""
+    from .dense import DENSE_FILL, DenseLindbladOperator, dense_fill
     a_terms = [((-1j) * m, c) for m, c in qobjevo_terms(rhs.H_nh)]
     c_terms = []
     for c in rhs.c_ops:
@@ -704,6 +710,13 @@ def lindblad_operator(rhs, dtype="c128"):
             raise TypeError("matrix_form on the GPU needs each collapse operator to be a "
                             "single (possibly time-dependent) term")
         c_terms.append(terms[0])
+    d = a_terms[0][0].shape[0]
+    if dense is True and (dtype != "c64" or d > _lib.QG_DENSE_MAX_D):
+        raise ValueError(f"the dense bucket runs the mixed form (precision='mixed') for "
+                         f"d <= {_lib.QG_DENSE_MAX_D}")
+    if dense is not False and dtype == "c64" and d <= _lib.QG_DENSE_MAX_D and (
+            dense is True or dense_fill([m for m, _ in a_terms + c_terms]) >= DENSE_FILL):
+        return DenseLindbladOperator(a_terms, c_terms, device=_device())
     return LindbladOperator(a_terms, c_terms, dtype=dtype, device=_device())
 
 
@@ -731,6 +744,7 @@ class IntegratorGpuVern7(Integrator):
         "min_step": 0,
         "interpolate": True,
         "precision": "double",
+        "dense": "auto",
     }
     rhs_format = "solver"
     support_time_dependant = True
@@ -758,7 +772,7 @@ class IntegratorGpuVern7(Integrator):
         self._terms = None
         self._groups = None
         if _is_matrix_form(rhs):
-            self._op = lindblad_operator(rhs, dt)
+            self._op = lindblad_operator(rhs, dt, self._options.get("dense", "auto"))
         else:
             self._terms = qobjevo_terms(rhs)
             self._groups = _coefficient_groups(self._terms)
@@ -858,7 +872,9 @@ class IntegratorGpuVern7(Integrator):
     @property
     def options(self):
         """atol, rtol, nsteps, first_step, max_step, min_step, interpolate: as the
-        reference ``vern7``; precision: ``"double"`` or ``"mixed"``."""
+        reference ``vern7``; precision: ``"double"`` or ``"mixed"``; dense (matrix form
+        only): ``"auto"`` sends small systems with dense operators in the mixed form to
+        the tensor-core bucket, ``True`` forces it, ``False`` keeps the sparse kernel."""
         return self._options
 
     @options.setter
