@@ -70,9 +70,9 @@ def parse():
                     help="whole mesolve calls timed for e2e (at most --steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline workload only")
-    ap.add_argument("--sections", default="served,mc,matrix,large",
+    ap.add_argument("--sections", default="served,mc,matrix,dense,large",
                     help="extra sections after the headline (comma list of served, mc, "
-                         "matrix, large)")
+                         "matrix, dense, large)")
     ap.add_argument("--matrix-sites", type=int, default=13,
                     help="spins of the short matrix-form solve in the matrix section (0: skip)")
     ap.add_argument("--served-jobs", type=int, default=10000)
@@ -81,7 +81,7 @@ def parse():
     ap.add_argument("--mc-ntraj", type=int, default=4096)
     ap.add_argument("--large-sites", type=int, default=12,
                     help="Ising chain length of the large mixed-precision section (0: skip)")
-    ap.add_argument("--profile", default=None, choices=["stage", "batch", "matrix"],
+    ap.add_argument("--profile", default=None, choices=["stage", "batch", "matrix", "dense"],
                     help="run the ncu profiling case only (fused stage kernel, untuned); "
                          "prints nothing to parse")
     ap.add_argument("--profile-sites", type=int, default=10)
@@ -709,6 +709,100 @@ def large_cpu_baseline(host_groups, state0, rhs_full, reps=2):
             "rhs_call_s": rhs_s, "rhs_full": rhs_full}
 
 
+def run_dense(args):
+    """The dense small-dimension bucket (tensor-core Lindblad generator, mixed form) against
+    the sparse paths, one request at a time: Jaynes-Cummings mesolve (N = 5..60, d = 2N,
+    tlist linspace(0, 20, 101)) and dense random systems (d = 32, 64, 128, t in [0, 2]).
+    Sparse paths: the matrix-free kernel (one system, whole GPU) and the batched kernel's
+    sparse row loop (the served path, one request in one launch).  Also the generator
+    application alone, with the tensor-core rate of the MMAs it issues."""
+    import scipy.sparse as sp
+    import torch
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import BatchProblem, check_status
+    from qutip_gb300.coefficients import coefficient
+    from qutip_gb300.dense import DenseLindbladOperator
+    from qutip_gb300.lindblad import LindbladOperator
+    from qutip_gb300.solver import ExpectOps, solve_system
+    from qutip_gb300.systems import OpenSystem
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        return 1e3 * best
+
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    tf32_peak = 0.5 * float(peaks.get("bf16_tflops", 1900.0))
+    out = {"jc": [], "dense_random": []}
+    tl = np.linspace(0.0, 20.0, 101)
+    for N in (5, 10, 20, 30, 45, 60):
+        s = S.jaynes_cummings(N, kind="me")
+        ex = ExpectOps(s.e_ops)
+        dop = DenseLindbladOperator.from_hamiltonian(s.h_terms, s.c_ops)
+        sop = LindbladOperator.from_hamiltonian(s.h_terms, s.c_ops, dtype="c64")
+        ms_dense = timed(lambda: solve_system(s, tl, {"precision": "mixed"}, op=dop, ex=ex))
+        ms_mf = timed(lambda: solve_system(s, tl, {"precision": "mixed"}, op=sop, ex=ex))
+
+        def batched():
+            bp = BatchProblem("c64")
+            bp.add_item(bp.add_system(s.terms, s.e_ops, tl, "me"), s.state0)
+            bp.build(group="cta")
+            bp.launch()
+            check_status(bp.results())
+        ms_b = timed(batched)
+        out["jc"].append({"N": N, "d": 2 * N, "dense_bucket_ms": ms_dense,
+                          "matrix_free_sparse_ms": ms_mf, "batched_sparse_row_loop_ms": ms_b})
+        log(f"dense: JC N={N}: tensor cores {ms_dense:.1f} ms, matrix-free {ms_mf:.1f} ms, "
+            f"batched row loop {ms_b:.1f} ms")
+    rng = np.random.default_rng(11)
+    for d in (32, 64, 128):
+        def rmat(herm=False):
+            m = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+            return (m + m.conj().T) / 2 if herm else m
+        h_terms = [(sp.csr_matrix(rmat(True) / np.sqrt(d)), None),
+                   (sp.csr_matrix(0.3 * rmat(True) / np.sqrt(d)), coefficient("cos(1.1*t)"))]
+        c_ops = [sp.csr_matrix(0.1 * rmat() / np.sqrt(d)), sp.csr_matrix(0.05 * rmat() / np.sqrt(d))]
+        psi = rng.normal(size=d) + 1j * rng.normal(size=d)
+        psi /= np.linalg.norm(psi)
+        e_ops = [sp.csr_matrix(rmat(True))]
+        s = OpenSystem("dense_random", "me", d, None, np.outer(psi, psi.conj()).reshape(-1, order="F"),
+                       e_ops, c_ops, h_terms)
+        ex = ExpectOps(e_ops)
+        trand = np.linspace(0.0, 2.0, 21)
+        dop = DenseLindbladOperator.from_hamiltonian(h_terms, c_ops)
+        sop = LindbladOperator.from_hamiltonian(h_terms, c_ops, dtype="c64")
+        ms_dense = timed(lambda: solve_system(s, trand, {"precision": "mixed"}, op=dop, ex=ex))
+        ms_mf = timed(lambda: solve_system(s, trand, {"precision": "mixed"}, op=sop, ex=ex))
+        x = torch.randn(d * d, dtype=torch.complex64, device="cuda")
+        y = torch.empty_like(x)
+        dop.matvec(0.3, x, y)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 50
+        e0.record()
+        for _ in range(reps):
+            dop.matvec(0.3, x, y)
+        e1.record()
+        e1.synchronize()
+        us = 1e3 * e0.elapsed_time(e1) / reps
+        tflops = dop.gemm_flops() / (us * 1e-6) / 1e12
+        out["dense_random"].append({"d": d, "dense_bucket_ms": ms_dense, "matrix_free_sparse_ms": ms_mf,
+                                    "apply_us": us, "issued_tf32_tflops": tflops,
+                                    "frac_of_one_sm_tf32": tflops / (tf32_peak / 152.0)})
+        log(f"dense: random d={d}: tensor cores {ms_dense:.1f} ms, matrix-free {ms_mf:.1f} ms, "
+            f"apply {us:.1f} us = {tflops:.2f} TFLOP/s issued TF32 on one SM")
+    out["note"] = ("one CTA (one SM) per application; TF32 rate per SM taken as half the measured "
+                   "bf16 GEMM rate / 152 SMs")
+    return out
+
+
 def run_matrix_form(args, sysm, tlist, ex, want, hbm_peak):
     """The headline workload through mesolve's matrix form (``matrix_form=True``): the
     Lindblad generator applied to vec(rho) without its superoperator
@@ -932,6 +1026,9 @@ def run_ours(args, dist):
     if dist.rank == 0 and "mc" in sections:
         log("batched mcsolve")
         out["mc_batched"] = run_mc_batch(args)
+    if dist.rank == 0 and "dense" in sections:
+        log("dense small-dimension bucket")
+        out["dense_bucket"] = run_dense(args)
     if dist.rank == 0 and "matrix" in sections:
         log("matrix form")
         sysm = S.ising_chain(N_SITES, build_terms=False)
@@ -995,6 +1092,28 @@ def run_profile_matrix(args):
     print(f"matrix form: {op.launch_desc()}, {op.operator_bytes() / 1e6:.1f} MB generator")
 
 
+def run_profile_dense(args):
+    """ncu case for the dense tensor-core Lindblad kernel: a dense random system of
+    dimension ``--profile-sites`` (default 10 is raised to 128 here: d = 128), ten
+    applications of the generator."""
+    import scipy.sparse as sp
+    import torch
+    from qutip_gb300.dense import DenseLindbladOperator
+    torch.cuda.set_device(0)
+    d = 128
+    rng = np.random.default_rng(3)
+    m = lambda: rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))  # noqa: E731
+    h = m()
+    op = DenseLindbladOperator.from_hamiltonian([(sp.csr_matrix((h + h.conj().T) / 2), None)],
+                                                [sp.csr_matrix(0.1 * m()), sp.csr_matrix(0.1 * m())])
+    x = torch.randn(d * d, dtype=torch.complex64, device="cuda")
+    y = torch.empty_like(x)
+    for _ in range(10):
+        op.matvec(0.1, x, y)
+    torch.cuda.synchronize()
+    print(f"dense: {op.launch_desc()}, {op.gemm_flops() / 1e6:.1f} MFLOP issued per application")
+
+
 def run_profile_batch(args):
     """ncu case for the batched trajectory kernel: ``--profile-ntraj`` Bose-Hubbard
     trajectories (default 256) over t in [0, ``--profile-tend``] (default 5, 10
@@ -1021,6 +1140,9 @@ def main():
         return
     if args.profile == "matrix":
         run_profile_matrix(args)
+        return
+    if args.profile == "dense":
+        run_profile_dense(args)
         return
     dist = Dist(args.gpus)
     if args.impl == "reference":
