@@ -30,7 +30,7 @@ __all__ = ["DenseLindbladOperator", "dense_fill", "DENSE_FILL"]
 
 #: fraction of nonzero entries of A = -i H_nh and the collapse operators from which the
 #: dense bucket takes a matrix-form generator (below it the sparse kernels do less work)
-DENSE_FILL = 0.25
+DENSE_FILL = 0.5
 
 
 def dense_fill(mats) -> float:
