@@ -8,10 +8,13 @@
 //
 // the reference's LindbladMatrixForm (qutip/core/cy/lindblad_matrix_form.pyx:105-204,
 // full non-Hermitian branch) with dense operators.  Per collapse operator two products:
-// T = X C^dag, then C T.  Everything accumulates into one TMEM accumulator D (real part
-// in columns 0..127, imaginary part in 128..255; T uses 256..511), read back once per
-// application and passed through the same fused Vern7 epilogue as the sparse kernels
-// (stage.cuh).  The stage vectors are complex64: this is the mixed form's generator.
+// T = X C^dag, then C T.  Each product runs into fresh TMEM accumulators: D (columns
+// 0..255: real, imaginary) takes the hi*hi terms and E (256..511) the small hi*lo + lo*hi
+// corrections, so no rounding of a correction happens at the magnitude of the product;
+// D + E is then flushed by the CUDA cores, in FP32 with round-to-nearest, into the
+// caller's workspace (the generator's accumulator, or T).  The accumulated generator
+// goes through the same fused Vern7 epilogue as the sparse kernels (stage.cuh).  The
+// stage vectors are complex64: this is the mixed form's generator.
 //
 // One CTA of 256 threads per application.  Operands are staged through shared memory in
 // K chunks of 32: for each chunk every thread writes its share of the A- and B-operand
@@ -35,7 +38,7 @@ constexpr int DN_TMEM_COLS = 512;
 __device__ unsigned int g_dense_fault = 0u;
 
 // Where the rows of an operand chunk come from.
-enum Src { SRC_OPA = 0, SRC_OPC = 1, SRC_XB = 2, SRC_XA = 3 };
+enum Src { SRC_OPA = 0, SRC_OPC = 1, SRC_XB = 2, SRC_XA = 3, SRC_TB = 4 };
 
 struct DenseCtx {
   const qg_dense_lindblad* L;
@@ -43,6 +46,7 @@ struct DenseCtx {
   int d, np;           // dimension, N (rows of the B operand) = d rounded up to 16
   int cop;             // collapse operator of SRC_OPC
   const float2* ca;    // a_g(t) in shared memory
+  const float2* t;     // T = X C^dag, row-major: T[r][c] at r*d + c
 };
 
 // element (r, k) of a source: the operator sum A(t), C_cop, X read as (n, k) -> X[k][n]
@@ -53,6 +57,7 @@ __device__ __forceinline__ float2 src_at(const DenseCtx& c, int src, int r, int 
   if (r >= d || k >= d) return make_float2(0.f, 0.f);
   if (src == SRC_XB) return c.x[(size_t)r * d + k];
   if (src == SRC_XA) return c.x[(size_t)k * d + r];
+  if (src == SRC_TB) return c.t[(size_t)k * d + r];   // (n, k) -> T[k][n]
   const float2* base = static_cast<const float2*>(src == SRC_OPA ? L.a : L.c);
   if (src == SRC_OPC) return __ldg(base + ((size_t)c.cop * d + r) * d + k);
   float re = 0.f, im = 0.f;
@@ -87,28 +92,33 @@ __device__ __forceinline__ void stage_planes(const DenseCtx& c, int src, int row
   }
 }
 
-// One K chunk of D (+)= Aop Bop^T for complex operands (Bop conjugated when conj_b):
-// re += Ar Br -/+ Ai Bi, im += +/- Ar Bi + Ai Br, each real product in three TF32 terms.
-// Issued by one thread.  d_col: TMEM column of the real part (imaginary at + 128).
-__device__ __forceinline__ void issue_chunk(uint32_t taddr, uint32_t d_col, uint32_t a_base,
-                                            uint32_t b_base, uint32_t b_plane, int np,
-                                            int ksteps, bool conj_b, bool init) {
+// One K chunk of Aop Bop^T for complex operands (Bop conjugated when conj_b):
+// re = Ar Br -/+ Ai Bi, im = +/- Ar Bi + Ai Br, each real product in three TF32 terms,
+// hi*hi into D (TMEM columns 0 / 128 for re / im) and hi*lo, lo*hi into E (256 / 384).
+// Issued by one thread; init: the chunk starts the product (first MMA of each region
+// overwrites).
+__device__ __forceinline__ void issue_chunk(uint32_t taddr, uint32_t a_base, uint32_t b_base,
+                                            uint32_t b_plane, int np, int ksteps, bool conj_b,
+                                            bool init) {
   const uint32_t sbo = tc::band_bytes(DN_KC);
   const uint32_t id_pos = tc::idesc_tf32(128, np, false), id_neg = tc::idesc_tf32(128, np, true);
   // (A plane pair, B plane pair, destination: 0 re / 1 im, negated)
   const int ap[4] = {0, 2, 0, 2}, bp[4] = {0, 2, 2, 0}, dst[4] = {0, 0, 1, 1};
   const bool neg[4] = {false, !conj_b, conj_b, false};
-  bool first[2] = {init, init};
+  bool first[4] = {init, init, init, init};  // D re, D im, E re, E im
   for (int ks = 0; ks < ksteps; ++ks) {
+#pragma unroll
     for (int q = 0; q < 4; ++q) {
-      // hi*hi, hi*lo, lo*hi
+      // hi*hi -> D; hi*lo, lo*hi -> E
       const int at[3] = {0, 0, 1}, bt[3] = {0, 1, 0};
+#pragma unroll
       for (int tt = 0; tt < 3; ++tt) {
+        const int region = dst[q] + (tt ? 2 : 0);
         const uint32_t a = a_base + (uint32_t)(ap[q] + at[tt]) * DN_PLANE_A + ks * 2 * tc::LBO;
         const uint32_t b = b_base + (uint32_t)(bp[q] + bt[tt]) * b_plane + ks * 2 * tc::LBO;
-        tc::mma_tf32(taddr + d_col + 128u * dst[q], tc::smem_desc(a, tc::LBO, sbo),
-                     tc::smem_desc(b, tc::LBO, sbo), neg[q] ? id_neg : id_pos, !first[dst[q]]);
-        first[dst[q]] = false;
+        tc::mma_tf32(taddr + 128u * region, tc::smem_desc(a, tc::LBO, sbo),
+                     tc::smem_desc(b, tc::LBO, sbo), neg[q] ? id_neg : id_pos, !first[region]);
+        first[region] = false;
       }
     }
   }
@@ -158,13 +168,15 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
   tc::fence_after();
   const uint32_t taddr = taddr_s;
   const uint32_t a_base = smem_u32(a_planes), b_base = smem_u32(b_planes);
-  DenseCtx c{&L, x, d, np, 0, ca};
+  float2* acc = static_cast<float2*>(L.work);          // vec order, (m, n) at n*d + m
+  float2* tmat = acc + (size_t)d * d;                    // T row-major, (m, n) at m*d + n
+  DenseCtx c{&L, x, d, np, 0, ca, tmat};
   const int nchunks = (d + DN_KC - 1) / DN_KC;
   unsigned parity = 0u;
   bool ok = true;
 
-  // one GEMM: D[d_col] (+)= op(srcA) op(srcB)^T over every K chunk
-  auto gemm = [&](int src_a, int src_b, bool conj_b, uint32_t d_col, bool init) {
+  // one product op(srcA) op(srcB)^T over every K chunk, into fresh D and E
+  auto gemm = [&](int src_a, int src_b, bool conj_b) {
     for (int kc = 0; kc < nchunks && ok; ++kc) {
       stage_planes(c, src_a, 128, kc, a_planes, DN_PLANE_A);
       stage_planes(c, src_b, np, kc, b_planes, b_plane);
@@ -174,74 +186,61 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
       tc::fence_after();
       if (tid == 0) {
         const int ksteps = min(4, (d - kc * DN_KC + 7) >> 3);
-        issue_chunk(taddr, d_col, a_base, b_base, b_plane, np, ksteps, conj_b, init && kc == 0);
+        issue_chunk(taddr, a_base, b_base, b_plane, np, ksteps, conj_b, kc == 0);
         tc::mma_commit(&bar);
       }
       ok = wait_mma(&bar, parity);
     }
   };
-
-  gemm(SRC_OPA, SRC_XB, false, 0u, true);    // D  = A X
-  gemm(SRC_XA, SRC_OPA, true, 0u, false);    // D += X A^dag
-  for (int i = 0; i < L.n_cops && ok; ++i) {
-    c.cop = i;
-    gemm(SRC_XA, SRC_OPC, true, 256u, true);  // T = X C^dag
-    // D += w C T: the B operand (n, k) = w T[k][n] comes from T's TMEM lanes k
-    for (int kc = 0; kc < nchunks && ok; ++kc) {
-      stage_planes(c, SRC_OPC, 128, kc, a_planes, DN_PLANE_A);
-      if ((warp & 3) == (kc & 3) && kc * DN_KC < 128) {
-        // warps kc and kc + 4 hold lanes 32 kc .. 32 kc + 31 (rows k of T)
-        const int k = kc * DN_KC + lane;
-        const float w = wc[i];
-        for (int cb = (warp >> 2) * 16; cb < np; cb += 32) {
-          float re[16], im[16];
-          const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-          tc::tmem_ld16(taddr + lane_base + 256u + (uint32_t)cb, re);
-          tc::tmem_ld16(taddr + lane_base + 384u + (uint32_t)cb, im);
+  // D + E of the last product, times w, into the accumulator (add) or into T; row m of
+  // the product lives in TMEM lane m, warps w and w + 4 share lanes 32 (w % 4) ...
+  const int m = 32 * (warp & 3) + lane;
+  const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+  auto flush = [&](bool to_t, bool add, float w) {
+    if (!ok) return;
+    for (int cb = (warp >> 2) * 16; cb < np; cb += 32) {
+      float dr[16], di[16], er[16], ei[16];
+      tc::tmem_ld16(taddr + lane_base + (uint32_t)cb, dr);
+      tc::tmem_ld16(taddr + lane_base + 128u + (uint32_t)cb, di);
+      tc::tmem_ld16(taddr + lane_base + 256u + (uint32_t)cb, er);
+      tc::tmem_ld16(taddr + lane_base + 384u + (uint32_t)cb, ei);
+      if (m < d) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int n = cb + j;
-            float rh, rl, ih, il;
-            const bool in = k < d && n < d;
-            tc::tf32_split(in ? w * re[j] : 0.f, rh, rl);
-            tc::tf32_split(in ? w * im[j] : 0.f, ih, il);
-            const uint32_t off = tc::core_off(n, lane, DN_KC);
-            *reinterpret_cast<float*>(b_planes + off) = rh;
-            *reinterpret_cast<float*>(b_planes + b_plane + off) = rl;
-            *reinterpret_cast<float*>(b_planes + 2 * b_plane + off) = ih;
-            *reinterpret_cast<float*>(b_planes + 3 * b_plane + off) = il;
+        for (int j = 0; j < 16; ++j) {
+          const int n = cb + j;
+          if (n >= d) continue;
+          const float2 v = make_float2(w * (dr[j] + er[j]), w * (di[j] + ei[j]));
+          if (to_t) {
+            tmat[(size_t)m * d + n] = v;
+          } else {
+            float2* p = acc + (size_t)n * d + m;
+            *p = add ? make_float2(p->x + v.x, p->y + v.y) : v;
           }
         }
       }
-      tc::fence_smem_to_async();
-      tc::fence_before();
-      __syncthreads();
-      tc::fence_after();
-      if (tid == 0) {
-        const int ksteps = min(4, (d - kc * DN_KC + 7) >> 3);
-        issue_chunk(taddr, 0u, a_base, b_base, b_plane, np, ksteps, false, false);
-        tc::mma_commit(&bar);
-      }
-      ok = wait_mma(&bar, parity);
     }
+    tc::fence_before();
+    __syncthreads();  // the flushed values are visible to the block; TMEM may be rewritten
+    tc::fence_after();
+  };
+
+  gemm(SRC_OPA, SRC_XB, false);  // A X
+  flush(false, false, 1.f);
+  gemm(SRC_XA, SRC_OPA, true);   // X A^dag
+  flush(false, true, 1.f);
+  for (int i = 0; i < L.n_cops && ok; ++i) {
+    c.cop = i;
+    gemm(SRC_XA, SRC_OPC, true);  // T = X C^dag
+    flush(true, false, 1.f);
+    gemm(SRC_OPC, SRC_TB, false);  // C T
+    flush(false, true, wc[i]);
   }
 
   double err_acc = 0.0;
   if (ok) {
-    // row m of D lives in TMEM lane m: warps w and w + 4 share lanes 32 (w % 4) ..
-    const int m = 32 * (warp & 3) + lane;
-    const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-    for (int cb = (warp >> 2) * 16; cb < np; cb += 32) {
-      float re[16], im[16];
-      tc::tmem_ld16(taddr + lane_base + (uint32_t)cb, re);
-      tc::tmem_ld16(taddr + lane_base + 128u + (uint32_t)cb, im);
-      if (m < d) {
-        for (int j = 0; j < 16; ++j) {
-          const int n = cb + j;
-          if (n < d)
-            epilogue<QG_C64, YDT, EPI>(n * d + m, cx<float>{re[j], im[j]}, ax, rk, err_acc);
-        }
-      }
+    for (int idx = tid; idx < d * d; idx += DN_THREADS) {
+      const float2 v = acc[idx];
+      epilogue<QG_C64, YDT, EPI>(idx, cx<float>{v.x, v.y}, ax, rk, err_acc);
     }
   } else if (tid == 0) {
     atomicOr(&g_dense_fault, 1u);
@@ -293,6 +292,7 @@ static int check_dense(const qg_dense_lindblad* L) {
   if (L->n_cops < 0 || L->n_cops > QG_MAX_COPS)
     return set_error(QG_ERR_ARG, "collapse operator count out of range");
   if (!L->a || (L->n_cops > 0 && !L->c)) return set_error(QG_ERR_ARG, "null operator storage");
+  if (!L->work) return set_error(QG_ERR_ARG, "null workspace (2*d*d complex64 values)");
   if ((L->a_coef_code && (!L->a_coef_start || !L->a_coef_consts)) ||
       (L->c_coef_code && (!L->c_coef_start || !L->c_coef_consts)))
     return set_error(QG_ERR_ARG, "coefficient program tables incomplete");

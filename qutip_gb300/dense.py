@@ -8,7 +8,9 @@ system of Hilbert dimension ``d <= 128`` whose operators are dense, those produc
 small dense GEMMs: :class:`DenseLindbladOperator` keeps ``A_g`` and ``C_i`` as complex64
 ``d x d`` matrices and applies the generator in one CTA with ``tcgen05`` tensor-core
 MMAs (TF32 inputs split hi + lo, FP32 accumulation in tensor memory; ``qg_dense_lindblad_*``
-in ``csrc/dense.cu``).  The stages are complex64, so it serves the mixed form
+in ``csrc/dense.cu``; each product in fresh accumulators, the large hi*hi part and the
+small hi*lo + lo*hi corrections apart, summed on the CUDA cores).  The stages are
+complex64, so it serves the mixed form
 (``precision="mixed"``: FP64 state, step control and expectation values).
 
 Sparse operators (a Jaynes-Cummings system has three entries per row) keep the sparse
@@ -81,9 +83,12 @@ class DenseLindbladOperator:
         self._a_prog = self._programs(self.a_coeffs)
         self._c_prog = self._programs(self.c_coeffs)
         self.coeffs = self.a_coeffs + self.c_coeffs
+        # the generator's FP32 accumulator and the product X C_i^dag (one application at a
+        # time on this operator: its launches are ordered on the caller's stream)
+        self.work = torch.zeros(2 * d * d, dtype=torch.complex64, device=self.device)
         st = _lib.DenseLindblad()
         st.d, st.n_groups, st.n_cops, st.reserved = d, len(a_terms), len(c_terms), 0
-        st.a, st.c = _ptr(self.a), _ptr(self.c)
+        st.a, st.c, st.work = _ptr(self.a), _ptr(self.c), _ptr(self.work)
         st.a_coef_code, st.a_coef_start, st.a_coef_consts = (_ptr(v) for v in self._a_prog)
         st.c_coef_code, st.c_coef_start, st.c_coef_consts = (_ptr(v) for v in self._c_prog)
         self.struct = st
