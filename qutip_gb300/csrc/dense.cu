@@ -8,19 +8,22 @@
 //
 // the reference's LindbladMatrixForm (qutip/core/cy/lindblad_matrix_form.pyx:105-204,
 // full non-Hermitian branch) with dense operators.  Per collapse operator two products:
-// T = X C^dag, then C T.  Each product runs into fresh TMEM accumulators: D (columns
-// 0..255: real, imaginary) takes the hi*hi terms and E (256..511) the small hi*lo + lo*hi
-// corrections, so no rounding of a correction happens at the magnitude of the product;
-// D + E is then flushed by the CUDA cores, in FP32 with round-to-nearest, into the
-// caller's workspace (the generator's accumulator, or T).  The accumulated generator
-// goes through the same fused Vern7 epilogue as the sparse kernels (stage.cuh).  The
-// stage vectors are complex64: this is the mixed form's generator.
+// T = X C^dag, then C T.
 //
-// One CTA of 256 threads per application.  Operands are staged through shared memory in
-// K chunks of 32: for each chunk every thread writes its share of the A- and B-operand
-// planes (real / imaginary x hi / lo), then one thread issues the MMAs (12 per 8-wide K
-// step: four real products of the complex product, three TF32 terms each) and commits
-// them to an mbarrier that every thread waits on, with a bounded wait.
+// Work split: CTA j owns the 16 output columns [16 j, 16 j + 16) of every product; column n
+// of A X, X A^dag, T = X C^dag and C T needs only column n of X, of A^dag, of C^dag and of
+// T, so the CTAs never exchange data and T's block stays in the CTA's shared memory.
+// One CTA of 256 threads computes Y = Aop Bop^T (M = 128 rows, N = 16 columns) in K chunks
+// of 32: every thread writes its share of the chunk's operand planes (real / imaginary x
+// TF32 hi / lo) into one of two shared-memory buffers, one thread issues the 12 MMAs per
+// 8-wide K step, and while they run the block reads the previous chunk's result out of
+// tensor memory.  Each chunk runs into fresh accumulators: D takes the hi*hi terms and E
+// the small hi*lo + lo*hi corrections, and the CUDA cores add D + E of every chunk into
+// FP32 registers with round-to-nearest.  The tensor core's own accumulation (which does
+// not round to nearest) is thereby limited to one chunk: that keeps the result at FP32
+// level (a chain over all of K loses up to 5x more, growing with d).  The accumulated
+// generator goes through the same fused Vern7 epilogue as the sparse kernels (stage.cuh).
+// The stage vectors are complex64: this is the mixed form's generator.
 #include <mutex>
 
 #include "capi_internal.h"
@@ -32,8 +35,14 @@ namespace qg {
 
 constexpr int DN_THREADS = 256;
 constexpr int DN_KC = 32;                          // K chunk
+constexpr int DN_NB = 16;                          // output columns per CTA (MMA N)
 constexpr uint32_t DN_PLANE_A = 128u * DN_KC * 4u;  // one A-operand plane (M = 128 rows)
-constexpr int DN_TMEM_COLS = 512;
+constexpr uint32_t DN_PLANE_B = DN_NB * DN_KC * 4u; // one B-operand plane
+constexpr uint32_t DN_BUF_A = 4u * DN_PLANE_A, DN_BUF_B = 4u * DN_PLANE_B;
+constexpr int DN_TS = 129;                         // row stride (float2) of the T block
+constexpr int DN_TMEM_COLS = 128;                  // 2 buffers x (D re, D im, E re, E im) x 16
+constexpr size_t DN_SMEM = 2 * (size_t)DN_BUF_A + 2 * (size_t)DN_BUF_B +
+                           (size_t)DN_NB * DN_TS * sizeof(float2);
 
 __device__ unsigned int g_dense_fault = 0u;
 
@@ -43,21 +52,22 @@ enum Src { SRC_OPA = 0, SRC_OPC = 1, SRC_XB = 2, SRC_XA = 3, SRC_TB = 4 };
 struct DenseCtx {
   const qg_dense_lindblad* L;
   const float2* x;     // the argument, vec(X): X[r][c] at c*d + r
-  int d, np;           // dimension, N (rows of the B operand) = d rounded up to 16
+  int d, n0;           // dimension, first output column of this CTA
   int cop;             // collapse operator of SRC_OPC
   const float2* ca;    // a_g(t) in shared memory
-  const float2* t;     // T = X C^dag, row-major: T[r][c] at r*d + c
+  const float2* t;     // this CTA's columns of T = X C^dag: T[k][n0 + j] at j*DN_TS + k
 };
 
 // element (r, k) of a source: the operator sum A(t), C_cop, X read as (n, k) -> X[k][n]
-// (B operand of A X and C X ...), or X read as (m, k) -> X[m][k] (A operand of X B^dag)
+// (B operand of A X), X read as (m, k) -> X[m][k] (A operand of X B^dag), or T read as
+// (n, k) -> T[k][n] (B operand of C T).  r is the global row (output column for B).
 __device__ __forceinline__ float2 src_at(const DenseCtx& c, int src, int r, int k,
                                          const qg_dense_lindblad& L) {
   const int d = c.d;
   if (r >= d || k >= d) return make_float2(0.f, 0.f);
   if (src == SRC_XB) return c.x[(size_t)r * d + k];
   if (src == SRC_XA) return c.x[(size_t)k * d + r];
-  if (src == SRC_TB) return c.t[(size_t)k * d + r];   // (n, k) -> T[k][n]
+  if (src == SRC_TB) return c.t[(r - c.n0) * DN_TS + k];
   const float2* base = static_cast<const float2*>(src == SRC_OPA ? L.a : L.c);
   if (src == SRC_OPC) return __ldg(base + ((size_t)c.cop * d + r) * d + k);
   float re = 0.f, im = 0.f;
@@ -70,17 +80,18 @@ __device__ __forceinline__ float2 src_at(const DenseCtx& c, int src, int r, int 
   return make_float2(re, im);
 }
 
-// Write rows [0, rows) x K chunk kc of a source into four planes (re hi, re lo, im hi,
-// im lo), each rows x 32 values in the core-matrix layout.  Element e of the chunk maps to
-// (r, kk) with the low 3 bits of e the row within an 8-row band and the next 2 bits the
-// column within a 4-column core: a warp's 32 stores fall in 32 different banks.
-__device__ __forceinline__ void stage_planes(const DenseCtx& c, int src, int rows, int kc,
-                                             unsigned char* planes, uint32_t plane_bytes) {
+// Write rows [row0, row0 + rows) x K chunk kc of a source into four planes (re hi, re lo,
+// im hi, im lo), each rows x 32 values in the core-matrix layout.  Element e of the chunk
+// maps to (r, kk) with the low 3 bits of e the row within an 8-row band and the next 2
+// bits the column within a 4-column core: a warp's 32 stores fall in 32 different banks.
+__device__ __forceinline__ void stage_planes(const DenseCtx& c, int src, int rows, int row0,
+                                             int kc, unsigned char* planes,
+                                             uint32_t plane_bytes) {
   const qg_dense_lindblad& L = *c.L;
   for (int e = threadIdx.x; e < rows * DN_KC; e += DN_THREADS) {
     const int r = (e >> 8) * 8 + (e & 7);
     const int kk = ((e >> 5) & 7) * 4 + ((e >> 3) & 3);
-    const float2 v = src_at(c, src, r, kc * DN_KC + kk, L);
+    const float2 v = src_at(c, src, row0 + r, kc * DN_KC + kk, L);
     float rh, rl, ih, il;
     tc::tf32_split(v.x, rh, rl);
     tc::tf32_split(v.y, ih, il);
@@ -94,18 +105,17 @@ __device__ __forceinline__ void stage_planes(const DenseCtx& c, int src, int row
 
 // One K chunk of Aop Bop^T for complex operands (Bop conjugated when conj_b):
 // re = Ar Br -/+ Ai Bi, im = +/- Ar Bi + Ai Br, each real product in three TF32 terms,
-// hi*hi into D (TMEM columns 0 / 128 for re / im) and hi*lo, lo*hi into E (256 / 384).
-// Issued by one thread; init: the chunk starts the product (first MMA of each region
-// overwrites).
-__device__ __forceinline__ void issue_chunk(uint32_t taddr, uint32_t a_base, uint32_t b_base,
-                                            uint32_t b_plane, int np, int ksteps, bool conj_b,
-                                            bool init) {
+// hi*hi into D (TMEM columns +0 / +16 for re / im) and hi*lo, lo*hi into E (+32 / +48).
+// Issued by one thread; the chunk's first MMA into each region overwrites it.
+__device__ __forceinline__ void issue_chunk(uint32_t tcols, uint32_t a_base, uint32_t b_base,
+                                            int ksteps, bool conj_b) {
   const uint32_t sbo = tc::band_bytes(DN_KC);
-  const uint32_t id_pos = tc::idesc_tf32(128, np, false), id_neg = tc::idesc_tf32(128, np, true);
+  const uint32_t id_pos = tc::idesc_tf32(128, DN_NB, false);
+  const uint32_t id_neg = tc::idesc_tf32(128, DN_NB, true);
   // (A plane pair, B plane pair, destination: 0 re / 1 im, negated)
   const int ap[4] = {0, 2, 0, 2}, bp[4] = {0, 2, 2, 0}, dst[4] = {0, 0, 1, 1};
   const bool neg[4] = {false, !conj_b, conj_b, false};
-  bool first[4] = {init, init, init, init};  // D re, D im, E re, E im
+  bool first[4] = {true, true, true, true};  // D re, D im, E re, E im
   for (int ks = 0; ks < ksteps; ++ks) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -115,21 +125,13 @@ __device__ __forceinline__ void issue_chunk(uint32_t taddr, uint32_t a_base, uin
       for (int tt = 0; tt < 3; ++tt) {
         const int region = dst[q] + (tt ? 2 : 0);
         const uint32_t a = a_base + (uint32_t)(ap[q] + at[tt]) * DN_PLANE_A + ks * 2 * tc::LBO;
-        const uint32_t b = b_base + (uint32_t)(bp[q] + bt[tt]) * b_plane + ks * 2 * tc::LBO;
-        tc::mma_tf32(taddr + 128u * region, tc::smem_desc(a, tc::LBO, sbo),
+        const uint32_t b = b_base + (uint32_t)(bp[q] + bt[tt]) * DN_PLANE_B + ks * 2 * tc::LBO;
+        tc::mma_tf32(tcols + (uint32_t)DN_NB * region, tc::smem_desc(a, tc::LBO, sbo),
                      tc::smem_desc(b, tc::LBO, sbo), neg[q] ? id_neg : id_pos, !first[region]);
         first[region] = false;
       }
     }
   }
-}
-
-// Wait for the MMAs committed to bar (phase `parity`); false when the bounded wait gave up
-__device__ __forceinline__ bool wait_mma(uint64_t* bar, unsigned& parity) {
-  const bool ok = __syncthreads_and(mbar_poll(bar, parity) ? 1 : 0) != 0;
-  parity ^= 1u;
-  tc::fence_after();
-  return ok;
 }
 
 template <int YDT, int EPI>
@@ -140,14 +142,14 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
   __shared__ float2 ca[QG_MAX_GROUPS];
   __shared__ float wc[QG_MAX_COPS];
   __shared__ uint32_t taddr_s;
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t bar[2];
   __shared__ double red[DN_THREADS / 32];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int d = L.d;
-  const int np = (d + 15) & ~15;
-  const uint32_t b_plane = (uint32_t)np * DN_KC * 4u;
-  unsigned char* a_planes = dn_smem;
-  unsigned char* b_planes = dn_smem + 4 * DN_PLANE_A;
+  const int n0 = blockIdx.x * DN_NB;
+  unsigned char* a_planes = dn_smem;                      // 2 buffers
+  unsigned char* b_planes = dn_smem + 2 * DN_BUF_A;       // 2 buffers
+  float2* t_blk = reinterpret_cast<float2*>(dn_smem + 2 * DN_BUF_A + 2 * DN_BUF_B);
   if (tid < L.n_groups) {
     cplx a{1.0, 0.0};
     if (L.a_coef_code) a = eval_coef(L.a_coef_code + L.a_coef_start[tid], L.a_coef_consts, t);
@@ -159,7 +161,8 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
     wc[tid] = (float)(f.re * f.re + f.im * f.im);
   }
   if (tid == 0) {
-    mbar_init(&bar, 1);
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) tc::tmem_alloc(&taddr_s, DN_TMEM_COLS);
@@ -167,84 +170,114 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
   __syncthreads();
   tc::fence_after();
   const uint32_t taddr = taddr_s;
-  const uint32_t a_base = smem_u32(a_planes), b_base = smem_u32(b_planes);
-  float2* acc = static_cast<float2*>(L.work);          // vec order, (m, n) at n*d + m
-  float2* tmat = acc + (size_t)d * d;                    // T row-major, (m, n) at m*d + n
-  DenseCtx c{&L, x, d, np, 0, ca, tmat};
+  DenseCtx c{&L, x, d, n0, 0, ca, t_blk};
   const int nchunks = (d + DN_KC - 1) / DN_KC;
-  unsigned parity = 0u;
+  // Thread roles when reading tensor memory: warps 0-3 the real part, 4-7 the imaginary
+  // part; warp w reads TMEM lanes 32 (w % 4) ... (its rows m).
+  const int part = warp >> 2;
+  const int m = 32 * (warp & 3) + lane;
+  const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+  unsigned par[2] = {0u, 0u};
+  bool pend[2] = {false, false};  // a commit to bar[b] not yet waited for
   bool ok = true;
+  int buf = 0;
+  float prod[DN_NB], gen[DN_NB];
+#pragma unroll
+  for (int j = 0; j < DN_NB; ++j) gen[j] = 0.f;
 
-  // one product op(srcA) op(srcB)^T over every K chunk, into fresh D and E
+  auto wait_buf = [&](int b) {
+    const bool r = __syncthreads_and(mbar_poll(&bar[b], par[b]) ? 1 : 0) != 0;
+    if (r) {
+      par[b] ^= 1u;
+      pend[b] = false;
+    }
+    tc::fence_after();
+    return r;
+  };
+  // add D + E of buffer b (this thread's part, rows m, 16 columns) into prod
+  auto take = [&](int b, bool first) {
+    float dv[DN_NB], ev[DN_NB];
+    const uint32_t cols = taddr + lane_base + (uint32_t)(4 * DN_NB * b + DN_NB * part);
+    tc::tmem_ld16(cols, dv);
+    tc::tmem_ld16(cols + 2 * DN_NB, ev);
+#pragma unroll
+    for (int j = 0; j < DN_NB; ++j) {
+      const float v = dv[j] + ev[j];
+      prod[j] = first ? v : prod[j] + v;
+    }
+  };
+  // one product op(srcA) op(srcB)^T of this CTA's columns into prod
   auto gemm = [&](int src_a, int src_b, bool conj_b) {
     for (int kc = 0; kc < nchunks && ok; ++kc) {
-      stage_planes(c, src_a, 128, kc, a_planes, DN_PLANE_A);
-      stage_planes(c, src_b, np, kc, b_planes, b_plane);
+      const int b = buf;
+      stage_planes(c, src_a, 128, 0, kc, a_planes + b * DN_BUF_A, DN_PLANE_A);
+      stage_planes(c, src_b, DN_NB, n0, kc, b_planes + b * DN_BUF_B, DN_PLANE_B);
       tc::fence_smem_to_async();
       tc::fence_before();
       __syncthreads();
       tc::fence_after();
       if (tid == 0) {
         const int ksteps = min(4, (d - kc * DN_KC + 7) >> 3);
-        issue_chunk(taddr, a_base, b_base, b_plane, np, ksteps, conj_b, kc == 0);
-        tc::mma_commit(&bar);
+        issue_chunk(taddr + (uint32_t)(4 * DN_NB * b), smem_u32(a_planes + b * DN_BUF_A),
+                    smem_u32(b_planes + b * DN_BUF_B), ksteps, conj_b);
+        tc::mma_commit(&bar[b]);
       }
-      ok = wait_mma(&bar, parity);
+      pend[b] = true;
+      if (kc > 0) {  // the previous chunk, while this one runs
+        ok = wait_buf(b ^ 1);
+        if (ok) take(b ^ 1, kc == 1);
+      }
+      buf ^= 1;
     }
-  };
-  // D + E of the last product, times w, into the accumulator (add) or into T; row m of
-  // the product lives in TMEM lane m, warps w and w + 4 share lanes 32 (w % 4) ...
-  const int m = 32 * (warp & 3) + lane;
-  const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-  auto flush = [&](bool to_t, bool add, float w) {
-    if (!ok) return;
-    for (int cb = (warp >> 2) * 16; cb < np; cb += 32) {
-      float dr[16], di[16], er[16], ei[16];
-      tc::tmem_ld16(taddr + lane_base + (uint32_t)cb, dr);
-      tc::tmem_ld16(taddr + lane_base + 128u + (uint32_t)cb, di);
-      tc::tmem_ld16(taddr + lane_base + 256u + (uint32_t)cb, er);
-      tc::tmem_ld16(taddr + lane_base + 384u + (uint32_t)cb, ei);
-      if (m < d) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int n = cb + j;
-          if (n >= d) continue;
-          const float2 v = make_float2(w * (dr[j] + er[j]), w * (di[j] + ei[j]));
-          if (to_t) {
-            tmat[(size_t)m * d + n] = v;
-          } else {
-            float2* p = acc + (size_t)n * d + m;
-            *p = add ? make_float2(p->x + v.x, p->y + v.y) : v;
-          }
-        }
-      }
+    if (ok) {
+      ok = wait_buf(buf ^ 1);
+      if (ok) take(buf ^ 1, nchunks == 1);
     }
     tc::fence_before();
-    __syncthreads();  // the flushed values are visible to the block; TMEM may be rewritten
+    __syncthreads();  // every read of TMEM and of the planes is done
     tc::fence_after();
+  };
+  auto accumulate = [&](float w) {
+#pragma unroll
+    for (int j = 0; j < DN_NB; ++j) gen[j] = fmaf(w, prod[j], gen[j]);
   };
 
   gemm(SRC_OPA, SRC_XB, false);  // A X
-  flush(false, false, 1.f);
+#pragma unroll
+  for (int j = 0; j < DN_NB; ++j) gen[j] = prod[j];
   gemm(SRC_XA, SRC_OPA, true);   // X A^dag
-  flush(false, true, 1.f);
+  accumulate(1.f);
   for (int i = 0; i < L.n_cops && ok; ++i) {
     c.cop = i;
-    gemm(SRC_XA, SRC_OPC, true);  // T = X C^dag
-    flush(true, false, 1.f);
+    gemm(SRC_XA, SRC_OPC, true);  // T = X C^dag, this CTA's columns
+    float* tp = reinterpret_cast<float*>(t_blk) + part;
+#pragma unroll
+    for (int j = 0; j < DN_NB; ++j) tp[2 * (j * DN_TS + m)] = prod[j];
+    __syncthreads();
     gemm(SRC_OPC, SRC_TB, false);  // C T
-    flush(false, true, wc[i]);
+    accumulate(wc[i]);
   }
 
   double err_acc = 0.0;
   if (ok) {
-    for (int idx = tid; idx < d * d; idx += DN_THREADS) {
-      const float2 v = acc[idx];
-      epilogue<QG_C64, YDT, EPI>(idx, cx<float>{v.x, v.y}, ax, rk, err_acc);
+    // real and imaginary parts meet in shared memory (the A planes are free now)
+    float* ex = reinterpret_cast<float*>(a_planes) + part;
+#pragma unroll
+    for (int j = 0; j < DN_NB; ++j) ex[2 * (j * 128 + m)] = gen[j];
+    __syncthreads();
+    const float2* exv = reinterpret_cast<const float2*>(a_planes);
+    const int ncols = min(DN_NB, d - n0);
+    for (int e = tid; e < ncols * d; e += DN_THREADS) {
+      const int jl = e / d, mm = e - jl * d;
+      const float2 v = exv[jl * 128 + mm];
+      epilogue<QG_C64, YDT, EPI>((n0 + jl) * d + mm, cx<float>{v.x, v.y}, ax, rk,
+                                 err_acc);
     }
   } else if (tid == 0) {
     atomicOr(&g_dense_fault, 1u);
-    (void)mbar_poll(&bar, parity ^ 1u);  // let an outstanding commit land before freeing TMEM
+    // let outstanding commits land before the tensor memory is freed
+    for (int b = 0; b < 2; ++b)
+      if (pend[b]) (void)mbar_poll(&bar[b], par[b]);
   }
   tc::fence_before();
   __syncthreads();
@@ -255,10 +288,7 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
   }
 }
 
-static size_t dense_smem(int d) {
-  const int np = (d + 15) & ~15;
-  return 4 * (size_t)DN_PLANE_A + 4 * (size_t)np * DN_KC * 4;
-}
+static size_t dense_smem(int) { return DN_SMEM; }
 
 template <int YDT, int EPI>
 static int launch_dense(cudaStream_t st, const qg_dense_lindblad& L, double t, const void* x,
@@ -279,7 +309,8 @@ static int launch_dense(cudaStream_t st, const qg_dense_lindblad& L, double t, c
       set_bytes[dev] = smem;
     }
   }
-  kern<<<1, DN_THREADS, smem, st>>>(L, t, static_cast<const float2*>(x), ax, rk);
+  const int grid = (L.d + DN_NB - 1) / DN_NB;
+  kern<<<grid, DN_THREADS, smem, st>>>(L, t, static_cast<const float2*>(x), ax, rk);
   return check_launch("dense_lindblad_kernel");
 }
 
