@@ -793,13 +793,14 @@ def run_dense(args):
         e1.synchronize()
         us = 1e3 * e0.elapsed_time(e1) / reps
         tflops = dop.gemm_flops() / (us * 1e-6) / 1e12
+        n_sm = dop.n_ctas
         out["dense_random"].append({"d": d, "dense_bucket_ms": ms_dense, "matrix_free_sparse_ms": ms_mf,
-                                    "apply_us": us, "issued_tf32_tflops": tflops,
-                                    "frac_of_one_sm_tf32": tflops / (tf32_peak / 152.0)})
+                                    "apply_us": us, "issued_tf32_tflops": tflops, "sms": n_sm,
+                                    "frac_of_sms_tf32": tflops / (tf32_peak * n_sm / 152.0)})
         log(f"dense: random d={d}: tensor cores {ms_dense:.1f} ms, matrix-free {ms_mf:.1f} ms, "
-            f"apply {us:.1f} us = {tflops:.2f} TFLOP/s issued TF32 on one SM")
-    out["note"] = ("one CTA (one SM) per application; TF32 rate per SM taken as half the measured "
-                   "bf16 GEMM rate / 152 SMs")
+            f"apply {us:.1f} us = {tflops:.2f} TFLOP/s issued TF32 on {n_sm} SMs")
+    out["note"] = ("one CTA (one SM) per 16 output columns per application; TF32 rate per SM "
+                   "taken as half the measured bf16 GEMM rate / 152 SMs")
     return out
 
 

@@ -183,9 +183,8 @@ typedef struct qg_lindblad {
  * A = sum_g a_g(t) A_g = -i H_nh, applied as GEMMs on the tensor cores (TF32 split into
  * hi + lo parts, FP32 accumulation).  Operators are complex64, row-major:
  * A_g[m][k] at a + (g*d + m)*d + k, C_i[m][k] at c + (i*d + m)*d + k.  Coefficient
- * programs as in qg_lindblad (NULL code: all 1).  work: caller-owned workspace of
- * 2*d*d complex64 values (the generator's FP32 accumulator and the product X C_i^dag);
- * calls that share it must not overlap on the GPU. */
+ * programs as in qg_lindblad (NULL code: all 1).  One CTA per 16 columns of the
+ * result; no workspace. */
 #define QG_DENSE_MAX_D 128
 typedef struct qg_dense_lindblad {
   int32_t d;
@@ -194,7 +193,6 @@ typedef struct qg_dense_lindblad {
   int32_t reserved; /* 0 */
   const void* a;
   const void* c;
-  void* work;
   const int32_t* a_coef_code;
   const int32_t* a_coef_start;
   const double* a_coef_consts;

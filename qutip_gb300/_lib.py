@@ -49,7 +49,7 @@ class Lindblad(C.Structure):
 
 class DenseLindblad(C.Structure):
     _fields_ = [("d", C.c_int32), ("n_groups", C.c_int32), ("n_cops", C.c_int32),
-                ("reserved", C.c_int32), ("a", C.c_void_p), ("c", C.c_void_p), ("work", C.c_void_p),
+                ("reserved", C.c_int32), ("a", C.c_void_p), ("c", C.c_void_p),
                 ("a_coef_code", C.c_void_p), ("a_coef_start", C.c_void_p),
                 ("a_coef_consts", C.c_void_p), ("c_coef_code", C.c_void_p),
                 ("c_coef_start", C.c_void_p), ("c_coef_consts", C.c_void_p)]

@@ -16,8 +16,8 @@
 // One CTA of 256 threads computes Y = Aop Bop^T (M = 128 rows, N = 16 columns) in K chunks
 // of 32: every thread writes its share of the chunk's operand planes (real / imaginary x
 // TF32 hi / lo) into one of two shared-memory buffers, one thread issues the 12 MMAs per
-// 8-wide K step, and while they run the block reads the previous chunk's result out of
-// tensor memory.  Each chunk runs into fresh accumulators: D takes the hi*hi terms and E
+// 8-wide K step, and while they run the block loads the next chunk's operands into
+// registers and reads the previous chunk's result out of tensor memory.  Each chunk runs into fresh accumulators: D takes the hi*hi terms and E
 // the small hi*lo + lo*hi corrections, and the CUDA cores add D + E of every chunk into
 // FP32 registers with round-to-nearest.  The tensor core's own accumulation (which does
 // not round to nearest) is thereby limited to one chunk: that keeps the result at FP32
@@ -58,44 +58,87 @@ struct DenseCtx {
   const float2* t;     // this CTA's columns of T = X C^dag: T[k][n0 + j] at j*DN_TS + k
 };
 
-// element (r, k) of a source: the operator sum A(t), C_cop, X read as (n, k) -> X[k][n]
-// (B operand of A X), X read as (m, k) -> X[m][k] (A operand of X B^dag), or T read as
-// (n, k) -> T[k][n] (B operand of C T).  r is the global row (output column for B).
-__device__ __forceinline__ float2 src_at(const DenseCtx& c, int src, int r, int k,
-                                         const qg_dense_lindblad& L) {
+// Operand chunks.  Element e of a rows x 32 chunk maps to (r, kk) with the low 3 bits of
+// e the row within an 8-row band and the next 2 bits the column within a 4-column core: a
+// warp's 32 shared-memory stores fall in 32 different banks.  Thread t holds elements
+// t, t + 256, ...: all of them are loaded first (the loads in flight together), then
+// split and stored, so a chunk costs one memory latency, hidden behind the previous
+// chunk's MMAs.
+template <int ROWS>
+struct Chunk {
+  static constexpr int PER = ROWS * DN_KC / DN_THREADS;
+  float2 v[PER];
+};
+
+__device__ __forceinline__ int chunk_row(int e) { return (e >> 8) * 8 + (e & 7); }
+__device__ __forceinline__ int chunk_col(int e) { return ((e >> 5) & 7) * 4 + ((e >> 3) & 3); }
+
+// Rows [row0, row0 + ROWS) x K chunk kc of a source: the operator sum A(t), C_cop, X read
+// as (n, k) -> X[k][n] (B operand of A X), X read as (m, k) -> X[m][k] (A operand of
+// X B^dag), or T read as (n, k) -> T[k][n] (B operand of C T); zero outside d x d.
+template <int ROWS>
+__device__ __forceinline__ void load_chunk(const DenseCtx& c, int src, int row0, int kc,
+                                           Chunk<ROWS>& ch) {
+  constexpr int PER = Chunk<ROWS>::PER;
+  const qg_dense_lindblad& L = *c.L;
   const int d = c.d;
-  if (r >= d || k >= d) return make_float2(0.f, 0.f);
-  if (src == SRC_XB) return c.x[(size_t)r * d + k];
-  if (src == SRC_XA) return c.x[(size_t)k * d + r];
-  if (src == SRC_TB) return c.t[(r - c.n0) * DN_TS + k];
-  const float2* base = static_cast<const float2*>(src == SRC_OPA ? L.a : L.c);
-  if (src == SRC_OPC) return __ldg(base + ((size_t)c.cop * d + r) * d + k);
-  float re = 0.f, im = 0.f;
-  for (int g = 0; g < L.n_groups; ++g) {
-    const float2 v = __ldg(base + ((size_t)g * d + r) * d + k);
-    const float2 a = c.ca[g];
-    re = fmaf(a.x, v.x, fmaf(-a.y, v.y, re));
-    im = fmaf(a.x, v.y, fmaf(a.y, v.x, im));
+  int off[PER];
+  bool in[PER];
+  int sr = d, sk = 1;  // element (r, k) at base + r * sr + k * sk
+  const float2* base;
+  if (src == SRC_XB) {
+    base = c.x;
+  } else if (src == SRC_XA) {
+    base = c.x;
+    sr = 1;
+    sk = d;
+  } else if (src == SRC_TB) {
+    base = c.t - (size_t)c.n0 * DN_TS;
+    sr = DN_TS;
+  } else if (src == SRC_OPC) {
+    base = static_cast<const float2*>(L.c) + (size_t)c.cop * d * d;
+  } else {
+    base = static_cast<const float2*>(L.a);
   }
-  return make_float2(re, im);
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int e = threadIdx.x + i * DN_THREADS;
+    const int r = row0 + chunk_row(e), k = kc * DN_KC + chunk_col(e);
+    in[i] = r < d && k < d;
+    off[i] = in[i] ? r * sr + k * sk : 0;
+    ch.v[i] = make_float2(0.f, 0.f);
+  }
+  if (src != SRC_OPA) {
+#pragma unroll
+    for (int i = 0; i < PER; ++i)
+      if (in[i]) ch.v[i] = base[off[i]];
+    return;
+  }
+  for (int g = 0; g < L.n_groups; ++g) {  // A(t) = sum_g a_g(t) A_g
+    const float2 a = c.ca[g];
+    const float2* bg = base + (size_t)g * d * d;
+    float2 w[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) w[i] = in[i] ? __ldg(bg + off[i]) : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      ch.v[i].x = fmaf(a.x, w[i].x, fmaf(-a.y, w[i].y, ch.v[i].x));
+      ch.v[i].y = fmaf(a.x, w[i].y, fmaf(a.y, w[i].x, ch.v[i].y));
+    }
+  }
 }
 
-// Write rows [row0, row0 + rows) x K chunk kc of a source into four planes (re hi, re lo,
-// im hi, im lo), each rows x 32 values in the core-matrix layout.  Element e of the chunk
-// maps to (r, kk) with the low 3 bits of e the row within an 8-row band and the next 2
-// bits the column within a 4-column core: a warp's 32 stores fall in 32 different banks.
-__device__ __forceinline__ void stage_planes(const DenseCtx& c, int src, int rows, int row0,
-                                             int kc, unsigned char* planes,
-                                             uint32_t plane_bytes) {
-  const qg_dense_lindblad& L = *c.L;
-  for (int e = threadIdx.x; e < rows * DN_KC; e += DN_THREADS) {
-    const int r = (e >> 8) * 8 + (e & 7);
-    const int kk = ((e >> 5) & 7) * 4 + ((e >> 3) & 3);
-    const float2 v = src_at(c, src, row0 + r, kc * DN_KC + kk, L);
+// The chunk as four planes (re hi, re lo, im hi, im lo) in the core-matrix layout.
+template <int ROWS>
+__device__ __forceinline__ void store_chunk(const Chunk<ROWS>& ch, unsigned char* planes,
+                                            uint32_t plane_bytes) {
+#pragma unroll
+  for (int i = 0; i < Chunk<ROWS>::PER; ++i) {
+    const int e = threadIdx.x + i * DN_THREADS;
     float rh, rl, ih, il;
-    tc::tf32_split(v.x, rh, rl);
-    tc::tf32_split(v.y, ih, il);
-    const uint32_t off = tc::core_off(r, kk, DN_KC);
+    tc::tf32_split(ch.v[i].x, rh, rl);
+    tc::tf32_split(ch.v[i].y, ih, il);
+    const uint32_t off = tc::core_off(chunk_row(e), chunk_col(e), DN_KC);
     *reinterpret_cast<float*>(planes + off) = rh;
     *reinterpret_cast<float*>(planes + plane_bytes + off) = rl;
     *reinterpret_cast<float*>(planes + 2 * plane_bytes + off) = ih;
@@ -207,11 +250,15 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
     }
   };
   // one product op(srcA) op(srcB)^T of this CTA's columns into prod
+  Chunk<128> cha;
+  Chunk<DN_NB> chb;
   auto gemm = [&](int src_a, int src_b, bool conj_b) {
+    load_chunk(c, src_a, 0, 0, cha);
+    load_chunk(c, src_b, n0, 0, chb);
     for (int kc = 0; kc < nchunks && ok; ++kc) {
       const int b = buf;
-      stage_planes(c, src_a, 128, 0, kc, a_planes + b * DN_BUF_A, DN_PLANE_A);
-      stage_planes(c, src_b, DN_NB, n0, kc, b_planes + b * DN_BUF_B, DN_PLANE_B);
+      store_chunk(cha, a_planes + b * DN_BUF_A, DN_PLANE_A);
+      store_chunk(chb, b_planes + b * DN_BUF_B, DN_PLANE_B);
       tc::fence_smem_to_async();
       tc::fence_before();
       __syncthreads();
@@ -223,6 +270,10 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
         tc::mma_commit(&bar[b]);
       }
       pend[b] = true;
+      if (kc + 1 < nchunks) {  // the next chunk's loads, in flight during the MMAs
+        load_chunk(c, src_a, 0, kc + 1, cha);
+        load_chunk(c, src_b, n0, kc + 1, chb);
+      }
       if (kc > 0) {  // the previous chunk, while this one runs
         ok = wait_buf(b ^ 1);
         if (ok) take(b ^ 1, kc == 1);
@@ -323,7 +374,6 @@ static int check_dense(const qg_dense_lindblad* L) {
   if (L->n_cops < 0 || L->n_cops > QG_MAX_COPS)
     return set_error(QG_ERR_ARG, "collapse operator count out of range");
   if (!L->a || (L->n_cops > 0 && !L->c)) return set_error(QG_ERR_ARG, "null operator storage");
-  if (!L->work) return set_error(QG_ERR_ARG, "null workspace (2*d*d complex64 values)");
   if ((L->a_coef_code && (!L->a_coef_start || !L->a_coef_consts)) ||
       (L->c_coef_code && (!L->c_coef_start || !L->c_coef_consts)))
     return set_error(QG_ERR_ARG, "coefficient program tables incomplete");

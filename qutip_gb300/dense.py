@@ -8,8 +8,9 @@ system of Hilbert dimension ``d <= 128`` whose operators are dense, those produc
 small dense GEMMs: :class:`DenseLindbladOperator` keeps ``A_g`` and ``C_i`` as complex64
 ``d x d`` matrices and applies the generator in one CTA with ``tcgen05`` tensor-core
 MMAs (TF32 inputs split hi + lo, FP32 accumulation in tensor memory; ``qg_dense_lindblad_*``
-in ``csrc/dense.cu``; each product in fresh accumulators, the large hi*hi part and the
-small hi*lo + lo*hi corrections apart, summed on the CUDA cores).  The stages are
+in ``csrc/dense.cu``; one CTA per 16 output columns; each K chunk of 32 in fresh
+accumulators, the large hi*hi part and the small hi*lo + lo*hi corrections apart, summed
+on the CUDA cores with round-to-nearest).  The stages are
 complex64, so it serves the mixed form
 (``precision="mixed"``: FP64 state, step control and expectation values).
 
@@ -83,12 +84,9 @@ class DenseLindbladOperator:
         self._a_prog = self._programs(self.a_coeffs)
         self._c_prog = self._programs(self.c_coeffs)
         self.coeffs = self.a_coeffs + self.c_coeffs
-        # the generator's FP32 accumulator and the product X C_i^dag (one application at a
-        # time on this operator: its launches are ordered on the caller's stream)
-        self.work = torch.zeros(2 * d * d, dtype=torch.complex64, device=self.device)
         st = _lib.DenseLindblad()
         st.d, st.n_groups, st.n_cops, st.reserved = d, len(a_terms), len(c_terms), 0
-        st.a, st.c, st.work = _ptr(self.a), _ptr(self.c), _ptr(self.work)
+        st.a, st.c = _ptr(self.a), _ptr(self.c)
         st.a_coef_code, st.a_coef_start, st.a_coef_consts = (_ptr(v) for v in self._a_prog)
         st.c_coef_code, st.c_coef_start, st.c_coef_consts = (_ptr(v) for v in self._c_prog)
         self.struct = st
@@ -142,9 +140,14 @@ class DenseLindbladOperator:
         """Bytes of the dense operators (complex64)."""
         return 8 * self.d * self.d * (self.n_groups + self.n_cops)
 
+    @property
+    def n_ctas(self) -> int:
+        """CTAs (one per SM) of one application: one per 16 output columns."""
+        return (self.d + 15) // 16
+
     def gemm_flops(self) -> int:
         """Real multiply-adds x 2 of one application as issued: per complex product of two
-        d x d matrices (padded to 128 rows, 16 columns, 8-wide K steps) four real
+        d x d matrices (padded to 128 rows, 16-column blocks, 8-wide K steps) four real
         products in three TF32 terms."""
         d = self.d
         np_ = (d + 15) // 16 * 16
