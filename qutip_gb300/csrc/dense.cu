@@ -15,8 +15,8 @@
 // T, so the CTAs never exchange data and T's block stays in the CTA's shared memory.
 // One CTA of 256 threads computes Y = Aop Bop^T (M = 128 rows, N = 16 columns) in K chunks
 // of 32: every thread writes its share of the chunk's operand planes (real / imaginary x
-// TF32 hi / lo) into one of two shared-memory buffers, one thread issues the 12 MMAs per
-// 8-wide K step, and while they run the block loads the next chunk's operands into
+// TF32 hi / lo) into one of two shared-memory buffers, one thread issues the 6 MMAs per
+// 8-wide K step (real and imaginary output columns side by side, N = 32), and while they run the block loads the next chunk's operands into
 // registers and reads the previous chunk's result out of tensor memory.  Each chunk runs into fresh accumulators: D takes the hi*hi terms and E
 // the small hi*lo + lo*hi corrections, and the CUDA cores add D + E of every chunk into
 // FP32 registers with round-to-nearest.  The tensor core's own accumulation (which does
@@ -37,7 +37,7 @@ constexpr int DN_THREADS = 256;
 constexpr int DN_KC = 32;                          // K chunk
 constexpr int DN_NB = 16;                          // output columns per CTA (MMA N)
 constexpr uint32_t DN_PLANE_A = 128u * DN_KC * 4u;  // one A-operand plane (M = 128 rows)
-constexpr uint32_t DN_PLANE_B = DN_NB * DN_KC * 4u; // one B-operand plane
+constexpr uint32_t DN_PLANE_B = 2 * DN_NB * DN_KC * 4u;  // one B-operand plane (N = 32 rows)
 constexpr uint32_t DN_BUF_A = 4u * DN_PLANE_A, DN_BUF_B = 4u * DN_PLANE_B;
 constexpr int DN_TS = 129;                         // row stride (float2) of the T block
 constexpr int DN_TMEM_COLS = 128;                  // 2 buffers x (D re, D im, E re, E im) x 16
@@ -146,34 +146,55 @@ __device__ __forceinline__ void store_chunk(const Chunk<ROWS>& ch, unsigned char
   }
 }
 
-// One K chunk of Aop Bop^T for complex operands (Bop conjugated when conj_b):
-// re = Ar Br -/+ Ai Bi, im = +/- Ar Bi + Ai Br, each real product in three TF32 terms,
-// hi*hi into D (TMEM columns +0 / +16 for re / im) and hi*lo, lo*hi into E (+32 / +48).
-// Issued by one thread; the chunk's first MMA into each region overwrites it.
+// The B operand (this CTA's 16 rows of Bop, conjugated when conj) stacked for complex
+// products with N = 32: B1 = [Br ; s Bi] and B2 = [-s Bi ; Br] (s = -1 when conjugated), so
+// that Ar B1^T + Ai B2^T = [re | im] of Aop Bop^T in 32 accumulator columns.  Planes:
+// B1 hi, B1 lo, B2 hi, B2 lo.
+__device__ __forceinline__ void store_chunk_b(const Chunk<DN_NB>& ch, unsigned char* planes,
+                                              bool conj) {
+#pragma unroll
+  for (int i = 0; i < Chunk<DN_NB>::PER; ++i) {
+    const int e = threadIdx.x + i * DN_THREADS;
+    const int r = chunk_row(e), kk = chunk_col(e);
+    const float re = ch.v[i].x, im = conj ? -ch.v[i].y : ch.v[i].y;
+    float rh, rl, ih, il;
+    tc::tf32_split(re, rh, rl);
+    tc::tf32_split(im, ih, il);
+    const uint32_t top = tc::core_off(r, kk, DN_KC), bot = tc::core_off(r + DN_NB, kk, DN_KC);
+    float* p = reinterpret_cast<float*>(planes);
+    constexpr uint32_t P = DN_PLANE_B / 4;
+    p[(top >> 2)] = rh;            // B1 = [Br ; s Bi]
+    p[(bot >> 2)] = ih;
+    p[P + (top >> 2)] = rl;
+    p[P + (bot >> 2)] = il;
+    p[2 * P + (top >> 2)] = -ih;   // B2 = [-s Bi ; Br]
+    p[2 * P + (bot >> 2)] = rh;
+    p[3 * P + (top >> 2)] = -il;
+    p[3 * P + (bot >> 2)] = rl;
+  }
+}
+
+// One K chunk of Aop Bop^T (M = 128, N = 32: real and imaginary columns), each real
+// product in three TF32 terms: hi*hi into D (TMEM columns +0..31), hi*lo and lo*hi into E
+// (+32..63), 6 MMAs per 8-wide K step.  Issued by one thread; the chunk's first MMA into
+// D and into E overwrites.  Descriptors advance by integer adds (16-byte units; shared
+// memory addresses stay below 2^18 bytes, inside the 14-bit field).
 __device__ __forceinline__ void issue_chunk(uint32_t tcols, uint32_t a_base, uint32_t b_base,
-                                            int ksteps, bool conj_b) {
+                                            int ksteps) {
   const uint32_t sbo = tc::band_bytes(DN_KC);
-  const uint32_t id_pos = tc::idesc_tf32(128, DN_NB, false);
-  const uint32_t id_neg = tc::idesc_tf32(128, DN_NB, true);
-  // (A plane pair, B plane pair, destination: 0 re / 1 im, negated)
-  const int ap[4] = {0, 2, 0, 2}, bp[4] = {0, 2, 2, 0}, dst[4] = {0, 0, 1, 1};
-  const bool neg[4] = {false, !conj_b, conj_b, false};
-  bool first[4] = {true, true, true, true};  // D re, D im, E re, E im
+  const uint64_t da = tc::smem_desc(a_base, tc::LBO, sbo), db = tc::smem_desc(b_base, tc::LBO, sbo);
+  constexpr uint64_t PA = DN_PLANE_A >> 4, PB = DN_PLANE_B >> 4;
+  constexpr uint32_t id = tc::idesc_tf32(128, 2 * DN_NB, false);
+  const uint32_t td = tcols, te = tcols + 2 * DN_NB;
   for (int ks = 0; ks < ksteps; ++ks) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      // hi*hi -> D; hi*lo, lo*hi -> E
-      const int at[3] = {0, 0, 1}, bt[3] = {0, 1, 0};
-#pragma unroll
-      for (int tt = 0; tt < 3; ++tt) {
-        const int region = dst[q] + (tt ? 2 : 0);
-        const uint32_t a = a_base + (uint32_t)(ap[q] + at[tt]) * DN_PLANE_A + ks * 2 * tc::LBO;
-        const uint32_t b = b_base + (uint32_t)(bp[q] + bt[tt]) * DN_PLANE_B + ks * 2 * tc::LBO;
-        tc::mma_tf32(tcols + (uint32_t)DN_NB * region, tc::smem_desc(a, tc::LBO, sbo),
-                     tc::smem_desc(b, tc::LBO, sbo), neg[q] ? id_neg : id_pos, !first[region]);
-        first[region] = false;
-      }
-    }
+    const uint64_t k = (uint64_t)ks * (2 * tc::LBO >> 4);
+    const bool acc = ks > 0;
+    tc::mma_tf32(td, da + k, db + k, id, acc);                    // Ar hi . B1 hi
+    tc::mma_tf32(td, da + 2 * PA + k, db + 2 * PB + k, id, true);  // Ai hi . B2 hi
+    tc::mma_tf32(te, da + k, db + PB + k, id, acc);               // Ar hi . B1 lo
+    tc::mma_tf32(te, da + PA + k, db + k, id, true);              // Ar lo . B1 hi
+    tc::mma_tf32(te, da + 2 * PA + k, db + 3 * PB + k, id, true);  // Ai hi . B2 lo
+    tc::mma_tf32(te, da + 3 * PA + k, db + 2 * PB + k, id, true);  // Ai lo . B2 hi
   }
 }
 
@@ -258,7 +279,7 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
     for (int kc = 0; kc < nchunks && ok; ++kc) {
       const int b = buf;
       store_chunk(cha, a_planes + b * DN_BUF_A, DN_PLANE_A);
-      store_chunk(chb, b_planes + b * DN_BUF_B, DN_PLANE_B);
+      store_chunk_b(chb, b_planes + b * DN_BUF_B, conj_b);
       tc::fence_smem_to_async();
       tc::fence_before();
       __syncthreads();
@@ -266,7 +287,7 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
       if (tid == 0) {
         const int ksteps = min(4, (d - kc * DN_KC + 7) >> 3);
         issue_chunk(taddr + (uint32_t)(4 * DN_NB * b), smem_u32(a_planes + b * DN_BUF_A),
-                    smem_u32(b_planes + b * DN_BUF_B), ksteps, conj_b);
+                    smem_u32(b_planes + b * DN_BUF_B), ksteps);
         tc::mma_commit(&bar[b]);
       }
       pend[b] = true;
