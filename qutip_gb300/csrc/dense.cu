@@ -13,7 +13,7 @@
 // Work split: CTA j owns the 16 output columns [16 j, 16 j + 16) of every product; column n
 // of A X, X A^dag, T = X C^dag and C T needs only column n of X, of A^dag, of C^dag and of
 // T, so the CTAs never exchange data and T's block stays in the CTA's shared memory.
-// One CTA of 256 threads computes Y = Aop Bop^T (M = 128 rows, N = 16 columns) in K chunks
+// One CTA of 512 threads computes Y = Aop Bop^T (M = 128 rows, N = 16 columns) in K chunks
 // of 32: every thread writes its share of the chunk's operand planes (real / imaginary x
 // TF32 hi / lo) into one of two shared-memory buffers, one thread issues the 6 MMAs per
 // 8-wide K step (real and imaginary output columns side by side, N = 32), and while they run the block loads the next chunk's operands into
@@ -33,9 +33,10 @@
 
 namespace qg {
 
-constexpr int DN_THREADS = 256;
+constexpr int DN_THREADS = 512;
 constexpr int DN_KC = 32;                          // K chunk
 constexpr int DN_NB = 16;                          // output columns per CTA (MMA N)
+constexpr int DN_CW = 8;                           // columns of one part per thread
 constexpr uint32_t DN_PLANE_A = 128u * DN_KC * 4u;  // one A-operand plane (M = 128 rows)
 constexpr uint32_t DN_PLANE_B = 2 * DN_NB * DN_KC * 4u;  // one B-operand plane (N = 32 rows)
 constexpr uint32_t DN_BUF_A = 4u * DN_PLANE_A, DN_BUF_B = 4u * DN_PLANE_B;
@@ -236,18 +237,20 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
   const uint32_t taddr = taddr_s;
   DenseCtx c{&L, x, d, n0, 0, ca, t_blk};
   const int nchunks = (d + DN_KC - 1) / DN_KC;
-  // Thread roles when reading tensor memory: warps 0-3 the real part, 4-7 the imaginary
-  // part; warp w reads TMEM lanes 32 (w % 4) ... (its rows m).
-  const int part = warp >> 2;
+  // Thread roles when reading tensor memory: warp w reads TMEM lanes 32 (w % 4) ... (its
+  // rows m), the real (part 0) or imaginary (part 1) columns of bit 2 of w, and of those the
+  // 8 columns cw0 ... cw0 + 7 chosen by bit 3.
+  const int part = (warp >> 2) & 1;
+  const int cw0 = DN_CW * (warp >> 3);
   const int m = 32 * (warp & 3) + lane;
   const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
   unsigned par[2] = {0u, 0u};
   bool pend[2] = {false, false};  // a commit to bar[b] not yet waited for
   bool ok = true;
   int buf = 0;
-  float prod[DN_NB], gen[DN_NB];
+  float prod[DN_CW], gen[DN_CW];
 #pragma unroll
-  for (int j = 0; j < DN_NB; ++j) gen[j] = 0.f;
+  for (int j = 0; j < DN_CW; ++j) gen[j] = 0.f;
 
   auto wait_buf = [&](int b) {
     const bool r = __syncthreads_and(mbar_poll(&bar[b], par[b]) ? 1 : 0) != 0;
@@ -258,14 +261,14 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
     tc::fence_after();
     return r;
   };
-  // add D + E of buffer b (this thread's part, rows m, 16 columns) into prod
+  // add D + E of buffer b (this thread's part, row m, 8 columns) into prod
   auto take = [&](int b, bool first) {
-    float dv[DN_NB], ev[DN_NB];
-    const uint32_t cols = taddr + lane_base + (uint32_t)(4 * DN_NB * b + DN_NB * part);
-    tc::tmem_ld16(cols, dv);
-    tc::tmem_ld16(cols + 2 * DN_NB, ev);
+    float dv[DN_CW], ev[DN_CW];
+    const uint32_t cols = taddr + lane_base + (uint32_t)(4 * DN_NB * b + DN_NB * part + cw0);
+    tc::tmem_ld8(cols, dv);
+    tc::tmem_ld8(cols + 2 * DN_NB, ev);
 #pragma unroll
-    for (int j = 0; j < DN_NB; ++j) {
+    for (int j = 0; j < DN_CW; ++j) {
       const float v = dv[j] + ev[j];
       prod[j] = first ? v : prod[j] + v;
     }
@@ -311,12 +314,12 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
   };
   auto accumulate = [&](float w) {
 #pragma unroll
-    for (int j = 0; j < DN_NB; ++j) gen[j] = fmaf(w, prod[j], gen[j]);
+    for (int j = 0; j < DN_CW; ++j) gen[j] = fmaf(w, prod[j], gen[j]);
   };
 
   gemm(SRC_OPA, SRC_XB, false);  // A X
 #pragma unroll
-  for (int j = 0; j < DN_NB; ++j) gen[j] = prod[j];
+  for (int j = 0; j < DN_CW; ++j) gen[j] = prod[j];
   gemm(SRC_XA, SRC_OPA, true);   // X A^dag
   accumulate(1.f);
   for (int i = 0; i < L.n_cops && ok; ++i) {
@@ -324,7 +327,7 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
     gemm(SRC_XA, SRC_OPC, true);  // T = X C^dag, this CTA's columns
     float* tp = reinterpret_cast<float*>(t_blk) + part;
 #pragma unroll
-    for (int j = 0; j < DN_NB; ++j) tp[2 * (j * DN_TS + m)] = prod[j];
+    for (int j = 0; j < DN_CW; ++j) tp[2 * ((cw0 + j) * DN_TS + m)] = prod[j];
     __syncthreads();
     gemm(SRC_OPC, SRC_TB, false);  // C T
     accumulate(wc[i]);
@@ -335,7 +338,7 @@ __global__ void __launch_bounds__(DN_THREADS, 1)
     // real and imaginary parts meet in shared memory (the A planes are free now)
     float* ex = reinterpret_cast<float*>(a_planes) + part;
 #pragma unroll
-    for (int j = 0; j < DN_NB; ++j) ex[2 * (j * 128 + m)] = gen[j];
+    for (int j = 0; j < DN_CW; ++j) ex[2 * ((cw0 + j) * 128 + m)] = gen[j];
     __syncthreads();
     const float2* exv = reinterpret_cast<const float2*>(a_planes);
     const int ncols = min(DN_NB, d - n0);
