@@ -300,6 +300,23 @@ class Server:
         return jobs, time.perf_counter() - t0
 
 
+def serve_plain(jobs, precision="double"):
+    """The plain per-request drop-in served in real time: one request at a time in arrival
+    order (a single FIFO server), each solved by :func:`solve_plain` once it has arrived.
+    Sets ``result`` and ``done`` of every job; returns the wall time."""
+    order = sorted(jobs, key=lambda j: j.spec.arrival)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for j in order:
+        wait = j.spec.arrival - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        j.result = solve_plain(j, precision)
+        torch.cuda.synchronize()
+        j.done = time.perf_counter() - t0
+    return time.perf_counter() - t0
+
+
 def solve_plain(job: Job, precision="double"):
     """The plain per-request drop-in: one job alone, complex128, no batching across
     requests -- ``mesolve`` through the single-system integrator, ``mcsolve`` through
