@@ -377,6 +377,30 @@ def stage_bytes(op, n, stage, mixed):
     return b
 
 
+def stage_fp64_fmas(op, n, stage):
+    """Algorithmic FP64 fused multiply-adds of one complex128 fused Vern7 stage launch: the
+    generator (two per nonzero real or imaginary part of the operator with the real /
+    imaginary split dictionary, four per complex entry otherwise; two per row per
+    time-dependent group for its coefficient) and the stage combination (two per row per
+    nonzero tableau factor; the WRMS error adds four per row at the last stage)."""
+    import torch
+    from qutip_gb300 import vern7_tableau as T
+    if getattr(op, "dict_split", False):
+        gen = 2 * int(torch.count_nonzero(op.col).item())
+    else:
+        gen = 4 * int(op.nnz)
+    gen += 2 * n * sum(1 for c in getattr(op, "coeffs", []) if c is not None)
+    if stage == T.RK_STEP - 1:
+        comb = 2 * n * sum(1 for j in range(T.RK_STEP) if T.B[j] != 0)
+        comb += 2 * n * sum(1 for j in range(T.RK_STEP) if T.E[j] != 0) + 4 * n
+    else:
+        comb = 2 * n * sum(1 for j in range(stage + 1) if T.A[stage + 1][j] != 0)
+    return gen + comb
+
+
+#: FP64 peak of GB300 (nominal): 2 FP64 FMAs per clock per SM x 152 SMs x 2.07 GHz x 2
+FP64_PEAK_TFLOPS = 2 * 152 * 2.07e9 * 2 / 1e12
+
 TRAFFIC_PROFILE = "profiles/spmv_dict_c128_ising_L10_stage.md"
 SLICED_PROFILE = "profiles/spmv_sliced_ising_L10_stage.md"
 
@@ -393,9 +417,10 @@ def profiled_traffic(path=TRAFFIC_PROFILE):
     return None
 
 
-def measure_stage_roofline(op, state0, precision, reps=20):
+def measure_stage_roofline(op, state0, precision, reps=20, fmas=None):
     """Average duration and algorithmic GB/s of the fused stage kernel (events on its stream),
-    from the initial state ``state0`` (host vector)."""
+    from the initial state ``state0`` (host vector); ``fmas`` (a list) receives the average
+    algorithmic FP64 FMAs per launch."""
     import ctypes as C
     import torch
     from qutip_gb300 import _lib
@@ -420,6 +445,8 @@ def measure_stage_roofline(op, state0, precision, reps=20):
     e1.synchronize()
     ms = e0.elapsed_time(e1) / (reps * 10)
     per_launch = total_bytes / 10
+    if fmas is not None:
+        fmas.append(sum(stage_fp64_fmas(op, ig.n, s) for s in range(10)) / 10)
     return ms, per_launch, per_launch / (ms * 1e-3) / 1e9
 
 
@@ -850,6 +877,7 @@ def run_matrix_form(args, sysm, tlist, ex, want, hbm_peak):
            "solves_per_sec": 1.0 / float(np.median(times)),
            "rel_err_vs_reference_fp64": rel, "max_abs_err_vs_reference_fp64": absmax,
            "within_reference_tolerance": within,
+           "hermitian_branch": bool(lop.hermitian),
            "stage_kernel": {"kernel": "lindblad_kernel<C64,C128,RK>", "ms": ms,
                             "algorithmic_bytes": int(b), "gbs": gbs, "frac_hbm": gbs / hbm_peak,
                             "bound": "instruction issue (operators L1-resident, state "
@@ -988,7 +1016,9 @@ def run_ours(args, dist):
 
     log("roofline measurements")
     state0 = rho0.full().reshape(-1, order="F")
-    stage_ms, stage_b, stage_gbs = measure_stage_roofline(op, state0, "double")
+    fmas = []
+    stage_ms, stage_b, stage_gbs = measure_stage_roofline(op, state0, "double", fmas=fmas)
+    fp64_tflops = 2 * fmas[0] / (stage_ms * 1e-3) / 1e12
     spmv_ms, spmv_b, spmv_gbs = measure_spmv(op)
     st64_ms, st64_b, st64_gbs = measure_stage_roofline(op64, state0, "mixed")
     spmv64_ms, spmv64_b, spmv64_gbs = measure_spmv(op64)
@@ -1025,6 +1055,14 @@ def run_ours(args, dist):
                                 "spmv_sliced_kernel<C128,C128,RK> (fused Vern7 stage)"),
                      "bytes_per_launch": stage_b, "ms_per_launch": stage_ms,
                      "peak_source": f"{peak_src} hbm_gbs (of {peak_src})"},
+        "roofline_fp64": {"bound": "fp64", "achieved": fp64_tflops, "unit": "TFLOP/s",
+                          "peak": FP64_PEAK_TFLOPS, "frac": fp64_tflops / FP64_PEAK_TFLOPS,
+                          "fmas_per_launch": fmas[0], "ms_per_launch": stage_ms,
+                          "peak_source": "nominal: 2 FP64 FMAs per clock per SM x 152 SMs x "
+                                         "2.07 GHz (no measured FP64 peak)",
+                          "note": "the complex128 stage kernel is bound by the FP64 pipe "
+                                  "(sm__pipe_fp64_cycles_active 85 % of active cycles, "
+                                  f"{TRAFFIC_PROFILE}); its HBM fraction is the roofline key"},
         "spmv": {"c128_gbs": spmv_gbs, "c128_ms": spmv_ms, "c128_bytes": spmv_b,
                  "frac_c128": spmv_gbs / hbm_peak, "c64_gbs": spmv64_gbs, "c64_ms": spmv64_ms,
                  "c64_bytes": spmv64_b, "frac_c64": spmv64_gbs / hbm_peak},

@@ -161,6 +161,10 @@ typedef struct qg_lindblad {
   int32_t n_cops;
   int32_t a_diag_const; /* bit g: the diagonal of A_g is folded into d_const */
   int32_t n_const_diag; /* leading diagonal collapse operators folded into d_const */
+  int32_t hermitian;    /* 1: rho is Hermitian; elements r >= c are evaluated and mirrored
+                           (out[c + r d] = conj(out[r + c d]), real diagonal), the reference's
+                           assume_hermitian_state branch (lindblad_matrix_form.pyx:171-188) */
+  int32_t reserved;     /* 0 */
   int32_t a_width[QG_MAX_GROUPS];
   int32_t c_width[QG_MAX_COPS];
   const void* d_const;

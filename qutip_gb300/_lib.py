@@ -39,6 +39,7 @@ class Lindblad(C.Structure):
     _fields_ = [("d", C.c_int64), ("dtype", C.c_int32), ("n_groups", C.c_int32),
                 ("n_diag_cops", C.c_int32), ("n_cops", C.c_int32),
                 ("a_diag_const", C.c_int32), ("n_const_diag", C.c_int32),
+                ("hermitian", C.c_int32), ("reserved", C.c_int32),
                 ("a_width", C.c_int32 * QG_MAX_GROUPS), ("c_width", C.c_int32 * QG_MAX_COPS),
                 ("d_const", C.c_void_p), ("a_diag", C.c_void_p), ("a_col", C.c_void_p), ("a_val", C.c_void_p),
                 ("c_diag", C.c_void_p), ("c_col", C.c_void_p), ("c_val", C.c_void_p),

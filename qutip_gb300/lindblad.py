@@ -15,8 +15,11 @@ order, the same vector as the superoperator form, so the integrator, the expecta
 values and the outputs are shared with it.
 
 The reference computes ``A + A^dag`` when rho is Hermitian and the full form otherwise
-(lindblad_matrix_form.pyx:160-200); both are the same generator and this kernel always
-evaluates the full form, which also evolves non-Hermitian rho.
+(lindblad_matrix_form.pyx:160-200).  ``hermitian = True`` is that branch here: the kernel
+evaluates the elements on and below the diagonal only and writes each one's conjugate to
+its mirror (real diagonal), half the generator's work; ``False`` evaluates every element
+and also evolves non-Hermitian rho.  The plugin follows the reference's choice
+(``LindbladMatrixForm.assume_hermitian_state``, set by mesolve from ``rho0.isherm``).
 """
 from __future__ import annotations
 
@@ -183,6 +186,7 @@ class LindbladOperator:
         st.n_cops = self.n_cops
         st.a_diag_const = self.a_diag_const
         st.n_const_diag = self.n_const_diag
+        st.hermitian = int(getattr(self, "_hermitian", False))
         st.d_const = _ptr(self.d_const)
         for g, w in enumerate(self.a_width):
             st.a_width[g] = w
@@ -210,6 +214,16 @@ class LindbladOperator:
 
     # -- properties ---------------------------------------------------------
     @property
+    def hermitian(self) -> bool:
+        """Evaluate only the elements r >= c and mirror them (rho Hermitian)."""
+        return bool(getattr(self, "_hermitian", False))
+
+    @hermitian.setter
+    def hermitian(self, value: bool):
+        self._hermitian = bool(value)
+        self.struct.hermitian = int(self._hermitian)
+
+    @property
     def n_groups(self) -> int:
         return len(self.a_terms)
 
@@ -222,7 +236,8 @@ class LindbladOperator:
         return ("lindblad", 0, 1)
 
     def launch_desc(self) -> str:
-        return f"matrix-free Lindblad (d={self.d}, {self.n_cops} collapse operators)"
+        half = ", Hermitian rho: half the elements" if self.hermitian else ""
+        return f"matrix-free Lindblad (d={self.d}, {self.n_cops} collapse operators{half})"
 
     def tune(self, *args, **kwargs):
         """One launch shape (one thread per element, grid from the occupancy query)."""

@@ -814,6 +814,10 @@ class IntegratorGpuVern7(Integrator):
                              f"{self._op.n_rows}")
         if self._ode.op is not op:
             self._ode = self._integrator(op)
+        if isinstance(op, LindbladOperator):
+            # the reference's branch choice: MESolver._prepare_state sets it from rho0.isherm
+            # (qutip/solver/mesolve.py:270-277; lindblad_matrix_form.pyx:171-200)
+            op.hermitian = bool(getattr(self._rhs(), "assume_hermitian_state", False))
         self._ode.set_initial_value(_as_gpu(state0).buf, t)
         self._shape = state0.shape
         self._is_set = True

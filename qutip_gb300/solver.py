@@ -165,6 +165,11 @@ def solve_system(system: OpenSystem, tlist, options=None, op: DeviceOperator | N
                   max_step=opt["max_step"], interpolate=opt["interpolate"], precision=prec)
     rho0 = np.asarray(system.state0, dtype=np.complex128)
     d = system.dim
+    if isinstance(op, LindbladOperator):
+        # the reference's branch: A + A^dag when rho0 is Hermitian (mesolve.py:270-277;
+        # Qobj.isherm at the default atol 1e-12)
+        r = rho0.reshape(d, d, order="F")
+        op.hermitian = bool(np.all(np.abs(r - r.conj().T) <= 1e-12))
     tr0 = np.trace(rho0.reshape(d, d, order="F"))
     normalize = opt["normalize_output"] and abs(tr0 - 1) <= 1e-12
     ig.set_initial_value(torch.from_numpy(rho0).to(op.device), float(tlist[0]))

@@ -91,6 +91,46 @@ def test_apply_matches_the_superoperator(dev, dtype, case):
         assert np.abs(got - want).max() <= tol * scale, (case, t)
 
 
+@pytest.mark.parametrize("dtype", ["c128", "c64"])
+@pytest.mark.parametrize("case", ["jc", "random37", "random100"])
+def test_hermitian_half_matches_the_superoperator(dev, dtype, case):
+    """The Hermitian branch (elements r >= c evaluated, mirrored as conjugates): on a
+    Hermitian rho it equals the superoperator product within the full form's tolerance,
+    its output is exactly Hermitian with a real diagonal, and it agrees with the full form."""
+    from qutip_gb300 import systems as S
+    from qutip_gb300.lindblad import LindbladOperator
+    if case == "jc":
+        s = S.jaynes_cummings(n_cav=6)
+        lop = LindbladOperator.from_hamiltonian(s.h_terms, s.c_ops, dtype=dtype)
+    else:
+        h_terms, cops, LO = _random_generator(int(case[6:]), seed=int(case[6:]))
+        lop = LO.from_hamiltonian(h_terms, cops, dtype=dtype)
+    d = lop.d
+    rng = np.random.default_rng(5)
+    m = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    rho = (m + m.conj().T).astype(np.complex64 if dtype == "c64" else np.complex128)
+    x = torch.from_numpy(rho.reshape(-1, order="F").copy()).to(dev)
+    xs = rho.astype(np.complex128).reshape(-1, order="F")
+    tol = 1e-12 if dtype == "c128" else 2e-6
+    for t in (0.0, 0.83):
+        L = _kron_generator(lop.a_terms, lop.c_terms, t)
+        want = L @ xs
+        scale = (abs(L) @ abs(xs)).max()
+        lop.hermitian = True
+        yh = torch.empty_like(x)
+        lop.matvec(t, x, yh)
+        lop.hermitian = False
+        yf = torch.empty_like(x)
+        lop.matvec(t, x, yf)
+        gh = yh.cpu().numpy().astype(np.complex128)
+        gf = yf.cpu().numpy().astype(np.complex128)
+        assert np.abs(gh - want).max() <= tol * scale, (case, t)
+        assert np.abs(gh - gf).max() <= tol * scale, (case, t)
+        M = gh.reshape(d, d, order="F")
+        np.testing.assert_array_equal(M, M.conj().T)
+        assert np.all(np.diag(M).imag == 0)
+
+
 @pytest.mark.parametrize("case", ["jc", "ising"])
 def test_matrix_form_solve_matches_the_oracle(dev, case):
     from oracle.solvers import mesolve as oracle_mesolve
@@ -201,6 +241,25 @@ def test_plugin_non_hermitian_rho(qt):
         np.testing.assert_allclose(g.full(), r.full(), atol=1e-7)
         np.testing.assert_allclose(g.full(), s.full(), atol=1e-7)
         assert abs(g.full()[0, 1] - e) <= 1e-6
+
+
+def test_plugin_follows_the_references_hermitian_branch(qt):
+    """mesolve's matrix form takes the reference's A + A^dag branch for a Hermitian rho0
+    and the full form for a non-Hermitian one (MESolver._prepare_state sets
+    assume_hermitian_state from rho0.isherm); both match the reference's own runs."""
+    a = qt.destroy(N)
+    H, c_ops = a.dag() * a + 0.3 * (a + a.dag()), [np.sqrt(KAPPA) * a]
+    opts = {"method": "gpu_vern7", "matrix_form": True, "progress_bar": None}
+    tl = np.linspace(0, 3, 31)
+    for rho0, herm in ((qt.coherent_dm(N, 0.8), True),
+                       (qt.basis(N, 0) * qt.basis(N, 1).dag(), False)):
+        solver = qt.MESolver(H, c_ops, options=opts)
+        got = solver.run(rho0, tl)
+        assert solver._integrator._op.hermitian is herm
+        ref = qt.mesolve(H, rho0, tl, c_ops, options={"method": "vern7", "matrix_form": True,
+                                                      "progress_bar": None})
+        for g, r in zip(got.states, ref.states):
+            np.testing.assert_allclose(g.full(), r.full(), atol=1e-7)
 
 
 def test_plugin_jaynes_cummings_mixed_precision(qt):
