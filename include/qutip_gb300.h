@@ -361,6 +361,9 @@ typedef struct qg_batch_system {
   int32_t n_cops;
   int32_t nsteps;    /* maximum steps per output interval (reference option nsteps) */
   double atol, rtol;
+  int64_t cop_coef_off; /* n_cops program starts in coef_start, collapse operator c being
+                           f_c(t) C_c (mcsolve.py:168-170 wraps every c_op in a QobjEvo);
+                           -1: constant collapse operators */
 } qg_batch_system;
 
 /* One unit of work: a system solved from an initial state, or one trajectory

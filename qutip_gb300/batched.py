@@ -39,7 +39,8 @@ SYSTEM_DTYPE = np.dtype([("n", "<i4"), ("d", "<i4"), ("n_groups", "<i4"), ("n_eo
                          ("rp_off", "<i8"), ("coef_off", "<i8"), ("eop_rp_off", "<i8"),
                          ("cop_rp_off", "<i8"), ("tlist_off", "<i8"), ("n_out", "<i4"),
                          ("kind", "<i4"), ("n_cops", "<i4"), ("nsteps", "<i4"),
-                         ("atol", "<f8"), ("rtol", "<f8")], align=True)
+                         ("atol", "<f8"), ("rtol", "<f8"), ("cop_coef_off", "<i8")],
+                        align=True)
 ITEM_DTYPE = np.dtype([("system", "<i4"), ("pad", "<i4"), ("y0_off", "<i8"), ("out_off", "<i8"),
                        ("sh", "<u8"), ("sl", "<u8"), ("ih", "<u8"), ("il", "<u8"),
                        ("floor", "<f8")], align=True)
@@ -125,9 +126,36 @@ class BatchProblem:
         self._out_len = 0
         self.sys_info = []
 
+    def _add_programs(self, coeffs) -> int:
+        """Append the coefficient programs of ``coeffs`` (None: constant 1) to the launch's
+        pools; returns the offset of their starts in ``coef_start``, or -1 when all are
+        constant."""
+        if all(c is None for c in coeffs):
+            return -1
+        code, starts, consts = pack_programs(coeffs)
+        # starts index the global code pool; constants are shifted inside the code
+        code = code.copy()
+        i = 0
+        while i < len(code):
+            if code[i] == 1:  # OP_CONST
+                code[i + 1] += self._const_len // 2
+                i += 1
+            i += 1
+        self._coef_code.append(code)
+        self._coef_start.append(starts + self._code_len)
+        self._coef_consts.append(consts)
+        off = self._start_len
+        self._code_len += len(code)
+        self._start_len += len(starts)
+        self._const_len += len(consts)
+        return off
+
     def add_system(self, terms, e_ops, tlist, kind="me", c_ops=(), dim=None, atol=1e-8,
                    rtol=1e-6, nsteps=1000) -> int:
-        """Register a generator (list of (matrix, coefficient)), its e_ops and tlist."""
+        """Register a generator (list of (matrix, coefficient)), its e_ops and tlist.
+        ``c_ops`` (trajectories): matrices, or ``(matrix, Coefficient | None)`` pairs for
+        collapse operators ``f(t) C``; the generator must then carry their
+        ``-1/2 |f|^2 C^dag C`` terms, as the reference's H_nh does."""
         terms = merge_terms(terms)
         if len(terms) > _lib.QG_MAX_GROUPS:
             raise ValueError(f"at most {_lib.QG_MAX_GROUPS} coefficient groups")
@@ -143,26 +171,7 @@ class BatchProblem:
         rp_off = self._rp_len
         self._rp_len += len(rp)
         self._entries += len(col)
-        coeffs = [c for _, c in terms]
-        if all(c is None for c in coeffs):
-            coef_off = -1
-        else:
-            code, starts, consts = pack_programs(coeffs)
-            # starts index the global code pool; constants are shifted inside the code
-            code = code.copy()
-            i = 0
-            while i < len(code):
-                if code[i] == 1:  # OP_CONST
-                    code[i + 1] += self._const_len // 2
-                    i += 1
-                i += 1
-            self._coef_code.append(code)
-            self._coef_start.append(starts + self._code_len)
-            self._coef_consts.append(consts)
-            coef_off = self._start_len
-            self._code_len += len(code)
-            self._start_len += len(starts)
-            self._const_len += len(consts)
+        coef_off = self._add_programs([c for _, c in terms])
         e_rp, e_col, e_val = _group_major(e_ops, d)
         self._eop_rp.append(e_rp + self._eop_entries)
         self._eop_col.append(e_col)
@@ -170,7 +179,9 @@ class BatchProblem:
         eop_rp_off = self._eop_rp_len
         self._eop_rp_len += len(e_rp)
         self._eop_entries += len(e_col)
-        c_rp, c_col, c_val = _group_major(list(c_ops), d)
+        c_ops = [c if isinstance(c, tuple) else (c, None) for c in c_ops]
+        cop_coef_off = self._add_programs([f for _, f in c_ops])
+        c_rp, c_col, c_val = _group_major([m for m, _ in c_ops], d)
         self._cop_rp.append(c_rp + self._cop_entries)
         self._cop_col.append(c_col)
         self._cop_val.append(c_val)
@@ -183,7 +194,7 @@ class BatchProblem:
         self._tlist_len += len(tl)
         self.systems.append((n, d, len(terms), len(e_ops), rp_off, coef_off, eop_rp_off,
                              cop_rp_off, tlist_off, len(tl), 0 if kind == "me" else 1,
-                             len(c_ops), int(nsteps), float(atol), float(rtol)))
+                             len(c_ops), int(nsteps), float(atol), float(rtol), cop_coef_off))
         self.sys_info.append(dict(n=n, d=d, kind=kind, n_eops=len(e_ops), n_out=len(tl),
                                   nnz=len(col), tlist=tl, rp_len=len(rp)))
         return len(self.systems) - 1

@@ -806,11 +806,19 @@ __device__ __noinline__ void record(const GT& g, const Ctx<DT>& X, const Ctl& c,
   g.sync();
 }
 
-// ||c_i psi||^2 for psi in ctmp[0]; optionally store c_i psi in ctmp[1]
+// ||c_i(t) psi||^2 for psi in ctmp[0]; optionally store c_i(t) psi in ctmp[1].
+// c_i(t) = f_i(t) C_i for a time-dependent collapse operator (the product with f_i after
+// the row sum, as the reference's QobjEvo matmul scales a term's product).
 template <int DT, class GT>
-__device__ double cop_apply(const GT& g, Ctx<DT>& X, int i, bool store) {
+__device__ double cop_apply(const GT& g, Ctx<DT>& X, int i, bool store, double t) {
   const int d = X.d;
   const int* rp = X.B->cop_rp + X.S->cop_rp_off + (int64_t)i * (d + 1);
+  const bool scaled = X.S->cop_coef_off >= 0;
+  cplx f{1.0, 0.0};
+  if (scaled) {
+    const int st = __ldg(X.B->coef_start + X.S->cop_coef_off + i);
+    f = eval_coef(X.B->coef_code + st, X.B->coef_consts, t);
+  }
   double acc = 0.0;
   for (int r = g.rank; r < d; r += GT::SIZE) {
     const int s = __ldg(rp + r), e = __ldg(rp + r + 1);
@@ -821,6 +829,11 @@ __device__ double cop_apply(const GT& g, Ctx<DT>& X, int i, bool store) {
       const double2 z = X.ctmp[0][col];
       sr += vr * z.x - vi * z.y;
       si += vr * z.y + vi * z.x;
+    }
+    if (scaled) {
+      const double fr = f.re * sr - f.im * si;
+      si = f.re * si + f.im * sr;
+      sr = fr;
     }
     if (store) X.ctmp[1][r] = make_double2(sr, si);
     acc += sr * sr + si * si;
@@ -960,14 +973,14 @@ __device__ void run_item(const GT& g, const qg_batch& B, Ctx<DT>& X, int item) {
           // sum of the jump probabilities, then the reference's walk over them;
           // each probability is recomputed (bit-identical, no per-operator array)
           double sum = 0.0;
-          for (int i = 0; i < nc; ++i) sum += cop_apply(g, X, i, false);
-          double tgt = sum * pcg_random(rng) - cop_apply(g, X, 0, false);
+          for (int i = 0; i < nc; ++i) sum += cop_apply(g, X, i, false, t_guess);
+          double tgt = sum * pcg_random(rng) - cop_apply(g, X, 0, false, t_guess);
           while (tgt > 0 && which < nc - 1) {
             ++which;
-            tgt -= cop_apply(g, X, which, false);
+            tgt -= cop_apply(g, X, which, false, t_guess);
           }
         }
-        const double new_norm = sqrt(cop_apply(g, X, which, true));
+        const double new_norm = sqrt(cop_apply(g, X, which, true, t_guess));
         if (new_norm < B.mc_corr_eps) {
           // the jump is numerical noise: renormalise the state, keep the target
           const double pn = sqrt(vec_norm2(g, X.ctmp[0], X.n));

@@ -898,6 +898,20 @@ def _constant_matrix(op, what):
     return _scipy(op.data)
 
 
+def _collapse_term(op):
+    """A collapse operator as ``(matrix, Coefficient | None)``: ``f(t) C`` for a
+    one-term QobjEvo (mcsolve.py:168-170 wraps every c_op in one), ``C`` for a constant
+    one.  The jump probabilities use ``|f(t)|^2 ||C psi||^2`` on the device; the solver's
+    H_nh already carries the ``-1/2 conj(f) f C^dag C`` terms."""
+    if isinstance(op, qutip.QobjEvo) and not op.isconstant:
+        terms = qobjevo_terms(op)
+        if len(terms) != 1:
+            raise TypeError("map='gpu' needs each time-dependent collapse operator to be a "
+                            "single term f(t) C")
+        return terms[0]
+    return (_constant_matrix(op, "collapse operators"), None)
+
+
 def _mc_map_items(task, values, task_args, task_kwargs):
     """Decode the trajectory task an ``MCSolver`` hands to its map.
 
@@ -999,7 +1013,7 @@ def gpu_map(task, values, task_args=None, task_kwargs=None, reduce_func=None, ma
     if not e_list:
         raise TypeError("map='gpu' needs e_ops")
     e_mats = [_constant_matrix(e, "e_ops") for e in e_list]
-    c_mats = [_constant_matrix(c, "collapse operators") for c in solver._c_ops]
+    c_mats = [_collapse_term(c) for c in solver._c_ops]
     terms = qobjevo_terms(solver.rhs())
     iopts = {**IntegratorGpuVern7.integrator_options,
              **{k: opts[k] for k in IntegratorGpuVern7.integrator_options if k in opts}}

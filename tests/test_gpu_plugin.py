@@ -181,6 +181,25 @@ def test_mcsolve_gpu_map_batched(qt, plugin):
         np.testing.assert_allclose(np.asarray(g), np.asarray(w), atol=2e-6)
 
 
+def test_mcsolve_gpu_map_time_dependent_collapse(qt, plugin):
+    """A collapse operator f(t) C with a string coefficient and one with a complex phase
+    (mcsolve.py:168-170): the device evaluates |f(t)|^2 ||C psi||^2 for the jump choice
+    and f(t) C psi for the jump; jump records and averages match the reference's own
+    serial run with the same seeds."""
+    H, c_ops, psi0, e_ops = _jc(qt, N=6)
+    a = qt.tensor(qt.destroy(6), qt.qeye(2))
+    sm = qt.tensor(qt.qeye(6), qt.sigmam())
+    c_td = [[np.sqrt(0.1) * a, "exp(-0.05*t)"], [np.sqrt(0.05) * sm, "exp(1j*t)*(1+0.5*sin(t))"]]
+    tl = np.linspace(0, 20, 101)
+    opts = {"method": "vern7", "map": "serial", "keep_runs_results": True}
+    ref = qt.mcsolve(H, psi0, tl, c_td, e_ops=e_ops, ntraj=24, seeds=11, options=opts)
+    got = qt.mcsolve(H, psi0, tl, c_td, e_ops=e_ops, ntraj=24, seeds=11,
+                     options={**opts, "method": "gpu_vern7", "map": "gpu"})
+    _same_jumps(_records(got), _records(ref))
+    for g, w in zip(got.expect, ref.expect):
+        np.testing.assert_allclose(np.asarray(g), np.asarray(w), atol=2e-6)
+
+
 def test_gpudense_data_layer(qt, plugin):
     from qutip.core import data as D
     rng = np.random.default_rng(7)
