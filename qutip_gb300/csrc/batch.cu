@@ -447,12 +447,11 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
         split_f(yi, shi, sli);
         X.ys[cur ^ 1][r] = make_float2(shr, shi);
         X.yl[cur ^ 1][r] = make_float2(slr, sli);
-        // WRMS error term (wrmn_error_dense, qutip/core/data/ode.pyx:27-52) as
-        // |e|^2 / (atol + rtol |y|)^2: the per-row ratio in FP32 from the float-float
-        // estimate and the state's float shadow, the sum over rows in FP64
-        const float er = erh + erl, ei = eih + eil;
-        const float sc = (float)X.S->atol + (float)X.S->rtol * sqrtf(shr * shr + shi * shi);
-        err_acc += (double)((er * er + ei * ei) / (sc * sc));
+        // WRMS error term in FP64 against the FP64 state (wrmn_error_dense,
+        // qutip/core/data/ode.pyx:27-52), written as |e|^2 / (atol + rtol |y|)^2
+        const double er = (double)erh + (double)erl, ei = (double)eih + (double)eil;
+        const double sc = X.S->atol + X.S->rtol * sqrt(yr * yr + yi * yi);
+        err_acc += (er * er + ei * ei) / (sc * sc);
       } else {
         CT er = 0, ei = 0;
         double yr = X.y[cur][r].x, yi = X.y[cur][r].y;

@@ -150,16 +150,12 @@ __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
         const double2 yp = static_cast<const double2*>(rk.y_prev)[row];
         const double2 yf = make_double2(yp.x + (double)inc.re, yp.y + (double)inc.im);
         static_cast<double2*>(rk.y_front)[row] = yf;
-        const float2 yfs = make_float2((float)yf.x, (float)yf.y);
-        static_cast<float2*>(rk.y_front_s)[row] = yfs;
-        // WRMS error term (wrmn_error_dense, qutip/core/data/ode.pyx:27-52) as
-        // |e|^2 / (atol + rtol |y|)^2 of the float-float estimate against the state: the
-        // per-row ratio in FP32 (seven significant digits; an FP64 square root and
-        // division per row would cost the last stage ~25 FP64 operations per row on a
-        // pipe running at 1/64 of FP32), the sum over rows in FP64.
-        const float er = erh + erl, ei = eih + eil;
-        const float sc = (float)rk.atol + (float)rk.rtol * sqrtf(yfs.x * yfs.x + yfs.y * yfs.y);
-        err_acc += (double)((er * er + ei * ei) / (sc * sc));
+        static_cast<float2*>(rk.y_front_s)[row] = make_float2((float)yf.x, (float)yf.y);
+        // WRMS error term in FP64 against the FP64 state (wrmn_error_dense,
+        // qutip/core/data/ode.pyx:27-52), written as |e|^2 / (atol + rtol |y|)^2
+        const double er = (double)erh + (double)erl, ei = (double)eih + (double)eil;
+        const double sc = rk.atol + rk.rtol * sqrt(yf.x * yf.x + yf.y * yf.y);
+        err_acc += (er * er + ei * ei) / (sc * sc);
         return;
       } else {
         // reference order: y_front = y_prev, then += fb_j k_j term by term
