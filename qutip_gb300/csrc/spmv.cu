@@ -567,118 +567,141 @@ __global__ void __launch_bounds__(LB_BLOCK)
   int nw1 = 0;  // leading general collapse operators of width 1
   while (nw1 < NE && L.c_width[nw1] == 1) ++nw1;
   double err_acc = 0.0;
-  // (r, c) of idx, advanced by the grid stride without a division per element
-  const int stride = gridDim.x * LB_BLOCK;
-  const int sc = stride / d, sr = stride - (stride / d) * d;
-  int idx = blockIdx.x * LB_BLOCK + threadIdx.x;
-  int c = idx / d;
-  int r = idx - c * d;
-  const bool herm = L.hermitian != 0;
-  for (; idx < n; idx += stride) {
-    // Hermitian rho: elements on and below the diagonal, each written to its mirror too
-    if (!herm || r >= c) {
-      const int cd = c * d;
-      // diagonal factor D(r, c): the precomputed constant part plus the time-dependent rest
-      R dr = 0, di = 0;
-      if (dconst) {
-        const ST p = __ldg(dconst + idx);
-        dr = p.x;
-        di = p.y;
-      }
-      for (int g = 0; g < G; ++g) {
-        if ((dmask >> g) & 1) continue;
-        const cx<R> k = ca[g];
-        const ST p = __ldg(adiag + g * d + r), q = __ldg(adiag + g * d + c);
-        dr += k.re * (p.x + q.x) - k.im * (p.y - q.y);  // k p + conj(k q)
-        di += k.re * (p.y - q.y) + k.im * (p.x + q.x);
-      }
-      for (int i = nd0; i < ND; ++i) {
-        const R w = wc[i];
-        const ST p = __ldg(cdiag + i * d + r), q = __ldg(cdiag + i * d + c);
-        dr += w * (p.x * q.x + p.y * q.y);  // w p conj(q)
-        di += w * (p.y * q.x - p.x * q.y);
-      }
-      const ST xe = ld_gather(x + idx);
-      cx<R> acc{dr * xe.x - di * xe.y, dr * xe.y + di * xe.x};
-      // off-diagonal A: A rho (row r against column c) and rho A^dag (row c against row r)
-      int base = 0;
-      for (int g = 0; g < G; ++g) {
-        const int W = L.a_width[g];
-        if (W == 0) continue;
-        R lr = 0, li = 0, qr = 0, qi = 0;
-  #pragma unroll 4
-        for (int j = 0; j < W; ++j) {
-          const int e = base + j * d;
-          const int cr = __ldg(acol + e + r), cc = __ldg(acol + e + c);
-          const ST vr = __ldg(aval + e + r), vc = __ldg(aval + e + c);
-          cmac_any(lr, li, vr, ld_gather(x + (cr + cd)));
-          cmac_conj(qr, qi, vc, ld_gather(x + (r + cc * d)));
-        }
-        const cx<R> k = ca[g];
-        acc.re += k.re * lr - k.im * li + k.re * qr + k.im * qi;
-        acc.im += k.re * li + k.im * lr + k.re * qi - k.im * qr;
-        base += W * d;
-      }
-      // general collapse operators: C rho C^dag.  The leading width-1 operators (s-, a, ...)
-      // run branch-free in complex64 (a padding entry has value 0 and a valid column), so
-      // the gathers of several operators are in flight at once: 56 -> 48 us per stage at
-      // L = 10.  The FP64-bound complex128 form skips padding instead.
-      base = 0;
-      int i = 0;
-  #pragma unroll 4
-      for (; i < nw1; ++i) {
-        const R w = wc[ND + i];
-        const int er = base + r, ec = base + c;
-        const ST b = __ldg(cval + ec), v = __ldg(cval + er);
-        if constexpr (DT == QG_C128) {  // FP64-bound: skip padding rather than multiply by 0
-          if ((b.x == (R)0 && b.y == (R)0) || (v.x == (R)0 && v.y == (R)0)) {
-            base += d;
-            continue;
-          }
-        }
-        const ST xv = ld_gather(x + (__ldg(ccol + er) + __ldg(ccol + ec) * d));
-        const R pr = w * (v.x * b.x + v.y * b.y), pi = w * (v.y * b.x - v.x * b.y);  // w v conj(b)
-        acc.re += pr * xv.x - pi * xv.y;
-        acc.im += pr * xv.y + pi * xv.x;
-        base += d;
-      }
-      for (; i < NE; ++i) {
-        const int W = L.c_width[i];
-        const R w = wc[ND + i];
-        if (W > 0) {
-          R sr2 = 0, si2 = 0;
-          for (int q = 0; q < W; ++q) {
-            const int eq = base + q * d + c;
-            const ST b = __ldg(cval + eq);
-            if (b.x == (R)0 && b.y == (R)0) continue;  // warp-uniform: padding of row c
-            const int kd = __ldg(ccol + eq) * d;
-            R ir = 0, ii = 0;
-            for (int p = 0; p < W; ++p) {
-              const int ep = base + p * d + r;
-              const ST v = __ldg(cval + ep);
-              if (v.x != (R)0 || v.y != (R)0) cmac_any(ir, ii, v, ld_gather(x + (__ldg(ccol + ep) + kd)));
-            }
-            sr2 += b.x * ir + b.y * ii;  // conj(b) * inner
-            si2 += b.x * ii - b.y * ir;
-          }
-          acc.re += w * sr2;
-          acc.im += w * si2;
-        }
-        base += W * d;
-      }
-      if (herm) {
-        if (r == c)
-          acc.im = 0;  // A + A^dag: real diagonal
-        else
-          epilogue<DT, YDT, EPI>(c + r * d, cx<R>{acc.re, -acc.im}, ax, rk, err_acc);
-      }
-      epilogue<DT, YDT, EPI>(idx, acc, ax, rk, err_acc);
+  // L[x] at (r, c)
+  auto element = [&](int r, int c) -> cx<R> {
+    const int cd = c * d;
+    // diagonal factor D(r, c): the precomputed constant part plus the time-dependent rest
+    R dr = 0, di = 0;
+    if (dconst) {
+      const ST p = __ldg(dconst + (r + cd));
+      dr = p.x;
+      di = p.y;
     }
-    c += sc;
-    r += sr;
-    if (r >= d) {
-      r -= d;
-      ++c;
+    for (int g = 0; g < G; ++g) {
+      if ((dmask >> g) & 1) continue;
+      const cx<R> k = ca[g];
+      const ST p = __ldg(adiag + g * d + r), q = __ldg(adiag + g * d + c);
+      dr += k.re * (p.x + q.x) - k.im * (p.y - q.y);  // k p + conj(k q)
+      di += k.re * (p.y - q.y) + k.im * (p.x + q.x);
+    }
+    for (int i = nd0; i < ND; ++i) {
+      const R w = wc[i];
+      const ST p = __ldg(cdiag + i * d + r), q = __ldg(cdiag + i * d + c);
+      dr += w * (p.x * q.x + p.y * q.y);  // w p conj(q)
+      di += w * (p.y * q.x - p.x * q.y);
+    }
+    const ST xe = ld_gather(x + (r + cd));
+    cx<R> acc{dr * xe.x - di * xe.y, dr * xe.y + di * xe.x};
+    // off-diagonal A: A rho (row r against column c) and rho A^dag (row c against row r)
+    int base = 0;
+    for (int g = 0; g < G; ++g) {
+      const int W = L.a_width[g];
+      if (W == 0) continue;
+      R lr = 0, li = 0, qr = 0, qi = 0;
+  #pragma unroll 4
+      for (int j = 0; j < W; ++j) {
+        const int e = base + j * d;
+        const int cr = __ldg(acol + e + r), cc = __ldg(acol + e + c);
+        const ST vr = __ldg(aval + e + r), vc = __ldg(aval + e + c);
+        cmac_any(lr, li, vr, ld_gather(x + (cr + cd)));
+        cmac_conj(qr, qi, vc, ld_gather(x + (r + cc * d)));
+      }
+      const cx<R> k = ca[g];
+      acc.re += k.re * lr - k.im * li + k.re * qr + k.im * qi;
+      acc.im += k.re * li + k.im * lr + k.re * qi - k.im * qr;
+      base += W * d;
+    }
+    // general collapse operators: C rho C^dag.  The leading width-1 operators (s-, a, ...)
+    // run branch-free in complex64 (a padding entry has value 0 and a valid column), so
+    // the gathers of several operators are in flight at once: 56 -> 48 us per stage at
+    // L = 10.  The FP64-bound complex128 form skips padding instead.
+    base = 0;
+    int i = 0;
+  #pragma unroll 4
+    for (; i < nw1; ++i) {
+      const R w = wc[ND + i];
+      const int er = base + r, ec = base + c;
+      const ST b = __ldg(cval + ec), v = __ldg(cval + er);
+      if constexpr (DT == QG_C128) {  // FP64-bound: skip padding rather than multiply by 0
+        if ((b.x == (R)0 && b.y == (R)0) || (v.x == (R)0 && v.y == (R)0)) {
+          base += d;
+          continue;
+        }
+      }
+      const ST xv = ld_gather(x + (__ldg(ccol + er) + __ldg(ccol + ec) * d));
+      const R pr = w * (v.x * b.x + v.y * b.y), pi = w * (v.y * b.x - v.x * b.y);  // w v conj(b)
+      acc.re += pr * xv.x - pi * xv.y;
+      acc.im += pr * xv.y + pi * xv.x;
+      base += d;
+    }
+    for (; i < NE; ++i) {
+      const int W = L.c_width[i];
+      const R w = wc[ND + i];
+      if (W > 0) {
+        R sr2 = 0, si2 = 0;
+        for (int q = 0; q < W; ++q) {
+          const int eq = base + q * d + c;
+          const ST b = __ldg(cval + eq);
+          if (b.x == (R)0 && b.y == (R)0) continue;  // warp-uniform: padding of row c
+          const int kd = __ldg(ccol + eq) * d;
+          R ir = 0, ii = 0;
+          for (int p = 0; p < W; ++p) {
+            const int ep = base + p * d + r;
+            const ST v = __ldg(cval + ep);
+            if (v.x != (R)0 || v.y != (R)0) cmac_any(ir, ii, v, ld_gather(x + (__ldg(ccol + ep) + kd)));
+          }
+          sr2 += b.x * ir + b.y * ii;  // conj(b) * inner
+          si2 += b.x * ii - b.y * ir;
+        }
+        acc.re += w * sr2;
+        acc.im += w * si2;
+      }
+      base += W * d;
+    }
+    return acc;
+  };
+  if (!L.hermitian) {
+    // (r, c) of idx, advanced by the grid stride without a division per element
+    const int stride = gridDim.x * LB_BLOCK;
+    const int sc = stride / d, sr = stride - (stride / d) * d;
+    int idx = blockIdx.x * LB_BLOCK + threadIdx.x;
+    int c = idx / d;
+    int r = idx - c * d;
+    for (; idx < n; idx += stride) {
+      epilogue<DT, YDT, EPI>(idx, element(r, c), ax, rk, err_acc);
+      c += sc;
+      r += sr;
+      if (r >= d) {
+        r -= d;
+        ++c;
+      }
+    }
+  } else {
+    // Hermitian rho: tiles of 32 rows x 8 columns on or below the diagonal; a warp
+    // evaluates 32 consecutive r of one column c (r >= c), then the block writes the
+    // conjugates to the mirrors (c, r) through shared memory, 8 consecutive c per row r.
+    __shared__ cx<R> tile[8][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int n_rt = (d + 31) / 32, n_cb = (d + 7) / 8;
+    for (int tau = blockIdx.x; tau < n_rt * n_cb; tau += gridDim.x) {
+      const int r0 = (tau % n_rt) * 32, c0 = (tau / n_rt) * 8;
+      if (r0 + 31 < c0) continue;  // above the diagonal (uniform over the block)
+      const int r = r0 + lane, c = c0 + w;
+      cx<R> acc{0, 0};
+      if (r < d && c < d && r >= c) {
+        acc = element(r, c);
+        if (r == c) acc.im = 0;  // A + A^dag: real diagonal
+        epilogue<DT, YDT, EPI>(r + c * d, acc, ax, rk, err_acc);
+      }
+      tile[w][lane] = acc;
+      __syncthreads();
+      const int ml = threadIdx.x & 7, rl = threadIdx.x >> 3;
+      const int mr = r0 + rl, mc = c0 + ml;  // the mirror of (mr, mc)
+      if (mr < d && mc < d && mr > mc) {
+        const cx<R> v = tile[ml][rl];
+        epilogue<DT, YDT, EPI>(mc + mr * d, cx<R>{v.re, -v.im}, ax, rk, err_acc);
+      }
+      __syncthreads();
     }
   }
   if constexpr (EPI == EPI_RK) {
