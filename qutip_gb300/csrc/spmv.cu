@@ -677,29 +677,36 @@ __global__ void __launch_bounds__(LB_BLOCK)
       }
     }
   } else {
-    // Hermitian rho: tiles of 32 rows x 8 columns on or below the diagonal; a warp
-    // evaluates 32 consecutive r of one column c (r >= c), then the block writes the
-    // conjugates to the mirrors (c, r) through shared memory, 8 consecutive c per row r.
-    __shared__ cx<R> tile[8][33];
+    // Hermitian rho: 32 x 32 tiles on or below the diagonal; warp w evaluates 32
+    // consecutive r of the columns w, w + 8, w + 16, w + 24 (elements r >= c), then the
+    // block writes the conjugates to the mirrors (c, r) through shared memory, a warp
+    // covering 32 consecutive c of one row r.
+    __shared__ cx<R> tile[32][33];  // [c - c0][r - r0]
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int n_rt = (d + 31) / 32, n_cb = (d + 7) / 8;
-    for (int tau = blockIdx.x; tau < n_rt * n_cb; tau += gridDim.x) {
-      const int r0 = (tau % n_rt) * 32, c0 = (tau / n_rt) * 8;
-      if (r0 + 31 < c0) continue;  // above the diagonal (uniform over the block)
-      const int r = r0 + lane, c = c0 + w;
-      cx<R> acc{0, 0};
-      if (r < d && c < d && r >= c) {
-        acc = element(r, c);
-        if (r == c) acc.im = 0;  // A + A^dag: real diagonal
-        epilogue<DT, YDT, EPI>(r + c * d, acc, ax, rk, err_acc);
+    const int n_t = (d + 31) / 32;
+    for (int tau = blockIdx.x; tau < n_t * n_t; tau += gridDim.x) {
+      const int r0 = (tau % n_t) * 32, c0 = (tau / n_t) * 32;
+      if (r0 < c0) continue;  // above the diagonal (uniform over the block)
+#pragma unroll 1
+      for (int q = 0; q < 4; ++q) {
+        const int cl = w + 8 * q, r = r0 + lane, c = c0 + cl;
+        cx<R> acc{0, 0};
+        if (r < d && c < d && r >= c) {
+          acc = element(r, c);
+          if (r == c) acc.im = 0;  // A + A^dag: real diagonal
+          epilogue<DT, YDT, EPI>(r + c * d, acc, ax, rk, err_acc);
+        }
+        tile[cl][lane] = acc;
       }
-      tile[w][lane] = acc;
       __syncthreads();
-      const int ml = threadIdx.x & 7, rl = threadIdx.x >> 3;
-      const int mr = r0 + rl, mc = c0 + ml;  // the mirror of (mr, mc)
-      if (mr < d && mc < d && mr > mc) {
-        const cx<R> v = tile[ml][rl];
-        epilogue<DT, YDT, EPI>(mc + mr * d, cx<R>{v.re, -v.im}, ax, rk, err_acc);
+#pragma unroll 1
+      for (int q = 0; q < 4; ++q) {
+        const int rl = w + 8 * q;
+        const int mr = r0 + rl, mc = c0 + lane;  // the mirror of (mr, mc)
+        if (mr < d && mc < d && mr > mc) {
+          const cx<R> v = tile[lane][rl];
+          epilogue<DT, YDT, EPI>(mc + mr * d, cx<R>{v.re, -v.im}, ax, rk, err_acc);
+        }
       }
       __syncthreads();
     }
