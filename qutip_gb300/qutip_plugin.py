@@ -745,6 +745,7 @@ class IntegratorGpuVern7(Integrator):
         "interpolate": True,
         "precision": "double",
         "dense": "auto",
+        "hermitian_branch": "auto",
     }
     rhs_format = "solver"
     support_time_dependant = True
@@ -816,8 +817,11 @@ class IntegratorGpuVern7(Integrator):
             self._ode = self._integrator(op)
         if isinstance(op, LindbladOperator):
             # the reference's branch choice: MESolver._prepare_state sets it from rho0.isherm
-            # (qutip/solver/mesolve.py:270-277; lindblad_matrix_form.pyx:171-200)
-            op.hermitian = bool(getattr(self._rhs(), "assume_hermitian_state", False))
+            # (qutip/solver/mesolve.py:270-277; lindblad_matrix_form.pyx:171-200); taken
+            # where it is also the faster form
+            op.hermitian = bool(getattr(self._rhs(), "assume_hermitian_state", False)) and \
+                (self._options.get("hermitian_branch") is True or (
+                    self._options.get("hermitian_branch") == "auto" and op.hermitian_pays()))
         self._ode.set_initial_value(_as_gpu(state0).buf, t)
         self._shape = state0.shape
         self._is_set = True
@@ -878,7 +882,10 @@ class IntegratorGpuVern7(Integrator):
         """atol, rtol, nsteps, first_step, max_step, min_step, interpolate: as the
         reference ``vern7``; precision: ``"double"`` or ``"mixed"``; dense (matrix form
         only): ``"auto"`` sends small systems with dense operators in the mixed form to
-        the tensor-core bucket, ``True`` forces it, ``False`` keeps the sparse kernel."""
+        the tensor-core bucket, ``True`` forces it, ``False`` keeps the sparse kernel;
+        hermitian_branch (matrix form only): with a Hermitian rho0, ``"auto"`` evaluates
+        half the elements where that is faster (large rho), ``True`` always, ``False``
+        never."""
         return self._options
 
     @options.setter

@@ -29,7 +29,8 @@ __all__ = ["MEResult", "mesolve", "solve_system", "liouvillian_terms", "ExpectOp
 
 ME_DEFAULTS = dict(atol=1e-8, rtol=1e-6, nsteps=1000, first_step=0.0, min_step=0.0,
                    max_step=0.0, interpolate=True, precision="double", store_states=False,
-                   store_final_state=False, normalize_output=True, matrix_form=False)
+                   store_final_state=False, normalize_output=True, matrix_form=False,
+                   hermitian_branch="auto")
 
 
 @dataclass
@@ -169,7 +170,9 @@ def solve_system(system: OpenSystem, tlist, options=None, op: DeviceOperator | N
         # the reference's branch: A + A^dag when rho0 is Hermitian (mesolve.py:270-277;
         # Qobj.isherm at the default atol 1e-12)
         r = rho0.reshape(d, d, order="F")
-        op.hermitian = bool(np.all(np.abs(r - r.conj().T) <= 1e-12))
+        branch = opt.get("hermitian_branch", "auto")
+        op.hermitian = bool(np.all(np.abs(r - r.conj().T) <= 1e-12)) and (
+            branch is True or (branch == "auto" and op.hermitian_pays()))
     tr0 = np.trace(rho0.reshape(d, d, order="F"))
     normalize = opt["normalize_output"] and abs(tr0 - 1) <= 1e-12
     ig.set_initial_value(torch.from_numpy(rho0).to(op.device), float(tlist[0]))

@@ -246,16 +246,22 @@ def test_plugin_non_hermitian_rho(qt):
 def test_plugin_follows_the_references_hermitian_branch(qt):
     """mesolve's matrix form takes the reference's A + A^dag branch for a Hermitian rho0
     and the full form for a non-Hermitian one (MESolver._prepare_state sets
-    assume_hermitian_state from rho0.isherm); both match the reference's own runs."""
+    assume_hermitian_state from rho0.isherm), when asked to (hermitian_branch=True; "auto"
+    takes it only for large rho); both match the reference's own runs."""
     a = qt.destroy(N)
     H, c_ops = a.dag() * a + 0.3 * (a + a.dag()), [np.sqrt(KAPPA) * a]
-    opts = {"method": "gpu_vern7", "matrix_form": True, "progress_bar": None}
+    opts = {"method": "gpu_vern7", "matrix_form": True, "progress_bar": None,
+            "hermitian_branch": True}
     tl = np.linspace(0, 3, 31)
     for rho0, herm in ((qt.coherent_dm(N, 0.8), True),
                        (qt.basis(N, 0) * qt.basis(N, 1).dag(), False)):
         solver = qt.MESolver(H, c_ops, options=opts)
         got = solver.run(rho0, tl)
         assert solver._integrator._op.hermitian is herm
+        # "auto" takes it only where it is the faster form: not at d = 10
+        auto = qt.MESolver(H, c_ops, options={**opts, "hermitian_branch": "auto"})
+        auto.run(rho0, tl[:3])
+        assert auto._integrator._op.hermitian is False
         ref = qt.mesolve(H, rho0, tl, c_ops, options={"method": "vern7", "matrix_form": True,
                                                       "progress_bar": None})
         for g, r in zip(got.states, ref.states):
