@@ -224,10 +224,27 @@ struct ClusterGroup {
 // Per-thread replicated control state of the item being integrated.
 struct Ctl {
   double t, t_prev, t_front, dt_safe, dt_int;
-  double bf[16];  // dense-output factors (dt-scaled) of the current output
-  float bfh[16], bfl[16];  // the same as float pairs hi + lo (mixed form)
   int status, cur, interp_ready, out_front, steps, rhs;
 };
+
+// Per-warp factor slice in shared memory (WF_FLOATS floats, 512 B): the stage factors
+// (mixed: dt a_j, its low part, dt e_j, its low part as float[16] each; double:
+// dt a_j, dt e_j as double[16]) and the combination / dense-output factors bf (double[16],
+// dt-scaled) with their float pairs bfh, bfl (mixed form).  Lanes 0-15 of the warp write
+// factor j = lane between two __syncwarp(); every lane reads them as broadcasts.  Held
+// per thread, the arrays were indexed at run time and lived in local memory (1.6 KB of
+// stack per thread, ~1.1e9 local-load sectors in one 4096-trajectory launch).
+// The group coefficients at the current stage time follow (double2[8], float2[8]).
+constexpr int WF_FLOATS = 128 + 4 * QG_MAX_GROUPS + 2 * QG_MAX_GROUPS;
+__device__ __forceinline__ double* wf_bf(float* wf) { return reinterpret_cast<double*>(wf + 64); }
+__device__ __forceinline__ float* wf_bfh(float* wf) { return wf + 96; }
+__device__ __forceinline__ float* wf_bfl(float* wf) { return wf + 112; }
+__device__ __forceinline__ double2* wf_coef(float* wf) {
+  return reinterpret_cast<double2*>(wf + 128);
+}
+__device__ __forceinline__ float2* wf_coef_f(float* wf) {
+  return reinterpret_cast<float2*>(wf + 128 + 4 * QG_MAX_GROUPS);
+}
 
 template <int DT>
 struct Ctx {
@@ -244,8 +261,7 @@ struct Ctx {
   const ST* opval;        // generator entries: global pool, or the staged copy
   const int* op_col;
   const int* op_rp;
-  double2 coef[QG_MAX_GROUPS];  // coefficients at the current stage time
-  float2 coef_f[QG_MAX_GROUPS];  // the same in FP32 (mixed form)
+  float* wf;  // this warp's factor and coefficient slice (shared memory)
 };
 
 template <typename T>
@@ -276,11 +292,12 @@ __device__ __forceinline__ void load_coef(Ctx<DT>& X, double t) {
     const int st = __ldg(X.B->coef_start + X.S->coef_off + lane_id());
     mine = eval_coef(X.B->coef_code + st, X.B->coef_consts, t);
   }
-  for (int g = 0; g < X.G; ++g) {
-    const double re = shfl_d(mine.re, g), im = shfl_d(mine.im, g);
-    X.coef[g] = make_double2(re, im);
-    X.coef_f[g] = make_float2((float)re, (float)im);
+  __syncwarp();  // the warp's earlier readers are done
+  if (lane_id() < X.G) {
+    wf_coef(X.wf)[lane_id()] = make_double2(mine.re, mine.im);
+    wf_coef_f(X.wf)[lane_id()] = make_float2((float)mine.re, (float)mine.im);
   }
+  __syncwarp();
 }
 
 // row r of A(t) x in the compute type
@@ -304,11 +321,13 @@ __device__ __forceinline__ void row_matvec(const Ctx<DT>& X, int r, const XT* x,
     }
     CT cr, ci;
     if constexpr (DT == QG_C64) {
-      cr = X.coef_f[g].x;
-      ci = X.coef_f[g].y;
+      const float2 k = wf_coef_f(X.wf)[g];
+      cr = k.x;
+      ci = k.y;
     } else {
-      cr = X.coef[g].x;
-      ci = X.coef[g].y;
+      const double2 k = wf_coef(X.wf)[g];
+      cr = k.x;
+      ci = k.y;
     }
     ar += cr * gr - ci * gi;
     ai += cr * gi + ci * gr;
@@ -344,46 +363,58 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
   const bool forms_input = !last && s != RK_EXTRA_STEP - 1;
   const int nk = last ? RK_STEP : s + 1;  // k_j that enter the combination
   // factors: FP64 for the double form; float pairs from the hi/lo tableau for the
-  // mixed form (no FP64 work per stage)
-  CT fa[16], fe[16];
-  float fl[16], fel[16];
-  if constexpr (MIXED) {
-    float dh, dl;
-    split_f(dt, dh, dl);
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      float ah = 0.f, al = 0.f, eh = 0.f, el = 0.f;
-      if (j < nk) {
-        if (last) {
-          ah = VERN7_BH[j];
-          al = VERN7_BL[j];
-          eh = VERN7_EF[j];
-          el = VERN7_EL[j];
-        } else if (forms_input) {
-          ah = VERN7_AH[s + 1][j];
-          al = VERN7_AL[s + 1][j];
+  // mixed form (no FP64 work per stage); lane j of each warp forms factor j
+  const CT* fa;
+  const CT* fe;
+  const float* fl;
+  const float* fel;
+  {
+    const int j = lane_id();
+    __syncwarp();  // the warp's earlier readers of the slice are done
+    if constexpr (MIXED) {
+      float* w = X.wf;
+      if (j < 16) {
+        float dh, dl;
+        split_f(dt, dh, dl);
+        float ah = 0.f, al = 0.f, eh = 0.f, el = 0.f;
+        if (j < nk) {
+          if (last) {
+            ah = VERN7_BH[j];
+            al = VERN7_BL[j];
+            eh = VERN7_EF[j];
+            el = VERN7_EL[j];
+          } else if (forms_input) {
+            ah = VERN7_AH[s + 1][j];
+            al = VERN7_AL[s + 1][j];
+          }
         }
+        ff_factor(dh, dl, ah, al, w[j], w[16 + j]);
+        ff_factor(dh, dl, eh, el, w[32 + j], w[48 + j]);
       }
-      ff_factor(dh, dl, ah, al, fa[j], fl[j]);
-      ff_factor(dh, dl, eh, el, fe[j], fel[j]);
-    }
-  } else {
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      double a = 0.0, e = 0.0;
-      if (j < nk) {
-        if (last) {
-          a = dt * VERN7_B[j];
-          e = dt * VERN7_E[j];
-        } else if (forms_input) {
-          a = dt * VERN7_A[s + 1][j];
+      fa = reinterpret_cast<const CT*>(w);
+      fl = w + 16;
+      fe = reinterpret_cast<const CT*>(w + 32);
+      fel = w + 48;
+    } else {
+      double* w = reinterpret_cast<double*>(X.wf);
+      if (j < 16) {
+        double a = 0.0, e = 0.0;
+        if (j < nk) {
+          if (last) {
+            a = dt * VERN7_B[j];
+            e = dt * VERN7_E[j];
+          } else if (forms_input) {
+            a = dt * VERN7_A[s + 1][j];
+          }
         }
+        w[j] = a;
+        w[16 + j] = e;
       }
-      fa[j] = (CT)a;
-      fe[j] = (CT)e;
-      fl[j] = 0.f;
-      fel[j] = 0.f;
+      fa = reinterpret_cast<const CT*>(w);
+      fe = reinterpret_cast<const CT*>(w + 16);
+      fl = fel = nullptr;  // not used by the double form
     }
+    __syncwarp();
   }
   load_coef(X, c.t_prev + VERN7_C[s] * dt);
   const int cur = c.cur;
@@ -488,14 +519,17 @@ template <int DT, class GT>
 __device__ void form_input_mixed(const GT& g, Ctx<DT>& X, const Ctl& c, typename elem<DT>::T* out,
                                  int row, int nk, double dt) {
   using ST = typename elem<DT>::T;
-  float fa[16], fl[16];
-  float dh, dl;
-  split_f(dt, dh, dl);
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
+  float* fa = X.wf;
+  float* fl = X.wf + 16;
+  __syncwarp();
+  if (lane_id() < 16) {
+    const int j = lane_id();
+    float dh, dl;
+    split_f(dt, dh, dl);
     const float ah = j < nk ? VERN7_AH[row][j] : 0.f, al = j < nk ? VERN7_AL[row][j] : 0.f;
     ff_factor(dh, dl, ah, al, fa[j], fl[j]);
   }
+  __syncwarp();
   const int cur = c.cur;
   const int64_t n = X.n;
   for (int r = g.rank; r < X.n; r += GT::SIZE) {
@@ -513,13 +547,14 @@ __device__ void form_input_mixed(const GT& g, Ctx<DT>& X, const Ctl& c, typename
   g.sync();
 }
 
-// out = base + sum_{j<nk} c.bf[j] k_j
+// out = base + sum_{j<nk} bf[j] k_j (bf: the warp's factor slice)
 template <int DT, class GT, typename OT, typename BT>
 __device__ void combine(const GT& g, Ctx<DT>& X, const Ctl& c, OT* out, const BT* base, int nk) {
+  const double* bf = wf_bf(X.wf);
   for (int r = g.rank; r < X.n; r += GT::SIZE) {
     double vr = (double)base[r].x, vi = (double)base[r].y;
     for (int j = 0; j < nk; ++j) {
-      const double f = c.bf[j];
+      const double f = bf[j];
       if (f != 0.0) {
         vr = fma(f, (double)X.k[(int64_t)j * X.n + r].x, vr);
         vi = fma(f, (double)X.k[(int64_t)j * X.n + r].y, vi);
@@ -536,20 +571,23 @@ template <int DT>
 __device__ __forceinline__ double2 state_at(const Ctx<DT>& X, const Ctl& c, int i) {
   if (c.out_front) return X.y[c.cur ^ 1][i];
   if constexpr (DT == QG_C64) {
+    const float* bfh = wf_bfh(X.wf);
+    const float* bfl = wf_bfl(X.wf);
     float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;
     for (int j = 0; j < RK_EXTRA_STEP; ++j) {
-      if (c.bfh[j] != 0.f || c.bfl[j] != 0.f) {
+      if (bfh[j] != 0.f || bfl[j] != 0.f) {
         const float2 kj = X.k[(int64_t)j * X.n + i];
-        ff_acc(hr, lr, c.bfh[j], c.bfl[j], kj.x);
-        ff_acc(hi, li, c.bfh[j], c.bfl[j], kj.y);
+        ff_acc(hr, lr, bfh[j], bfl[j], kj.x);
+        ff_acc(hi, li, bfh[j], bfl[j], kj.y);
       }
     }
     return make_double2(X.y[c.cur][i].x + ((double)hr + (double)lr),
                         X.y[c.cur][i].y + ((double)hi + (double)li));
   } else {
+    const double* bf = wf_bf(X.wf);
     double vr = X.y[c.cur][i].x, vi = X.y[c.cur][i].y;
     for (int j = 0; j < RK_EXTRA_STEP; ++j) {
-      const double f = c.bf[j];
+      const double f = bf[j];
       if (f != 0.0) {
         vr = fma(f, (double)X.k[(int64_t)j * X.n + i].x, vr);
         vi = fma(f, (double)X.k[(int64_t)j * X.n + i].y, vi);
@@ -619,8 +657,9 @@ __device__ __noinline__ void set_initial(const GT& g, Ctx<DT>& X, Ctl& c, const 
   else
     dt1 = pow(tol * fact, 1.0 / (RK_ORDER + 1)) * norm * 0.5;
   const double t1 = t + dt1 / 100;
-  for (int j = 0; j < 16; ++j) c.bf[j] = 0.0;
-  c.bf[0] = dt1 / 100;
+  __syncwarp();
+  if (lane_id() < 16) wf_bf(X.wf)[lane_id()] = lane_id() == 0 ? dt1 / 100 : 0.0;
+  __syncwarp();
   ST* yt = X.ytmp + X.n;
   combine(g, X, c, yt, x0, 1);
   matvec_to_k(g, X, c, t1, yt, 1);
@@ -642,7 +681,10 @@ __device__ __noinline__ void prep_dense_out(const GT& g, Ctx<DT>& X, Ctl& c) {
   if constexpr (DT == QG_C64) {
     form_input_mixed(g, X, c, x10, RK_STEP, RK_STEP, dt);
   } else {
-    for (int j = 0; j < 16; ++j) c.bf[j] = j < RK_STEP ? dt * VERN7_A[RK_STEP][j] : 0.0;
+    __syncwarp();
+    if (lane_id() < 16)
+      wf_bf(X.wf)[lane_id()] = lane_id() < RK_STEP ? dt * VERN7_A[RK_STEP][lane_id()] : 0.0;
+    __syncwarp();
     combine(g, X, c, x10, X.y[c.cur], RK_STEP);
   }
   for (int s = RK_STEP; s < RK_EXTRA_STEP; ++s) stage(g, X, c, s, dt);
@@ -651,7 +693,8 @@ __device__ __noinline__ void prep_dense_out(const GT& g, Ctx<DT>& X, Ctl& c) {
 
 // dense-output factors at t (Horner in tau, explicit_rk.pyx:412-430); lane i
 // evaluates factor i
-__device__ __forceinline__ void set_interp(Ctl& c, double t) {
+template <int DT>
+__device__ __forceinline__ void set_interp(const Ctx<DT>& X, Ctl& c, double t) {
   const double tau = (t - c.t_prev) / c.dt_int;
   double mine = 0.0;
   float mh = 0.f, ml = 0.f;
@@ -664,11 +707,13 @@ __device__ __forceinline__ void set_interp(Ctl& c, double t) {
     mine = c.dt_int * acc;
     split_f(mine, mh, ml);
   }
-  for (int i = 0; i < RK_EXTRA_STEP; ++i) {
-    c.bf[i] = shfl_d(mine, i);
-    c.bfh[i] = __shfl_sync(0xffffffffu, mh, i);
-    c.bfl[i] = __shfl_sync(0xffffffffu, ml, i);
+  __syncwarp();
+  if (lane_id() < RK_EXTRA_STEP) {
+    wf_bf(X.wf)[lane_id()] = mine;
+    wf_bfh(X.wf)[lane_id()] = mh;
+    wf_bfl(X.wf)[lane_id()] = ml;
   }
+  __syncwarp();
   c.out_front = 0;
   c.t = t;
 }
@@ -726,7 +771,7 @@ __device__ void integrate(const GT& g, Ctx<DT>& X, Ctl& c, double t, bool step) 
   }
   if (t < c.t_front) {
     if (!c.interp_ready) prep_dense_out(g, X, c);
-    set_interp(c, t);
+    set_interp(X, c, t);
     return;
   }
   c.status = QG_NORMAL;
@@ -741,7 +786,7 @@ __device__ void integrate(const GT& g, Ctx<DT>& X, Ctl& c, double t, bool step) 
   if (c.status < 0) return;
   if (c.t_front > t) {
     prep_dense_out(g, X, c);
-    set_interp(c, t);
+    set_interp(X, c, t);
   } else {
     c.out_front = 1;
     c.t = c.t_front;
@@ -1064,6 +1109,7 @@ template <int DT>
 __global__ void __launch_bounds__(WARP_BLOCK, 4) batch_warp_kernel(qg_batch B) {
   extern __shared__ __align__(256) unsigned char stage_smem[];
   __shared__ __align__(8) uint64_t op_bar;
+  __shared__ __align__(16) float wf_s[WARP_BLOCK / 32][WF_FLOATS];
   const int64_t slot = (int64_t)blockIdx.x * (WARP_BLOCK / 32) + (threadIdx.x >> 5);
   WarpGroup g{(int)(threadIdx.x & 31), slot};
   const unsigned int n_groups = gridDim.x * (WARP_BLOCK / 32);
@@ -1077,6 +1123,7 @@ __global__ void __launch_bounds__(WARP_BLOCK, 4) batch_warp_kernel(qg_batch B) {
   if (slot < B.n_slots) {
     Ctx<DT> X;
     bind_slot(X, B, slot);
+    X.wf = wf_s[threadIdx.x >> 5];
     if (staged) use_staged(X, B, smem_op);
     if (in_bytes > 0)
       X.ytmp = reinterpret_cast<typename elem<DT>::T*>(
@@ -1103,9 +1150,11 @@ __global__ void __launch_bounds__(BB, 65536 / (BB * 128)) batch_cta_kernel(qg_ba
   __shared__ int ibuf;
   extern __shared__ __align__(256) unsigned char stage_smem[];
   __shared__ __align__(8) uint64_t op_bar;
+  __shared__ __align__(16) float wf_s[BB / 32][WF_FLOATS];
   CtaGroup<BB> g{(int)threadIdx.x, (int64_t)blockIdx.x, red, &ibuf};
   Ctx<DT> X;
   bind_slot(X, B, blockIdx.x);
+  X.wf = wf_s[threadIdx.x >> 5];
   const int64_t in_bytes = stage_smem_bytes(B.max_n, DT, 1);
   if (in_bytes > 0) X.ytmp = reinterpret_cast<typename elem<DT>::T*>(stage_smem);
   unsigned char* smem_op = stage_smem + in_bytes;
@@ -1136,9 +1185,11 @@ __global__ void __launch_bounds__(CTA_BLOCK, 2) batch_cluster_kernel(qg_batch B)
   cgrp::cluster_group cl = cgrp::this_cluster();
   const int crank = (int)cl.block_rank();
   const int64_t slot = blockIdx.x / CLUSTER_CTAS;
+  __shared__ __align__(16) float wf_s[CTA_BLOCK / 32][WF_FLOATS];
   ClusterGroup<CTA_BLOCK, CLUSTER_CTAS> g{crank * CTA_BLOCK + (int)threadIdx.x, slot, red, &ibuf};
   Ctx<DT> X;
   bind_slot(X, B, slot);
+  X.wf = wf_s[threadIdx.x >> 5];
   while (true) {
     int it = 0;
     if (g.rank == 0) {
