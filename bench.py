@@ -487,8 +487,7 @@ def run_served(args):
     warm = [build_job(sp) for sp in specs[:8]]
     Server("mixed").serve(warm, realtime=False)
     # throughput: every job available at t = 0
-    side = 3600   # mesolve requests of N >= 30 (d^2 >= 3600) may take the side path
-    srv = Server("mixed", launch_timeout=60.0, side_min_len=side)
+    srv = Server("mixed", launch_timeout=60.0)
     _, wall = srv.serve(jobs, realtime=False)
     thr = n / wall
     log(f"served: throughput {thr:.1f} solves/s")
@@ -497,7 +496,7 @@ def run_served(args):
     specs_r = jc_request_stream(n, rate=rate, ntraj=args.served_ntraj, seed=2026)
     assert all(a.n_cav == b.n_cav and a.seed == b.seed for a, b in zip(specs, specs_r))
     jobs_r = rearrive(jobs, specs_r)
-    srv_r = Server("mixed", launch_timeout=60.0, side_min_len=side)
+    srv_r = Server("mixed", launch_timeout=60.0)
     _, wall_r = srv_r.serve(jobs_r, realtime=True)
     lat = percentiles([j.latency for j in jobs_r])
     log(f"served: latency {lat}")
@@ -518,8 +517,7 @@ def run_served(args):
     m = min(400, n)
     specs_l = jc_request_stream(n, rate=low_rate, ntraj=args.served_ntraj, seed=2026)[:m]
     jobs_l = rearrive(jobs[:m], specs_l)
-    srv_l = Server("mixed", launch_timeout=60.0, side_min_len=side)
-    srv_l.serve(jobs_l, realtime=True)
+    Server("mixed", launch_timeout=60.0).serve(jobs_l, realtime=True)
     lat_low = percentiles([j.latency for j in jobs_l])
     # the plain arm served in real time on the same arrivals (measured, not modelled)
     jobs_lp = rearrive(jobs[:m], specs_l)
@@ -546,12 +544,6 @@ def run_served(args):
     return {
         "workload": f"{n} Jaynes-Cummings jobs, N~U{{5..60}}, {n_me} mesolve / {n - n_me} mcsolve "
                     f"(ntraj={args.served_ntraj}), tlist linspace(0,20,101), seed 2026",
-        "side_path": {"min_state_len": side, "jobs_throughput_run": srv.stats["side_jobs"],
-                      "jobs_high_rate": srv_r.stats["side_jobs"],
-                      "jobs_low_rate": srv_l.stats["side_jobs"],
-                      "what": "mesolve requests of at least this many state entries that arrive "
-                              "while the side worker is idle run one at a time on the "
-                              "matrix-free Lindblad kernel (own stream and host thread)"},
         "served_mixed": {"solves_per_sec": thr, "wall_s": wall, "launches": srv.stats["launches"],
                          "latency_at_rate": {**lat, "rate_per_s": rate, "wall_s": wall_r,
                                              "max_concurrent_launches": srv_r.stats["max_concurrent"]}},

@@ -21,8 +21,6 @@ tests check bitwise.
 from __future__ import annotations
 
 import gc
-import queue
-import threading
 import time
 from collections import deque
 from dataclasses import dataclass, field
@@ -35,7 +33,7 @@ from .batched import BatchProblem, check_status
 from .systems import OpenSystem, jaynes_cummings
 
 __all__ = ["JobSpec", "Job", "jc_request_stream", "build_job", "Server", "percentiles",
-           "fifo_latencies", "serve_plain", "solve_plain"]
+           "fifo_latencies", "solve_plain"]
 
 BUCKETS = (128, 512, 2048, 8192, 1 << 30)
 
@@ -127,20 +125,12 @@ class Server:
     """Continuous batching over a fixed number of CUDA streams and an HBM budget."""
 
     def __init__(self, precision="mixed", n_streams=4, hbm_budget=8 << 30, max_items=8192,
-                 max_jobs_per_launch=512, max_jumps=256, launch_timeout=120.0, group="load",
-                 side_min_len=None):
+                 max_jobs_per_launch=512, max_jumps=256, launch_timeout=120.0, group="load"):
         """``group``: ``"load"`` gives each item of a launch with few large items a
         thread-block cluster (8 SMs), each item of a launch of at most two items per SM
         a CTA, and packs fuller launches one item per warp; ``"auto"``, ``"warp"``,
         ``"cta"`` or ``"cluster"`` fix the shape for every launch (results then do not
-        depend on how requests were grouped into launches).
-
-        ``side_min_len``: a mesolve request with a state of at least this many entries
-        that arrives while the side worker is idle runs there instead: one request at a
-        time on the matrix-free Lindblad kernel (the whole GPU's bandwidth for one
-        system, on its own stream and host thread).  A large JC mesolve (N = 60, 14,400
-        entries) takes ~7 ms there against ~19 ms as one item of a batched launch;
-        None: no side path."""
+        depend on how requests were grouped into launches)."""
         self.precision = precision
         self.dtype = "c64" if precision == "mixed" else "c128"
         self.qdt = _lib.QG_C64 if self.dtype == "c64" else _lib.QG_C128
@@ -158,61 +148,7 @@ class Server:
         self.cta_items = 2 * torch.cuda.get_device_properties(0).multi_processor_count \
             if torch.cuda.is_available() else 0
         self.stats = {"launches": 0, "items": 0, "max_inflight_bytes": 0, "max_concurrent": 0,
-                      "max_launch_s": 0.0, "side_jobs": 0}
-        self.side_min_len = side_min_len
-        self._side = None
-
-    # -- side path: large mesolve requests on the matrix-free kernel, one at a time ----
-    def _side_start(self):
-        if self._side is None:
-            self._side = {"queue": queue.Queue(), "busy": threading.Event(),
-                          "stream": torch.cuda.Stream(), "error": []}
-            self._side["thread"] = threading.Thread(target=self._side_loop, daemon=True)
-            self._side["thread"].start()
-        return self._side
-
-    def _side_loop(self):
-        from .lindblad import LindbladOperator
-        from .solver import solve_system
-        side = self._side
-        while True:
-            item = side["queue"].get()
-            if item is None:
-                return
-            j, t0 = item
-            try:
-                with torch.cuda.stream(side["stream"]):
-                    s = j.system
-                    op = LindbladOperator.from_hamiltonian(s.h_terms, s.c_ops, dtype=self.dtype)
-                    res = solve_system(s, j.tlist, {"precision": self.precision,
-                                                    "matrix_form": True}, op=op)
-                j.result = [np.asarray(e) for e in res.expect]
-                j.extra["launch"] = ("side", 1, 1)
-                j.done = time.perf_counter() - t0
-            except Exception as exc:  # noqa: BLE001  (re-raised by the serving loop)
-                side["error"].append(exc)
-            finally:
-                side["busy"].clear()
-
-    def _side_take(self, j, t0) -> bool:
-        """Hand ``j`` to the side worker if it qualifies and the worker is idle."""
-        if (self.side_min_len is None or j.spec.kind != "me" or
-                j.state_len < self.side_min_len or not j.system.h_terms):
-            return False
-        side = self._side_start()
-        if side["busy"].is_set():
-            return False
-        side["busy"].set()
-        self.stats["side_jobs"] += 1
-        side["queue"].put((j, t0))
-        return True
-
-    def close(self):
-        """Stop the side worker (if one was started)."""
-        if self._side is not None:
-            self._side["queue"].put(None)
-            self._side["thread"].join()
-            self._side = None
+                      "max_launch_s": 0.0}
 
     def _cluster_slots(self, max_n):
         if max_n not in self._cluster_cache:
@@ -286,7 +222,6 @@ class Server:
         try:
             return self._serve(jobs, realtime)
         finally:
-            self.close()
             if gc_was_enabled:
                 gc.enable()
 
@@ -299,20 +234,10 @@ class Server:
         used = 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        side_jobs = []
-
-        def side_busy():
-            if self._side is not None and self._side["error"]:
-                raise self._side["error"][0]
-            return any(j.done is None for j in side_jobs)
-
-        while pending or inflight or any(waiting.values()) or side_busy():
+        while pending or inflight or any(waiting.values()):
             now = time.perf_counter() - t0
             while pending and (not realtime or pending[0].spec.arrival <= now):
                 j = pending.popleft()
-                if self._side_take(j, t0):
-                    side_jobs.append(j)
-                    continue
                 b = next(b for b in BUCKETS if j.state_len <= b)
                 waiting[b].append(j)
             progressed = False

@@ -59,27 +59,6 @@ def test_served_mixed_precision_error_vs_plain_double():
     assert worst < 1e-6
 
 
-def test_side_path_for_large_mesolve_requests():
-    """Large mesolve requests that arrive while the side worker is idle run on the
-    matrix-free Lindblad kernel on their own stream; their results stay within the mixed
-    form's bound of the plain complex128 solve, and every request completes."""
-    from qutip_gb300.serving import Server, solve_plain
-    jobs = _jobs(n=30, rate=200.0)
-    srv = Server("mixed", side_min_len=100)
-    srv.serve(jobs, realtime=True)
-    assert srv.stats["side_jobs"] >= 1
-    side = [j for j in jobs if j.extra.get("launch", (None,))[0] == "side"]
-    assert len(side) == srv.stats["side_jobs"]
-    assert all(j.done is not None and j.latency > 0 for j in jobs)
-    worst = 0.0
-    for j in side:
-        plain = solve_plain(j, "double")
-        d = max(float(np.max(np.abs(np.real(a) - np.real(b)))) for a, b in zip(j.result, plain))
-        worst = max(worst, d / max(float(np.max(np.abs(np.real(b)))) for b in plain))
-    print(f"\nside path: {len(side)} requests, max relative difference vs complex128 {worst:.2e}")
-    assert worst < 1e-6
-
-
 def test_load_policy_results_match_fixed_shape():
     """With the load-dependent group shape, master-equation results equal those of a
     fixed shape to rounding (only the order of the FP64 reductions differs)."""
