@@ -314,6 +314,44 @@ int qg_dense_lindblad_apply(const qg_dense_lindblad* L, double t, const void* x,
 int qg_dense_lindblad_stage(const qg_dense_lindblad* L, const qg_rk_buffers* B, int stage,
                             double t_prev, double dt, double atol, double rtol, void* stream);
 
+/* Stochastic Schrodinger / master equations (ssesolve / smesolve), the reference's
+ * explicit Platen scheme (qutip/solver/sode/_sode.pyx:58-120) on the systems of
+ * qutip/solver/sode/ssystem.pyx:119-250:
+ *   SSE (open = 0, state psi, n = d):  drift = L psi + sum_i (-e_i^2/8 psi + e_i/2 C_i psi),
+ *     L = -i H - 1/2 sum_i C_i^dag C_i, e_i = <psi| M_i |psi> with M_i = C_i + C_i^dag;
+ *     diffusion_i = C_i psi - e_i/2 psi.
+ *   SME (open = 1, state vec(rho), n = d*d): drift = L rho (L the Liouvillian of H, sc_ops
+ *     and c_ops), diffusion_i = C_i rho - tr(C_i rho) rho with C_i = spre(c_i) + spost(c_i^dag).
+ * Operators are complex128 CSR with 32-bit indices; the n_sc stochastic operators (and the
+ * SSE expectation operators) are stacked by rows: block i holds rows i*n .. i*n + n - 1. */
+typedef struct qg_sde {
+  int64_t n;        /* state length */
+  int32_t open;     /* 0: SSE (ket), 1: SME (vec(rho), column-stacked) */
+  int32_t n_sc;     /* stochastic operators (1..QG_MAX_COPS) */
+  int32_t d;        /* Hilbert-space dimension */
+  int32_t reserved; /* 0 */
+  const int32_t* l_rp;
+  const int32_t* l_col;
+  const void* l_val;
+  const int32_t* c_rp;
+  const int32_t* c_col;
+  const void* c_val;
+  const int32_t* m_rp;  /* SSE only (NULL for SME) */
+  const int32_t* m_col;
+  const void* m_val;
+  void* work;       /* n_traj * qg_sde_work_values(n, n_sc) complex128 values */
+} qg_sde;
+
+/* Workspace of one trajectory, in complex128 values. */
+int64_t qg_sde_work_values(int64_t n, int32_t n_sc);
+
+/* n_steps Platen steps of dt for each of n_traj trajectories (one CTA each): states holds
+ * n_traj complex128 states of length n (updated in place); dW holds the Wiener increments,
+ * n_traj x n_steps x n_sc doubles (trajectory-major), as the reference's Wiener.dW draws
+ * them.  Replaces PlatenSODE.integrate / _sode.Platen.run (sode.py:151-173). */
+int qg_sde_platen(const qg_sde* S, int32_t n_traj, void* states, const double* dW,
+                  int32_t n_steps, double dt, void* stream);
+
 /* Non-zero when a kernel of this library gave up a bounded wait on the current
  * device (the result of that launch is invalid); reading clears the flag. */
 int qg_device_fault(void);

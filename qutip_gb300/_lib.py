@@ -48,6 +48,14 @@ class Lindblad(C.Structure):
                 ("c_coef_start", C.c_void_p), ("c_coef_consts", C.c_void_p)]
 
 
+class Sde(C.Structure):
+    _fields_ = [("n", C.c_int64), ("open", C.c_int32), ("n_sc", C.c_int32), ("d", C.c_int32),
+                ("reserved", C.c_int32), ("l_rp", C.c_void_p), ("l_col", C.c_void_p),
+                ("l_val", C.c_void_p), ("c_rp", C.c_void_p), ("c_col", C.c_void_p),
+                ("c_val", C.c_void_p), ("m_rp", C.c_void_p), ("m_col", C.c_void_p),
+                ("m_val", C.c_void_p), ("work", C.c_void_p)]
+
+
 class DenseLindblad(C.Structure):
     _fields_ = [("d", C.c_int32), ("n_groups", C.c_int32), ("n_cops", C.c_int32),
                 ("reserved", C.c_int32), ("a", C.c_void_p), ("c", C.c_void_p),
@@ -101,6 +109,9 @@ _SIGS = {
                                           C.c_void_p]),
     "qg_dense_lindblad_stage": (C.c_int, [_P(DenseLindblad), _P(RkBuffers), C.c_int, C.c_double,
                                           C.c_double, C.c_double, C.c_double, C.c_void_p]),
+    "qg_sde_work_values": (C.c_int64, [C.c_int64, C.c_int32]),
+    "qg_sde_platen": (C.c_int, [_P(Sde), C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                                C.c_double, C.c_void_p]),
     "qg_rk_combine": (C.c_int, [_P(StateView), C.c_void_p, C.c_int, C.c_void_p]),
     "qg_norm2": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                            C.c_void_p]),
@@ -125,6 +136,7 @@ COMPUTE_ENTRY_POINTS = {
     "qg_spmv_csr", "qg_spmm_csr", "qg_spmv_dia", "qg_vern7_stage", "qg_rk_combine", "qg_norm2",
     "qg_expect_dm", "qg_expect_ket", "qg_batch_vern7", "qg_batch_vern7_noalloc",
     "qg_lindblad_apply", "qg_lindblad_stage", "qg_dense_lindblad_apply", "qg_dense_lindblad_stage",
+    "qg_sde_platen",
 }
 LAUNCHES = [0]
 

@@ -47,7 +47,7 @@ extern "C" int qg_abi_sizes(int64_t* out, int n) {
                        (int64_t)sizeof(qg_rk_buffers),   (int64_t)sizeof(qg_state_view),
                        (int64_t)sizeof(qg_batch_system), (int64_t)sizeof(qg_batch_item),
                        (int64_t)sizeof(qg_batch),        (int64_t)sizeof(qg_lindblad),
-                       (int64_t)sizeof(qg_dense_lindblad)};
+                       (int64_t)sizeof(qg_dense_lindblad), (int64_t)sizeof(qg_sde)};
   const int m = (int)(sizeof(s) / sizeof(s[0]));
   if (!out) return qg::set_error(QG_ERR_ARG, "null output");
   for (int i = 0; i < m && i < n; ++i) out[i] = s[i];

@@ -28,6 +28,10 @@ Importing this module (QuTiP must be importable) registers:
   fused Vern7 stage kernels; its options are the reference Vern7's
   (qutip/solver/integrator/qutip_integrator.py:51-59) plus ``precision``
   (``"double"`` or ``"mixed"``).
+* :class:`IntegratorGpuPlaten` as ``method="gpu_platen"`` on ``SSESolver`` and
+  ``SMESolver`` (``StochasticSolver.add_integrator``): the reference's Platen scheme,
+  every step of an output interval in one ``qg_sde_platen`` launch, with the Wiener
+  increments drawn by the reference's own ``Wiener`` object.
 * ``map="gpu"`` for ``MCSolver`` (``qutip.solver.parallel._maps``,
   qutip/solver/parallel.py:541-559): all trajectories of a ``run`` -- with one
   initial state or a mixed initial ensemble -- go to one persistent
@@ -59,6 +63,9 @@ from qutip.solver.mcsolve import MCSolver
 from qutip.solver.mesolve import MESolver
 from qutip.solver.sesolve import SESolver
 from qutip.solver import parallel as _parallel
+from qutip.solver.stochastic import StochasticSolver
+from qutip.solver.sode.sode import SIntegrator
+from qutip.solver.sode._noise import PreSetWiener, Wiener
 
 from . import _lib
 from .coefficients import Coefficient, coefficient, interpolation
@@ -893,6 +900,111 @@ class IntegratorGpuVern7(Integrator):
         Integrator.options.fset(self, new_options)
 
 
+# ----------------------------------------------------------- stochastic (SODE) --
+def sde_operator(rhs):
+    """The device drift / diffusion operators of the reference's ``_StochasticRHS``
+    (qutip/solver/stochastic.py:234-290), built as ``StochasticClosedSystem`` /
+    ``StochasticOpenSystem`` build them (qutip/solver/sode/ssystem.pyx:131-139, 211-225)."""
+    from .stochastic import SdeOperator
+    evos = [rhs.H] + list(rhs.sc_ops) + list(rhs.c_ops)
+    if not all(getattr(e, "isconstant", True) for e in evos):
+        raise TypeError("method='gpu_platen' integrates constant H, sc_ops and c_ops")
+    H = rhs.H(0)
+    sc = [c(0) for c in rhs.sc_ops]
+    if rhs.issuper:
+        L = H + qutip.liouvillian(None, sc) if H.issuper else qutip.liouvillian(H, sc)
+        if rhs.c_ops:
+            L = L + qutip.liouvillian(None, [c(0) for c in rhs.c_ops])
+        cs = [qutip.spre(c) + qutip.spost(c.dag()) for c in sc]
+        d = int(round(np.sqrt(L.shape[0])))
+        return SdeOperator(_scipy(L.data), [_scipy(c.data) for c in cs], open=True, d=d,
+                           device=_device())
+    L = -1j * H
+    for c in sc:
+        L = L + (-0.5 * c.dag() * c)
+    ms = [c + c.dag() for c in sc]
+    return SdeOperator(_scipy(L.data), [_scipy(c.data) for c in sc],
+                       [_scipy(m.data) for m in ms], open=False, d=H.shape[0], device=_device())
+
+
+class IntegratorGpuPlaten(SIntegrator):
+    """The reference's explicit Platen scheme (``PlatenSODE``, strong order 1,
+    qutip/solver/sode/sode.py:235-251) on the device: each ``integrate`` call runs the
+    interval's fixed steps in one ``qg_sde_platen`` launch, with the increments the
+    reference's ``Wiener`` draws from the trajectory's generator.  Options: ``dt``
+    (default 0.001) and ``tol``, as the reference's."""
+    integrator_options = {"dt": 0.001, "tol": 1e-10}
+    N_dw = 1
+    _stepper_options = []
+
+    def __init__(self, rhs, options):
+        self._options = self.integrator_options.copy()
+        self.options = options
+        self.rhs = rhs
+        self._op = None
+
+    def set_state(self, t, state0, generator):
+        if self._op is None:
+            self._op = sde_operator(self.rhs)
+        self.t = t
+        buf = _as_gpu(state0).buf
+        if buf.numel() != self._op.n:
+            raise ValueError(f"state of {buf.numel()} entries for a system of {self._op.n}")
+        self._state = buf.clone()
+        if isinstance(generator, PreSetWiener):
+            if generator.is_measurement:
+                raise NotImplementedError("gpu_platen does not support running the evolution "
+                                          "from measurements")
+            self.wiener = generator
+        elif isinstance(generator, Wiener):
+            self.wiener = generator
+        else:
+            self.wiener = Wiener(t, self.options["dt"], generator,
+                                 (self.N_dw, len(self.rhs.sc_ops)))
+        self.rhs._register_feedback(self.wiener)
+        self._is_set = True
+
+    def get_state(self, copy=True):
+        buf = self._state.clone() if copy else self._state
+        return self.t, GpuDense(buf, shape=(self._op.n, 1), copy=False), self.wiener
+
+    def integrate(self, t, copy=True):
+        """Reference control flow of ``_Explicit_Simple_Integrator.integrate``
+        (sode.py:151-173): the number of dt steps to t, rounded up past half a step."""
+        delta_t = t - self.t
+        dt = self.options["dt"]
+        if delta_t < 0:
+            raise ValueError("Integration time, can't be negative.")
+        elif delta_t < 0.5 * dt:
+            import warnings
+            warnings.warn(f"Step under minimum step ({dt}), skipped.", RuntimeWarning)
+            return self.t, GpuDense(self._state, shape=(self._op.n, 1), copy=copy), \
+                np.zeros(self.N_dw)
+        N, extra = np.divmod(delta_t, dt)
+        N = int(N)
+        if extra > 0.5 * dt:
+            N += 1
+        dW = self.wiener.dW(self.t, N)
+        dev = torch.from_numpy(np.ascontiguousarray(dW[:, 0, :], dtype=np.float64)).to(
+            self._state.device, non_blocking=False)
+        self._op.platen(self._state.view(1, -1), dev, N, dt)
+        self.t += dt * N
+        return self.t, GpuDense(self._state, shape=(self._op.n, 1), copy=copy), \
+            np.sum(dW[:, 0, :], axis=0)
+
+    def mcstep(self, t, copy=True):
+        raise NotImplementedError
+
+    @property
+    def options(self):
+        """dt : float, default 0.001 -- the fixed step; tol : float, default 1e-10."""
+        return self._options
+
+    @options.setter
+    def options(self, new_options):
+        Integrator.options.fset(self, new_options)
+
+
 # ------------------------------------------------------------- trajectories ---
 def _constant_matrix(op, what):
     if isinstance(op, qutip.QobjEvo):
@@ -1153,6 +1265,7 @@ def register():
     _data.transpose.add_specialisations([(GpuDense, GpuDense, transpose_gpu)])
     for solver in (MESolver, SESolver, MCSolver, BRSolver):
         solver.add_integrator(IntegratorGpuVern7, "gpu_vern7")
+    StochasticSolver.add_integrator(IntegratorGpuPlaten, "gpu_platen")
     _parallel._maps["gpu"] = gpu_map
     _REGISTERED = True
 

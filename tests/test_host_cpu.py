@@ -79,12 +79,13 @@ def test_struct_layouts_match_the_library():
     import ctypes as C
     from qutip_gb300 import _lib
     from qutip_gb300.batched import ITEM_DTYPE, SYSTEM_DTYPE, BatchStruct
-    out = np.zeros(9, dtype=np.int64)
-    n = _lib.load().qg_abi_sizes(out.ctypes.data_as(C.c_void_p), 9)
-    assert n == 9
+    out = np.zeros(10, dtype=np.int64)
+    n = _lib.load().qg_abi_sizes(out.ctypes.data_as(C.c_void_p), 10)
+    assert n == 10
     mine = [C.sizeof(_lib.CsrGroups), C.sizeof(_lib.Dia), C.sizeof(_lib.RkBuffers),
             C.sizeof(_lib.StateView), SYSTEM_DTYPE.itemsize, ITEM_DTYPE.itemsize,
-            C.sizeof(BatchStruct), C.sizeof(_lib.Lindblad), C.sizeof(_lib.DenseLindblad)]
+            C.sizeof(BatchStruct), C.sizeof(_lib.Lindblad), C.sizeof(_lib.DenseLindblad),
+            C.sizeof(_lib.Sde)]
     assert list(out) == mine
 
 
