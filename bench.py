@@ -70,9 +70,9 @@ def parse():
                     help="whole mesolve calls timed for e2e (at most --steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline workload only")
-    ap.add_argument("--sections", default="served,mc,matrix,dense,large",
+    ap.add_argument("--sections", default="served,mc,matrix,dense,sde,large",
                     help="extra sections after the headline (comma list of served, mc, "
-                         "matrix, dense, large)")
+                         "matrix, dense, sde, large)")
     ap.add_argument("--matrix-sites", type=int, default=13,
                     help="spins of the short matrix-form solve in the matrix section (0: skip)")
     ap.add_argument("--served-jobs", type=int, default=10000)
@@ -753,6 +753,51 @@ def large_cpu_baseline(host_groups, state0, rhs_full, reps=2):
             "rhs_call_s": rhs_s, "rhs_full": rhs_full}
 
 
+def run_sde(args):
+    """Stochastic solvers through QuTiP's own API: ``ssesolve`` (homodyne) and ``smesolve``
+    (with a deterministic collapse operator) of a driven cavity (N = 20), tlist
+    linspace(0, 1, 11) at dt = 1e-3 (1000 Platen steps per trajectory), the reference's
+    ``platen`` against ``gpu_platen`` with the same seeds: wall time per trajectory and
+    the largest difference of the per-trajectory expectation values."""
+    qt, _ = host_qutip()
+    N = 20
+    a = qt.destroy(N)
+    H = a.dag() * a + 0.5 * (a + a.dag())
+    e_ops = [a.dag() * a, a + a.dag()]
+    tl = np.linspace(0, 1, 11)
+    out = {}
+    cases = {
+        "ssesolve": lambda m, nt: qt.ssesolve(
+            H, qt.basis(N, 3), tl, [np.sqrt(0.3) * a], e_ops=e_ops, ntraj=nt,
+            seeds=list(range(100, 100 + nt)),
+            options={"method": m, "keep_runs_results": True, "progress_bar": None}),
+        "smesolve": lambda m, nt: qt.smesolve(
+            H, qt.coherent_dm(N, 1.0), tl, c_ops=[np.sqrt(0.1) * a.dag() * a],
+            sc_ops=[np.sqrt(0.2) * a], e_ops=e_ops, ntraj=nt, seeds=list(range(200, 200 + nt)),
+            options={"method": m, "keep_runs_results": True, "progress_bar": None}),
+    }
+    for name, run in cases.items():
+        run("gpu_platen", 1)                            # warm-up (operator build, kernels)
+        nt = 8
+        t0 = time.perf_counter()
+        got = run("gpu_platen", nt)
+        t_gpu = (time.perf_counter() - t0) / nt
+        t0 = time.perf_counter()
+        ref = run("platen", nt)
+        t_ref = (time.perf_counter() - t0) / nt
+        diff = max(float(np.max(np.abs(np.asarray(g) - np.asarray(r))))
+                   for g, r in zip(got.runs_expect, ref.runs_expect))
+        out[name] = {"trajectories": nt, "gpu_s_per_traj": t_gpu, "reference_s_per_traj": t_ref,
+                     "speedup": t_ref / t_gpu, "max_abs_diff_runs_expect": diff,
+                     "steps_per_traj": 1000}
+        log(f"sde: {name} {t_gpu * 1e3:.1f} ms per trajectory on the GPU, reference "
+            f"{t_ref * 1e3:.1f} ms; max |diff| {diff:.1e}")
+    out["workload"] = (f"driven cavity N={N}, sc_op sqrt(0.3) a (smesolve: sqrt(0.2) a and "
+                       "c_op sqrt(0.1) n), tlist linspace(0,1,11), dt 1e-3, 8 trajectories, "
+                       "same seeds for both arms; the reference single-threaded on the host")
+    return out
+
+
 def run_dense(args):
     """The dense small-dimension bucket (tensor-core Lindblad generator, mixed form) against
     the sparse paths, one request at a time: Jaynes-Cummings mesolve (N = 5..60, d = 2N,
@@ -1085,6 +1130,9 @@ def run_ours(args, dist):
     if dist.rank == 0 and "dense" in sections:
         log("dense small-dimension bucket")
         out["dense_bucket"] = run_dense(args)
+    if dist.rank == 0 and "sde" in sections:
+        log("stochastic solvers")
+        out["sde"] = run_sde(args)
     if dist.rank == 0 and "matrix" in sections:
         log("matrix form")
         sysm = S.ising_chain(N_SITES, build_terms=False)
