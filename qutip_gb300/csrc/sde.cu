@@ -1,9 +1,11 @@
 // Stochastic Schrodinger and master equations with the reference's explicit Platen scheme
 // (qutip/solver/sode/_sode.pyx:58-120, Breuer & Petruccione eq. 7.47), drift and diffusion
-// of qutip/solver/sode/ssystem.pyx:119-250.  One CTA integrates one trajectory through
-// n_steps fixed steps with the Wiener increments the host drew (the reference's own
+// of qutip/solver/sode/ssystem.pyx:119-250.  A group of threads integrates one trajectory
+// through n_steps fixed steps with the Wiener increments the host drew (the reference's own
 // generator stream), so a launch covers a whole output interval of one or many
-// trajectories.  Every vector operation follows the reference's order of operations
+// trajectories.  A state of up to 512 entries is integrated by one warp (4 trajectories
+// per CTA; syncs are __syncwarp), a larger one by a CTA of 256 threads.  Every vector
+// operation follows the reference's order of operations
 // (`_data.add(a, b, s)` is a + s b element by element, the complex scalars formed the way
 // the reference forms them); CSR rows are summed in column order.
 #include "capi_internal.h"
@@ -11,7 +13,53 @@
 
 namespace qg {
 
-constexpr int SDE_BLOCK = 256;
+constexpr int SDE_BLOCK = 256;   // CTA shape: one trajectory per CTA
+constexpr int SDE_WARPS = 4;     // warp shape: one trajectory per warp, 4 per CTA
+constexpr int SDE_WARP_MAX_N = 512;  // states up to this length take the warp shape
+
+// A group of GS threads integrating one trajectory: a warp (GS = 32, syncs are
+// __syncwarp, sums are XOR butterflies) or a CTA (GS = SDE_BLOCK).  Sums come back to
+// every thread with the same bits.
+template <int GS>
+struct SdeGroup;
+template <>
+struct SdeGroup<32> {
+  int rank;
+  __device__ __forceinline__ void sync() const { __syncwarp(); }
+  __device__ __forceinline__ double2 sum(double2 v, double*) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+  }
+};
+template <>
+struct SdeGroup<SDE_BLOCK> {
+  int rank;
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+  __device__ double2 sum(double2 v, double* red) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+    constexpr int W = SDE_BLOCK / 32;
+    __syncthreads();  // earlier readers of red are done
+    if ((threadIdx.x & 31) == 0) {
+      red[threadIdx.x >> 5] = v.x;
+      red[W + (threadIdx.x >> 5)] = v.y;
+    }
+    __syncthreads();
+    double re = 0.0, im = 0.0;
+    for (int w = 0; w < W; ++w) {
+      re += red[w];
+      im += red[W + w];
+    }
+    return make_double2(re, im);
+  }
+};
 
 struct Sde {
   const qg_sde* S;
@@ -25,6 +73,7 @@ struct Sde {
   double2* VM;  // m support vectors (-)
   double2* D2P; // m diffusions at VP_i
   double2* D2M; // m diffusions at VM_i
+  double* red;  // reduction scratch (CTA shape)
 };
 
 __device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
@@ -39,11 +88,12 @@ __device__ __forceinline__ double2 axpy(double2 a, double s, double2 b) {
   return make_double2(a.x + s * b.x, a.y + s * b.y);
 }
 
-// y = rows [row0, row0 + n) of a CSR operator times x (block-wide; x complete on entry)
-__device__ void csr_mv(const int* __restrict__ rp, const int* __restrict__ col,
-                       const double2* __restrict__ val, int64_t row0, const double2* x,
-                       double2* y, int n) {
-  for (int r = threadIdx.x; r < n; r += SDE_BLOCK) {
+// y = rows [row0, row0 + n) of a CSR operator times x (x complete on entry)
+template <int GS>
+__device__ void csr_mv(const SdeGroup<GS>& g, const int* __restrict__ rp,
+                       const int* __restrict__ col, const double2* __restrict__ val,
+                       int64_t row0, const double2* x, double2* y, int n) {
+  for (int r = g.rank; r < n; r += GS) {
     const int s = __ldg(rp + row0 + r), e = __ldg(rp + row0 + r + 1);
     double ar = 0.0, ai = 0.0;
     for (int p = s; p < e; ++p) {
@@ -56,103 +106,89 @@ __device__ void csr_mv(const int* __restrict__ rp, const int* __restrict__ col,
   }
 }
 
-// complex block sum, in one fixed order, returned to every thread
-__device__ double2 block_csum(double2 v, double* red) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    v.x += __shfl_down_sync(0xffffffffu, v.x, o);
-    v.y += __shfl_down_sync(0xffffffffu, v.y, o);
-  }
-  constexpr int W = SDE_BLOCK / 32;
-  __syncthreads();  // earlier readers of red are done
-  if ((threadIdx.x & 31) == 0) {
-    red[threadIdx.x >> 5] = v.x;
-    red[W + (threadIdx.x >> 5)] = v.y;
-  }
-  __syncthreads();
-  double re = 0.0, im = 0.0;
-  for (int w = 0; w < W; ++w) {
-    re += red[w];
-    im += red[W + w];
-  }
-  return make_double2(re, im);
-}
-
 // SSE: <x| M_i |x> (M_i x goes through TMP)
-__device__ double2 expect_m(const Sde& q, int i, const double2* x, double* red) {
+template <int GS>
+__device__ double2 expect_m(const SdeGroup<GS>& g, const Sde& q, int i, const double2* x) {
   const qg_sde& S = *q.S;
-  __syncthreads();
-  csr_mv(S.m_rp, S.m_col, static_cast<const double2*>(S.m_val), (int64_t)i * q.n, x, q.TMP, q.n);
+  g.sync();
+  csr_mv(g, S.m_rp, S.m_col, static_cast<const double2*>(S.m_val), (int64_t)i * q.n, x, q.TMP,
+         q.n);
   double2 acc = make_double2(0.0, 0.0);
-  for (int r = threadIdx.x; r < q.n; r += SDE_BLOCK) {
+  for (int r = g.rank; r < q.n; r += GS) {
     const double2 a = x[r], b = q.TMP[r];
     acc.x += a.x * b.x + a.y * b.y;  // conj(a) b
     acc.y += a.x * b.y - a.y * b.x;
   }
-  return block_csum(acc, red);
+  return g.sum(acc, q.red);
 }
 
 // SME: tr of the d x d matrix whose column-stacked form is v
-__device__ double2 trace_vec(const Sde& q, const double2* v, double* red) {
+template <int GS>
+__device__ double2 trace_vec(const SdeGroup<GS>& g, const Sde& q, const double2* v) {
   const int d = q.S->d;
   double2 acc = make_double2(0.0, 0.0);
-  for (int k = threadIdx.x; k < d; k += SDE_BLOCK) {
+  for (int k = g.rank; k < d; k += GS) {
     const double2 a = v[(int64_t)k * (d + 1)];
     acc.x += a.x;
     acc.y += a.y;
   }
-  return block_csum(acc, red);
+  return g.sum(acc, q.red);
 }
 
 // out = drift(x)   (ssystem.pyx:141-154 closed, 227-228 open)
-__device__ void drift(const Sde& q, const double2* x, double2* out, double* red) {
+template <int GS>
+__device__ void drift(const SdeGroup<GS>& g, const Sde& q, const double2* x, double2* out) {
   const qg_sde& S = *q.S;
-  __syncthreads();
-  csr_mv(S.l_rp, S.l_col, static_cast<const double2*>(S.l_val), 0, x, out, q.n);
+  g.sync();
+  csr_mv(g, S.l_rp, S.l_col, static_cast<const double2*>(S.l_val), 0, x, out, q.n);
   if (S.open) return;
   for (int i = 0; i < q.m; ++i) {
-    const double2 e = expect_m(q, i, x, red);
-    __syncthreads();
-    csr_mv(S.c_rp, S.c_col, static_cast<const double2*>(S.c_val), (int64_t)i * q.n, x, q.TMP, q.n);
+    const double2 e = expect_m(g, q, i, x);
+    g.sync();
+    csr_mv(g, S.c_rp, S.c_col, static_cast<const double2*>(S.c_val), (int64_t)i * q.n, x,
+           q.TMP, q.n);
     const double2 s1 = cmul2(make_double2(-0.125 * e.x, -0.125 * e.y), e);  // -0.125 * e * e
     const double2 s2 = make_double2(0.5 * e.x, 0.5 * e.y);
-    for (int r = threadIdx.x; r < q.n; r += SDE_BLOCK) {
-      double2 o = axpy(out[r], s1, x[r]);
+    for (int r = g.rank; r < q.n; r += GS) {
+      const double2 o = axpy(out[r], s1, x[r]);
       out[r] = axpy(o, s2, q.TMP[r]);
     }
   }
 }
 
 // d2[i] = diffusion_i(x) for every i   (ssystem.pyx:156-166 closed, 230-240 open)
-__device__ void diffusion(const Sde& q, const double2* x, double2* d2, double* red) {
+template <int GS>
+__device__ void diffusion(const SdeGroup<GS>& g, const Sde& q, const double2* x, double2* d2) {
   const qg_sde& S = *q.S;
   for (int i = 0; i < q.m; ++i) {
     double2* out = d2 + (int64_t)i * q.n;
-    __syncthreads();
-    csr_mv(S.c_rp, S.c_col, static_cast<const double2*>(S.c_val), (int64_t)i * q.n, x, out, q.n);
+    g.sync();
+    csr_mv(g, S.c_rp, S.c_col, static_cast<const double2*>(S.c_val), (int64_t)i * q.n, x, out,
+           q.n);
     double2 e;
     if (S.open) {
-      __syncthreads();
-      e = trace_vec(q, out, red);
+      g.sync();
+      e = trace_vec(g, q, out);
       e = make_double2(-e.x, -e.y);
     } else {
-      e = expect_m(q, i, x, red);
+      e = expect_m(g, q, i, x);
       e = make_double2(-0.5 * e.x, -0.5 * e.y);
     }
-    for (int r = threadIdx.x; r < q.n; r += SDE_BLOCK) out[r] = axpy(out[r], e, x[r]);
+    for (int r = g.rank; r < q.n; r += GS) out[r] = axpy(out[r], e, x[r]);
   }
 }
 
 // One Platen step from X into OUT (_sode.pyx:62-120).
-__device__ void platen_step(const Sde& q, const double2* X, double2* OUT, const double* dW,
-                            double dt, double* red) {
+template <int GS>
+__device__ void platen_step(const SdeGroup<GS>& g, const Sde& q, const double2* X, double2* OUT,
+                            const double* dW, double dt) {
   const int n = q.n, m = q.m;
   const double sqrt_dt = sqrt(dt);
   const double sqrt_dt_inv = 0.25 / sqrt_dt;
-  drift(q, X, q.F, red);
-  for (int r = threadIdx.x; r < n; r += SDE_BLOCK) q.D1[r] = axpy(X[r], dt, q.F[r]);
-  diffusion(q, X, q.D2, red);
-  for (int r = threadIdx.x; r < n; r += SDE_BLOCK) {
+  drift(g, q, X, q.F);
+  for (int r = g.rank; r < n; r += GS) q.D1[r] = axpy(X[r], dt, q.F[r]);
+  diffusion(g, q, X, q.D2);
+  for (int r = g.rank; r < n; r += GS) {
     const double2 d1 = q.D1[r];
     OUT[r] = make_double2(d1.x * 0.5, d1.y * 0.5);
     double2 vt = d1;
@@ -164,16 +200,16 @@ __device__ void platen_step(const Sde& q, const double2* X, double2* OUT, const 
     }
     q.VT[r] = vt;
   }
-  drift(q, q.VT, q.F, red);
-  for (int r = threadIdx.x; r < n; r += SDE_BLOCK) {
+  drift(g, q, q.VT, q.F);
+  for (int r = g.rank; r < n; r += GS) {
     const double2 o = axpy(OUT[r], 0.5 * dt, q.F[r]);
     OUT[r] = axpy(o, 0.5, X[r]);
   }
   for (int i = 0; i < m; ++i) {
-    diffusion(q, q.VP + (int64_t)i * n, q.D2P, red);
-    diffusion(q, q.VM + (int64_t)i * n, q.D2M, red);
+    diffusion(g, q, q.VP + (int64_t)i * n, q.D2P);
+    diffusion(g, q, q.VM + (int64_t)i * n, q.D2M);
     const double dw = dW[i] * 0.25;
-    for (int r = threadIdx.x; r < n; r += SDE_BLOCK) {
+    for (int r = g.rank; r < n; r += GS) {
       double2 o = axpy(OUT[r], 2 * dw, q.D2[(int64_t)i * n + r]);
       for (int j = 0; j < m; ++j) {
         double dw2p, dw2m;
@@ -193,16 +229,15 @@ __device__ void platen_step(const Sde& q, const double2* X, double2* OUT, const 
   }
 }
 
-__global__ void __launch_bounds__(SDE_BLOCK) sde_platen_kernel(qg_sde S, double2* states,
-                                                               const double* __restrict__ dW,
-                                                               int n_steps, double dt,
-                                                               int64_t work_values) {
-  __shared__ double red[2 * SDE_BLOCK / 32];
-  const int traj = blockIdx.x;
+template <int GS>
+__device__ void run_trajectory(const SdeGroup<GS>& g, const qg_sde& S, int traj,
+                               double2* states, const double* dW, int n_steps, double dt,
+                               int64_t work_values, double* red) {
   Sde q;
   q.S = &S;
   q.n = (int)S.n;
   q.m = S.n_sc;
+  q.red = red;
   const int64_t n = S.n, m = S.n_sc;
   double2* w = static_cast<double2*>(S.work) + (int64_t)traj * work_values;
   q.F = w;
@@ -215,20 +250,38 @@ __global__ void __launch_bounds__(SDE_BLOCK) sde_platen_kernel(qg_sde S, double2
   q.VM = q.VP + m * n;
   q.D2P = q.VM + m * n;
   q.D2M = q.D2P + m * n;
-  double2* X = states + (int64_t)traj * n;
+  double2* home = states + (int64_t)traj * n;
+  double2* X = home;
   double2* OUT = spare;
   const double* dwt = dW + (int64_t)traj * n_steps * m;
   for (int k = 0; k < n_steps; ++k) {
-    platen_step(q, X, OUT, dwt + (int64_t)k * m, dt, red);
-    __syncthreads();
+    platen_step(g, q, X, OUT, dwt + (int64_t)k * m, dt);
+    g.sync();
     double2* t = X;
     X = OUT;
     OUT = t;
   }
-  if (X != states + (int64_t)traj * n) {  // odd step count: the state ended in the spare
-    double2* dst = states + (int64_t)traj * n;
-    for (int r = threadIdx.x; r < q.n; r += SDE_BLOCK) dst[r] = X[r];
+  if (X != home) {  // odd step count: the state ended in the spare
+    for (int r = g.rank; r < q.n; r += GS) home[r] = X[r];
   }
+}
+
+__global__ void __launch_bounds__(SDE_BLOCK) sde_platen_cta_kernel(qg_sde S, double2* states,
+                                                                   const double* __restrict__ dW,
+                                                                   int n_steps, double dt,
+                                                                   int64_t work_values) {
+  __shared__ double red[2 * SDE_BLOCK / 32];
+  const SdeGroup<SDE_BLOCK> g{(int)threadIdx.x};
+  run_trajectory(g, S, blockIdx.x, states, dW, n_steps, dt, work_values, red);
+}
+
+__global__ void __launch_bounds__(32 * SDE_WARPS) sde_platen_warp_kernel(
+    qg_sde S, int n_traj, double2* states, const double* __restrict__ dW, int n_steps, double dt,
+    int64_t work_values) {
+  const int traj = blockIdx.x * SDE_WARPS + (threadIdx.x >> 5);
+  if (traj >= n_traj) return;  // whole warps leave together
+  const SdeGroup<32> g{(int)(threadIdx.x & 31)};
+  run_trajectory(g, S, traj, states, dW, n_steps, dt, work_values, nullptr);
 }
 
 }  // namespace qg
@@ -256,7 +309,14 @@ extern "C" int qg_sde_platen(const qg_sde* S, int32_t n_traj, void* states, cons
   if (n_traj < 0 || n_steps < 0 || !(dt > 0.0)) return set_error(QG_ERR_ARG, "bad launch");
   if (n_traj == 0 || n_steps == 0) return QG_OK;
   if (!states || !dW) return set_error(QG_ERR_ARG, "null states or noise");
-  sde_platen_kernel<<<n_traj, SDE_BLOCK, 0, (cudaStream_t)stream>>>(
-      *S, static_cast<double2*>(states), dW, n_steps, dt, qg_sde_work_values(S->n, S->n_sc));
-  return check_launch("sde_platen_kernel");
+  const int64_t wv = qg_sde_work_values(S->n, S->n_sc);
+  if (S->n <= SDE_WARP_MAX_N) {
+    sde_platen_warp_kernel<<<(n_traj + SDE_WARPS - 1) / SDE_WARPS, 32 * SDE_WARPS, 0,
+                             (cudaStream_t)stream>>>(*S, n_traj, static_cast<double2*>(states),
+                                                     dW, n_steps, dt, wv);
+    return check_launch("sde_platen_warp_kernel");
+  }
+  sde_platen_cta_kernel<<<n_traj, SDE_BLOCK, 0, (cudaStream_t)stream>>>(
+      *S, static_cast<double2*>(states), dW, n_steps, dt, wv);
+  return check_launch("sde_platen_cta_kernel");
 }

@@ -1100,6 +1100,8 @@ def gpu_map(task, values, task_args=None, task_kwargs=None, reduce_func=None, ma
     The per-initial-state no-jump runs of improved sampling with mixed states
     (``_no_jump_simulation``, mcsolve.py:756-763) are single deterministic solves: they
     run one after another through the solver's own ``gpu_vern7`` integrator."""
+    if isinstance(getattr(task, "__self__", None), StochasticSolver):
+        return _gpu_map_sde(task, values, task_args, task_kwargs, reduce_func)
     if getattr(task, "__name__", "") == "_no_jump_simulation" and \
             isinstance(getattr(task, "__self__", None), MCSolver):
         out = [task(v, *(task_args or ()), **(task_kwargs or {})) for v in values]
@@ -1217,6 +1219,118 @@ def gpu_map(task, values, task_args=None, task_kwargs=None, reduce_func=None, ma
 
 
 gpu_map.launched_items = 0
+
+
+def _sde_expect_rows(op_mats, n, open_, device):
+    """Per operator E a vector w with <E> = sum_r conj(psi_r) (E psi)_r (kets: returned as
+    the dense E) or Tr(E rho) = vec(E^T) . vec(rho) (column-stacked rho)."""
+    out = []
+    for m in op_mats:
+        a = m.toarray() if sp.issparse(m) else np.asarray(m)
+        herm = bool(np.allclose(a, a.conj().T, rtol=0, atol=1e-14 * max(1.0, np.abs(a).max())))
+        w = a.T.reshape(-1, order="F") if open_ else a
+        out.append((torch.from_numpy(np.ascontiguousarray(w, dtype=np.complex128)).to(device),
+                    herm))
+    return out
+
+
+def _sde_expect(states, ops, open_):
+    """Expectation values of every trajectory (rows of ``states``) for each operator."""
+    vals = []
+    for w, herm in ops:
+        if open_:
+            v = states @ w
+        else:
+            v = (states.conj() * (states @ w.T)).sum(dim=1)
+        v = v.cpu().numpy()
+        vals.append(v.real.copy() if herm else v)
+    return vals
+
+
+def _gpu_map_sde(task, values, task_args, task_kwargs, reduce_func):
+    """``map="gpu"`` for ``SSESolver`` / ``SMESolver``: every trajectory of a ``run`` in
+    one ``qg_sde_platen`` launch per output interval (the reference's Platen scheme;
+    ``_run_one_traj``, qutip/solver/multitraj.py:272-283).  Each trajectory's Wiener
+    increments come from the reference's ``Wiener`` on the trajectory's own generator
+    (``_get_generator``, multitraj.py:382-393), so the trajectories are the reference's;
+    the results go to ``reduce_func`` as the reference's ``StochasticTrajResult``."""
+    solver = task.__self__
+    if getattr(task, "__name__", "") != "_run_one_traj":
+        raise TypeError(f"map='gpu' does not run the task {getattr(task, '__name__', task)!r}")
+    if task_kwargs:
+        raise TypeError(f"map='gpu' does not support the trajectory options {sorted(task_kwargs)}")
+    opts = solver.options
+    if opts.get("method") not in ("platen", "gpu_platen"):
+        raise TypeError("map='gpu' integrates stochastic equations with the Platen scheme "
+                        "(method 'platen' or 'gpu_platen')")
+    if opts.get("store_states") or opts.get("store_final_state"):
+        raise TypeError("map='gpu' records expectation values and measurements only")
+    state0, tlist, e_ops = task_args
+    if isinstance(e_ops, dict):
+        e_list = list(e_ops.values())
+    elif e_ops is None:
+        e_list = []
+    elif isinstance(e_ops, (list, tuple)):
+        e_list = list(e_ops)
+    else:
+        e_list = [e_ops]
+    e_mats = [_constant_matrix(e, "e_ops") for e in e_list]
+    op = sde_operator(solver.rhs)
+    dt = float(solver._integrator.options["dt"])
+    tl = np.asarray(tlist, dtype=np.float64)
+    # steps per output interval, as _Explicit_Simple_Integrator.integrate counts them
+    steps, t_cur = [], float(tl[0])
+    for t in tl[1:]:
+        N, extra = np.divmod(t - t_cur, dt)
+        N = int(N) + (1 if extra > 0.5 * dt else 0)
+        if t - t_cur < 0.5 * dt:
+            N = 0
+        steps.append(N)
+        t_cur += dt * N
+    total = int(sum(steps))
+    m = op.n_sc
+    seeds = list(values)
+    n_traj = len(seeds)
+    dW = np.empty((n_traj, total, m))
+    for k, seed in enumerate(seeds):
+        w = Wiener(float(tl[0]), dt, solver._get_generator(seed), (1, m))
+        if total:
+            dW[k] = w.dW(float(tl[0]), total)[:, 0, :]
+    dev = _device()
+    psi = _as_gpu(state0).buf
+    states = psi.reshape(1, -1).repeat(n_traj, 1).contiguous()
+    e_w = _sde_expect_rows(e_mats, op.n, op.open, dev)
+    store_m = bool(opts.get("store_measurement"))
+    m_w = _sde_expect_rows([_constant_matrix(mo, "m_ops") for mo in solver.m_ops], op.n,
+                           op.open, dev) if store_m else []
+    e_vals = [_sde_expect(states, e_w, op.open)]
+    m_vals = [_sde_expect(states, m_w, op.open)] if store_m else []
+    noise = []
+    pos = 0
+    for N in steps:
+        if N:
+            block = torch.from_numpy(np.ascontiguousarray(dW[:, pos:pos + N, :])).to(dev)
+            op.platen(states, block, N, dt)
+        noise.append(dW[:, pos:pos + N, :].sum(axis=1) if N else np.zeros((n_traj, 1)))
+        pos += N
+        e_vals.append(_sde_expect(states, e_w, op.open))
+        if store_m:
+            m_vals.append(_sde_expect(states, m_w, op.open))
+    left = None
+    for k, seed in enumerate(seeds):
+        traj = solver._trajectory_resultclass(e_ops, opts)
+        traj.times = [float(t) for t in tl]
+        for j, key in enumerate(traj.e_data):
+            traj.e_data[key] = [v[j][k] for v in e_vals]
+        traj.noise = [nz[k] for nz in noise]
+        if store_m:
+            for j in range(len(traj.m_expect)):
+                traj.m_expect[j][:] = [v[j][k] for v in m_vals]
+        if reduce_func is not None:
+            left = reduce_func((seed, traj, 1))
+            if left is not None and left <= 0:
+                break
+    return None
 
 
 # ---------------------------------------------------------------- register ----

@@ -96,3 +96,29 @@ def test_sde_kernel_matches_the_oracle_restatement(qt):
     for k in range(n_traj):
         want = platen_steps(L, cs, [c + c.conj().T for c in cs], psi[k], dW[k], dt, open_=False)
         np.testing.assert_allclose(got[k], want, atol=1e-12, rtol=0)
+
+
+@pytest.mark.parametrize("solver", ["sse", "sme"])
+def test_gpu_map_runs_every_trajectory_in_one_batch(qt, solver):
+    """map="gpu": all trajectories of a run in one launch per output interval, noise from
+    the reference's Wiener on each trajectory's generator; every trajectory equals the
+    reference's serial run with the same seeds (expectation values and measurements)."""
+    N = 6
+    a = qt.destroy(N)
+    H = a.dag() * a + 0.3 * (a + a.dag())
+    e_ops = [a.dag() * a, a + a.dag()]
+    tl = np.linspace(0, 0.5, 6)
+    seeds = [21, 22, 23, 24, 25]
+    if solver == "sse":
+        def run(opts):
+            return qt.ssesolve(H, qt.basis(N, 1), tl, [np.sqrt(0.3) * a], e_ops=e_ops,
+                               ntraj=len(seeds), seeds=seeds, options=opts)
+    else:
+        def run(opts):
+            return qt.smesolve(H, qt.coherent_dm(N, 0.6), tl, c_ops=[np.sqrt(0.1) * a],
+                               sc_ops=[np.sqrt(0.2) * a], e_ops=e_ops, ntraj=len(seeds),
+                               seeds=seeds, options=opts)
+    ref = run(_opts("platen"))
+    got = run({**_opts("platen"), "map": "gpu"})
+    _same(got, ref)
+    assert len(got.runs_expect[0]) == len(seeds)
