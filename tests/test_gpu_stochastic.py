@@ -72,18 +72,24 @@ def test_smesolve_matches_the_reference(qt, heterodyne):
     _same(got, ref)
 
 
-def test_sde_kernel_matches_the_oracle_restatement(qt):
-    """qg_sde_platen on a batch of trajectories (one CTA each, two stochastic operators,
-    an odd number of steps) against the numpy restatement of the Platen step."""
+@pytest.mark.parametrize("d", [7, 520])
+def test_sde_kernel_matches_the_oracle_restatement(qt, d):
+    """qg_sde_platen on a batch of trajectories (d = 7: one warp each; d = 520: one CTA
+    each), two stochastic operators, an odd number of steps, against the numpy
+    restatement of the Platen step."""
     import scipy.sparse as sp
     from oracle.sde import platen_steps
     from qutip_gb300.stochastic import SdeOperator
     rng = np.random.default_rng(3)
-    d = 7
-    h = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    dens = 1.0 if d < 64 else 0.02
+
+    def rand():
+        m = sp.random(d, d, density=dens, random_state=rng, format="csr")
+        m.data = rng.normal(size=m.nnz) + 1j * rng.normal(size=m.nnz)
+        return m
+    h = rand()
     H = sp.csr_matrix(h + h.conj().T)
-    cs = [sp.csr_matrix(0.3 * (rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))))
-          for _ in range(2)]
+    cs = [0.3 * rand() for _ in range(2)]
     op = SdeOperator.sse(H, cs)
     n_traj, n_steps, dt = 5, 37, 1e-3
     psi = rng.normal(size=(n_traj, d)) + 1j * rng.normal(size=(n_traj, d))
