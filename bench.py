@@ -756,9 +756,11 @@ def large_cpu_baseline(host_groups, state0, rhs_full, reps=2):
 def run_sde(args):
     """Stochastic solvers through QuTiP's own API: ``ssesolve`` (homodyne) and ``smesolve``
     (with a deterministic collapse operator) of a driven cavity (N = 20), tlist
-    linspace(0, 1, 11) at dt = 1e-3 (1000 Platen steps per trajectory), the reference's
-    ``platen`` against ``gpu_platen`` with the same seeds: wall time per trajectory and
-    the largest difference of the per-trajectory expectation values."""
+    linspace(0, 1, 11) at dt = 1e-3 (1000 Platen steps per trajectory).  Three ways with
+    the same seeds: the reference's ``platen`` (8 trajectories, serial), the drop-in
+    integrator ``gpu_platen`` (8 trajectories, one at a time) and ``map="gpu"`` (256
+    trajectories in one launch per output interval); wall time per trajectory and the
+    largest difference of the first 8 trajectories' expectation values."""
     qt, _ = host_qutip()
     N = 20
     a = qt.destroy(N)
@@ -766,35 +768,47 @@ def run_sde(args):
     e_ops = [a.dag() * a, a + a.dag()]
     tl = np.linspace(0, 1, 11)
     out = {}
+
+    def opts(method, **kw):
+        return {"method": method, "keep_runs_results": True, "progress_bar": None, **kw}
     cases = {
-        "ssesolve": lambda m, nt: qt.ssesolve(
+        "ssesolve": lambda o, nt, s0: qt.ssesolve(
             H, qt.basis(N, 3), tl, [np.sqrt(0.3) * a], e_ops=e_ops, ntraj=nt,
-            seeds=list(range(100, 100 + nt)),
-            options={"method": m, "keep_runs_results": True, "progress_bar": None}),
-        "smesolve": lambda m, nt: qt.smesolve(
+            seeds=list(range(s0, s0 + nt)), options=o),
+        "smesolve": lambda o, nt, s0: qt.smesolve(
             H, qt.coherent_dm(N, 1.0), tl, c_ops=[np.sqrt(0.1) * a.dag() * a],
-            sc_ops=[np.sqrt(0.2) * a], e_ops=e_ops, ntraj=nt, seeds=list(range(200, 200 + nt)),
-            options={"method": m, "keep_runs_results": True, "progress_bar": None}),
+            sc_ops=[np.sqrt(0.2) * a], e_ops=e_ops, ntraj=nt, seeds=list(range(s0, s0 + nt)),
+            options=o),
     }
     for name, run in cases.items():
-        run("gpu_platen", 1)                            # warm-up (operator build, kernels)
-        nt = 8
+        s0 = 100
+        run(opts("gpu_platen"), 1, s0)                   # warm-up (operator build, kernels)
+        run(opts("platen", map="gpu"), 4, s0)
+        nt, nb = 8, 256
         t0 = time.perf_counter()
-        got = run("gpu_platen", nt)
-        t_gpu = (time.perf_counter() - t0) / nt
-        t0 = time.perf_counter()
-        ref = run("platen", nt)
+        ref = run(opts("platen"), nt, s0)
         t_ref = (time.perf_counter() - t0) / nt
-        diff = max(float(np.max(np.abs(np.asarray(g) - np.asarray(r))))
-                   for g, r in zip(got.runs_expect, ref.runs_expect))
-        out[name] = {"trajectories": nt, "gpu_s_per_traj": t_gpu, "reference_s_per_traj": t_ref,
-                     "speedup": t_ref / t_gpu, "max_abs_diff_runs_expect": diff,
+        t0 = time.perf_counter()
+        one = run(opts("gpu_platen"), nt, s0)
+        t_one = (time.perf_counter() - t0) / nt
+        t0 = time.perf_counter()
+        bat = run(opts("platen", map="gpu"), nb, s0)
+        t_bat = (time.perf_counter() - t0) / nb
+
+        def diff(res):
+            return max(float(np.max(np.abs(np.asarray(g)[:nt] - np.asarray(r))))
+                       for g, r in zip(res.runs_expect, ref.runs_expect))
+        out[name] = {"reference_s_per_traj": t_ref, "gpu_platen_s_per_traj": t_one,
+                     "map_gpu_s_per_traj": t_bat, "map_gpu_trajectories": nb,
+                     "speedup_map_gpu": t_ref / t_bat, "speedup_gpu_platen": t_ref / t_one,
+                     "max_abs_diff_gpu_platen": diff(one), "max_abs_diff_map_gpu": diff(bat),
                      "steps_per_traj": 1000}
-        log(f"sde: {name} {t_gpu * 1e3:.1f} ms per trajectory on the GPU, reference "
-            f"{t_ref * 1e3:.1f} ms; max |diff| {diff:.1e}")
+        log(f"sde: {name} reference {t_ref * 1e3:.1f} ms per trajectory, gpu_platen "
+            f"{t_one * 1e3:.1f} ms, map='gpu' {t_bat * 1e3:.2f} ms ({nb} trajectories); "
+            f"max |diff| {max(diff(one), diff(bat)):.1e}")
     out["workload"] = (f"driven cavity N={N}, sc_op sqrt(0.3) a (smesolve: sqrt(0.2) a and "
-                       "c_op sqrt(0.1) n), tlist linspace(0,1,11), dt 1e-3, 8 trajectories, "
-                       "same seeds for both arms; the reference single-threaded on the host")
+                       "c_op sqrt(0.1) n), tlist linspace(0,1,11), dt 1e-3, same seeds in every "
+                       "arm; the reference single-threaded on the host")
     return out
 
 
