@@ -3,7 +3,7 @@
 // of qutip/solver/sode/ssystem.pyx:119-250.  A group of threads integrates one trajectory
 // through n_steps fixed steps with the Wiener increments the host drew (the reference's own
 // generator stream), so a launch covers a whole output interval of one or many
-// trajectories.  A state of up to 512 entries is integrated by one warp (4 trajectories
+// trajectories.  A state of up to 64 entries is integrated by one warp (4 trajectories
 // per CTA; syncs are __syncwarp), a larger one by a CTA of 256 threads.  Every vector
 // operation follows the reference's order of operations
 // (`_data.add(a, b, s)` is a + s b element by element, the complex scalars formed the way
@@ -15,7 +15,7 @@ namespace qg {
 
 constexpr int SDE_BLOCK = 256;   // CTA shape: one trajectory per CTA
 constexpr int SDE_WARPS = 4;     // warp shape: one trajectory per warp, 4 per CTA
-constexpr int SDE_WARP_MAX_N = 512;  // states up to this length take the warp shape
+constexpr int SDE_WARP_MAX_N = 64;  // states up to this length take the warp shape
 
 // A group of GS threads integrating one trajectory: a warp (GS = 32, syncs are
 // __syncwarp, sums are XOR butterflies) or a CTA (GS = SDE_BLOCK).  Sums come back to
