@@ -1239,7 +1239,9 @@ def _sde_expect(states, ops, open_):
     vals = []
     for w, herm in ops:
         if open_:
-            v = states @ w
+            # element-wise product and row sums: a complex128 matrix-vector product through
+            # torch took ~57 ms for 256 x 400 here (cuBLAS gemv path), this ~0.05 ms
+            v = (states * w).sum(dim=1)
         else:
             v = (states.conj() * (states @ w.T)).sum(dim=1)
         v = v.cpu().numpy()
