@@ -81,7 +81,8 @@ def parse():
     ap.add_argument("--mc-ntraj", type=int, default=4096)
     ap.add_argument("--large-sites", type=int, default=12,
                     help="Ising chain length of the large mixed-precision section (0: skip)")
-    ap.add_argument("--profile", default=None, choices=["stage", "batch", "matrix", "dense"],
+    ap.add_argument("--profile", default=None,
+                    choices=["stage", "batch", "matrix", "dense", "sde"],
                     help="run the ncu profiling case only (fused stage kernel, untuned); "
                          "prints nothing to parse")
     ap.add_argument("--profile-sites", type=int, default=10)
@@ -1232,6 +1233,34 @@ def run_profile_dense(args):
     print(f"dense: {op.launch_desc()}, {op.gemm_flops() / 1e6:.1f} MFLOP issued per application")
 
 
+def run_profile_sde(args):
+    """ncu case for the stochastic Platen kernel: the smesolve system of the ``sde`` section
+    (driven cavity N = 20, vec(rho) of 400 entries), 10 steps for 1, 8, 64 and 256
+    trajectories, each shape launched twice (the second one timed with CUDA events)."""
+    import torch
+    qt, _ = host_qutip()
+    from qutip_gb300 import qutip_plugin as P
+    torch.cuda.set_device(0)
+    N = 20
+    a = qt.destroy(N)
+    H = a.dag() * a + 0.5 * (a + a.dag())
+    sol = qt.SMESolver(H, [np.sqrt(0.2) * a], heterodyne=False,
+                       c_ops=[np.sqrt(0.1) * a.dag() * a], options={"method": "platen"})
+    op = P.sde_operator(sol.rhs)
+    rho = qt.coherent_dm(N, 1.0).full().reshape(-1, order="F")
+    steps = 10
+    for nt in (1, 8, 64, 256):
+        states = torch.from_numpy(np.tile(rho, (nt, 1))).cuda()
+        dW = torch.from_numpy(np.random.default_rng(1).normal(0, 0.03, size=(nt, steps, 1))).cuda()
+        op.platen(states, dW, steps, 1e-3)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        op.platen(states, dW, steps, 1e-3)
+        e1.record()
+        e1.synchronize()
+        print(f"sde: {nt} trajectories, {1e3 * e0.elapsed_time(e1) / steps:.1f} us per step")
+
+
 def run_profile_batch(args):
     """ncu case for the batched trajectory kernel: ``--profile-ntraj`` Bose-Hubbard
     trajectories (default 256) over t in [0, ``--profile-tend``] (default 5, 10
@@ -1261,6 +1290,9 @@ def main():
         return
     if args.profile == "dense":
         run_profile_dense(args)
+        return
+    if args.profile == "sde":
+        run_profile_sde(args)
         return
     dist = Dist(args.gpus)
     if args.impl == "reference":
