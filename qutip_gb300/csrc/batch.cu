@@ -481,8 +481,7 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
         // WRMS error term in FP64 against the FP64 state (wrmn_error_dense,
         // qutip/core/data/ode.pyx:27-52), written as |e|^2 / (atol + rtol |y|)^2
         const double er = (double)erh + (double)erl, ei = (double)eih + (double)eil;
-        const double sc = X.S->atol + X.S->rtol * sqrt(yr * yr + yi * yi);
-        err_acc += (er * er + ei * ei) / (sc * sc);
+        err_acc += wrms_term(er * er + ei * ei, yr * yr + yi * yi, X.S->atol, X.S->rtol);
       } else {
         CT er = 0, ei = 0;
         double yr = X.y[cur][r].x, yi = X.y[cur][r].y;
@@ -500,9 +499,8 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
           }
         }
         X.y[cur ^ 1][r] = make_double2(yr, yi);
-        const double w = sqrt((double)er * er + (double)ei * ei) /
-                         (X.S->atol + X.S->rtol * sqrt(yr * yr + yi * yi));
-        err_acc += w * w;
+        err_acc += wrms_term((double)er * er + (double)ei * ei, yr * yr + yi * yi, X.S->atol,
+                             X.S->rtol);
       }
     }
   }

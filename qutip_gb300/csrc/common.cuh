@@ -124,6 +124,26 @@ __device__ __forceinline__ double block_sum(double v, double* smem /* [BLOCK/32]
   return r;
 }
 
+// WRMS term |e|^2 / (atol + rtol sqrt(u))^2 in FP64 (u = |y|^2, e2 = |e|^2) to ~1e-13
+// relative without an FP64 square root or division: 1/sqrt(u) and 1/sc start from the FP32
+// intrinsics and take one Newton-Raphson step each in FP64 (r <- r (3 - u r^2) / 2 and
+// i <- i (2 - sc i), each doubling the correct digits).  An FP64 sqrt and divide cost ~25
+// FP64 operations per row, which made the last Vern7 stage the slowest by far on a GPU
+// whose FP64 pipe runs at 1/64 of FP32.  Magnitudes below 1e-15 count as zero (their share
+// of atol + rtol |y| is below 1e-13 of atol).
+__device__ __forceinline__ double wrms_term(double e2, double u, double atol, double rtol) {
+  double mag = 0.0;
+  if (u > 1e-30) {
+    const double r0 = (double)rsqrtf((float)u);
+    const double r1 = r0 * fma(-0.5 * u * r0, r0, 1.5);
+    mag = u * r1;
+  }
+  const double sc = fma(rtol, mag, atol);
+  const double i0 = (double)__frcp_rn((float)sc);
+  const double i1 = i0 * fma(-sc, i0, 2.0);
+  return e2 * (i1 * i1);
+}
+
 // ---------------------------------------------------- coefficient programs --
 // Opcodes shared with qutip_gb300/coefficients.py (OPCODES).
 enum : int {

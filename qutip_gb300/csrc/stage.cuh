@@ -154,8 +154,7 @@ __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
         // WRMS error term in FP64 against the FP64 state (wrmn_error_dense,
         // qutip/core/data/ode.pyx:27-52), written as |e|^2 / (atol + rtol |y|)^2
         const double er = (double)erh + (double)erl, ei = (double)eih + (double)eil;
-        const double sc = rk.atol + rk.rtol * sqrt(yf.x * yf.x + yf.y * yf.y);
-        err_acc += (er * er + ei * ei) / (sc * sc);
+        err_acc += wrms_term(er * er + ei * ei, yf.x * yf.x + yf.y * yf.y, rk.atol, rk.rtol);
         return;
       } else {
         // reference order: y_front = y_prev, then += fb_j k_j term by term
@@ -173,8 +172,7 @@ __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
         ymag2 = (double)ys.re * ys.re + (double)ys.im * ys.im;
       }
       // wrmn_error_dense (qutip/core/data/ode.pyx:27-52) as |e|^2 / (atol + rtol |y|)^2
-      const double sc = rk.atol + rk.rtol * sqrt(ymag2);
-      err_acc += ((double)e.re * e.re + (double)e.im * e.im) / (sc * sc);
+      err_acc += wrms_term((double)e.re * e.re + (double)e.im * e.im, ymag2, rk.atol, rk.rtol);
     }
   }
 }
