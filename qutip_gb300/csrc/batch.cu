@@ -499,8 +499,11 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
           }
         }
         X.y[cur ^ 1][r] = make_double2(yr, yi);
-        err_acc += wrms_term((double)er * er + (double)ei * ei, yr * yr + yi * yi, X.S->atol,
-                             X.S->rtol);
+        // IEEE square roots and division: the complex128 form takes the reference's steps
+        // (a 1e-13 change of the error norm moved one of 4096 BH trajectories' jumps)
+        const double w = sqrt((double)er * er + (double)ei * ei) /
+                         (X.S->atol + X.S->rtol * sqrt(yr * yr + yi * yi));
+        err_acc += w * w;
       }
     }
   }

@@ -130,7 +130,9 @@ __device__ __forceinline__ double block_sum(double v, double* smem /* [BLOCK/32]
 // i <- i (2 - sc i), each doubling the correct digits).  An FP64 sqrt and divide cost ~25
 // FP64 operations per row, which made the last Vern7 stage the slowest by far on a GPU
 // whose FP64 pipe runs at 1/64 of FP32.  Magnitudes below 1e-15 count as zero (their share
-// of atol + rtol |y| is below 1e-13 of atol).
+// of atol + rtol |y| is below 1e-13 of atol).  Used by the mixed form, whose error estimate
+// carries complex64 rounding anyway; the complex128 form keeps IEEE sqrt and division so
+// that its step sequence and jump records are the reference's.
 __device__ __forceinline__ double wrms_term(double e2, double u, double atol, double rtol) {
   double mag = 0.0;
   if (u > 1e-30) {

@@ -171,8 +171,10 @@ __device__ __forceinline__ void epilogue(int row, cx<typename elem<DT>::R> acc,
         const cx<CT> ys = ld_cx<CT>(static_cast<const YT*>(rk.y_front) + row);
         ymag2 = (double)ys.re * ys.re + (double)ys.im * ys.im;
       }
-      // wrmn_error_dense (qutip/core/data/ode.pyx:27-52) as |e|^2 / (atol + rtol |y|)^2
-      err_acc += wrms_term((double)e.re * e.re + (double)e.im * e.im, ymag2, rk.atol, rk.rtol);
+      // wrmn_error_dense (qutip/core/data/ode.pyx:27-52) as |e|^2 / (atol + rtol |y|)^2,
+      // with IEEE square root and division: the complex128 form takes the reference's steps
+      const double sc = rk.atol + rk.rtol * sqrt(ymag2);
+      err_acc += ((double)e.re * e.re + (double)e.im * e.im) / (sc * sc);
     }
   }
 }
