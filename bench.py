@@ -771,7 +771,7 @@ def run_sde(args):
     out = {}
 
     def opts(method, **kw):
-        return {"method": method, "keep_runs_results": True, "progress_bar": None, **kw}
+        return {"method": method, "keep_runs_results": True, "progress_bar": False, **kw}
     cases = {
         "ssesolve": lambda o, nt, s0: qt.ssesolve(
             H, qt.basis(N, 3), tl, [np.sqrt(0.3) * a], e_ops=e_ops, ntraj=nt,

@@ -534,7 +534,7 @@ __device__ __forceinline__ cplx prog_coef(const int* code, const int* start, con
   return eval_coef(code + start[g], consts, t);
 }
 
-template <int DT, int YDT, int EPI>
+template <int DT, int YDT, int EPI, bool HERM>
 __global__ void __launch_bounds__(LB_BLOCK)
     lindblad_kernel(qg_lindblad L, double t, const typename elem<DT>::T* __restrict__ x,
                     AxpbyArgs ax, RkArgs rk) {
@@ -660,7 +660,7 @@ __global__ void __launch_bounds__(LB_BLOCK)
     }
     return acc;
   };
-  if (!L.hermitian) {
+  if constexpr (!HERM) {
     // (r, c) of idx, advanced by the grid stride without a division per element
     const int stride = gridDim.x * LB_BLOCK;
     const int sc = stride / d, sr = stride - (stride / d) * d;
@@ -844,11 +844,13 @@ static int launch_any(cudaStream_t st, const qg_csr_groups& A, double t, const v
   return check_launch("spmv_direct_kernel");
 }
 
-template <int DT, int YDT, int EPI>
-static int launch_lindblad(cudaStream_t st, const qg_lindblad& L, double t, const void* x,
-                           const AxpbyArgs& ax, const RkArgs& rk) {
+// The full form and the Hermitian branch are separate instantiations: sharing one kernel
+// body, the full form's code generation degraded (dense d = 128 operators: 3x slower).
+template <int DT, int YDT, int EPI, bool HERM>
+static int launch_lindblad_form(cudaStream_t st, const qg_lindblad& L, double t, const void* x,
+                                const AxpbyArgs& ax, const RkArgs& rk) {
   using ST = typename elem<DT>::T;
-  auto kern = lindblad_kernel<DT, YDT, EPI>;
+  auto kern = lindblad_kernel<DT, YDT, EPI, HERM>;
   static OccCache cache;  // one per instantiation
   const int per_sm = staged_occupancy(kern, LB_BLOCK, 0, cache);
   if (per_sm <= 0) return set_error(QG_ERR_CUDA, "occupancy query failed");
@@ -859,6 +861,13 @@ static int launch_lindblad(cudaStream_t st, const qg_lindblad& L, double t, cons
   const int grid = (int)(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
   kern<<<grid, LB_BLOCK, 0, st>>>(L, t, (const ST*)x, ax, rk);
   return check_launch("lindblad_kernel");
+}
+
+template <int DT, int YDT, int EPI>
+static int launch_lindblad(cudaStream_t st, const qg_lindblad& L, double t, const void* x,
+                           const AxpbyArgs& ax, const RkArgs& rk) {
+  return L.hermitian ? launch_lindblad_form<DT, YDT, EPI, true>(st, L, t, x, ax, rk)
+                     : launch_lindblad_form<DT, YDT, EPI, false>(st, L, t, x, ax, rk);
 }
 
 static int check_groups(const qg_csr_groups* A) {
