@@ -1136,6 +1136,8 @@ def run_ours(args, dist):
         "clocks": clk,
     }
     sections = set() if args.quick else set(args.sections.split(","))
+    # stdout carries the one JSON line: anything a library prints goes to stderr meanwhile
+    _stdout, sys.stdout = sys.stdout, sys.stderr
     if dist.rank == 0 and "served" in sections:
         log("served stream")
         out["served"] = run_served(args)
@@ -1166,6 +1168,7 @@ def run_ours(args, dist):
             out["cpu_baseline"] = cpu_baseline(k, rhs_sample, int(rhs_full))
         except Exception as exc:  # noqa: BLE001
             out["cpu_baseline"] = {"value": None, "error": repr(exc)[:300]}
+    sys.stdout = _stdout
     if dist.rank == 0:
         print(json.dumps(out))
     dist.close()
