@@ -352,6 +352,11 @@ int64_t qg_sde_work_values(int64_t n, int32_t n_sc);
 int qg_sde_platen(const qg_sde* S, int32_t n_traj, void* states, const double* dW,
                   int32_t n_steps, double dt, void* stream);
 
+/* The same with the Euler-Maruyama scheme (EulerSODE, qutip/solver/sode/itotaylor.py:12-26;
+ * steps in qutip/solver/sode/_sode.pyx:32-55): x + dt drift(x) + sum_i dW_i diffusion_i(x). */
+int qg_sde_euler(const qg_sde* S, int32_t n_traj, void* states, const double* dW,
+                 int32_t n_steps, double dt, void* stream);
+
 /* Non-zero when a kernel of this library gave up a bounded wait on the current
  * device (the result of that launch is invalid); reading clears the flag. */
 int qg_device_fault(void);

@@ -79,3 +79,19 @@ def platen_steps(L, C, M, x, dW, dt, open_):
     for k in range(len(dW)):
         x = platen_step(L, C, M, x, dW[k], dt, open_)
     return x
+
+
+def euler_step(L, C, M, x, dW, dt, open_):
+    """One Euler-Maruyama step (_sode.pyx:32-55)."""
+    out = x + dt * drift(L, C, M, x, open_)
+    d2 = diffusion(C, M, x, open_)
+    for i in range(len(C)):
+        out = out + dW[i] * d2[i]
+    return out
+
+
+def euler_steps(L, C, M, x, dW, dt, open_):
+    x = np.asarray(x, dtype=np.complex128)
+    for k in range(len(dW)):
+        x = euler_step(L, C, M, x, dW[k], dt, open_)
+    return x

@@ -112,6 +112,8 @@ _SIGS = {
     "qg_sde_work_values": (C.c_int64, [C.c_int64, C.c_int32]),
     "qg_sde_platen": (C.c_int, [_P(Sde), C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                 C.c_double, C.c_void_p]),
+    "qg_sde_euler": (C.c_int, [_P(Sde), C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                               C.c_double, C.c_void_p]),
     "qg_rk_combine": (C.c_int, [_P(StateView), C.c_void_p, C.c_int, C.c_void_p]),
     "qg_norm2": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                            C.c_void_p]),
@@ -136,7 +138,7 @@ COMPUTE_ENTRY_POINTS = {
     "qg_spmv_csr", "qg_spmm_csr", "qg_spmv_dia", "qg_vern7_stage", "qg_rk_combine", "qg_norm2",
     "qg_expect_dm", "qg_expect_ket", "qg_batch_vern7", "qg_batch_vern7_noalloc",
     "qg_lindblad_apply", "qg_lindblad_stage", "qg_dense_lindblad_apply", "qg_dense_lindblad_stage",
-    "qg_sde_platen",
+    "qg_sde_platen", "qg_sde_euler",
 }
 LAUNCHES = [0]
 

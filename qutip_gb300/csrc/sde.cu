@@ -229,7 +229,22 @@ __device__ void platen_step(const SdeGroup<GS>& g, const Sde& q, const double2* 
   }
 }
 
+// One Euler-Maruyama step from X into OUT (_sode.pyx:32-55): X + dt drift + sum_i dW_i d2_i.
 template <int GS>
+__device__ void euler_step(const SdeGroup<GS>& g, const Sde& q, const double2* X, double2* OUT,
+                           const double* dW, double dt) {
+  drift(g, q, X, q.F);
+  diffusion(g, q, X, q.D2);
+  for (int r = g.rank; r < q.n; r += GS) {
+    double2 o = axpy(X[r], dt, q.F[r]);
+    for (int i = 0; i < q.m; ++i) o = axpy(o, dW[i], q.D2[(int64_t)i * q.n + r]);
+    OUT[r] = o;
+  }
+}
+
+constexpr int SDE_PLATEN = 0, SDE_EULER = 1;
+
+template <int GS, int SCHEME>
 __device__ void run_trajectory(const SdeGroup<GS>& g, const qg_sde& S, int traj,
                                double2* states, const double* dW, int n_steps, double dt,
                                int64_t work_values, double* red) {
@@ -255,7 +270,10 @@ __device__ void run_trajectory(const SdeGroup<GS>& g, const qg_sde& S, int traj,
   double2* OUT = spare;
   const double* dwt = dW + (int64_t)traj * n_steps * m;
   for (int k = 0; k < n_steps; ++k) {
-    platen_step(g, q, X, OUT, dwt + (int64_t)k * m, dt);
+    if constexpr (SCHEME == SDE_EULER)
+      euler_step(g, q, X, OUT, dwt + (int64_t)k * m, dt);
+    else
+      platen_step(g, q, X, OUT, dwt + (int64_t)k * m, dt);
     g.sync();
     double2* t = X;
     X = OUT;
@@ -266,34 +284,27 @@ __device__ void run_trajectory(const SdeGroup<GS>& g, const qg_sde& S, int traj,
   }
 }
 
-__global__ void __launch_bounds__(SDE_BLOCK) sde_platen_cta_kernel(qg_sde S, double2* states,
-                                                                   const double* __restrict__ dW,
-                                                                   int n_steps, double dt,
-                                                                   int64_t work_values) {
+template <int SCHEME>
+__global__ void __launch_bounds__(SDE_BLOCK) sde_cta_kernel(qg_sde S, double2* states,
+                                                            const double* __restrict__ dW,
+                                                            int n_steps, double dt,
+                                                            int64_t work_values) {
   __shared__ double red[2 * SDE_BLOCK / 32];
   const SdeGroup<SDE_BLOCK> g{(int)threadIdx.x};
-  run_trajectory(g, S, blockIdx.x, states, dW, n_steps, dt, work_values, red);
+  run_trajectory<SDE_BLOCK, SCHEME>(g, S, blockIdx.x, states, dW, n_steps, dt, work_values, red);
 }
 
-__global__ void __launch_bounds__(32 * SDE_WARPS) sde_platen_warp_kernel(
+template <int SCHEME>
+__global__ void __launch_bounds__(32 * SDE_WARPS) sde_warp_kernel(
     qg_sde S, int n_traj, double2* states, const double* __restrict__ dW, int n_steps, double dt,
     int64_t work_values) {
   const int traj = blockIdx.x * SDE_WARPS + (threadIdx.x >> 5);
   if (traj >= n_traj) return;  // whole warps leave together
   const SdeGroup<32> g{(int)(threadIdx.x & 31)};
-  run_trajectory(g, S, traj, states, dW, n_steps, dt, work_values, nullptr);
+  run_trajectory<32, SCHEME>(g, S, traj, states, dW, n_steps, dt, work_values, nullptr);
 }
 
-}  // namespace qg
-
-using namespace qg;
-
-extern "C" int64_t qg_sde_work_values(int64_t n, int32_t n_sc) {
-  return (5 + 5 * (int64_t)n_sc) * n;
-}
-
-extern "C" int qg_sde_platen(const qg_sde* S, int32_t n_traj, void* states, const double* dW,
-                             int32_t n_steps, double dt, void* stream) {
+static int check_sde(const qg_sde* S) {
   if (!S) return set_error(QG_ERR_ARG, "null system");
   if (S->n < 1 || S->n >= (int64_t)INT32_MAX / (QG_MAX_COPS + 1))
     return set_error(QG_ERR_ARG, "state length out of range");
@@ -306,17 +317,43 @@ extern "C" int qg_sde_platen(const qg_sde* S, int32_t n_traj, void* states, cons
     return set_error(QG_ERR_ARG, "null operator or workspace");
   if (!S->open && (!S->m_rp || !S->m_col || !S->m_val))
     return set_error(QG_ERR_ARG, "SSE needs the expectation operators");
+  return QG_OK;
+}
+
+template <int SCHEME>
+static int launch_sde(const qg_sde* S, int32_t n_traj, void* states, const double* dW,
+                      int32_t n_steps, double dt, void* stream) {
+  int rc = check_sde(S);
+  if (rc) return rc;
   if (n_traj < 0 || n_steps < 0 || !(dt > 0.0)) return set_error(QG_ERR_ARG, "bad launch");
   if (n_traj == 0 || n_steps == 0) return QG_OK;
   if (!states || !dW) return set_error(QG_ERR_ARG, "null states or noise");
-  const int64_t wv = qg_sde_work_values(S->n, S->n_sc);
+  const int64_t wv = (5 + 5 * (int64_t)S->n_sc) * S->n;
   if (S->n <= SDE_WARP_MAX_N) {
-    sde_platen_warp_kernel<<<(n_traj + SDE_WARPS - 1) / SDE_WARPS, 32 * SDE_WARPS, 0,
-                             (cudaStream_t)stream>>>(*S, n_traj, static_cast<double2*>(states),
-                                                     dW, n_steps, dt, wv);
-    return check_launch("sde_platen_warp_kernel");
+    sde_warp_kernel<SCHEME><<<(n_traj + SDE_WARPS - 1) / SDE_WARPS, 32 * SDE_WARPS, 0,
+                              (cudaStream_t)stream>>>(*S, n_traj, static_cast<double2*>(states),
+                                                      dW, n_steps, dt, wv);
+    return check_launch("sde_warp_kernel");
   }
-  sde_platen_cta_kernel<<<n_traj, SDE_BLOCK, 0, (cudaStream_t)stream>>>(
+  sde_cta_kernel<SCHEME><<<n_traj, SDE_BLOCK, 0, (cudaStream_t)stream>>>(
       *S, static_cast<double2*>(states), dW, n_steps, dt, wv);
-  return check_launch("sde_platen_cta_kernel");
+  return check_launch("sde_cta_kernel");
+}
+
+}  // namespace qg
+
+using namespace qg;
+
+extern "C" int64_t qg_sde_work_values(int64_t n, int32_t n_sc) {
+  return (5 + 5 * (int64_t)n_sc) * n;
+}
+
+extern "C" int qg_sde_platen(const qg_sde* S, int32_t n_traj, void* states, const double* dW,
+                             int32_t n_steps, double dt, void* stream) {
+  return launch_sde<SDE_PLATEN>(S, n_traj, states, dW, n_steps, dt, stream);
+}
+
+extern "C" int qg_sde_euler(const qg_sde* S, int32_t n_traj, void* states, const double* dW,
+                            int32_t n_steps, double dt, void* stream) {
+  return launch_sde<SDE_EULER>(S, n_traj, states, dW, n_steps, dt, stream);
 }

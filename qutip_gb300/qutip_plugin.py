@@ -936,6 +936,7 @@ class IntegratorGpuPlaten(SIntegrator):
     integrator_options = {"dt": 0.001, "tol": 1e-10}
     N_dw = 1
     _stepper_options = []
+    scheme = "platen"
 
     def __init__(self, rhs, options):
         self._options = self.integrator_options.copy()
@@ -987,7 +988,7 @@ class IntegratorGpuPlaten(SIntegrator):
         dW = self.wiener.dW(self.t, N)
         dev = torch.from_numpy(np.ascontiguousarray(dW[:, 0, :], dtype=np.float64)).to(
             self._state.device, non_blocking=False)
-        self._op.platen(self._state.view(1, -1), dev, N, dt)
+        self._op.platen(self._state.view(1, -1), dev, N, dt, scheme=self.scheme)
         self.t += dt * N
         return self.t, GpuDense(self._state, shape=(self._op.n, 1), copy=copy), \
             np.sum(dW[:, 0, :], axis=0)
@@ -1003,6 +1004,12 @@ class IntegratorGpuPlaten(SIntegrator):
     @options.setter
     def options(self, new_options):
         Integrator.options.fset(self, new_options)
+
+
+class IntegratorGpuEuler(IntegratorGpuPlaten):
+    """The reference's Euler-Maruyama scheme (``EulerSODE``, strong order 0.5,
+    qutip/solver/sode/itotaylor.py:12-26) on the device, as :class:`IntegratorGpuPlaten`."""
+    scheme = "euler"
 
 
 # ------------------------------------------------------------- trajectories ---
@@ -1261,10 +1268,13 @@ def _gpu_map_sde(task, values, task_args, task_kwargs, reduce_func):
         raise TypeError(f"map='gpu' does not run the task {getattr(task, '__name__', task)!r}")
     if task_kwargs:
         raise TypeError(f"map='gpu' does not support the trajectory options {sorted(task_kwargs)}")
+    from .stochastic import SCHEMES
     opts = solver.options
-    if opts.get("method") not in ("platen", "gpu_platen"):
-        raise TypeError("map='gpu' integrates stochastic equations with the Platen scheme "
-                        "(method 'platen' or 'gpu_platen')")
+    scheme = SCHEMES.get(opts.get("method"))
+    if scheme is None:
+        raise TypeError("map='gpu' integrates stochastic equations with the Platen or the "
+                        "Euler-Maruyama scheme (method 'platen', 'euler', 'gpu_platen' or "
+                        "'gpu_euler')")
     if opts.get("store_states") or opts.get("store_final_state"):
         raise TypeError("map='gpu' records expectation values and measurements only")
     state0, tlist, e_ops = task_args
@@ -1312,7 +1322,7 @@ def _gpu_map_sde(task, values, task_args, task_kwargs, reduce_func):
     for N in steps:
         if N:
             block = torch.from_numpy(np.ascontiguousarray(dW[:, pos:pos + N, :])).to(dev)
-            op.platen(states, block, N, dt)
+            op.platen(states, block, N, dt, scheme=scheme)
         noise.append(dW[:, pos:pos + N, :].sum(axis=1) if N else np.zeros((n_traj, 1)))
         pos += N
         e_vals.append(_sde_expect(states, e_w, op.open))
@@ -1382,6 +1392,7 @@ def register():
     for solver in (MESolver, SESolver, MCSolver, BRSolver):
         solver.add_integrator(IntegratorGpuVern7, "gpu_vern7")
     StochasticSolver.add_integrator(IntegratorGpuPlaten, "gpu_platen")
+    StochasticSolver.add_integrator(IntegratorGpuEuler, "gpu_euler")
     _parallel._maps["gpu"] = gpu_map
     _REGISTERED = True
 

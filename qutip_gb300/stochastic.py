@@ -5,13 +5,14 @@ explicit Platen scheme by default (``PlatenSODE``, qutip/solver/sode/sode.py:235
 steps in qutip/solver/sode/_sode.pyx:58-120), drawing the Wiener increments of each
 output interval from the trajectory's own generator (``Wiener.dW``,
 qutip/solver/sode/_noise.py:22-30).  Here ``qg_sde_platen`` (``csrc/sde.cu``) runs all
-the steps of an output interval in one launch, one CTA per trajectory, with increments
-drawn by the same ``Wiener`` object on the host: the trajectories are the reference's,
-to rounding.
+the steps of an output interval in one launch, one warp or CTA per trajectory, with
+increments drawn by the same ``Wiener`` object on the host: the trajectories are the
+reference's, to rounding.  ``qg_sde_euler`` does the same with the Euler-Maruyama scheme
+(``EulerSODE``, qutip/solver/sode/itotaylor.py:12-26).
 
 :class:`SdeOperator` holds the drift and diffusion operators of one system on the device;
-:class:`IntegratorGpuPlaten` is the drop-in stochastic integrator (``method="gpu_platen"``
-in the solver options), registered by :mod:`qutip_gb300.qutip_plugin`.
+``IntegratorGpuPlaten`` / ``IntegratorGpuEuler`` in :mod:`qutip_gb300.qutip_plugin` are the
+drop-in stochastic integrators (``method="gpu_platen"`` / ``"gpu_euler"``).
 """
 from __future__ import annotations
 
@@ -25,6 +26,9 @@ from . import _lib
 from .operator import stream_ptr
 
 __all__ = ["SdeOperator", "platen"]
+
+#: the reference's stochastic methods this module integrates, by name
+SCHEMES = {"platen": "platen", "gpu_platen": "platen", "euler": "euler", "gpu_euler": "euler"}
 
 
 def _csr_blocks(mats, device):
@@ -92,16 +96,20 @@ class SdeOperator:
             self.struct.work = self._work.data_ptr()
         return self._work
 
-    def platen(self, states: torch.Tensor, dW: torch.Tensor, n_steps: int, dt: float):
-        """``n_steps`` Platen steps of every trajectory in ``states`` (n_traj x n,
-        complex128, in place) with increments ``dW`` (n_traj x n_steps x n_sc, float64)."""
+    def platen(self, states: torch.Tensor, dW: torch.Tensor, n_steps: int, dt: float,
+               scheme: str = "platen"):
+        """``n_steps`` steps of every trajectory in ``states`` (n_traj x n, complex128, in
+        place) with increments ``dW`` (n_traj x n_steps x n_sc, float64): the Platen scheme,
+        or ``scheme="euler"`` for Euler-Maruyama."""
         n_traj = states.shape[0] if states.dim() == 2 else 1
         if states.dtype != torch.complex128 or states.numel() != n_traj * self.n:
             raise ValueError("states must be n_traj x n complex128")
         if dW.dtype != torch.float64 or dW.numel() != n_traj * n_steps * self.n_sc:
             raise ValueError("dW must be n_traj x n_steps x n_sc float64")
+        if scheme not in ("platen", "euler"):
+            raise ValueError("scheme must be 'platen' or 'euler'")
         self._workspace(n_traj)
-        _lib.call("qg_sde_platen", C.byref(self.struct), int(n_traj), states.data_ptr(),
+        _lib.call(f"qg_sde_{scheme}", C.byref(self.struct), int(n_traj), states.data_ptr(),
                   dW.data_ptr(), int(n_steps), float(dt), stream_ptr())
 
 

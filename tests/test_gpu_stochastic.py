@@ -128,3 +128,27 @@ def test_gpu_map_runs_every_trajectory_in_one_batch(qt, solver):
     got = run({**_opts("platen"), "map": "gpu"})
     _same(got, ref)
     assert len(got.runs_expect[0]) == len(seeds)
+
+
+@pytest.mark.parametrize("solver", ["sse", "sme"])
+def test_euler_matches_the_reference(qt, solver):
+    """method="gpu_euler" (one trajectory at a time) and map="gpu" with method="euler"
+    against the reference's Euler-Maruyama runs with the same seeds."""
+    N = 6
+    a = qt.destroy(N)
+    H = a.dag() * a + 0.3 * (a + a.dag())
+    e_ops = [a.dag() * a, a + a.dag()]
+    tl = np.linspace(0, 0.5, 6)
+    seeds = [31, 32, 33]
+    if solver == "sse":
+        def run(opts):
+            return qt.ssesolve(H, qt.basis(N, 1), tl, [np.sqrt(0.3) * a], e_ops=e_ops,
+                               ntraj=len(seeds), seeds=seeds, options=opts)
+    else:
+        def run(opts):
+            return qt.smesolve(H, qt.coherent_dm(N, 0.6), tl, c_ops=[np.sqrt(0.1) * a],
+                               sc_ops=[np.sqrt(0.2) * a], e_ops=e_ops, ntraj=len(seeds),
+                               seeds=seeds, options=opts)
+    ref = run(_opts("euler"))
+    _same(run(_opts("gpu_euler")), ref)
+    _same(run({**_opts("euler"), "map": "gpu"}), ref)

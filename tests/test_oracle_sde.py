@@ -1,4 +1,4 @@
-"""The numpy restatement of the Platen SODE step (oracle/sde.py) pinned to the reference's
+"""The numpy restatement of the Platen and Euler SODE steps (oracle/sde.py) pinned to the reference's
 own stochastic solvers: ``run_from_experiment`` with a preset noise record integrates one
 step per output interval, which the restatement reproduces to rounding."""
 import numpy as np
@@ -6,7 +6,7 @@ import pytest
 import scipy.sparse as sp
 
 from oracle.ref_workloads import import_reference, reference_available
-from oracle.sde import platen_steps
+from oracle.sde import euler_steps, platen_steps
 
 
 @pytest.fixture(scope="module")
@@ -63,3 +63,25 @@ def test_sme_platen_restatement_matches_the_reference(qt):
         x = platen_steps(L, C, None, x, noise[:, k - 1][None, :], dt, open_=True)
         np.testing.assert_allclose(x, res.states[k].full().reshape(-1, order="F"),
                                    atol=1e-13, rtol=0)
+
+
+def test_sse_euler_restatement_matches_the_reference(qt):
+    N = 6
+    a = qt.destroy(N)
+    H = a.dag() * a + 0.4 * (a + a.dag())
+    sc = [np.sqrt(0.3) * a]
+    psi0 = qt.basis(N, 1)
+    dt = 1e-3
+    tl = np.arange(21) * dt
+    noise = np.random.default_rng(5).normal(0, np.sqrt(dt), size=(1, len(tl) - 1))
+    solver = qt.SSESolver(H, sc, heterodyne=False,
+                          options={"method": "euler", "dt": dt, "store_states": True,
+                                   "progress_bar": None})
+    res = solver.run_from_experiment(psi0, tl, noise)
+    C = [_csr(c) for c in sc]
+    L = -1j * _csr(H) - 0.5 * sum(c.conj().T @ c for c in C)
+    M = [c + c.conj().T for c in C]
+    x = psi0.full()[:, 0]
+    for k in range(1, len(tl)):
+        x = euler_steps(L, C, M, x, noise[:, k - 1][None, :], dt, open_=False)
+        np.testing.assert_allclose(x, res.states[k].full()[:, 0], atol=1e-13, rtol=0)
