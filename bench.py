@@ -91,6 +91,8 @@ def parse():
     ap.add_argument("--profile-dtype", default="c64", choices=["c64", "c128"],
                     help="operator dtype of the stage profiling case")
     ap.add_argument("--profile-ntraj", type=int, default=256)
+    ap.add_argument("--profile-branch", default="full", choices=["full", "hermitian"],
+                    help="matrix profile: the full form or the Hermitian branch")
     ap.add_argument("--profile-tend", type=float, default=5.0)
     ap.add_argument("--profile-group", default="auto",
                     choices=["auto", "warp", "cta", "cta128", "cluster"])
@@ -1206,6 +1208,7 @@ def run_profile_matrix(args):
     torch.cuda.set_device(0)
     s = S.ising_chain(args.profile_sites, build_terms=False)
     op = LindbladOperator.from_hamiltonian(s.h_terms, s.c_ops, dtype="c64")
+    op.hermitian = args.profile_branch == "hermitian"
     ig = GpuVern7(op, precision="mixed")
     ig.set_initial_value(torch.from_numpy(s.state0).cuda(), 0.0)
     for _ in range(2):
