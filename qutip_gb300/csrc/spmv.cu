@@ -683,10 +683,17 @@ __global__ void __launch_bounds__(LB_BLOCK)
     // covering 32 consecutive c of one row r.
     __shared__ cx<R> tile[32][33];  // [c - c0][r - r0]
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    // only the n_t (n_t + 1) / 2 tiles on or below the diagonal are enumerated, column
+    // block j holding row blocks j .. n_t - 1, so the blocks share the work evenly
     const int n_t = (d + 31) / 32;
-    for (int tau = blockIdx.x; tau < n_t * n_t; tau += gridDim.x) {
-      const int r0 = (tau % n_t) * 32, c0 = (tau / n_t) * 32;
-      if (r0 < c0) continue;  // above the diagonal (uniform over the block)
+    const int n_tiles = n_t * (n_t + 1) / 2;
+    int tj = 0, tbase = 0;  // column block of tau and the index of its first tile
+    for (int tau = blockIdx.x; tau < n_tiles; tau += gridDim.x) {
+      while (tau >= tbase + (n_t - tj)) {
+        tbase += n_t - tj;
+        ++tj;
+      }
+      const int r0 = (tj + (tau - tbase)) * 32, c0 = tj * 32;
 #pragma unroll 1
       for (int q = 0; q < 4; ++q) {
         const int cl = w + 8 * q, r = r0 + lane, c = c0 + cl;
@@ -855,7 +862,8 @@ static int launch_lindblad_form(cudaStream_t st, const qg_lindblad& L, double t,
   const int per_sm = staged_occupancy(kern, LB_BLOCK, 0, cache);
   if (per_sm <= 0) return set_error(QG_ERR_CUDA, "occupancy query failed");
   const int64_t n = L.d * L.d;
-  const int64_t blocks = (n + LB_BLOCK - 1) / LB_BLOCK;
+  const int64_t n_t = (L.d + 31) / 32;
+  const int64_t blocks = HERM ? n_t * (n_t + 1) / 2 : (n + LB_BLOCK - 1) / LB_BLOCK;
   int64_t cap = (int64_t)sm_count() * per_sm;
   if (cap > qg_scratch_doubles()) cap = qg_scratch_doubles();
   const int grid = (int)(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
