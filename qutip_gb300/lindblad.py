@@ -227,12 +227,11 @@ class LindbladOperator:
 
     def hermitian_pays(self) -> bool:
         """Whether the Hermitian branch is the faster form for this size.  It halves the
-        generator's arithmetic but writes half the elements through 32 x 32 shared-memory
-        tiles: measured on the Ising chain (mixed form), 58 -> 71 us per stage at L = 10,
-        where a stage's vectors stay in the 129 MB L2, and 4.8 -> 3.1 ms at L = 13, where
-        they stream from HBM.  Taken when one stage vector exceeds 16 MB (its ~8 vectors
-        per stage overflow L2)."""
-        return self.n_rows * self.value_bytes() > (16 << 20)
+        generator's arithmetic and writes the mirrored half through 32 x 32 shared-memory
+        tiles, only the tiles on or below the diagonal being enumerated: measured on the
+        Ising chain (mixed form), 58 -> 43 us per stage at L = 10 and 4.8 -> 2.6 ms at
+        L = 13.  Below d = 64 most of a tile's threads would idle: the full form stays."""
+        return self.d >= 64
 
     @property
     def n_groups(self) -> int:
