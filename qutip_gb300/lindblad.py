@@ -228,10 +228,13 @@ class LindbladOperator:
     def hermitian_pays(self) -> bool:
         """Whether the Hermitian branch is the faster form for this size.  It halves the
         generator's arithmetic and writes the mirrored half through 32 x 32 shared-memory
-        tiles, only the tiles on or below the diagonal being enumerated: measured on the
-        Ising chain (mixed form), 58 -> 43 us per stage at L = 10 and 4.8 -> 2.6 ms at
-        L = 13.  Below d = 64 most of a tile's threads would idle: the full form stays."""
-        return self.d >= 64
+        tiles, one CTA per tile on or below the diagonal: measured on the Ising chain
+        (mixed form), 58 -> 43 us per stage at L = 10 (528 tiles) and 4.8 -> 2.6 ms at
+        L = 13.  With fewer tiles than two per SM the GPU idles (dense random d = 128,
+        10 tiles: 534 -> 2133 ms per solve), so the full form stays there."""
+        n_t = (self.d + 31) // 32
+        sms = torch.cuda.get_device_properties(self.device).multi_processor_count
+        return n_t * (n_t + 1) // 2 >= 2 * sms
 
     @property
     def n_groups(self) -> int:

@@ -891,7 +891,8 @@ class IntegratorGpuVern7(Integrator):
         only): ``"auto"`` sends small systems with dense operators in the mixed form to
         the tensor-core bucket, ``True`` forces it, ``False`` keeps the sparse kernel;
         hermitian_branch (matrix form only): with a Hermitian rho0, ``"auto"`` evaluates
-        half the elements where that is faster (d >= 64), ``True`` always, ``False``
+        half the elements where that is faster (at least two 32 x 32 tiles per SM),
+        ``True`` always, ``False``
         never."""
         return self._options
 
