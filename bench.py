@@ -548,6 +548,10 @@ def run_served(args):
         "workload": f"{n} Jaynes-Cummings jobs, N~U{{5..60}}, {n_me} mesolve / {n - n_me} mcsolve "
                     f"(ntraj={args.served_ntraj}), tlist linspace(0,20,101), seed 2026",
         "served_mixed": {"solves_per_sec": thr, "wall_s": wall, "launches": srv.stats["launches"],
+                         "shape_retries": {k: v.stats.get("shape_retries", 0)
+                                           for k, v in (("throughput", srv), ("high_rate", srv_r))},
+                         "last_shape_error": srv_r.stats.get("last_shape_error",
+                                                             srv.stats.get("last_shape_error")),
                          "latency_at_rate": {**lat, "rate_per_s": rate, "wall_s": wall_r,
                                              "max_concurrent_launches": srv_r.stats["max_concurrent"]}},
         "plain_c128": {"solves_per_sec": plain_thr, "service_sample_jobs": k,

@@ -25,6 +25,7 @@
 // host-visible cancel flag is polled at each output time and inside long
 // trajectory intervals.
 #include <cooperative_groups.h>
+#include <cstdio>
 #include <mutex>
 
 #include "capi_internal.h"
@@ -1372,15 +1373,26 @@ static int group_slots(int64_t max_n, int dtype, int group, int64_t smem) {
     e = dtype == QG_C64
             ? cudaOccupancyMaxActiveClusters(&clusters, batch_cluster_kernel<QG_C64>, &cfg)
             : cudaOccupancyMaxActiveClusters(&clusters, batch_cluster_kernel<QG_C128>, &cfg);
-    if (e != cudaSuccess || clusters <= 0)
-      return set_error(QG_ERR_CUDA, "cluster occupancy query failed");
+    if (e != cudaSuccess || clusters <= 0) {
+      char msg[160];
+      snprintf(msg, sizeof(msg), "cluster occupancy query failed (%s, %d clusters)",
+               e == cudaSuccess ? "no error" : cudaGetErrorString(e), clusters);
+      return set_error(QG_ERR_CUDA, msg);
+    }
     return clusters;
   }
   if (smem > MAX_DYN_SMEM) return set_error(QG_ERR_ARG, "staged data exceed shared memory");
   const Shape sh = shape_of(max_n, dtype, group);
   if (!allow_smem(sh.kernel, smem)) return set_error(QG_ERR_CUDA, "shared-memory opt-in failed");
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh.kernel, sh.block, smem);
-  if (e != cudaSuccess || per_sm <= 0) return set_error(QG_ERR_CUDA, "occupancy query failed");
+  if (e != cudaSuccess || per_sm <= 0) {
+    char msg[200];
+    snprintf(msg, sizeof(msg),
+             "occupancy query failed (%s; group %d, block %d, %lld bytes of shared memory)",
+             e == cudaSuccess ? "0 blocks per SM" : cudaGetErrorString(e), group, sh.block,
+             (long long)smem);
+    return set_error(QG_ERR_CUDA, msg);
+  }
   // slots are warps in warp mode, CTAs otherwise
   return sm_count() * per_sm * sh.groups_per_cta;
 }

@@ -184,8 +184,19 @@ class Server:
                 group = "auto"
         with torch.cuda.stream(stream):
             cost = [bp.sys_info[it[0]]["nnz"] for it in bp.items]
-            bp.build(max_jumps=self.max_jumps if any(j.spec.kind == "mc" for j in jobs) else 0,
-                     order=np.argsort(cost, kind="stable")[::-1], group=group)
+            max_jumps = self.max_jumps if any(j.spec.kind == "mc" for j in jobs) else 0
+            order = np.argsort(cost, kind="stable")[::-1]
+            try:
+                bp.build(max_jumps=max_jumps, order=order, group=group)
+            except _lib.QgError as exc:
+                # a shape the load policy picked could not be sized (its occupancy query
+                # failed): the launch goes out in the default shape, and the event is kept
+                if group == "auto":
+                    raise
+                self.stats["shape_retries"] = self.stats.get("shape_retries", 0) + 1
+                self.stats["last_shape_error"] = f"{group}: {exc}"
+                group = "auto"
+                bp.build(max_jumps=max_jumps, order=order, group=group)
             bp.set_cancel(cancel)
             bp.cancel_flag = cancel
             bp.launch()
