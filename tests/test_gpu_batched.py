@@ -33,6 +33,27 @@ def test_batched_jc_config1_matches_reference(precision, atol):
     assert res[0]["steps"] >= len(g["step_ends"])
 
 
+def test_cta_shape_with_staged_vectors_near_the_default_limit():
+    """A CTA-shape launch whose staged vectors (46.6 KB for a 2916-entry mixed-form state)
+    plus the kernel's static shared memory exceed the 48 KB default: the launch is opted in
+    and its result equals the same system solved in the warp-free cluster shape."""
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import BatchProblem, check_status
+    s = S.jaynes_cummings(27, kind="me")
+    tl = np.linspace(0, 2, 11)
+
+    def run(group):
+        bp = BatchProblem("c64")
+        bp.add_item(bp.add_system(s.terms, s.e_ops, tl, "me"), s.state0)
+        bp.build(group=group)
+        bp.launch()
+        r = bp.results()
+        check_status(r)
+        return r[0]["expect"]
+    a, b = run("cta"), run("cluster")
+    np.testing.assert_allclose(a, b, atol=2e-6, rtol=0)
+
+
 def test_mixed_sizes_alone_equals_in_the_mix():
     """Each system of a mixed-size batch gives the result it gives when solved alone."""
     from qutip_gb300 import systems as S
