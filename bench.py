@@ -1262,10 +1262,10 @@ def run_profile_sde(args):
     for nt in (1, 8, 64, 256):
         states = torch.from_numpy(np.tile(rho, (nt, 1))).cuda()
         dW = torch.from_numpy(np.random.default_rng(1).normal(0, 0.03, size=(nt, steps, 1))).cuda()
-        op.platen(states, dW, steps, 1e-3)
+        op.advance(states, dW, steps, 1e-3)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        op.platen(states, dW, steps, 1e-3)
+        op.advance(states, dW, steps, 1e-3)
         e1.record()
         e1.synchronize()
         print(f"sde: {nt} trajectories, {1e3 * e0.elapsed_time(e1) / steps:.1f} us per step")

@@ -1,10 +1,14 @@
-"""Restatement of the reference's explicit Platen SODE step (FP64, numpy).
+"""Restatement of the reference's explicit Platen and Euler-Maruyama SODE steps (FP64, numpy).
 
-TEST INFRASTRUCTURE ONLY: the checker for ``qg_sde_platen``, never the product.
+TEST INFRASTRUCTURE ONLY: the checker for ``qg_sde_platen`` and ``qg_sde_euler``, never
+the product.
 
-Follows ``Platen.step`` (qutip/solver/sode/_sode.pyx:62-120) on the drift and diffusion
-of ``StochasticClosedSystem`` (qutip/solver/sode/ssystem.pyx:141-166) and
-``StochasticOpenSystem`` (ssystem.pyx:227-240), in the same order of operations.
+Follows ``Platen.step`` (qutip/solver/sode/_sode.pyx:62-120) and ``Euler.step``
+(_sode.pyx:32-55) on the drift and diffusion of ``StochasticClosedSystem``
+(qutip/solver/sode/ssystem.pyx:141-166) and ``StochasticOpenSystem`` (ssystem.pyx:227-240),
+in the same order of operations.  Pinned by tests/test_oracle_sde.py against the
+reference's own ``run_from_experiment`` with a preset noise record (SSE Platen, SME Platen,
+SSE Euler: 1e-13 absolute per state entry).
 """
 from __future__ import annotations
 

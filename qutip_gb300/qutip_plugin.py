@@ -989,7 +989,7 @@ class IntegratorGpuPlaten(SIntegrator):
         dW = self.wiener.dW(self.t, N)
         dev = torch.from_numpy(np.ascontiguousarray(dW[:, 0, :], dtype=np.float64)).to(
             self._state.device, non_blocking=False)
-        self._op.platen(self._state.view(1, -1), dev, N, dt, scheme=self.scheme)
+        self._op.advance(self._state.view(1, -1), dev, N, dt, scheme=self.scheme)
         self.t += dt * N
         return self.t, GpuDense(self._state, shape=(self._op.n, 1), copy=copy), \
             np.sum(dW[:, 0, :], axis=0)
@@ -1269,7 +1269,7 @@ def _gpu_map_sde(task, values, task_args, task_kwargs, reduce_func):
         raise TypeError(f"map='gpu' does not run the task {getattr(task, '__name__', task)!r}")
     if task_kwargs:
         raise TypeError(f"map='gpu' does not support the trajectory options {sorted(task_kwargs)}")
-    from .stochastic import SCHEMES
+    from .stochastic import SCHEMES, interval_steps
     opts = solver.options
     scheme = SCHEMES.get(opts.get("method"))
     if scheme is None:
@@ -1291,15 +1291,7 @@ def _gpu_map_sde(task, values, task_args, task_kwargs, reduce_func):
     op = sde_operator(solver.rhs)
     dt = float(solver._integrator.options["dt"])
     tl = np.asarray(tlist, dtype=np.float64)
-    # steps per output interval, as _Explicit_Simple_Integrator.integrate counts them
-    steps, t_cur = [], float(tl[0])
-    for t in tl[1:]:
-        N, extra = np.divmod(t - t_cur, dt)
-        N = int(N) + (1 if extra > 0.5 * dt else 0)
-        if t - t_cur < 0.5 * dt:
-            N = 0
-        steps.append(N)
-        t_cur += dt * N
+    steps = interval_steps(tl, dt)
     total = int(sum(steps))
     m = op.n_sc
     seeds = list(values)
@@ -1323,7 +1315,7 @@ def _gpu_map_sde(task, values, task_args, task_kwargs, reduce_func):
     for N in steps:
         if N:
             block = torch.from_numpy(np.ascontiguousarray(dW[:, pos:pos + N, :])).to(dev)
-            op.platen(states, block, N, dt, scheme=scheme)
+            op.advance(states, block, N, dt, scheme=scheme)
         noise.append(dW[:, pos:pos + N, :].sum(axis=1) if N else np.zeros((n_traj, 1)))
         pos += N
         e_vals.append(_sde_expect(states, e_w, op.open))

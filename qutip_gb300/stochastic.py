@@ -25,7 +25,7 @@ import torch
 from . import _lib
 from .operator import stream_ptr
 
-__all__ = ["SdeOperator", "platen"]
+__all__ = ["SdeOperator", "interval_steps", "SCHEMES"]
 
 #: the reference's stochastic methods this module integrates, by name
 SCHEMES = {"platen": "platen", "gpu_platen": "platen", "euler": "euler", "gpu_euler": "euler"}
@@ -96,8 +96,8 @@ class SdeOperator:
             self.struct.work = self._work.data_ptr()
         return self._work
 
-    def platen(self, states: torch.Tensor, dW: torch.Tensor, n_steps: int, dt: float,
-               scheme: str = "platen"):
+    def advance(self, states: torch.Tensor, dW: torch.Tensor, n_steps: int, dt: float,
+                scheme: str = "platen"):
         """``n_steps`` steps of every trajectory in ``states`` (n_traj x n, complex128, in
         place) with increments ``dW`` (n_traj x n_steps x n_sc, float64): the Platen scheme,
         or ``scheme="euler"`` for Euler-Maruyama."""
@@ -113,6 +113,20 @@ class SdeOperator:
                   dW.data_ptr(), int(n_steps), float(dt), stream_ptr())
 
 
-def platen(op: SdeOperator, states, dW, n_steps, dt):
-    """Functional form of :meth:`SdeOperator.platen`."""
-    op.platen(states, dW, n_steps, dt)
+def interval_steps(tlist, dt):
+    """Fixed steps of each output interval as the reference's explicit SODE integrators
+    count them (``_Explicit_Simple_Integrator.integrate``, qutip/solver/sode/sode.py:151-173):
+    ``N`` whole steps of ``dt`` to the next output time, one more when the remainder exceeds
+    half a step, none when the interval is under half a step; the integrator's time advances
+    by ``dt * N``.  Returns the list of ``N`` (one per interval)."""
+    steps, t_cur = [], float(tlist[0])
+    for t in tlist[1:]:
+        delta = float(t) - t_cur
+        if delta < 0.5 * dt:
+            steps.append(0)
+            continue
+        n, extra = np.divmod(delta, dt)
+        n = int(n) + (1 if extra > 0.5 * dt else 0)
+        steps.append(n)
+        t_cur += dt * n
+    return steps

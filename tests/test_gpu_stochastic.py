@@ -96,7 +96,7 @@ def test_sde_kernel_matches_the_oracle_restatement(qt, d):
     psi /= np.linalg.norm(psi, axis=1, keepdims=True)
     dW = rng.normal(0, np.sqrt(dt), size=(n_traj, n_steps, 2))
     states = torch.from_numpy(psi.copy()).cuda()
-    op.platen(states, torch.from_numpy(dW).cuda(), n_steps, dt)
+    op.advance(states, torch.from_numpy(dW).cuda(), n_steps, dt)
     got = states.cpu().numpy()
     L = -1j * H - 0.5 * sum(c.conj().T @ c for c in cs)
     for k in range(n_traj):

@@ -85,3 +85,31 @@ def test_sse_euler_restatement_matches_the_reference(qt):
     for k in range(1, len(tl)):
         x = euler_steps(L, C, M, x, noise[:, k - 1][None, :], dt, open_=False)
         np.testing.assert_allclose(x, res.states[k].full()[:, 0], atol=1e-13, rtol=0)
+
+
+@pytest.mark.parametrize("tlist,dt", [
+    (np.linspace(0, 1, 11), 1e-3),
+    (np.array([0.0, 0.0004, 0.0011, 0.5, 0.50049, 2.0]), 1e-3),
+    (np.linspace(0, 0.3, 4), 0.07),
+])
+def test_interval_steps_follow_the_reference_integrator(qt, tlist, dt):
+    """The map's host count of steps per output interval equals what the reference's
+    explicit integrator takes (its time after each interval, sode.py:151-173)."""
+    from qutip_gb300.stochastic import interval_steps
+    N = 3
+    a = qt.destroy(N)
+    solver = qt.SSESolver(a.dag() * a, [0.1 * a], heterodyne=False,
+                          options={"method": "euler", "dt": dt, "progress_bar": None})
+    ig = solver._integrator
+    ig.set_state(float(tlist[0]), qt.basis(N, 0).data, np.random.default_rng(0))
+    times = []
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", RuntimeWarning)
+        for t in tlist[1:]:
+            times.append(ig.integrate(float(t))[0])
+    steps = interval_steps(tlist, dt)
+    t_cur = float(tlist[0])
+    for n, t_ref in zip(steps, times):
+        t_cur += dt * n
+        assert t_cur == t_ref
