@@ -82,7 +82,7 @@ def parse():
     ap.add_argument("--large-sites", type=int, default=12,
                     help="Ising chain length of the large mixed-precision section (0: skip)")
     ap.add_argument("--profile", default=None,
-                    choices=["stage", "batch", "matrix", "dense", "sde"],
+                    choices=["stage", "batch", "matrix", "dense", "sde", "served-large"],
                     help="run the ncu profiling case only (fused stage kernel, untuned); "
                          "prints nothing to parse")
     ap.add_argument("--profile-sites", type=int, default=10)
@@ -1287,6 +1287,30 @@ def run_profile_batch(args):
     print(f"batch: {len(r.col_times)} trajectories, {sum(len(c) for c in r.col_times)} jumps")
 
 
+def run_profile_served_large(args):
+    """ncu case for the largest served requests: one Jaynes-Cummings mesolve item
+    (N = 57, vec(rho) of 12,996 entries, tlist linspace(0, 20, 101)) in the batched kernel
+    with the launch shape ``--profile-group`` (the serving policy's ``cluster``), two
+    launches (warm-up, then the captured one)."""
+    import torch
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import BatchProblem, check_status
+    torch.cuda.set_device(0)
+    s = S.jaynes_cummings(57, kind="me")
+    tl = np.linspace(0.0, 20.0, 101)
+    flag = torch.zeros(1, dtype=torch.int32).pin_memory()
+    for _ in range(2):
+        bp = BatchProblem("c64")
+        bp.add_item(bp.add_system(s.terms, s.e_ops, tl, "me"), s.state0)
+        bp.build(group=args.profile_group)
+        bp.set_cancel(flag)        # as served launches carry it
+        bp.launch()
+        res = bp.results()
+        check_status(res)
+    torch.cuda.synchronize()
+    print(f"served-large: {res[0]['steps']} steps, {res[0]['rhs']} stage evaluations")
+
+
 def main():
     args = parse()
     if args.profile == "stage":
@@ -1303,6 +1327,9 @@ def main():
         return
     if args.profile == "sde":
         run_profile_sde(args)
+        return
+    if args.profile == "served-large":
+        run_profile_served_large(args)
         return
     dist = Dist(args.gpus)
     if args.impl == "reference":

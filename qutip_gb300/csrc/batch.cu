@@ -67,6 +67,8 @@ constexpr int WARP_MAX_N = 2048;
 constexpr int WARP_BLOCK = 128;   // 4 warps (4 items) per CTA in warp mode
 constexpr int CTA_BLOCK = 256;    // threads per item in CTA mode (per CTA in cluster mode)
 constexpr int CLUSTER_CTAS = 8;   // CTAs per item in cluster mode (portable cluster size)
+// Expectation-value sums an output record gathers behind one pair of group barriers.
+constexpr int REC_SLOTS = 8;
 // Stage inputs (ytmp, 2 x max_n entries per item) live in shared memory when all
 // items of a CTA fit in this many bytes: the matvec gathers of x then hit shared
 // memory instead of L1/L2.
@@ -144,6 +146,7 @@ namespace cgrp = cooperative_groups;
 
 struct WarpGroup {
   static constexpr int SIZE = 32;
+  static constexpr bool DEFER = false;  // record sums: shuffles, no barrier to save
   int rank;
   int64_t slot;
   __device__ __forceinline__ void sync() const { __syncwarp(); }
@@ -152,16 +155,53 @@ struct WarpGroup {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
   }
+  // two sums in one pass: each component summed in the order of sum()
+  __device__ __forceinline__ double2 sum2(double a, double b) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    return make_double2(a, b);
+  }
   __device__ __forceinline__ int bcast(int v) const { return __shfl_sync(0xffffffffu, v, 0); }
 };
 
 template <int BB>
 struct CtaGroup {
   static constexpr int SIZE = BB;
+  static constexpr bool DEFER = true;  // record sums: put2 / sync / take2
   int rank;
   int64_t slot;
-  double* red;  // shared [BB/32]
+  double* red;  // shared [2 * BB/32]
   int* ibuf;    // shared [1]
+  double* rec;  // shared [REC_SLOTS * 2 * BB/32]: warp partials of deferred sums
+  // warp partial of deferred sum pair k; the totals are read by take2 after a sync()
+  __device__ __forceinline__ void put2(int k, double a, double b) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((rank & 31) == 0) {
+      rec[(2 * k) * (BB / 32) + (rank >> 5)] = a;
+      rec[(2 * k + 1) * (BB / 32) + (rank >> 5)] = b;
+    }
+  }
+  // sum pair k, each component in the order of sum()
+  __device__ __forceinline__ double2 take2(int k) const {
+    double ta = 0.0, tb = 0.0;
+#pragma unroll
+    for (int i = 0; i < BB / 32; ++i) {
+      ta += rec[(2 * k) * (BB / 32) + i];
+      tb += rec[(2 * k + 1) * (BB / 32) + i];
+    }
+    return make_double2(ta, tb);
+  }
+  __device__ __forceinline__ void put_flag(int v) const {
+    if (rank == 0) *ibuf = v;
+  }
+  __device__ __forceinline__ int take_flag() const { return *ibuf; }
   __device__ __forceinline__ void sync() const { __syncthreads(); }
   __device__ __forceinline__ double sum(double v) const {
 #pragma unroll
@@ -173,6 +213,27 @@ struct CtaGroup {
 #pragma unroll
     for (int i = 0; i < BB / 32; ++i) t += red[i];
     return t;
+  }
+  // two sums behind one pair of barriers, each component in the order of sum()
+  __device__ __forceinline__ double2 sum2(double a, double b) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    __syncthreads();
+    if ((rank & 31) == 0) {
+      red[rank >> 5] = a;
+      red[BB / 32 + (rank >> 5)] = b;
+    }
+    __syncthreads();
+    double ta = 0.0, tb = 0.0;
+#pragma unroll
+    for (int i = 0; i < BB / 32; ++i) {
+      ta += red[i];
+      tb += red[BB / 32 + i];
+    }
+    return make_double2(ta, tb);
   }
   __device__ __forceinline__ int bcast(int v) const {
     __syncthreads();
@@ -190,10 +251,43 @@ struct CtaGroup {
 template <int BB, int CS>
 struct ClusterGroup {
   static constexpr int SIZE = BB * CS;
+  static constexpr bool DEFER = true;  // record sums: put2 / sync / take2
   int rank;
   int64_t slot;
-  double* red;  // shared [BB/32] of this CTA
+  double* red;  // shared [2 * BB/32] of this CTA
   int* ibuf;    // shared [1] of this CTA
+  double* rec;  // shared [REC_SLOTS * 2 * BB/32] of this CTA: warp partials
+  __device__ __forceinline__ void put2(int k, double a, double b) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      rec[(2 * k) * (BB / 32) + (threadIdx.x >> 5)] = a;
+      rec[(2 * k + 1) * (BB / 32) + (threadIdx.x >> 5)] = b;
+    }
+  }
+  // every CTA's partials through distributed shared memory, in the order of sum()
+  __device__ __forceinline__ double2 take2(int k) const {
+    cgrp::cluster_group cl = cgrp::this_cluster();
+    double ta = 0.0, tb = 0.0;
+    for (int c = 0; c < CS; ++c) {
+      const double* rr = cl.map_shared_rank(rec, c);
+#pragma unroll
+      for (int i = 0; i < BB / 32; ++i) {
+        ta += rr[(2 * k) * (BB / 32) + i];
+        tb += rr[(2 * k + 1) * (BB / 32) + i];
+      }
+    }
+    return make_double2(ta, tb);
+  }
+  __device__ __forceinline__ void put_flag(int v) const {
+    if (rank == 0) *ibuf = v;
+  }
+  __device__ __forceinline__ int take_flag() const {
+    return *cgrp::this_cluster().map_shared_rank(ibuf, 0);
+  }
   __device__ __forceinline__ void sync() const { cgrp::this_cluster().sync(); }
   __device__ __forceinline__ double sum(double v) const {
     cgrp::cluster_group cl = cgrp::this_cluster();
@@ -209,6 +303,31 @@ struct ClusterGroup {
       for (int i = 0; i < BB / 32; ++i) t += rr[i];
     }
     return t;
+  }
+  // two sums behind one pair of cluster barriers, each component in the order of sum()
+  __device__ __forceinline__ double2 sum2(double a, double b) const {
+    cgrp::cluster_group cl = cgrp::this_cluster();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    cl.sync();
+    if ((threadIdx.x & 31) == 0) {
+      red[threadIdx.x >> 5] = a;
+      red[BB / 32 + (threadIdx.x >> 5)] = b;
+    }
+    cl.sync();
+    double ta = 0.0, tb = 0.0;
+    for (int c = 0; c < CS; ++c) {
+      const double* rr = cl.map_shared_rank(red, c);
+#pragma unroll
+      for (int i = 0; i < BB / 32; ++i) {
+        ta += rr[i];
+        tb += rr[BB / 32 + i];
+      }
+    }
+    return make_double2(ta, tb);
   }
   __device__ __forceinline__ int bcast(int v) const {
     cgrp::cluster_group cl = cgrp::this_cluster();
@@ -433,7 +552,9 @@ __device__ __noinline__ double stage(const GT& g, Ctx<DT>& X, Ctl& c, int s, dou
     CT ar, ai;
     row_matvec(X, r, x, ar, ai);
     st2(X.k + s * n + r, (double)ar, (double)ai);
-    const ST ks = X.k[s * n + r];
+    ST ks;  // the stored k_s entry, without reading it back
+    ks.x = ar;
+    ks.y = ai;
     if (forms_input) {
       if constexpr (MIXED) {
         float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;
@@ -799,8 +920,13 @@ __device__ void integrate(const GT& g, Ctx<DT>& X, Ctl& c, double t, bool step) 
 // expectation values of the current state into out[0..ne] (raw; host normalises).
 // A ket is interpolated once into ctmp[0] and every e_op reads it there; a density
 // matrix is read entry by entry (the e_ops touch a small part of it).
+// CTA and cluster groups gather the warp partials of up to REC_SLOTS sums behind one
+// pair of barriers (a barrier pair per sum made most of the cost of an output for
+// large items in a cluster).  Returns the host cancel flag, read once per record by
+// rank 0 and shared behind the same barriers (0 without a flag).
 template <int DT, class GT>
-__device__ __noinline__ void record(const GT& g, const Ctx<DT>& X, const Ctl& c, double2* out, bool ket) {
+__device__ __noinline__ int record(const GT& g, const Ctx<DT>& X, const Ctl& c, double2* out,
+                                   bool ket, const volatile int32_t* cancel) {
   const int ne = X.S->n_eops;
   const int d = X.d;
   const double2* psi = X.ctmp[0];
@@ -808,49 +934,66 @@ __device__ __noinline__ void record(const GT& g, const Ctx<DT>& X, const Ctl& c,
     for (int r = g.rank; r < X.n; r += GT::SIZE) X.ctmp[0][r] = state_at(X, c, r);
     g.sync();
   }
-  for (int e = 0; e < ne; ++e) {
-    const int* rp = X.B->eop_rp + X.S->eop_rp_off + (int64_t)e * (d + 1);
-    double ar = 0.0, ai = 0.0;
-    for (int r = g.rank; r < d; r += GT::SIZE) {
-      const int s = __ldg(rp + r), en = __ldg(rp + r + 1);
-      double sr = 0.0, si = 0.0;
-      for (int p = s; p < en; ++p) {
-        const int col = __ldg(X.B->eop_col + p);
-        const double vr = __ldg(X.B->eop_val + 2 * p), vi = __ldg(X.B->eop_val + 2 * p + 1);
-        const double2 z = ket ? psi[col] : state_at(X, c, col + r * d);
-        sr += vr * z.x - vi * z.y;
-        si += vr * z.y + vi * z.x;
+  int flag = 0;
+  for (int e0 = 0; e0 <= ne; e0 += REC_SLOTS) {
+    const int e1 = min(ne + 1, e0 + REC_SLOTS);
+    for (int e = e0; e < e1; ++e) {
+      double ar = 0.0, ai = 0.0;
+      if (e < ne) {
+        const int* rp = X.B->eop_rp + X.S->eop_rp_off + (int64_t)e * (d + 1);
+        for (int r = g.rank; r < d; r += GT::SIZE) {
+          const int s = __ldg(rp + r), en = __ldg(rp + r + 1);
+          double sr = 0.0, si = 0.0;
+          for (int p = s; p < en; ++p) {
+            const int col = __ldg(X.B->eop_col + p);
+            const double vr = __ldg(X.B->eop_val + 2 * p), vi = __ldg(X.B->eop_val + 2 * p + 1);
+            const double2 z = ket ? psi[col] : state_at(X, c, col + r * d);
+            sr += vr * z.x - vi * z.y;
+            si += vr * z.y + vi * z.x;
+          }
+          if (ket) {
+            const double2 pr = psi[r];
+            const double tr = pr.x * sr + pr.y * si, ti = pr.x * si - pr.y * sr;
+            sr = tr;
+            si = ti;
+          }
+          ar += sr;
+          ai += si;
+        }
+      } else if (ket) {  // the norm
+        for (int r = g.rank; r < X.n; r += GT::SIZE) {
+          const double2 z = psi[r];
+          ar += z.x * z.x + z.y * z.y;
+        }
+      } else {  // the trace
+        for (int r = g.rank; r < d; r += GT::SIZE) {
+          const double2 z = state_at(X, c, r + r * d);
+          ar += z.x;
+          ai += z.y;
+        }
       }
-      if (ket) {
-        const double2 pr = psi[r];
-        const double tr = pr.x * sr + pr.y * si, ti = pr.x * si - pr.y * sr;
-        sr = tr;
-        si = ti;
+      if constexpr (GT::DEFER) {
+        g.put2(e - e0, ar, ai);
+      } else {
+        const double2 t = g.sum2(ar, ai);
+        if (g.rank == 0) out[e] = t;
       }
-      ar += sr;
-      ai += si;
     }
-    const double tr_ = g.sum(ar);
-    const double ti_ = g.sum(ai);
-    if (g.rank == 0) out[e] = make_double2(tr_, ti_);
-  }
-  double ar = 0.0, ai = 0.0;
-  if (ket) {
-    for (int r = g.rank; r < X.n; r += GT::SIZE) {
-      const double2 z = psi[r];
-      ar += z.x * z.x + z.y * z.y;
-    }
-  } else {
-    for (int r = g.rank; r < d; r += GT::SIZE) {
-      const double2 z = state_at(X, c, r + r * d);
-      ar += z.x;
-      ai += z.y;
+    if constexpr (GT::DEFER) {
+      const bool final_chunk = e1 == ne + 1;
+      if (final_chunk && cancel) g.put_flag(g.rank == 0 ? read_flag(cancel) : 0);
+      g.sync();
+      if (final_chunk && cancel) flag = g.take_flag();
+      if (g.rank == 0)
+        for (int e = e0; e < e1; ++e) out[e] = g.take2(e - e0);
+      if (!final_chunk) g.sync();  // rank 0 has read the partials before they are reused
     }
   }
-  const double tr_ = g.sum(ar);
-  const double ti_ = g.sum(ai);
-  if (g.rank == 0) out[ne] = make_double2(tr_, ti_);
+  if constexpr (!GT::DEFER) {
+    if (cancel) flag = g.bcast(g.rank == 0 ? read_flag(cancel) : 0);
+  }
   g.sync();
+  return flag;
 }
 
 // ||c_i(t) psi||^2 for psi in ctmp[0]; optionally store c_i(t) psi in ctmp[1].
@@ -927,18 +1070,15 @@ __device__ void run_item(const GT& g, const qg_batch& B, Ctx<DT>& X, int item) {
   double target = ket ? __dadd_rn(__dmul_rn(pcg_random(rng), 1.0 - floor_p), floor_p) : 0.0;
   int njumps = 0;
   set_initial(g, X, c, reinterpret_cast<const double2*>(B.y0) + I.y0_off, tl[0]);
-  record(g, X, c, out, ket);
+  int cancelled = record(g, X, c, out, ket, B.cancel);
   for (int o = 1; o < S->n_out && c.status >= 0; ++o) {
     const double t = tl[o];
     if (B.progress && g.rank == 0)
       B.progress[g.slot] =
           ((int64_t)item << 32) | (int64_t)(unsigned)o;
-    if (B.cancel) {
-      const int f = g.bcast(g.rank == 0 ? read_flag(B.cancel) : 0);
-      if (f) {
-        c.status = QG_TIMEOUT;
-        break;
-      }
+    if (cancelled) {  // the flag as the last record read it
+      c.status = QG_TIMEOUT;
+      break;
     }
     if (!ket) {
       integrate(g, X, c, t, false);
@@ -1054,7 +1194,7 @@ __device__ void run_item(const GT& g, const qg_batch& B, Ctx<DT>& X, int item) {
       }
     }
     if (c.status < 0) break;
-    record(g, X, c, out + (int64_t)o * ne1, ket);
+    cancelled = record(g, X, c, out + (int64_t)o * ne1, ket, B.cancel);
   }
   if (g.rank == 0) {
     int32_t* st = B.status + 4 * (int64_t)item;
@@ -1148,12 +1288,13 @@ __global__ void __launch_bounds__(WARP_BLOCK, 4) batch_warp_kernel(qg_batch B) {
 // One CTA of BB threads per item; slot = block index.
 template <int DT, int BB>
 __global__ void __launch_bounds__(BB, 65536 / (BB * 128)) batch_cta_kernel(qg_batch B) {
-  __shared__ double red[BB / 32];
+  __shared__ double red[2 * (BB / 32)];
   __shared__ int ibuf;
+  __shared__ double rec[REC_SLOTS * 2 * (BB / 32)];
   extern __shared__ __align__(256) unsigned char stage_smem[];
   __shared__ __align__(8) uint64_t op_bar;
   __shared__ __align__(16) float wf_s[BB / 32][WF_FLOATS];
-  CtaGroup<BB> g{(int)threadIdx.x, (int64_t)blockIdx.x, red, &ibuf};
+  CtaGroup<BB> g{(int)threadIdx.x, (int64_t)blockIdx.x, red, &ibuf, rec};
   Ctx<DT> X;
   bind_slot(X, B, blockIdx.x);
   X.wf = wf_s[threadIdx.x >> 5];
@@ -1182,13 +1323,15 @@ __global__ void __launch_bounds__(BB, 65536 / (BB * 128)) batch_cta_kernel(qg_ba
 // One cluster of CLUSTER_CTAS CTAs per item; slot = cluster index.
 template <int DT>
 __global__ void __launch_bounds__(CTA_BLOCK, 2) batch_cluster_kernel(qg_batch B) {
-  __shared__ double red[CTA_BLOCK / 32];
+  __shared__ double red[2 * (CTA_BLOCK / 32)];
   __shared__ int ibuf;
   cgrp::cluster_group cl = cgrp::this_cluster();
   const int crank = (int)cl.block_rank();
   const int64_t slot = blockIdx.x / CLUSTER_CTAS;
   __shared__ __align__(16) float wf_s[CTA_BLOCK / 32][WF_FLOATS];
-  ClusterGroup<CTA_BLOCK, CLUSTER_CTAS> g{crank * CTA_BLOCK + (int)threadIdx.x, slot, red, &ibuf};
+  __shared__ double rec[REC_SLOTS * 2 * (CTA_BLOCK / 32)];
+  ClusterGroup<CTA_BLOCK, CLUSTER_CTAS> g{crank * CTA_BLOCK + (int)threadIdx.x, slot, red, &ibuf,
+                                          rec};
   Ctx<DT> X;
   bind_slot(X, B, slot);
   X.wf = wf_s[threadIdx.x >> 5];
