@@ -531,8 +531,14 @@ def run_served(args):
     log(f"served: at {low_rate:.1f} req/s served {lat_low}, plain {plain_low}")
     slow = sorted(jobs_l, key=lambda j: -(j.latency or 0))[:6]
     log("served: slowest at that rate: " + "; ".join(
-        f"{j.spec.kind} N={j.spec.n_cav} {1e3 * j.latency:.0f} ms launch={j.extra.get('launch')}"
+        f"{j.spec.kind} N={j.spec.n_cav} {1e3 * j.latency:.0f} ms launch={j.extra.get('launch')} "
+        f"(wait {j.extra.get('wait_ms', 0):.1f}, host {j.extra.get('host_ms', 0):.1f}, "
+        f"gpu {j.extra.get('gpu_ms', 0):.1f}, collect {j.extra.get('collect_ms', 0):.1f} ms)"
         for j in slow))
+    slowest = [{"kind": j.spec.kind, "n_cav": j.spec.n_cav, "latency_ms": 1e3 * j.latency,
+                "launch": list(j.extra.get("launch", ())),
+                **{k: j.extra.get(k) for k in ("wait_ms", "host_ms", "gpu_ms", "collect_ms")}}
+               for j in slow]
     # error of the served mixed form vs the plain complex128 solve (same requests, same
     # trajectory seeds), relative to the largest |<e_op>| of each request, per kind, over
     # every request of the low-rate stream (both arms solved them)
@@ -566,6 +572,7 @@ def run_served(args):
                                                      "method": "served in real time, one request "
                                                                "at a time in arrival order"},
                                       "plain_c128_fifo_model": plain_low_model,
+                                      "slowest_requests": slowest,
                                       "speedup_p99": plain_low["p99_ms"] / lat_low["p99_ms"]},
         "accuracy_vs_c128": {
             "requests": m, "mesolve": len(errs["me"]), "mcsolve": len(errs["mc"]),

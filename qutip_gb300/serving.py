@@ -199,8 +199,10 @@ class Server:
                 bp.build(max_jumps=max_jumps, order=order, group=group)
             bp.set_cancel(cancel)
             bp.cancel_flag = cancel
+            bp.ev_start = torch.cuda.Event(enable_timing=True)
+            bp.ev_start.record(stream)
             bp.launch()
-            ev = torch.cuda.Event()
+            ev = torch.cuda.Event(enable_timing=True)
             ev.record(stream)
         self.stats["launches"] += 1
         self.stats["items"] += len(bp.items)
@@ -278,8 +280,14 @@ class Server:
                         q.appendleft(j)
                     break
                 st = free_streams.pop()
+                t_admit = time.perf_counter()
                 bp, ev = self._launch(take, st)
                 bp.t_launch = time.perf_counter()
+                for j in take:
+                    # where a request's latency goes: waiting for admission, the host
+                    # side of its launch, the launch on the GPU, collection
+                    j.extra["wait_ms"] = 1e3 * (t_admit - t0 - j.spec.arrival)
+                    j.extra["host_ms"] = 1e3 * (bp.t_launch - t_admit)
                 used += fb
                 inflight.append((bp, ev, take, st, fb))
                 self.stats["max_inflight_bytes"] = max(self.stats["max_inflight_bytes"], used)
@@ -298,10 +306,14 @@ class Server:
                         raise TimeoutError(
                             f"launch of jobs {[j.spec.id for j in take][:20]} exceeded "
                             f"{self.launch_timeout:.0f} s and was cancelled")
-                    done = time.perf_counter() - t0
+                    t_seen = time.perf_counter()
                     self._collect(bp, take)
+                    done = time.perf_counter() - t0
+                    gpu_ms = bp.ev_start.elapsed_time(ev)
                     for j in take:
                         j.done = done
+                        j.extra["gpu_ms"] = gpu_ms
+                        j.extra["collect_ms"] = 1e3 * (time.perf_counter() - t_seen)
                     inflight.remove(rec)
                     free_streams.append(st)
                     used -= fb
