@@ -1322,7 +1322,7 @@ __global__ void __launch_bounds__(BB, 65536 / (BB * 128)) batch_cta_kernel(qg_ba
 
 // One cluster of CLUSTER_CTAS CTAs per item; slot = cluster index.
 template <int DT>
-__global__ void __launch_bounds__(CTA_BLOCK, 2) batch_cluster_kernel(qg_batch B) {
+__global__ void __launch_bounds__(CTA_BLOCK, 1) batch_cluster_kernel(qg_batch B) {
   __shared__ double red[2 * (CTA_BLOCK / 32)];
   __shared__ int ibuf;
   cgrp::cluster_group cl = cgrp::this_cluster();

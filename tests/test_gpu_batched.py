@@ -293,3 +293,51 @@ def test_jump_overflow_is_reported():
             assert len(r["col_times"]) == 1
     with pytest.raises(RuntimeError, match="max_jumps"):
         check_status(res)
+
+
+@pytest.mark.parametrize("kind", ["me", "mc"])
+def test_many_eops_in_every_group_shape(kind):
+    """Outputs with more e_ops than one barrier pair gathers (18 e_ops plus the trace or
+    norm: three chunks of sums in the CTA and cluster shapes) equal the warp shape's,
+    which sums each e_op on its own; the first four are also the reference's (Ising L=4)."""
+    import scipy.sparse as sp
+    from qutip_gb300 import systems as S
+    from qutip_gb300.batched import BatchProblem, check_status
+    g = golden("ising_L4_mesolve.npz")
+    s = S.ising_chain(4, kind=kind, gamma_minus=0.05 if kind == "me" else 1e-9,
+                      gamma_z=0.02 if kind == "me" else 1e-9)
+    eye = sp.identity(2, format="csr", dtype=np.complex128)
+    paulis = [sp.csr_matrix(np.array(m, dtype=np.complex128))
+              for m in ([[0, 1], [1, 0]], [[0, -1j], [1j, 0]], [[1, 0], [0, -1]])]
+
+    def site(o, i):
+        m = sp.identity(1, format="csr", dtype=np.complex128)
+        for k in range(4):
+            m = sp.kron(m, o if k == i else eye, format="csr")
+        return m
+    e_ops = list(s.e_ops) + [site(p, i) for p in paulis[:2] for i in range(4)] + \
+        [site(paulis[0], i) @ site(paulis[0], i + 1) for i in range(3)] + \
+        [site(paulis[2], 0) @ site(paulis[2], 3), site(paulis[1], 1) @ site(paulis[1], 2),
+         sp.identity(16, format="csr", dtype=np.complex128)]
+    assert len(e_ops) == 18
+    tl = g["tlist"] if kind == "me" else np.linspace(0.0, 2.0, 21)
+    out = {}
+    for group in ("warp", "cta", "cta128", "cluster"):
+        bp = BatchProblem("c128")
+        sid = bp.add_system(s.terms, e_ops, tl, kind,
+                            c_ops=s.c_ops if kind == "mc" else ())
+        for k in range(3):
+            bp.add_item(sid, s.state0, seed=np.random.SeedSequence(40 + k) if kind == "mc" else None)
+        bp.build(group=group, max_jumps=8 if kind == "mc" else 0)
+        bp.launch()
+        res = bp.results()
+        check_status(res)
+        out[group] = res
+    for group in ("cta", "cta128", "cluster"):
+        for a, b in zip(out[group], out["warp"]):
+            assert a["jumps"] == b["jumps"] == 0 or kind == "me"
+            np.testing.assert_allclose(a["expect"], b["expect"], atol=1e-11, rtol=0)
+            np.testing.assert_allclose(a["norm"], b["norm"], atol=1e-11, rtol=0)
+    if kind == "me":
+        for k in range(4):
+            _close(out["cluster"][0]["expect"][:, k].real, g["expect"][k])
