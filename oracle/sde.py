@@ -8,7 +8,7 @@ Follows ``Platen.step`` (qutip/solver/sode/_sode.pyx:62-120) and ``Euler.step``
 (qutip/solver/sode/ssystem.pyx:141-166) and ``StochasticOpenSystem`` (ssystem.pyx:227-240),
 in the same order of operations.  Pinned by tests/test_oracle_sde.py against the
 reference's own ``run_from_experiment`` with a preset noise record (SSE Platen, SME Platen,
-SSE Euler: 1e-13 absolute per state entry).
+SSE and SME Euler: 1e-13 absolute per state entry).
 """
 from __future__ import annotations
 

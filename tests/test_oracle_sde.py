@@ -87,6 +87,29 @@ def test_sse_euler_restatement_matches_the_reference(qt):
         np.testing.assert_allclose(x, res.states[k].full()[:, 0], atol=1e-13, rtol=0)
 
 
+def test_sme_euler_restatement_matches_the_reference(qt):
+    N = 5
+    a = qt.destroy(N)
+    H = a.dag() * a + 0.3 * (a + a.dag())
+    sc = [np.sqrt(0.2) * a, np.sqrt(0.05) * a.dag() * a]
+    cops = [np.sqrt(0.1) * a]
+    rho0 = qt.coherent_dm(N, 0.5)
+    dt = 1e-3
+    tl = np.arange(16) * dt
+    noise = np.random.default_rng(9).normal(0, np.sqrt(dt), size=(len(sc), len(tl) - 1))
+    solver = qt.SMESolver(H, sc, heterodyne=False, c_ops=cops,
+                          options={"method": "euler", "dt": dt, "store_states": True,
+                                   "progress_bar": None})
+    res = solver.run_from_experiment(rho0, tl, noise)
+    L = _csr(qt.liouvillian(H, sc) + qt.liouvillian(None, cops))
+    C = [_csr(qt.spre(c) + qt.spost(c.dag())) for c in sc]
+    x = rho0.full().reshape(-1, order="F")
+    for k in range(1, len(tl)):
+        x = euler_steps(L, C, None, x, noise[:, k - 1][None, :], dt, open_=True)
+        np.testing.assert_allclose(x, res.states[k].full().reshape(-1, order="F"),
+                                   atol=1e-13, rtol=0)
+
+
 @pytest.mark.parametrize("tlist,dt", [
     (np.linspace(0, 1, 11), 1e-3),
     (np.array([0.0, 0.0004, 0.0011, 0.5, 0.50049, 2.0]), 1e-3),
